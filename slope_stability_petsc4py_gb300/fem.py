@@ -1,0 +1,140 @@
+"""Quadrature rules and reference-element basis gradients of the supported simplex elements.
+
+The rules and node orderings must be the reference's, value for value, because every
+tangent and force entry is a sum over these points and weights:
+
+* quadrature: ``src/slope_stability/fem/quadrature.py:7-126`` (the tables below restate its
+  constants, including the truncated decimals and the negative centroid weight of the
+  11-point tetrahedron rule);
+* basis gradients: ``src/slope_stability/fem/basis.py:9-206`` and the generic barycentric
+  construction of ``src/slope_stability/core/simplex_lagrange.py:95-161`` for P4.
+
+Only small host tables live here; the per-point geometry (``dphi``, weights) is computed on
+the GPU by the ``ssp_geometry_*`` kernels.
+"""
+
+from __future__ import annotations
+
+from functools import lru_cache
+
+import numpy as np
+
+from .synthetic import tet_node_tuples
+
+N_NODES = {(2, "P1"): 3, (2, "P2"): 6, (3, "P1"): 4, (3, "P2"): 10, (3, "P4"): 35}
+
+
+def quadrature(dim: int, elem_type: str) -> tuple[np.ndarray, np.ndarray]:
+    """Reference-element points ``xi`` (dim, n_q) and weights ``wf`` (n_q,)."""
+    et = elem_type.upper()
+    if dim == 2:
+        if et == "P1":
+            return np.array([[1 / 3], [1 / 3]]), np.array([0.5])
+        if et == "P2":
+            a, b, c, d = 0.1012865073235, 0.7974269853531, 0.4701420641051, 0.0597158717898
+            xi = np.array([[a, b, a, c, c, d, 1 / 3], [a, a, b, d, c, c, 1 / 3]])
+            wf = np.array([0.1259391805448] * 3 + [0.1323941527885] * 3 + [0.225]) / 2
+            return xi, wf
+    if dim == 3:
+        if et == "P1":
+            return np.array([[0.25], [0.25], [0.25]]), np.array([1 / 6])
+        if et == "P2":
+            s, l, u, v = 0.0714285714285714, 0.785714285714286, 0.399403576166799, 0.100596423833201
+            xi = np.array(
+                [
+                    [1 / 4, s, l, s, s, u, v, v, u, u, v],
+                    [1 / 4, s, s, l, s, v, u, v, u, v, u],
+                    [1 / 4, s, s, s, l, v, v, u, v, u, u],
+                ]
+            )
+            wf = np.array([-0.013155555555555] + [0.007622222222222] * 4 + [0.024888888888888] * 6)
+            return xi, wf
+        if et == "P4":
+            a, b = 0.3561913862225449, 0.2146028712591517
+            c, d = 0.8779781243961660, 0.0406739585346113
+            e, f = 0.0329863295731731, 0.3223378901422757
+            g, h, k = 0.2696723314583159, 0.0636610018750175, 0.6030056647916491
+            xi = np.array(
+                [
+                    [a, b, b, b, c, d, d, d, e, f, f, f, g, h, h, k, h, h, h, g, k, h, g, k],
+                    [b, b, b, a, d, d, d, c, f, f, f, e, h, g, h, h, k, h, g, k, h, k, h, g],
+                    [b, b, a, b, d, d, c, d, f, f, e, f, h, h, g, h, h, k, k, h, g, g, k, h],
+                ]
+            )
+            wf = np.array(
+                [0.0399227502581679] * 4 + [0.0100772110553207] * 4 + [0.0553571815436544] * 4
+                + [0.0482142857142857] * 12
+            ) / 6.0
+            return xi, wf
+    raise ValueError(f"unsupported element {dim}D {elem_type!r}")
+
+
+def _lagrange_factor(order: int, degree: int, lam: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """prod_{m<degree} (order*lam - m)/(m+1) and its derivative in lam."""
+    if degree == 0:
+        return np.ones_like(lam), np.zeros_like(lam)
+    fac = [(order * lam - m) / (m + 1) for m in range(degree)]
+    val = np.ones_like(lam)
+    for f in fac:
+        val = val * f
+    der = np.zeros_like(lam)
+    for m in range(degree):
+        term = np.full_like(lam, order / (m + 1))
+        for n, f in enumerate(fac):
+            if n != m:
+                term = term * f
+        der = der + term
+    return val, der
+
+
+def _tet_lagrange_grads(order: int, xi: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    bary = (1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2])
+    tuples = tet_node_tuples(order)
+    n_q = xi.shape[1]
+    out = [np.empty((len(tuples), n_q)) for _ in range(3)]
+    for idx, counts in enumerate(tuples):
+        vals, ders = zip(*(_lagrange_factor(order, c, l) for l, c in zip(bary, counts)))
+        dl = []
+        for dv in range(4):
+            term = ders[dv]
+            for fv in range(4):
+                if fv != dv:
+                    term = term * vals[fv]
+            dl.append(term)
+        for ax in range(3):
+            out[ax][idx] = dl[ax + 1] - dl[0]
+    return out[0], out[1], out[2]
+
+
+@lru_cache(maxsize=None)
+def reference_gradients(dim: int, elem_type: str) -> np.ndarray:
+    """Basis gradients on the reference element at the quadrature points, shape (dim, n_p, n_q)."""
+    xi, _ = quadrature(dim, elem_type)
+    et = elem_type.upper()
+    n_q = xi.shape[1]
+    z = np.zeros(n_q)
+    if dim == 2:
+        x1, x2 = xi
+        x0 = 1.0 - x1 - x2
+        if et == "P1":
+            g1 = np.repeat(np.array([-1.0, 1.0, 0.0])[:, None], n_q, axis=1)
+            g2 = np.repeat(np.array([-1.0, 0.0, 1.0])[:, None], n_q, axis=1)
+        elif et == "P2":
+            g1 = np.array([1 - 4 * x0, 4 * x1 - 1, z, 4 * x2, -4 * x2, 4 * (x0 - x1)])
+            g2 = np.array([1 - 4 * x0, z, 4 * x2 - 1, 4 * x1, 4 * (x0 - x2), -4 * x1])
+        else:
+            raise ValueError(et)
+        return np.stack((g1, g2))
+    x1, x2, x3 = xi
+    x0 = 1.0 - x1 - x2 - x3
+    if et == "P1":
+        base = np.array([[-1.0, 1.0, 0.0, 0.0], [-1.0, 0.0, 1.0, 0.0], [-1.0, 0.0, 0.0, 1.0]])
+        return np.repeat(base[:, :, None], n_q, axis=2)
+    if et == "P2":
+        g1 = np.array([1 - 4 * x0, 4 * x1 - 1, z, z, 4 * (x0 - x1), 4 * x2, -4 * x2, 4 * x3, z, -4 * x3])
+        g2 = np.array([1 - 4 * x0, z, 4 * x2 - 1, z, -4 * x1, 4 * x1, 4 * (x0 - x2), z, 4 * x3, -4 * x3])
+        g3 = np.array([1 - 4 * x0, z, z, 4 * x3 - 1, -4 * x1, z, -4 * x2, 4 * x1, 4 * x2, 4 * (x0 - x3)])
+        return np.stack((g1, g2, g3))
+    if et == "P4":
+        return np.stack(_tet_lagrange_grads(4, xi))
+    raise ValueError(et)
