@@ -1,0 +1,368 @@
+"""Benchmark of the Newton hot path: quadrature points per second of one builder pass.
+
+One step = one Newton iteration of the reference's owned-row builder on a fixed synthetic slope:
+strength reduction -> strain B u -> Mohr-Coulomb return mapping (S and DS) -> owned internal
+force B^T (w S) -> tangent CSR values sum B^T (w DS) B -> constrained diagonals and the
+regularised blend (1-r) K + r K_elast.  ``value`` is measured with inputs resident in HBM;
+``e2e`` goes through the public ``ConstitutiveOperator`` API with pinned host inputs and host
+outputs (U uploaded, F_free and every CSR value copied back each step, as the PETSc hand-off
+needs).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3d_p2_homo] [--impl reference]
+
+``--impl reference`` times the reference algorithm on the host cores instead (the oracle's C
+restatement of the reference kernels, all threads), on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "quad-pts/s constitutive+tangent; FP64 plain vs mixed+learned at ≤1e-6 err"
+LAMBDA, R_REG = 1.1, 0.1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="3d_p2_homo")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- workload
+
+
+def workload(name: str):
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    cfg = synthetic.CONFIGS[name]
+    mesh = synthetic.build_config_mesh(name)
+    mats = synthetic.MaterialSet.layered(4, seed=0) if cfg["n_layers"] > 1 else synthetic.MaterialSet.homogeneous()
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=float(mats.gamma[i]), gamma_unsat=float(mats.gamma[i]))
+             for i in range(mats.c0.size)]
+    U = synthetic.displacement_field(mesh, mats, amplitude=cfg["amplitude"], seed=3)
+    return mesh, mats, specs, U
+
+
+def describe(name, mesh, n_int, nnz):
+    return (f"{name}: {mesh.n_elem:,} {mesh.dim}D {mesh.elem_type} elements, {n_int:,} quadrature points, "
+            f"{mesh.n_nodes * mesh.dim:,} dofs, {nnz:,} CSR nnz")
+
+
+# ----------------------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- CPU reference path
+
+
+class OracleRunner:
+    """The reference algorithm (oracle restatement of its C kernels) on the host cores."""
+
+    def __init__(self, mesh, specs, U, dphi=None, weight=None):
+        from oracle import oracle_py as oracle
+        from slope_stability_petsc4py_gb300 import fem
+        from slope_stability_petsc4py_gb300.distributed_tangent import _PatternBuild
+        from slope_stability_petsc4py_gb300.materials import heterogenous_materials
+
+        self.o = oracle
+        oracle.build()
+        pb = _PatternBuild(mesh.elem, mesh.q_mask, (0, mesh.n_nodes))
+        keys = ("overlap_nodes", "overlap_element_dof_lids", "row_slot_ptr", "slot_elem", "slot_lrow", "slot_pos",
+                "constrained_diag_positions", "owned_free_mask", "overlap_elements")
+        self.p = {k: pb.get(k) for k in keys}
+        self.nnz = pb.sizes["nnz"]
+        pb.close()
+        xi, wf = fem.quadrature(mesh.dim, mesh.elem_type)
+        self.n_q = xi.shape[1]
+        if dphi is None:
+            dphi, weight = oracle.geometry(mesh.coord, mesh.elem[:, self.p["overlap_elements"]], mesh.dim,
+                                           fem.reference_gradients(mesh.dim, mesh.elem_type), wf)
+        self.d, self.w = dphi, weight
+        nodes = self.p["overlap_nodes"]
+        dim = mesh.dim
+        gd = dim * np.repeat(nodes, dim) + np.tile(np.arange(dim), nodes.size)
+        self.u_ov = np.ascontiguousarray(U.reshape(-1, order="F")[gd])
+        n_int = mesh.n_elem * self.n_q
+        self.mat = dict(zip(("c0", "phi", "psi", "shear", "bulk", "lame"),
+                            heterogenous_materials(mesh.material_id, np.ones(n_int, bool), self.n_q, specs)[:6]))
+        self.n_int = n_int
+        self.dim = dim
+        self.elastic = None
+
+    def step(self):
+        o, p, d = self.o, self.p, self.d
+        cb, sp = o.reduction(self.mat["c0"], self.mat["phi"], self.mat["psi"], LAMBDA, "B")
+        E = o.strain_3d(d[0], d[1], d[2], self.u_ov, p["overlap_element_dof_lids"], self.n_q)
+        S, DS = o.constitutive_3d(E, cb, sp, self.mat["shear"], self.mat["bulk"], self.mat["lame"])
+        F = o.force_rows_3d(d[0], d[1], d[2], S, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"], self.n_q)
+        F[~p["owned_free_mask"].astype(bool)] = 0.0
+        K = o.tangent_rows_3d(d[0], d[1], d[2], DS, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"],
+                              p["slot_pos"], self.n_q, self.nnz)
+        K[p["constrained_diag_positions"]] = 1.0
+        if self.elastic is not None:
+            K *= 1.0 - R_REG
+            K += R_REG * self.elastic
+        return F, K
+
+    def time_steps(self, steps, warmup, budget_s=60.0):
+        for _ in range(warmup):
+            self.step()
+        times = []
+        t_start = time.perf_counter()
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            self.step()
+            times.append(time.perf_counter() - t0)
+            if time.perf_counter() - t_start > budget_s:
+                break
+        return times
+
+
+# ----------------------------------------------------------------------------- GPU arm
+
+
+def fp64_peak(torch, lib):
+    """Measured FP64 FMA rate of this device (TFLOP/s), from the ssp_probe_dfma kernel."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 8192
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        lib.call("ssp_probe_dfma", iters, blocks, threads, lib.ptr(out), lib.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    lib.call("ssp_probe_dfma", iters, blocks, threads, lib.ptr(out), lib.stream_handle())
+    e1.record()
+    torch.cuda.synchronize()
+    flops = 16.0 * iters * threads * blocks
+    return flops / (e0.elapsed_time(e1) * 1e-3) / 1e12
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import torch
+
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    mesh, mats, specs, U = workload(args.config)
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs,
+                                        elem_type=mesh.elem_type)
+    pat = op.owned_tangent_pattern
+    n_int, nnz = pat.n_local_int, pat.nnz
+    U_dev = torch.as_tensor(U, device="cuda")
+    op.host_outputs = False
+
+    def step():
+        op.reduction(LAMBDA)
+        op.constitutive_problem_stress_tangent(U_dev)
+        op.build_F_free_local()
+        op.build_K_regularized(R_REG)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    _lib.raise_on_device_status()
+
+    clocks = ClockSampler(local) if not args.no_clocks else None
+    op.tangent_events = []
+    launches0 = _lib.LAUNCHES["count"]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop() if clocks else None
+    if dist is not None:
+        dist.barrier()
+    launches = _lib.LAUNCHES["count"] - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    tang_ms = float(np.mean([a.elapsed_time(b) for a, b in op.tangent_events]))
+    op.tangent_events = None
+    _lib.raise_on_device_status()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # roofline of the dominant kernel (tangent values; algorithmic bytes and flops per launch)
+    dim, n_p, n_q = pat.dim, pat.n_p, pat.n_q
+    ns, n_ld, n_el = pat.n_strain, pat.dim * pat.n_p, int(pat.overlap_elements.size)
+    bytes_launch = n_el * (n_q * (8 * ns * ns + 8 * dim * n_p + 8) + 4 * n_ld * n_ld) + 8 * nnz
+    flops_launch = n_el * 2.0 * n_q * (n_ld * ns * dim + n_ld * (n_ld + 1) // 2 * dim)
+    hbm_peak, hbm_src = peaks()
+    achieved_gbs = bytes_launch / (tang_ms * 1e-3) / 1e9
+    fp64_tf = fp64_peak(torch, _lib)
+    achieved_tf = flops_launch / (tang_ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": world * n_int / (ms * 1e-3), "unit": "quad-pts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": "plain",
+                   "step": "reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + "
+                           "constrained diagonals + regularised blend",
+                   "l2": f"inputs larger than L2 (tangent-kernel working set {bytes_launch / 1e9:.2f} GB > 129 MB)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "assembled_nnz_per_s": world * nnz / (ms * 1e-3),
+        "roofline": {"bound": "hbm", "kernel": "ssp_tangent_element (symmetric FP64)", "achieved": achieved_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                     "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else hbm_src,
+                     "traffic": None, "ms_per_launch": tang_ms, "algorithmic_bytes": bytes_launch},
+        "roofline_fp64": {"bound": "fp64", "achieved": achieved_tf, "peak": fp64_tf, "unit": "TFLOP/s",
+                          "frac": achieved_tf / fp64_tf, "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)",
+                          "algorithmic_flops": flops_launch},
+        "gpu_launches": launches,
+        "clocks": clock_info,
+    }
+
+    if rank == 0 and not args.no_e2e:
+        op.host_outputs = True
+        U_pin = torch.as_tensor(U).pin_memory()
+        for _ in range(3):
+            F_free, K = op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)
+            K.getValuesCSR()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            F_free, K = op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)
+            K.getValuesCSR()  # synchronises: the CSR values are on the host
+            times.append(time.perf_counter() - t0)
+        t_e2e = float(np.median(times))
+        line["e2e"] = {"value": n_int / t_e2e, "unit": "quad-pts/s", "h2d_bytes_per_step": int(U.nbytes),
+                       "d2h_bytes_per_step": int(F_free.nbytes + 8 * nnz), "ms_per_step": t_e2e * 1e3,
+                       "api": "ConstitutiveOperator.build_F_K_regularized_all_free(lam, U_host, r) + K.getValuesCSR()"}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        runner = OracleRunner(mesh, specs, U, dphi=(pat.dphi1, pat.dphi2, pat.dphi3), weight=pat.overlap_assembly_weight)
+        runner.elastic = pat.elastic_values
+        times = runner.time_steps(steps=5, warmup=1, budget_s=30.0)
+        t_cpu = float(np.median(times))
+        line["cpu_baseline"] = {"value": n_int / t_cpu, "unit": "quad-pts/s", "cores": runner.o.num_threads(),
+                                "kind": "port",
+                                "sample": f"full workload, {len(times)} passes after 1 warm-up, median; oracle C "
+                                          f"restatement of the reference kernels (rows tangent), OpenMP"}
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, mats, specs, U = workload(args.config)
+    runner = OracleRunner(mesh, specs, U)
+    times = runner.time_steps(args.steps, args.warmup, budget_s=150.0)
+    t = float(np.median(times))
+    value = runner.n_int / t
+    line = {"metric": METRIC, "value": value, "unit": "quad-pts/s", "n_gpus": world, "steps": len(times),
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": describe(args.config, mesh, runner.n_int, runner.nnz), "form": "plain",
+                       "parallelism": "host cores (OpenMP)"},
+            "cpu_baseline": {"value": value, "unit": "quad-pts/s", "cores": runner.o.num_threads(), "kind": "port",
+                             "sample": f"full workload per step, median of {len(times)}; the reference's C kernels "
+                                       f"restated (oracle), constrained diagonals without the elastic blend"},
+            "e2e": {"value": value, "unit": "quad-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

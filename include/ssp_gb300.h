@@ -1,0 +1,183 @@
+/*
+ * ssp_gb300.h -- C ABI of the GB300 (sm_103a) Newton hot path of the slope-stability solver.
+ *
+ * Conventions shared by every entry point:
+ *   - plain pointers and sizes only; no framework types cross this boundary;
+ *   - array arguments are DEVICE pointers (caller-allocated, e.g. cudaMalloc or a torch
+ *     CUDA tensor) unless the comment says "host";
+ *   - layouts are the reference's C layouts: per-point AoS strains/stresses [n_int][6]
+ *     (2D: [n_int][3] in, [n_int][4] out), tangents [n_int][36] (2D [n_int][9]) column-major
+ *     per point (entry (i,j) at i + n_strain*j), dphi arrays [n_int][n_p], points
+ *     element-major (g = e*n_q + q);
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream); all work is
+ *     enqueued asynchronously on it;
+ *   - the return value is an ssp_status; the reference's C functions return void and its
+ *     Cython wrappers raise ValueError on bad shapes -- here a bad argument returns
+ *     SSP_ERR_INVALID before anything is launched;
+ *   - kernels that meet an out-of-range index skip the access and set a bit in a device
+ *     status word instead of faulting; ssp_device_status() reads it.
+ *
+ * Reference paths below are relative to the reference project root
+ * (Beremi/slope_stability_petsc4py).
+ */
+#ifndef SSP_GB300_H
+#define SSP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum ssp_status {
+    SSP_OK = 0,
+    SSP_ERR_INVALID = 1,     /* bad argument (shape, size, null pointer) */
+    SSP_ERR_CUDA = 2,        /* a CUDA call or launch failed */
+    SSP_ERR_UNSUPPORTED = 3, /* element type / quadrature combination without a kernel */
+    SSP_ERR_OVERFLOW = 4,    /* an index does not fit int32 (distributed_tangent.py:122-124) */
+    SSP_ERR_PATTERN = 5      /* structural entry missing from the pattern (distributed_tangent.py:431-432) */
+};
+
+/* bits of the device status word */
+#define SSP_DEV_BAD_INDEX 1
+#define SSP_DEV_NONFINITE 2
+
+/* ------------------------------------------------------------------ constitutive */
+
+/* Replaces constitutive_problem_3d_s_batch_c (src/slope_stability/cython/constitutive_3d_batch.h:4-13).
+ * S only (line search / residual-only Newton steps).  `bulk` is unused, as in the reference. */
+int ssp_constitutive_3d_s(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                          const double *bulk, const double *lame, int n_int, double *S_out, void *stream);
+
+/* Replaces constitutive_problem_3d_sds_batch_c (src/slope_stability/cython/constitutive_3d_batch.h:15-25).
+ * S and the consistent tangent DS; DS is symmetric (associated flow, sin(psi) = sin(phi)). */
+int ssp_constitutive_3d_sds(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                            const double *bulk, const double *lame, int n_int, double *S_out, double *DS_out,
+                            void *stream);
+
+/* S plus the return branch of every point (0 elastic, 1 smooth face, 2 left edge, 3 right edge,
+ * 4 apex); the branch decision of constitutive_3D_kernel.h:116-350.  Used to label training data
+ * of the learned branch proposal. */
+int ssp_constitutive_3d_branch(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                               const double *lame, int n_int, double *S_out, int8_t *branch_out, void *stream);
+
+/* Replaces constitutive_problem_2D (src/slope_stability/constitutive/problem.py:143-475), which the
+ * reference has only in NumPy: E [n_int][3] -> S [n_int][4] ([s11,s22,s12,s33]), DS [n_int][9]
+ * (DS_out may be NULL for stress only). */
+int ssp_constitutive_2d(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                        const double *bulk, const double *lame, int n_int, double *S_out, double *DS_out, void *stream);
+
+/* Replaces reduction(c0, phi, psi, lam, Davis_type) (src/slope_stability/constitutive/reduction.py:14-78).
+ * davis_type is 'A', 'B' or 'C'; lam must be > 0. */
+int ssp_reduction(const double *c0, const double *phi, const double *psi, int n_int, double lam, char davis_type,
+                  double *c_bar_out, double *sin_phi_out, void *stream);
+
+/* ------------------------------------------------------------------ geometry */
+
+/* Replaces the dphi/weight part of _assemble_3d / _assemble_2d (src/slope_stability/fem/assembly.py:139-245,
+ * 50-136).  coord [dim][n_nodes], elem [n_p][n_elem] (int64), dhat [dim][n_p][n_q] reference
+ * gradients, wf [n_q]; outputs dphi* [n_elem*n_q][n_p], weight [n_elem*n_q] (dphi3 unused in 2D). */
+int ssp_geometry(int dim, const double *coord, const int64_t *elem, const double *dhat, const double *wf, int n_nodes,
+                 int n_elem, int n_p, int n_q, double *dphi1, double *dphi2, double *dphi3, double *weight,
+                 void *stream);
+
+/* ------------------------------------------------------------------ strain / force */
+
+/* Replaces assemble_overlap_strain_3d_c (src/slope_stability/cython/assemble_tangent_values_3d.h:40-51).
+ * Adds n_u, the length of u_overlap, for bounds checking. */
+int ssp_assemble_overlap_strain_3d(const double *dphi1, const double *dphi2, const double *dphi3,
+                                   const double *u_overlap, int n_u, const int32_t *elem_dof_lids, int n_int,
+                                   int n_elem, int n_p, int n_q, double *out_values, void *stream);
+
+/* 2D counterpart of the strain kernel; replaces overlap_B @ u_overlap
+ * (src/slope_stability/fem/distributed_tangent.py:906-907) for plane strain. */
+int ssp_assemble_overlap_strain_2d(const double *dphi1, const double *dphi2, const double *u_overlap, int n_u,
+                                   const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                   double *out_values, void *stream);
+
+/* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
+ * Deterministic row gather; rows without slots come out 0. */
+int ssp_assemble_force_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *stress,
+                               const double *weight, const int32_t *row_slot_ptr, const int32_t *slot_elem,
+                               const uint8_t *slot_lrow, int n_int, int n_rows, int n_slots, int n_p, int n_q,
+                               double *out_values, void *stream);
+
+/* Owned internal force by element scatter, 2D or 3D: the same F = B^T (w S) restricted to owned
+ * free rows (distributed_tangent.py:845-883, 910-934).  elem_row [n_elem][dim*n_p] gives the owned
+ * free row of each local dof or -1.  out_values [n_rows] is zeroed first. */
+int ssp_assemble_force_element(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                               const double *stress, const double *weight, const int32_t *elem_row, int n_elem,
+                               int n_p, int n_q, int n_rows, double *out_values, void *stream);
+
+/* ------------------------------------------------------------------ tangent CSR values */
+
+/* Replaces assemble_tangent_values_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:21-38).
+ * out_values [nnz_out] is zeroed first; constrained diagonals are left at 0 as in the reference
+ * kernel (the caller sets them, see ssp_finish_values). */
+int ssp_assemble_tangent_values_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *ds,
+                                        const double *weight, const int32_t *row_slot_ptr, const int32_t *slot_elem,
+                                        const uint8_t *slot_lrow, const int32_t *slot_pos, int n_int, int n_rows,
+                                        int n_slots, int n_p, int n_q, int nnz_out, double *out_values, void *stream);
+
+/* Replaces assemble_tangent_values_3d_p2_c (src/slope_stability/cython/assemble_tangent_values_3d.h:6-19):
+ * element-dense K_e through scatter_map [n_elem][(3 n_p)^2] (-1 = skipped). */
+int ssp_assemble_tangent_values_3d_p2(const double *dphi1, const double *dphi2, const double *dphi3, const double *ds,
+                                      const double *weight, const int32_t *scatter_map, int n_int, int n_elem, int n_p,
+                                      int n_q, int nnz_out, double *out_values, void *stream);
+
+/* The element kernel behind ssp_assemble_tangent_values_3d_p2, for 2D and 3D, with a symmetric
+ * variant (symmetric != 0: evaluates alpha <= beta only; valid when every DS block is symmetric,
+ * which holds for tangents from ssp_constitutive_*).  accumulate == 0 zeroes out_values first.
+ * 2D also replaces the Python loop of distributed_tangent.py:1437-1484. */
+int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const double *dphi2, const double *dphi3,
+                        const double *ds, const double *weight, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
+                        long long nnz_out, double *out_values, int accumulate, void *stream);
+
+/* Constrained diagonals := 1.0 (distributed_tangent.py:1606-1607), then, when elastic_values is
+ * not NULL, values := (1-r) values + r elastic_values (constitutive/problem.py:1614-1615). */
+int ssp_finish_values(double *values, long long nnz, const int32_t *constrained_diag_positions, int n_diag,
+                      const double *elastic_values, double r, void *stream);
+
+/* dst[i] = src[idx[i]] (owned free rows of a force vector, problem.py:1008-1015). */
+int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *stream);
+
+/* Reads the device status word (SSP_DEV_* bits); clear != 0 resets it.  Synchronous. */
+int ssp_device_status(int *status_out, int clear);
+
+/* Measurement probe (no reference counterpart): blocks*threads threads each run `iters`
+ * iterations of 8 independent FP64 FMAs (16*iters flops per thread) and write one double to
+ * out[blocks*threads].  Timing it gives the device's FP64 FMA rate. */
+int ssp_probe_dfma(int iters, int blocks, int threads, double *out, void *stream);
+
+/* ------------------------------------------------------------------ pattern (host) */
+
+/* Fixed owned-row CSR pattern and element->CSR maps, built on the host in C++; replaces the
+ * dictionary loops of prepare_owned_tangent_pattern (src/slope_stability/fem/distributed_tangent.py:
+ * 297-478, 937-1175) with bit-identical output.  All pointers of the pattern API are HOST pointers.
+ *
+ * elem is [n_p][n_elem] int64 (global node ids), free_mask is [dim*n_nodes] (dof dim*node+comp,
+ * nonzero = free, i.e. q_mask flattened in Fortran order); the owned node block is [node0, node1). */
+typedef struct ssp_pattern ssp_pattern;
+
+int ssp_pattern_build(int dim, int n_nodes, int n_p, int n_elem, const int64_t *elem, const uint8_t *free_mask,
+                      int node0, int node1, ssp_pattern **out);
+
+/* sizes[0..6] = n_overlap_elements, n_overlap_nodes, n_rows, nnz, n_slots, n_constrained, n_ld */
+int ssp_pattern_sizes(const ssp_pattern *p, int64_t *sizes);
+
+/* Copies one named array into dst (host, caller-sized from ssp_pattern_sizes).  Names and types:
+ *   "overlap_elements" int64 [n_ov_el]        "overlap_nodes" int64 [n_ov_nodes]
+ *   "overlap_element_dof_lids" int32 [n_ov_el][n_ld]   "owned_local_overlap_dofs" int64 [n_rows]
+ *   "indptr" int32 [n_rows+1]   "indices" int32 [nnz]   "constrained_diag_positions" int32
+ *   "scatter_map" int32 [n_ov_el][n_ld*n_ld]   "row_slot_ptr" int32 [n_rows+1]
+ *   "slot_elem" int32 [n_slots]   "slot_lrow" uint8 [n_slots]   "slot_pos" int32 [n_slots][n_ld]
+ *   "elem_row" int32 [n_ov_el][n_ld]   "owned_free_mask" uint8 [n_rows] */
+int ssp_pattern_copy(const ssp_pattern *p, const char *name, void *dst);
+
+void ssp_pattern_free(ssp_pattern *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SSP_GB300_H */

@@ -1,0 +1,161 @@
+"""ctypes binding of ``_build/libssp_gb300.so`` (the C ABI of ``include/ssp_gb300.h``).
+
+There is no CPU fallback: if the library is missing or fails to load, every entry point of this
+package raises.  Device buffers are torch CUDA tensors; only their raw pointers and the raw
+``cudaStream_t`` of torch's current stream cross the boundary.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+_c_int, _c_ll, _c_dbl, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported element", 4: "int32 overflow",
+          5: "pattern is missing a structural entry"}
+
+_SIGS = {
+    "ssp_constitutive_3d_s": [_vp] * 6 + [_c_int, _vp, _vp],
+    "ssp_constitutive_3d_sds": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_constitutive_3d_branch": [_vp] * 5 + [_c_int, _vp, _vp, _vp],
+    "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_reduction": [_vp, _vp, _vp, _c_int, _c_dbl, ctypes.c_char, _vp, _vp, _vp],
+    "ssp_geometry": [_c_int, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_assemble_overlap_strain_3d": [_vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_overlap_strain_2d": [_vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_force_3d_rows": [_vp] * 8 + [_c_int] * 6 + [_vp, _vp],
+    "ssp_assemble_force_element": [_c_int] + [_vp] * 6 + [_c_int] * 4 + [_vp, _vp],
+    "ssp_assemble_tangent_values_3d_rows": [_vp] * 9 + [_c_int] * 6 + [_vp, _vp],
+    "ssp_assemble_tangent_values_3d_p2": [_vp] * 6 + [_c_int] * 5 + [_vp, _vp],
+    "ssp_tangent_element": [_c_int, _c_int] + [_vp] * 6 + [_c_int, _c_int, _c_int, _c_ll, _vp, _c_int, _vp],
+    "ssp_finish_values": [_vp, _c_ll, _vp, _c_int, _vp, _c_dbl, _vp],
+    "ssp_gather": [_vp, _vp, _c_int, _vp, _vp],
+    "ssp_device_status": [ctypes.POINTER(_c_int), _c_int],
+    "ssp_probe_dfma": [_c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_pattern_build": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _c_int, _c_int, ctypes.POINTER(_vp)],
+    "ssp_pattern_sizes": [_vp, _vp],
+    "ssp_pattern_copy": [_vp, ctypes.c_char_p, _vp],
+    "ssp_pattern_free": [_vp],
+}
+
+
+class SSPError(RuntimeError):
+    """A C-ABI call returned a non-zero ssp_status or a kernel flagged a bad index."""
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed and possible) the sm_103a library; raise if impossible."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not path.exists() or os.environ.get("SSP_FORCE_REBUILD"):
+        if not build_if_missing:
+            raise ImportError(f"CUDA library {path} is not built; run __graft_entry__.build()")
+        _build.build()
+    lib = ctypes.CDLL(str(path))
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = None if name == "ssp_pattern_free" else _c_int
+    _LIB = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGS)
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        raise SSPError(f"{what} failed: {STATUS.get(int(status), status)}")
+
+
+# kernels each entry point launches per call (for launch accounting); callables take the args
+_KERNELS_PER_CALL = {
+    "ssp_constitutive_3d_s": 1, "ssp_constitutive_3d_sds": 1, "ssp_constitutive_3d_branch": 1,
+    "ssp_constitutive_2d": 1, "ssp_reduction": 1, "ssp_geometry": 1, "ssp_assemble_overlap_strain_3d": 1,
+    "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
+    "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
+    "ssp_gather": 1, "ssp_probe_dfma": 1,
+    "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
+}
+LAUNCHES = {"count": 0}
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args), name)
+    k = _KERNELS_PER_CALL.get(name, 0)
+    LAUNCHES["count"] += k(args) if callable(k) else k
+
+
+def device_status(clear: bool = True) -> int:
+    v = _c_int(0)
+    check(load().ssp_device_status(ctypes.byref(v), 1 if clear else 0), "ssp_device_status")
+    return int(v.value)
+
+
+def raise_on_device_status() -> None:
+    st = device_status(clear=True)
+    if st:
+        raise SSPError(f"a kernel flagged invalid input (device status {st:#x})")
+
+
+# ----------------------------------------------------------------------------- torch helpers
+
+
+def torch():
+    import torch as _t
+
+    return _t
+
+
+def ptr(t) -> int | None:
+    """Raw device pointer of a contiguous CUDA tensor (None passes NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise SSPError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise SSPError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def stream_handle() -> int:
+    return torch().cuda.current_stream().cuda_stream
+
+
+def require_cuda():
+    t = torch()
+    if not t.cuda.is_available():
+        raise SSPError("no CUDA device: the GB300 hot path has no CPU fallback")
+    load()
+    return t
+
+
+def to_device(a, dtype=None):
+    """numpy / torch -> contiguous CUDA tensor (no copy if already there with that dtype)."""
+    t = torch()
+    if isinstance(a, t.Tensor):
+        out = a
+        if dtype is not None and out.dtype != dtype:
+            out = out.to(dtype)
+        if not out.is_cuda:
+            out = out.cuda()
+        return out.contiguous()
+    arr = np.ascontiguousarray(a)
+    out = t.from_numpy(arr)
+    if dtype is not None:
+        out = out.to(dtype)
+    return out.cuda(non_blocking=False).contiguous()

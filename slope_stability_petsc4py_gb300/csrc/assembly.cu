@@ -1,0 +1,574 @@
+// Strain, internal force and tangent CSR-value assembly on the fixed owned-row pattern.
+//
+// Reference routines (src/slope_stability/...):
+//   ssp_assemble_overlap_strain_3d   cython/assemble_tangent_values_3d.c:216-273
+//   ssp_assemble_force_3d_rows       cython/assemble_tangent_values_3d.c:275-327
+//   ssp_assemble_tangent_values_3d_rows  cython/assemble_tangent_values_3d.c:111-214
+//   ssp_assemble_tangent_values_3d_p2    cython/assemble_tangent_values_3d.c:13-109
+//   ssp_tangent_element_*            the same sum K = sum_q B^T (w D) B, scattered through the
+//                                    element->CSR map (fem/distributed_tangent.py:328-366)
+//   2D variants                      fem/distributed_tangent.py:845-907, 1437-1484
+//   ssp_geometry_*                   fem/assembly.py:50-136 (2D), 139-245 (3D)
+//   ssp_finish_values                fem/distributed_tangent.py:1606-1607 and
+//                                    constitutive/problem.py:1614-1615
+//
+// Layout (all FP64 unless stated): points are element-major (g = e*n_q + q); dphi arrays are
+// [n_int][n_p]; strains/stresses/tangents are per-point AoS ([n_int][6], [n_int][36]), which is
+// the reference's C layout and makes each element's data one contiguous block.
+#include "ssp_internal.cuh"
+
+namespace ssp {
+namespace {
+
+// ---------------------------------------------------------------------------- geometry
+
+template <int DIM>
+__global__ void geometry_kernel(const double *__restrict__ coord, const int64_t *__restrict__ elem,
+                                const double *__restrict__ dhat, const double *__restrict__ wf, int n_nodes,
+                                int n_elem, int n_p, int n_q, double *__restrict__ d1, double *__restrict__ d2,
+                                double *__restrict__ d3, double *__restrict__ weight) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const int e = static_cast<int>(g / n_q), q = static_cast<int>(g % n_q);
+    // dhat is [DIM][n_p][n_q]; elem is [n_p][n_elem]; coord is [DIM][n_nodes]
+    double J[DIM][DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) J[r][c] = 0.0;
+    for (int a = 0; a < n_p; ++a) {
+        const long long node = elem[(long long)a * n_elem + e];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+            const double h = dhat[((long long)r * n_p + a) * n_q + q];
+#pragma unroll
+            for (int c = 0; c < DIM; ++c) J[r][c] += coord[(long long)c * n_nodes + node] * h;
+        }
+    }
+    if (DIM == 3) {
+        const double c11 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c12 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
+        const double c13 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        const double det = J[0][0] * c11 - J[0][1] * c12 + J[0][2] * c13;
+        const double inv = 1.0 / det;
+        const double r12 = J[0][1] * J[2][2] - J[0][2] * J[2][1];
+        const double r13 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        const double r22 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+        const double r23 = J[0][0] * J[1][2] - J[0][2] * J[1][0];
+        const double r32 = J[0][0] * J[2][1] - J[0][1] * J[2][0];
+        const double r33 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        for (int a = 0; a < n_p; ++a) {
+            const double h1 = dhat[(0ll * n_p + a) * n_q + q];
+            const double h2 = dhat[(1ll * n_p + a) * n_q + q];
+            const double h3 = dhat[(2ll * n_p + a) * n_q + q];
+            d1[g * n_p + a] = (c11 * h1 - r12 * h2 + r13 * h3) * inv;
+            d2[g * n_p + a] = (-c12 * h1 + r22 * h2 - r23 * h3) * inv;
+            d3[g * n_p + a] = (c13 * h1 - r32 * h2 + r33 * h3) * inv;
+        }
+        weight[g] = wf[q] * fabs(det);
+    } else {
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const double i11 = J[1][1] / det, i12 = -J[0][1] / det, i21 = -J[1][0] / det, i22 = J[0][0] / det;
+        for (int a = 0; a < n_p; ++a) {
+            const double h1 = dhat[(0ll * n_p + a) * n_q + q];
+            const double h2 = dhat[(1ll * n_p + a) * n_q + q];
+            d1[g * n_p + a] = i11 * h1 + i12 * h2;
+            d2[g * n_p + a] = i21 * h1 + i22 * h2;
+        }
+        weight[g] = fabs(det) * wf[q];
+    }
+}
+
+// ---------------------------------------------------------------------------- strain
+
+__global__ void strain3_kernel(const double *__restrict__ d1, const double *__restrict__ d2,
+                               const double *__restrict__ d3, const double *__restrict__ u,
+                               const int32_t *__restrict__ dof, long long n_u, int n_elem, int n_p, int n_q,
+                               double *__restrict__ E) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const long long e = g / n_q;
+    const int32_t *dl = dof + e * 3 * n_p;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0, a4 = 0.0, a5 = 0.0;
+    for (int a = 0; a < n_p; ++a) {
+        const int32_t i0 = dl[3 * a], i1 = dl[3 * a + 1], i2 = dl[3 * a + 2];
+        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= n_u || i1 >= n_u || i2 >= n_u) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const double gx = d1[g * n_p + a], gy = d2[g * n_p + a], gz = d3[g * n_p + a];
+        const double ux = u[i0], uy = u[i1], uz = u[i2];
+        a0 += gx * ux;
+        a1 += gy * uy;
+        a2 += gz * uz;
+        a3 += gy * ux + gx * uy;
+        a4 += gz * uy + gy * uz;
+        a5 += gz * ux + gx * uz;
+    }
+    double2 *o = reinterpret_cast<double2 *>(E + 6 * g);
+    o[0] = make_double2(a0, a1);
+    o[1] = make_double2(a2, a3);
+    o[2] = make_double2(a4, a5);
+}
+
+__global__ void strain2_kernel(const double *__restrict__ d1, const double *__restrict__ d2,
+                               const double *__restrict__ u, const int32_t *__restrict__ dof, long long n_u, int n_elem,
+                               int n_p, int n_q, double *__restrict__ E) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const long long e = g / n_q;
+    const int32_t *dl = dof + e * 2 * n_p;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int a = 0; a < n_p; ++a) {
+        const int32_t i0 = dl[2 * a], i1 = dl[2 * a + 1];
+        if (i0 < 0 || i1 < 0 || i0 >= n_u || i1 >= n_u) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const double gx = d1[g * n_p + a], gy = d2[g * n_p + a];
+        const double ux = u[i0], uy = u[i1];
+        a0 += gx * ux;
+        a1 += gy * uy;
+        a2 += gy * ux + gx * uy;
+    }
+    E[3 * g] = a0;
+    E[3 * g + 1] = a1;
+    E[3 * g + 2] = a2;
+}
+
+// ---------------------------------------------------------------------------- force
+
+__device__ __forceinline__ double bt3(int comp, double gx, double gy, double gz, const double *s) {
+    return comp == 0 ? gx * s[0] + gy * s[3] + gz * s[5]
+                     : (comp == 1 ? gx * s[3] + gy * s[1] + gz * s[4] : gx * s[5] + gy * s[4] + gz * s[2]);
+}
+
+// Owned force by row gather: deterministic, one thread per owned row.
+__global__ void force_rows3_kernel(const double *__restrict__ d1, const double *__restrict__ d2,
+                                   const double *__restrict__ d3, const double *__restrict__ S,
+                                   const double *__restrict__ w, const int32_t *__restrict__ rsp,
+                                   const int32_t *__restrict__ slot_elem, const uint8_t *__restrict__ slot_lrow,
+                                   int n_rows, int n_elem, int n_p, int n_q, double *__restrict__ F) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    double acc = 0.0;
+    for (int s = rsp[r]; s < rsp[r + 1]; ++s) {
+        const int e = slot_elem[s];
+        const int alpha = slot_lrow[s];
+        const int node = alpha / 3, comp = alpha % 3;
+        if (e < 0 || e >= n_elem || node >= n_p) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        for (int q = 0; q < n_q; ++q) {
+            const long long g = (long long)e * n_q + q;
+            acc += w[g] * bt3(comp, d1[g * n_p + node], d2[g * n_p + node], d3[g * n_p + node], S + 6 * g);
+        }
+    }
+    F[r] = acc;
+}
+
+// Owned force by element scatter (2D and 3D): elem_row[e][alpha] is the owned free row of
+// local dof alpha or -1.  One thread per (element, local dof); atomics into F.
+template <int DIM>
+__global__ void force_element_kernel(const double *__restrict__ d1, const double *__restrict__ d2,
+                                     const double *__restrict__ d3, const double *__restrict__ S,
+                                     const double *__restrict__ w, const int32_t *__restrict__ elem_row, int n_rows,
+                                     int n_elem, int n_p, int n_q, double *__restrict__ F) {
+    constexpr int NS = DIM == 3 ? 6 : 3;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int nld = DIM * n_p;
+    if (t >= (long long)n_elem * nld) return;
+    const long long e = t / nld;
+    const int alpha = static_cast<int>(t % nld);
+    const int row = elem_row[t];
+    if (row < 0) return;
+    if (row >= n_rows) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    const int node = alpha / DIM, comp = alpha % DIM;
+    double acc = 0.0;
+    for (int q = 0; q < n_q; ++q) {
+        const long long g = e * n_q + q;
+        const double *s = S + NS * g;
+        const double gx = d1[g * n_p + node], gy = d2[g * n_p + node];
+        if (DIM == 3) {
+            acc += w[g] * bt3(comp, gx, gy, d3[g * n_p + node], s);
+        } else {
+            acc += w[g] * (comp == 0 ? gx * s[0] + gy * s[2] : gy * s[1] + gx * s[2]);
+        }
+    }
+    atomicAdd(F + row, acc);
+}
+
+// ---------------------------------------------------------------------------- tangent (rows)
+
+// Direct counterpart of the reference "rows" kernel: one thread per owned row, walking the
+// row's slots; deterministic.  out must be zeroed by the caller.
+__global__ void tangent_rows3_kernel(const double *__restrict__ d1, const double *__restrict__ d2,
+                                     const double *__restrict__ d3, const double *__restrict__ DS,
+                                     const double *__restrict__ w, const int32_t *__restrict__ rsp,
+                                     const int32_t *__restrict__ slot_elem, const uint8_t *__restrict__ slot_lrow,
+                                     const int32_t *__restrict__ slot_pos, int n_rows, int n_elem, int n_p, int n_q,
+                                     long long nnz, double *__restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    const int nld = 3 * n_p;
+    for (int s = rsp[r]; s < rsp[r + 1]; ++s) {
+        const int e = slot_elem[s];
+        const int alpha = slot_lrow[s];
+        const int node = alpha / 3, comp = alpha % 3;
+        if (e < 0 || e >= n_elem || node >= n_p) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const int32_t *pos = slot_pos + (long long)s * nld;
+        for (int q = 0; q < n_q; ++q) {
+            const long long g = (long long)e * n_q + q;
+            const double *D = DS + 36 * g;
+            const double wg = w[g];
+            const double gx = d1[g * n_p + node], gy = d2[g * n_p + node], gz = d3[g * n_p + node];
+            double t[6];
+#pragma unroll
+            for (int m = 0; m < 6; ++m) t[m] = wg * bt3(comp, gx, gy, gz, D + 6 * m);
+            for (int b = 0; b < n_p; ++b) {
+                const double bx = d1[g * n_p + b], by = d2[g * n_p + b], bz = d3[g * n_p + b];
+                const int32_t p0 = pos[3 * b], p1 = pos[3 * b + 1], p2 = pos[3 * b + 2];
+                if (p0 >= nnz || p1 >= nnz || p2 >= nnz) {
+                    flag(SSP_DEV_BAD_INDEX);
+                    continue;
+                }
+                if (p0 >= 0) out[p0] += t[0] * bx + t[3] * by + t[5] * bz;
+                if (p1 >= 0) out[p1] += t[3] * bx + t[1] * by + t[4] * bz;
+                if (p2 >= 0) out[p2] += t[5] * bx + t[4] * by + t[2] * bz;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- tangent (element)
+
+// One CTA per element (grid-stride).  K_e = sum_q B_q^T (w_q D_q) B_q is formed in two
+// stages per quadrature point through shared memory:
+//   H[alpha][m] = (B^T (w D))[alpha][m]      (n_ld x n_s, split over the CTA)
+//   K[alpha][beta] += sum_m H[alpha][m] B[m][beta]   (each thread owns fixed entries in registers)
+// and scattered with FP64 atomics through the element->CSR map (the reference's legacy
+// scatter_map).  SYM evaluates only alpha <= beta and writes both mirror positions; it is
+// valid when every D_q is symmetric (tangents produced by ssp_constitutive_*).
+template <int DIM, int NP, int NQ, int THREADS, bool SYM>
+__global__ void __launch_bounds__(THREADS) tangent_element_kernel(
+    const double *__restrict__ d1, const double *__restrict__ d2, const double *__restrict__ d3,
+    const double *__restrict__ DS, const double *__restrict__ w, const int32_t *__restrict__ emap, int n_elem,
+    long long nnz, double *__restrict__ values) {
+    constexpr int NS = DIM == 3 ? 6 : 3;
+    constexpr int NLD = DIM * NP;
+    constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
+    constexpr int PER = (NENT + THREADS - 1) / THREADS;
+    __shared__ double sg[NQ][DIM][NP];
+    __shared__ double sD[NQ][NS * NS];
+    __shared__ double sH[NLD * NS];
+
+    const int tid = threadIdx.x;
+    // per-thread entry descriptors: alpha | beta << 8 (alpha, beta < 256), or -1
+    int code[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int id = tid + i * THREADS;
+        int c = -1;
+        if (id < NENT) {
+            int a, b;
+            if (SYM) {
+                // row-major upper triangle: row a holds NLD - a entries
+                int rem = id;
+                a = 0;
+                while (rem >= NLD - a) {
+                    rem -= NLD - a;
+                    ++a;
+                }
+                b = a + rem;
+            } else {
+                a = id / NLD;
+                b = id % NLD;
+            }
+            c = a | (b << 8);
+        }
+        code[i] = c;
+    }
+
+    for (int e = blockIdx.x; e < n_elem; e += gridDim.x) {
+        const long long g0 = (long long)e * NQ;
+        for (int i = tid; i < NQ * NP; i += THREADS) {
+            const int q = i / NP, a = i % NP;
+            sg[q][0][a] = d1[g0 * NP + i];
+            sg[q][1][a] = d2[g0 * NP + i];
+            if (DIM == 3) sg[q][DIM - 1][a] = d3[g0 * NP + i];
+        }
+        for (int i = tid; i < NQ * NS * NS; i += THREADS) {
+            const int q = i / (NS * NS), k = i % (NS * NS);
+            sD[q][k] = w[g0 + q] * DS[(g0 + q) * (NS * NS) + k];
+        }
+        double acc[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) acc[i] = 0.0;
+        __syncthreads();
+
+        for (int q = 0; q < NQ; ++q) {
+            for (int it = tid; it < NLD * NS; it += THREADS) {
+                const int alpha = it / NS, m = it % NS;
+                const int a = alpha / DIM, c = alpha % DIM;
+                double h = 0.0;
+#pragma unroll
+                for (int r = 0; r < DIM; ++r) {
+                    const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
+                    h += sg[q][r][a] * sD[q][k + NS * m];
+                }
+                sH[it] = h;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const int c = code[i];
+                if (c >= 0) {
+                    const int alpha = c & 0xff, beta = c >> 8;
+                    const int b = beta / DIM, cp = beta % DIM;
+                    double v = acc[i];
+#pragma unroll
+                    for (int r = 0; r < DIM; ++r) {
+                        const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
+                        v += sH[alpha * NS + m] * sg[q][r][b];
+                    }
+                    acc[i] = v;
+                }
+            }
+            __syncthreads();
+        }
+
+        const int32_t *em = emap + (long long)e * NLD * NLD;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int c = code[i];
+            if (c < 0) continue;
+            const int alpha = c & 0xff, beta = c >> 8;
+            const int32_t p = em[alpha * NLD + beta];
+            if (p >= 0) {
+                if (p < nnz) atomicAdd(values + p, acc[i]);
+                else flag(SSP_DEV_BAD_INDEX);
+            }
+            if (SYM && alpha != beta) {
+                const int32_t p2 = em[beta * NLD + alpha];
+                if (p2 >= 0) {
+                    if (p2 < nnz) atomicAdd(values + p2, acc[i]);
+                    else flag(SSP_DEV_BAD_INDEX);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- epilogue
+
+__global__ void set_positions_kernel(double *__restrict__ values, const int32_t *__restrict__ pos, int n, long long nnz,
+                                     double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t p = pos[i];
+    if (p < 0 || p >= nnz) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    values[p] = v;
+}
+
+__global__ void blend_kernel(double *__restrict__ values, const double *__restrict__ elastic, long long nnz, double r) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nnz) return;
+    values[i] = values[i] * (1.0 - r) + r * elastic[i];
+}
+
+__global__ void gather_rows_kernel(const double *__restrict__ src, const int32_t *__restrict__ idx, int n,
+                                   double *__restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[idx[i]];
+}
+
+// ---------------------------------------------------------------------------- dispatch
+
+template <int DIM, int NP, int NQ, int THREADS, bool SYM>
+int launch_element(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
+                   const int32_t *emap, int n_elem, long long nnz, double *values, cudaStream_t st) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tangent_element_kernel<DIM, NP, NQ, THREADS, SYM>, THREADS, 0);
+    if (per_sm < 1) per_sm = 1;
+    long long grid = (long long)sms * per_sm;
+    if (grid > n_elem) grid = n_elem;
+    tangent_element_kernel<DIM, NP, NQ, THREADS, SYM>
+        <<<static_cast<unsigned>(grid), THREADS, 0, st>>>(d1, d2, d3, DS, w, emap, n_elem, nnz, values);
+    return launch_status();
+}
+
+template <bool SYM>
+int dispatch_element(int dim, int n_p, int n_q, const double *d1, const double *d2, const double *d3, const double *DS,
+                     const double *w, const int32_t *emap, int n_elem, long long nnz, double *values, cudaStream_t st) {
+    if (dim == 3 && n_p == 10 && n_q == 11)
+        return launch_element<3, 10, 11, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+    if (dim == 3 && n_p == 35 && n_q == 24)
+        return launch_element<3, 35, 24, 256, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+    if (dim == 3 && n_p == 4 && n_q == 1)
+        return launch_element<3, 4, 1, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+    if (dim == 2 && n_p == 6 && n_q == 7)
+        return launch_element<2, 6, 7, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+    if (dim == 2 && n_p == 3 && n_q == 1)
+        return launch_element<2, 3, 1, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+    return SSP_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace ssp
+
+using namespace ssp;
+
+extern "C" {
+
+int ssp_geometry(int dim, const double *coord, const int64_t *elem, const double *dhat, const double *wf, int n_nodes,
+                 int n_elem, int n_p, int n_q, double *dphi1, double *dphi2, double *dphi3, double *weight,
+                 void *stream) {
+    if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || n_nodes < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!coord || !elem || !dhat || !wf || !dphi1 || !dphi2 || !weight || (dim == 3 && !dphi3)) return SSP_ERR_INVALID;
+    const long long n = (long long)n_elem * n_q;
+    if (dim == 3)
+        geometry_kernel<3><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(coord, elem, dhat, wf, n_nodes, n_elem, n_p,
+                                                                            n_q, dphi1, dphi2, dphi3, weight);
+    else
+        geometry_kernel<2><<<grid_for(n, 128), 128, 0, as_stream(stream)>>>(coord, elem, dhat, wf, n_nodes, n_elem, n_p,
+                                                                            n_q, dphi1, dphi2, nullptr, weight);
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_3d(const double *dphi1, const double *dphi2, const double *dphi3,
+                                   const double *u_overlap, int n_u, const int32_t *elem_dof_lids, int n_int,
+                                   int n_elem, int n_p, int n_q, double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || !dphi3 || !u_overlap || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    strain3_kernel<<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(dphi1, dphi2, dphi3, u_overlap, elem_dof_lids, n_u,
+                                                                        n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_2d(const double *dphi1, const double *dphi2, const double *u_overlap, int n_u,
+                                   const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                   double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || !u_overlap || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    strain2_kernel<<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(dphi1, dphi2, u_overlap, elem_dof_lids, n_u,
+                                                                        n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *stress,
+                               const double *weight, const int32_t *row_slot_ptr, const int32_t *slot_elem,
+                               const uint8_t *slot_lrow, int n_int, int n_rows, int n_slots, int n_p, int n_q,
+                               double *out_values, void *stream) {
+    (void)n_slots;
+    if (n_rows < 0 || n_p <= 0 || n_q <= 0 || n_int < 0 || n_int % n_q) return SSP_ERR_INVALID;
+    if (n_rows == 0) return SSP_OK;
+    if (!row_slot_ptr || !out_values) return SSP_ERR_INVALID;
+    force_rows3_kernel<<<grid_for(n_rows, 128), 128, 0, as_stream(stream)>>>(
+        dphi1, dphi2, dphi3, stress, weight, row_slot_ptr, slot_elem, slot_lrow, n_rows, n_int / n_q, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_element(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                               const double *stress, const double *weight, const int32_t *elem_row, int n_elem,
+                               int n_p, int n_q, int n_rows, double *out_values, void *stream) {
+    if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !stress || !weight || !elem_row) return SSP_ERR_INVALID;
+    const long long n = (long long)n_elem * dim * n_p;
+    if (dim == 3)
+        force_element_kernel<3><<<grid_for(n, 128), 128, 0, st>>>(dphi1, dphi2, dphi3, stress, weight, elem_row, n_rows,
+                                                                  n_elem, n_p, n_q, out_values);
+    else
+        force_element_kernel<2><<<grid_for(n, 128), 128, 0, st>>>(dphi1, dphi2, nullptr, stress, weight, elem_row, n_rows,
+                                                                  n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_tangent_values_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *ds,
+                                        const double *weight, const int32_t *row_slot_ptr, const int32_t *slot_elem,
+                                        const uint8_t *slot_lrow, const int32_t *slot_pos, int n_int, int n_rows,
+                                        int n_slots, int n_p, int n_q, int nnz_out, double *out_values, void *stream) {
+    (void)n_slots;
+    if (n_rows < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0 || n_int < 0 || n_int % n_q) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (nnz_out > 0) {
+        if (!out_values) return SSP_ERR_INVALID;
+        if (cudaMemsetAsync(out_values, 0, sizeof(double) * nnz_out, st) != cudaSuccess) return SSP_ERR_CUDA;
+    }
+    if (n_rows == 0) return SSP_OK;
+    if (!row_slot_ptr) return SSP_ERR_INVALID;
+    tangent_rows3_kernel<<<grid_for(n_rows, 64), 64, 0, st>>>(dphi1, dphi2, dphi3, ds, weight, row_slot_ptr, slot_elem,
+                                                              slot_lrow, slot_pos, n_rows, n_int / n_q, n_p, n_q, nnz_out,
+                                                              out_values);
+    return launch_status();
+}
+
+int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const double *dphi2, const double *dphi3,
+                        const double *ds, const double *weight, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
+                        long long nnz_out, double *out_values, int accumulate, void *stream) {
+    if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (nnz_out > 0 && !out_values) return SSP_ERR_INVALID;
+    if (!accumulate && nnz_out > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * nnz_out, st) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !scatter_map) return SSP_ERR_INVALID;
+    return symmetric ? dispatch_element<true>(dim, n_p, n_q, dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out,
+                                              out_values, st)
+                     : dispatch_element<false>(dim, n_p, n_q, dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out,
+                                               out_values, st);
+}
+
+int ssp_assemble_tangent_values_3d_p2(const double *dphi1, const double *dphi2, const double *dphi3, const double *ds,
+                                      const double *weight, const int32_t *scatter_map, int n_int, int n_elem, int n_p,
+                                      int n_q, int nnz_out, double *out_values, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || (long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    return ssp_tangent_element(3, 0, dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, n_p, n_q, nnz_out, out_values, 0,
+                               stream);
+}
+
+int ssp_finish_values(double *values, long long nnz, const int32_t *constrained_diag_positions, int n_diag,
+                      const double *elastic_values, double r, void *stream) {
+    if (nnz < 0 || n_diag < 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_diag > 0) {
+        if (!values || !constrained_diag_positions) return SSP_ERR_INVALID;
+        set_positions_kernel<<<grid_for(n_diag, 128), 128, 0, st>>>(values, constrained_diag_positions, n_diag, nnz, 1.0);
+    }
+    if (elastic_values && nnz > 0) {
+        if (!values) return SSP_ERR_INVALID;
+        blend_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(values, elastic_values, nnz, r);
+    }
+    return launch_status();
+}
+
+int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *stream) {
+    if (n < 0) return SSP_ERR_INVALID;
+    if (n == 0) return SSP_OK;
+    if (!src || !idx || !dst) return SSP_ERR_INVALID;
+    gather_rows_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(src, idx, n, dst);
+    return launch_status();
+}
+
+}  // extern "C"

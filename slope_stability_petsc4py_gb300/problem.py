@@ -1,0 +1,530 @@
+"""``ConstitutiveOperator``: the reference's constitutive builder, with the hot path on the GPU.
+
+Drop-in for ``src/slope_stability/constitutive/problem.py:1192-2210``.  Newton, damping and the
+continuation drivers talk to the builder only through the method names below (they probe them
+with ``getattr`` and ``owned_tangent_pattern is not None``, nonlinear/newton.py:290-336); every
+one of them is provided with the reference's semantics:
+
+* ``reduction(lam)`` -> Davis-reduced ``c_bar``/``sin_phi`` per local point (CUDA kernel);
+* ``constitutive_problem_stress(U)`` / ``constitutive_problem_stress_tangent(U)`` -> strain
+  kernel + return-mapping kernel; S and DS stay in HBM (``_owned_local_S``/``_owned_local_DS``
+  are ``DeviceArray`` views that convert to NumPy on demand);
+* ``build_F*`` -> owned internal force (element kernel), returned as NumPy like the reference;
+* ``build_K_regularized(r)`` / ``build_F_K_*`` -> tangent CSR values on the fixed pattern,
+  constrained diagonals, the regularised blend, and an in-place update of one stable matrix
+  object (a PETSc AIJ matrix when petsc4py is importable, otherwise ``OwnedCSRMatrix``);
+* ``get_total_time()`` with the reference's keys, ``release_petsc_caches()``,
+  ``set_owned_tangent_pattern(...)``.
+
+Only the owned-pattern path exists (it is the reference's production path).  An operator without
+a pattern raises on the first hot-path call; ``ConstitutiveOperator.from_mesh`` builds one with
+the whole mesh owned.  Constitutive modes ``overlap``, ``unique_gather`` and ``unique_exchange``
+coincide on one device (they differ only in MPI traffic) and all run the overlap kernels.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from time import perf_counter
+from typing import Any
+
+import numpy as np
+from scipy.sparse import csr_matrix
+
+from . import _lib
+from .arrays import DeviceArray
+from .distributed_tangent import (
+    DEFAULT_TANGENT_KERNEL,
+    OwnedTangentPattern,
+    _normalize_tangent_kernel,
+    overlap_strain_device,
+    owned_force_device,
+    prepare_owned_tangent_pattern,
+    tangent_values_device,
+)
+
+try:  # pragma: no cover - PETSc is absent in most environments of this package
+    from petsc4py import PETSc
+except Exception:  # pragma: no cover
+    PETSc = None
+
+_OWNED_MODES = {"overlap", "unique_exchange", "unique", "unique_gather", "no_overlap", "partitioned"}
+
+
+class OwnedCSRMatrix:
+    """Owned-row CSR matrix on the fixed pattern, updated in place (stable ``handle``).
+
+    ``values`` is the CUDA tensor the kernels write; ``data`` is a pinned host mirror refreshed by
+    ``sync_host()`` (what a PETSc ``setValuesCSR`` would read, utils.py:288-306)."""
+
+    _next_handle = 1
+
+    def __init__(self, pattern: OwnedTangentPattern, values):
+        self.indptr = np.asarray(pattern.local_matrix_pattern.indptr, dtype=np.int32)
+        self.indices = np.asarray(pattern.local_matrix_pattern.indices, dtype=np.int32)
+        self.shape = pattern.local_matrix_pattern.shape
+        self.values = values
+        t = _lib.torch()
+        self._host = t.empty(values.numel(), dtype=t.float64, pin_memory=True)
+        self.data = self._host.numpy()
+        self.handle = OwnedCSRMatrix._next_handle
+        OwnedCSRMatrix._next_handle += 1
+
+    def sync_host(self, stream=None):
+        self._host.copy_(self.values, non_blocking=True)
+        return self
+
+    def getValuesCSR(self):
+        _lib.torch().cuda.current_stream().synchronize()
+        return self.indptr, self.indices, self.data
+
+    def to_scipy(self) -> csr_matrix:
+        _lib.torch().cuda.current_stream().synchronize()
+        return csr_matrix((self.data.copy(), self.indices.copy(), self.indptr.copy()), shape=self.shape)
+
+    def destroy(self):
+        self.values = None
+
+
+@dataclass
+class ConstitutiveOperator:
+    B: Any
+    c0: np.ndarray
+    phi: np.ndarray
+    psi: np.ndarray
+    Davis_type: str
+    shear: np.ndarray
+    bulk: np.ndarray
+    lame: np.ndarray
+    WEIGHT: np.ndarray
+    n_strain: int
+    n_int: int
+    dim: int
+    q_mask: np.ndarray | None = None
+
+    def __post_init__(self):
+        for name in ("c0", "phi", "psi", "shear", "bulk", "lame", "WEIGHT"):
+            setattr(self, name, np.asarray(getattr(self, name), dtype=np.float64))
+        self.q_mask = None if self.q_mask is None else np.asarray(self.q_mask, dtype=bool)
+        self.S = None
+        self.DS = None
+        self.c_bar = None
+        self.sin_phi = None
+        self.time_reduction = []
+        self.time_stress = []
+        self.time_stress_tangent = []
+        self.time_build_F = []
+        self.time_build_F_K_tangent = []
+        self.time_potential = []
+        self.time_build_tangent_local = []
+        self.time_local_strain = []
+        self.time_local_constitutive = []
+        self.time_local_constitutive_comm = []
+        self.time_local_force_assembly = []
+        self.time_local_force_gather = []
+        self.owned_tangent_pattern: OwnedTangentPattern | None = None
+        self.bddc_subdomain_pattern = None
+        self.use_compiled_owned_tangent = True
+        self.owned_tangent_kernel = DEFAULT_TANGENT_KERNEL
+        self.use_compiled_owned_constitutive = True
+        self.owned_constitutive_mode = "global"
+        # host (True) or device-resident (False) hand-off of F and K values
+        self.host_outputs = True
+        # list to collect (start, end) CUDA events around each tangent-kernel launch, or None
+        self.tangent_events = None
+        self._S_aos = None
+        self._DS_aos = None
+        self._ds_symmetric = False
+        self._owned_overlap_c_bar = None
+        self._owned_overlap_sin_phi = None
+        self._owned_unique_c_bar = None
+        self._owned_unique_sin_phi = None
+        self._dev_mat = None
+        self._owned_tangent_mat = None
+        self._owned_regularized_mat = None
+        self._tangent_values = None
+        self._regularized_values = None
+        self._force = None
+
+    # -------------------------------------------------------------------- construction
+
+    @classmethod
+    def from_mesh(cls, coord, elem, q_mask, material_identifier, materials, *, elem_type="P2", Davis_type="B",
+                  tangent_kernel=DEFAULT_TANGENT_KERNEL):
+        """Operator plus an owned pattern covering the whole mesh (one device owns every row)."""
+        from .materials import heterogenous_materials
+
+        coord = np.asarray(coord, dtype=np.float64)
+        elem = np.asarray(elem, dtype=np.int64)
+        pat = prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, materials, (0, coord.shape[1]),
+                                            elem_type=elem_type, include_legacy_scatter=False, keep_slot_metadata=False)
+        n_int = elem.shape[1] * pat.n_q
+        c0, phi, psi, shear, bulk, lame, _g = heterogenous_materials(material_identifier, np.ones(n_int, bool), pat.n_q,
+                                                                     materials)
+        op = cls(B=None, c0=c0, phi=phi, psi=psi, Davis_type=Davis_type, shear=shear, bulk=bulk, lame=lame,
+                 WEIGHT=np.zeros(0), n_strain=pat.n_strain, n_int=n_int, dim=pat.dim, q_mask=q_mask)
+        op.set_owned_tangent_pattern(pat, tangent_kernel=tangent_kernel, constitutive_mode="overlap")
+        return op
+
+    def set_owned_tangent_pattern(self, pattern, *, use_compiled=True, tangent_kernel=DEFAULT_TANGENT_KERNEL,
+                                  constitutive_mode="global", use_compiled_constitutive=True) -> None:
+        self.owned_tangent_pattern = pattern
+        self.use_compiled_owned_tangent = bool(use_compiled)
+        self.owned_tangent_kernel = _normalize_tangent_kernel(tangent_kernel)
+        self.use_compiled_owned_constitutive = bool(use_compiled_constitutive)
+        self.owned_constitutive_mode = str(constitutive_mode).lower()
+        self.release_petsc_caches()
+        self._dev = None
+        if pattern is not None:
+            t = _lib.require_cuda()
+            idx = np.asarray(pattern.local_int_indices, dtype=np.int64)
+            pick = lambda a: _lib.to_device(np.ascontiguousarray(np.asarray(a, dtype=np.float64)[idx]), t.float64)  # noqa
+            self._dev = {k: pick(getattr(self, k)) for k in ("c0", "phi", "psi", "shear", "bulk", "lame")}
+
+    def set_bddc_subdomain_pattern(self, pattern) -> None:
+        raise NotImplementedError("BDDC subdomain assembly is outside the GPU hot path")
+
+    # -------------------------------------------------------------------- state views
+
+    def _require_pattern(self) -> OwnedTangentPattern:
+        if self.owned_tangent_pattern is None:
+            raise RuntimeError("The GPU constitutive operator runs on an owned tangent pattern; call "
+                               "set_owned_tangent_pattern() or build it with ConstitutiveOperator.from_mesh()")
+        return self.owned_tangent_pattern
+
+    def _use_owned_constitutive(self) -> bool:
+        return self.owned_tangent_pattern is not None and str(self.owned_constitutive_mode).lower() != "global"
+
+    @property
+    def _owned_local_S(self):
+        return None if self._S_aos is None else DeviceArray(self._S_aos)
+
+    @_owned_local_S.setter
+    def _owned_local_S(self, value):
+        self._S_aos = self._ingest_field(value, self.n_strain)
+
+    @property
+    def _owned_local_DS(self):
+        return None if self._DS_aos is None else DeviceArray(self._DS_aos)
+
+    @_owned_local_DS.setter
+    def _owned_local_DS(self, value):
+        self._DS_aos = self._ingest_field(value, self.n_strain * self.n_strain)
+        self._ds_symmetric = False  # a caller-provided tangent is not known to be symmetric
+
+    def _ingest_field(self, value, rows):
+        if value is None:
+            return None
+        if isinstance(value, DeviceArray):
+            return value.aos
+        t = _lib.require_cuda()
+        if isinstance(value, t.Tensor):
+            return value.to(t.float64).cuda().T.contiguous()
+        arr = np.asarray(value, dtype=np.float64)
+        if arr.ndim != 2 or arr.shape[0] != rows:
+            raise ValueError(f"expected a ({rows}, n_int) field")
+        return _lib.to_device(np.ascontiguousarray(arr.T), t.float64)
+
+    def _clear_owned_local_cache(self):
+        self._S_aos = None
+        self._DS_aos = None
+        self._ds_symmetric = False
+
+    # -------------------------------------------------------------------- hot path
+
+    def reduction(self, lam: float):
+        t0 = perf_counter()
+        pat = self._require_pattern()
+        t = _lib.require_cuda()
+        if not (float(lam) > 0.0):
+            raise ValueError("Reduction parameter lambda must be positive")
+        davis = str(self.Davis_type).upper()
+        if davis not in ("A", "B", "C"):
+            raise ValueError("Incorrect choice of the Davis approach")
+        n = pat.n_local_int
+        cb = t.empty(n, dtype=t.float64, device="cuda")
+        sp = t.empty(n, dtype=t.float64, device="cuda")
+        d = self._dev
+        _lib.call("ssp_reduction", _lib.ptr(d["c0"]), _lib.ptr(d["phi"]), _lib.ptr(d["psi"]), n, float(lam),
+                  davis.encode(), _lib.ptr(cb), _lib.ptr(sp), _lib.stream_handle())
+        self._owned_overlap_c_bar, self._owned_overlap_sin_phi = cb, sp
+        self._owned_unique_c_bar, self._owned_unique_sin_phi = cb, sp
+        self.c_bar = None
+        self.sin_phi = None
+        self.time_reduction.append(perf_counter() - t0)
+
+    def _evaluate(self, U, *, tangent: bool):
+        pat = self._require_pattern()
+        if self._owned_overlap_c_bar is None:
+            raise ValueError("Material reduction not set. Call reduction(lambda) first.")
+        mode = str(self.owned_constitutive_mode).lower()
+        if mode != "global" and mode not in _OWNED_MODES:
+            raise ValueError(f"Unsupported owned constitutive mode {self.owned_constitutive_mode!r}")
+        t = _lib.require_cuda()
+        t0 = perf_counter()
+        E = overlap_strain_device(pat, U)
+        self.time_local_strain.append(perf_counter() - t0)
+        t1 = perf_counter()
+        n = pat.n_local_int
+        d = self._dev
+        S = t.empty((n, 6 if pat.dim == 3 else 4), dtype=t.float64, device="cuda")
+        DS = t.empty((n, self.n_strain * self.n_strain), dtype=t.float64, device="cuda") if tangent else None
+        st = _lib.stream_handle()
+        args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
+                _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
+        if pat.dim == 3:
+            if tangent:
+                _lib.call("ssp_constitutive_3d_sds", *args, _lib.ptr(S), _lib.ptr(DS), st)
+            else:
+                _lib.call("ssp_constitutive_3d_s", *args, _lib.ptr(S), st)
+        else:
+            _lib.call("ssp_constitutive_2d", *args, _lib.ptr(S), _lib.ptr(DS) if tangent else None, st)
+        self.time_local_constitutive.append(perf_counter() - t1)
+        self._S_aos = S
+        self._DS_aos = DS
+        self._ds_symmetric = bool(tangent)
+        self.S = None
+        self.DS = None
+
+    def constitutive_problem_stress(self, U):
+        t0 = perf_counter()
+        self._evaluate(U, tangent=False)
+        self.time_stress.append(perf_counter() - t0)
+        return self._owned_local_S
+
+    def constitutive_problem_stress_tangent(self, U):
+        t0 = perf_counter()
+        self._evaluate(U, tangent=True)
+        self.time_stress_tangent.append(perf_counter() - t0)
+        return self._owned_local_S
+
+    def _force_device(self):
+        pat = self._require_pattern()
+        if self._S_aos is None:
+            raise ValueError("Stress tensor not computed")
+        t0 = perf_counter()
+        S = self._S_aos[:, : self.n_strain].contiguous() if self._S_aos.shape[1] != self.n_strain else self._S_aos
+        F = owned_force_device(pat, S)
+        self.time_local_force_assembly.append(perf_counter() - t0)
+        return F
+
+    def _to_host(self, x):
+        return x.cpu().numpy() if self.host_outputs else x
+
+    def build_F_local(self):
+        t0 = perf_counter()
+        out = self._to_host(self._force_device())
+        self.time_build_F.append(perf_counter() - t0)
+        return out
+
+    def build_F_free_local(self):
+        t0 = perf_counter()
+        F = self._force_device()
+        t = _lib.torch()
+        idx = self.owned_tangent_pattern.device["owned_free_rows"]
+        free = t.empty(idx.numel(), dtype=t.float64, device="cuda")
+        _lib.call("ssp_gather", _lib.ptr(F), _lib.ptr(idx), int(idx.numel()), _lib.ptr(free), _lib.stream_handle())
+        out = self._to_host(free)
+        self.time_build_F.append(perf_counter() - t0)
+        return out
+
+    def _single_rank_check(self):
+        pat = self._require_pattern()
+        if pat.owned_row_range != (0, int(pat.local_matrix_pattern.shape[1])):
+            raise RuntimeError("Global force gathering needs every row owned by this device (one-GPU operator)")
+        return pat
+
+    def build_F(self):
+        pat = self._single_rank_check()
+        t0 = perf_counter()
+        F = self._force_device()
+        self.time_local_force_gather.append(0.0)
+        out = F.cpu().numpy().reshape(self.dim, -1, order="F") if self.host_outputs else F.reshape(-1, self.dim).T
+        self.time_build_F.append(perf_counter() - t0)
+        return out
+
+    def build_F_free(self):
+        self._single_rank_check()
+        return self.build_F_free_local()
+
+    def _tangent_into(self, values, r=None):
+        pat = self._require_pattern()
+        if self._DS_aos is None:
+            raise ValueError("Tangent DS not computed")
+        t0 = perf_counter()
+        ev = self.tangent_events
+        if ev is not None:  # optional CUDA-event bracket of the tangent kernel (measurement)
+            t = _lib.torch()
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            e0.record()
+        tangent_values_device(pat, self._DS_aos, kernel=self.owned_tangent_kernel, symmetric=self._ds_symmetric,
+                              out=values)
+        if ev is not None:
+            e1.record()
+            ev.append((e0, e1))
+        if r is not None:
+            _lib.call("ssp_finish_values", _lib.ptr(values), pat.nnz, None, 0, _lib.ptr(pat.device["elastic_values"]),
+                      float(r), _lib.stream_handle())
+        self.time_build_tangent_local.append(perf_counter() - t0)
+
+    def _matrix(self, which: str, values):
+        pat = self._require_pattern()
+        attr = "_owned_tangent_mat" if which == "tangent" else "_owned_regularized_mat"
+        mat = getattr(self, attr)
+        if PETSc is not None and self.host_outputs:  # pragma: no cover - needs petsc4py
+            vals = values.cpu().numpy()
+            lp = pat.local_matrix_pattern
+            if mat is None:
+                n_glob = int(lp.shape[1])
+                mat = PETSc.Mat().createAIJ(size=((lp.shape[0], n_glob), (lp.shape[0], n_glob)),
+                                            csr=(lp.indptr.astype(PETSc.IntType), lp.indices.astype(PETSc.IntType), vals))
+                mat.setBlockSize(self.dim)
+                mat.assemble()
+            else:
+                mat.setValuesCSR(lp.indptr.astype(PETSc.IntType), lp.indices.astype(PETSc.IntType), vals)
+                mat.assemble()
+        else:
+            if mat is None:
+                mat = OwnedCSRMatrix(pat, values)
+            if self.host_outputs:
+                mat.sync_host()
+        setattr(self, attr, mat)
+        return mat
+
+    def _build_owned_tangent_matrix(self):
+        t = _lib.require_cuda()
+        pat = self._require_pattern()
+        if self._tangent_values is None:
+            self._tangent_values = t.empty(pat.nnz, dtype=t.float64, device="cuda")
+        self._tangent_into(self._tangent_values)
+        return self._matrix("tangent", self._tangent_values)
+
+    def _build_owned_regularized_matrix(self, r: float):
+        t = _lib.require_cuda()
+        pat = self._require_pattern()
+        if self._regularized_values is None:
+            self._regularized_values = t.empty(pat.nnz, dtype=t.float64, device="cuda")
+        self._tangent_into(self._regularized_values, r=r)
+        return self._matrix("regularized", self._regularized_values)
+
+    def build_K_regularized(self, r: float):
+        if self.owned_tangent_pattern is None:
+            raise RuntimeError("Regularized in-place matrix path requires owned_tangent_pattern")
+        return self._build_owned_regularized_matrix(r)
+
+    def build_F_K_tangent(self):
+        if self._DS_aos is None:
+            raise ValueError("Tangent DS not computed")
+        t0 = perf_counter()
+        F = self.build_F()
+        K = self._build_owned_tangent_matrix()
+        self.time_build_F_K_tangent.append(perf_counter() - t0)
+        return F, K
+
+    # composite entry points (problem.py:2030-2146)
+    def build_F_all(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress(U)
+        return self.build_F()
+
+    def build_F_all_local(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress(U)
+        return self.build_F_local()
+
+    def build_F_all_free(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress(U)
+        return self.build_F_free()
+
+    def build_F_all_free_local(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress(U)
+        return self.build_F_free_local()
+
+    def build_F_K_tangent_all(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress_tangent(U)
+        return self.build_F_K_tangent()
+
+    def build_F_K_tangent_all_free(self, lam, U):
+        self.reduction(lam)
+        self.constitutive_problem_stress_tangent(U)
+        return self.build_F_free(), self._build_owned_tangent_matrix()
+
+    def build_F_reduced(self, U):
+        self.constitutive_problem_stress(U)
+        return self.build_F()
+
+    def build_F_reduced_local(self, U):
+        self.constitutive_problem_stress(U)
+        return self.build_F_local()
+
+    def build_F_reduced_free(self, U):
+        self.constitutive_problem_stress(U)
+        return self.build_F_free()
+
+    def build_F_reduced_free_local(self, U):
+        self.constitutive_problem_stress(U)
+        return self.build_F_free_local()
+
+    def build_F_K_tangent_reduced(self, U):
+        self.constitutive_problem_stress_tangent(U)
+        return self.build_F_K_tangent()
+
+    def build_F_K_tangent_reduced_free(self, U):
+        self.constitutive_problem_stress_tangent(U)
+        return self.build_F_free(), self._build_owned_tangent_matrix()
+
+    def _regularized_pair(self, F_fn, r):
+        t0 = perf_counter()
+        F = F_fn()
+        K = self.build_K_regularized(r)
+        self.time_build_F_K_tangent.append(perf_counter() - t0)
+        return F, K
+
+    def build_F_K_regularized_all(self, lam, U, r):
+        self.reduction(lam)
+        self.constitutive_problem_stress_tangent(U)
+        return self._regularized_pair(self.build_F, r)
+
+    def build_F_K_regularized_all_free(self, lam, U, r):
+        self.reduction(lam)
+        self.constitutive_problem_stress_tangent(U)
+        return self._regularized_pair(self.build_F_free, r)
+
+    def build_F_K_regularized_reduced(self, U, r):
+        self.constitutive_problem_stress_tangent(U)
+        return self._regularized_pair(self.build_F, r)
+
+    def build_F_K_regularized_reduced_free(self, U, r):
+        self.constitutive_problem_stress_tangent(U)
+        return self._regularized_pair(self.build_F_free, r)
+
+    def potential_energy(self, U):  # pragma: no cover - not on the Newton hot path
+        raise NotImplementedError("potential_energy is not part of the GPU hot path (the line search does not call it)")
+
+    def get_total_time(self):
+        return {
+            "reduction": sum(self.time_reduction),
+            "stress": sum(self.time_stress),
+            "stress_tangent": sum(self.time_stress_tangent),
+            "build_F": sum(self.time_build_F),
+            "build_F_K_tangent": sum(self.time_build_F_K_tangent),
+            "build_tangent_local": sum(self.time_build_tangent_local),
+            "local_strain": sum(self.time_local_strain),
+            "local_constitutive": sum(self.time_local_constitutive),
+            "local_constitutive_comm": sum(self.time_local_constitutive_comm),
+            "local_force_assembly": sum(self.time_local_force_assembly),
+            "local_force_gather": sum(self.time_local_force_gather),
+            "potential": sum(self.time_potential),
+        }
+
+    def release_petsc_caches(self) -> None:
+        for attr in ("_owned_tangent_mat", "_owned_regularized_mat"):
+            mat = getattr(self, attr, None)
+            if mat is not None and hasattr(mat, "destroy"):
+                mat.destroy()
+            setattr(self, attr, None)
+        self._tangent_values = None
+        self._regularized_values = None

@@ -1,0 +1,363 @@
+"""Parity of the CUDA hot path with the reference (golden fixtures) and with the oracle.
+
+Every comparison is a max-norm relative error at the plain-path tolerance (1e-12) unless stated;
+CSR indices and maps are compared bit for bit.  All calls go through the C ABI (directly or via
+the package's drop-in functions, which are thin ctypes wrappers)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import PLAIN_RTOL, golden, golden_files, rel_err
+
+pytestmark = pytest.mark.gpu
+
+MATERIAL = {"c0": 15.0, "phi": 30.0, "psi": 0.0, "young": 10000.0, "poisson": 0.33, "gamma_sat": 19.0,
+            "gamma_unsat": 19.0}
+
+
+@pytest.fixture(autouse=True)
+def _clean_status(cuda_device):
+    from slope_stability_petsc4py_gb300 import _lib
+
+    _lib.device_status(clear=True)
+    yield
+    assert _lib.device_status(clear=True) == 0
+
+
+def _dev(a, dtype=None):
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    return _lib.to_device(np.ascontiguousarray(a), dtype or torch.float64)
+
+
+def _constitutive(E, args, tangent=True, kernel="ssp_constitutive_3d_sds"):
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    n = E.shape[0]
+    Ed = _dev(E)
+    A = [_dev(a) for a in args]
+    S = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+    if tangent:
+        DS = torch.empty((n, 36), dtype=torch.float64, device="cuda")
+        _lib.call(kernel, _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.ptr(DS), _lib.stream_handle())
+        return S.cpu().numpy(), DS.cpu().numpy()
+    _lib.call("ssp_constitutive_3d_s", _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.stream_handle())
+    return S.cpu().numpy()
+
+
+def test_constitutive_3d_matches_reference_c_kernel():
+    g = golden("constitutive_3d.npz")
+    for tag in ("bench_l1.0", "bench_l1.3", "test_l1.0", "test_l1.3"):
+        args = [g[f"{tag}_{k}"] for k in ("c_bar", "sin_phi", "shear", "bulk", "lame")]
+        S, DS = _constitutive(g["E"], args)
+        assert rel_err(S, g[f"{tag}_S_c"]) <= PLAIN_RTOL
+        assert rel_err(DS, g[f"{tag}_DS_c"]) <= PLAIN_RTOL
+        # the stress-only kernel yields the same stresses bit for bit
+        assert np.array_equal(_constitutive(g["E"], args, tangent=False), S)
+        # the tangent is exactly symmetric
+        D = DS.reshape(-1, 6, 6)
+        assert np.array_equal(D, np.transpose(D, (0, 2, 1)))
+
+
+def test_constitutive_3d_matches_oracle_on_many_points(oracle):
+    rng = np.random.default_rng(2024)
+    n = 200_000
+    E = rng.standard_normal((n, 6)) * np.repeat(np.array([1e-4, 1e-3, 3e-3, 1e-2]), n // 4)[:, None]
+    young, nu = 2.0e4, 0.49
+    shear = np.full(n, young / (2 * (1 + nu)))
+    bulk = np.full(n, young / (3 * (1 - 2 * nu)))
+    lame = bulk - 2 * shear / 3
+    c_bar, sin_phi = oracle.reduction(np.full(n, 6.0), np.full(n, np.deg2rad(45.0)), np.zeros(n), 1.1, "B")
+    args = [c_bar, sin_phi, shear, bulk, lame]
+    S, DS = _constitutive(E, args)
+    S_o, DS_o = oracle.constitutive_3d(E, *args)
+    assert rel_err(S, S_o) <= PLAIN_RTOL
+    assert rel_err(DS, DS_o) <= PLAIN_RTOL
+
+
+def test_branch_labels_match_tangent_structure():
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    g = golden("constitutive_3d.npz")
+    tag = "bench_l1.0"
+    args = [g[f"{tag}_{k}"] for k in ("c_bar", "sin_phi", "shear", "lame")]
+    n = g["E"].shape[0]
+    Ed = _dev(g["E"])
+    A = [_dev(a) for a in args]
+    S = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+    br = torch.empty(n, dtype=torch.int8, device="cuda")
+    _lib.call("ssp_constitutive_3d_branch", _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.ptr(br),
+              _lib.stream_handle())
+    b = br.cpu().numpy()
+    DS = g[f"{tag}_DS_c"].reshape(-1, 6, 6)
+    assert set(np.unique(b)) <= {0, 1, 2, 3, 4}
+    assert np.all(np.abs(DS[b == 4]).max(initial=0.0) == 0.0)  # apex: zero tangent
+    assert np.allclose(DS[b == 0][:, 0, 1], g[f"{tag}_lame"][b == 0])  # elastic: lame off-diagonal
+    assert rel_err(S.cpu().numpy(), g[f"{tag}_S_c"]) <= PLAIN_RTOL
+
+
+def test_constitutive_2d_matches_reference_numpy():
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    g = golden("constitutive_2d.npz")
+    for tag in ("l1.0", "l1.2"):
+        n = g["E"].shape[1]
+        Ed = _dev(g["E"].T)
+        A = [_dev(g[f"{tag}_{k}"]) for k in ("c_bar", "sin_phi", "shear", "bulk", "lame")]
+        S = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+        DS = torch.empty((n, 9), dtype=torch.float64, device="cuda")
+        _lib.call("ssp_constitutive_2d", _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.ptr(DS),
+                  _lib.stream_handle())
+        assert rel_err(S.cpu().numpy().T, g[f"{tag}_S"]) <= PLAIN_RTOL
+        assert rel_err(DS.cpu().numpy().T, g[f"{tag}_DS"]) <= PLAIN_RTOL
+
+
+def test_reduction_matches_reference():
+    from slope_stability_petsc4py_gb300 import reduction
+
+    g = golden("reduction.npz")
+    for dav in ("A", "B", "C"):
+        for lam in (0.8, 1.0, 1.35):
+            cb, sp = reduction(g["c0"], g["phi"], g["psi"], lam, dav)
+            assert rel_err(cb, g[f"{dav}_{lam}_c_bar"]) <= 1e-14
+            assert rel_err(sp, g[f"{dav}_{lam}_sin_phi"]) <= 1e-14
+    with pytest.raises(ValueError):
+        reduction(g["c0"], g["phi"], g["psi"], -1.0, "A")
+
+
+def _pattern(g, **kw):
+    from slope_stability_petsc4py_gb300 import prepare_owned_tangent_pattern
+
+    return prepare_owned_tangent_pattern(g["coord"], g["elem"], g["q_mask"], np.zeros(g["elem"].shape[1], np.int64),
+                                         [MATERIAL] if g["coord"].shape[0] == 3 else [dict(MATERIAL, c0=6.0, phi=45.0,
+                                                                                           young=2.0e4, poisson=0.49,
+                                                                                           gamma_sat=20.0,
+                                                                                           gamma_unsat=20.0)],
+                                         tuple(int(v) for v in g["owned_node_range"]), elem_type=str(g["elem_type"]), **kw)
+
+
+@pytest.mark.parametrize("name", golden_files("pattern_"))
+def test_pattern_geometry_and_elastic_values(name):
+    g = golden(name)
+    pat = _pattern(g)
+    assert np.array_equal(pat.local_matrix_pattern.indptr, g["indptr"])
+    assert np.array_equal(pat.local_matrix_pattern.indices, g["indices"])
+    assert np.array_equal(pat.scatter_map, g["scatter_map"])
+    assert np.array_equal(pat.slot_pos, g["slot_pos"])
+    assert np.array_equal(pat.constrained_diag_positions, g["constrained_diag_positions"])
+    assert rel_err(pat.dphi1, g["dphi1"]) <= PLAIN_RTOL
+    assert rel_err(pat.dphi2, g["dphi2"]) <= PLAIN_RTOL
+    assert rel_err(pat.dphi3, g["dphi3"]) <= PLAIN_RTOL
+    assert rel_err(pat.overlap_assembly_weight, g["weight"]) <= PLAIN_RTOL
+    assert rel_err(pat.elastic_values, g["elastic_values"]) <= PLAIN_RTOL
+    assert np.all(pat.elastic_values[pat.constrained_diag_positions] == 1.0)
+
+
+@pytest.mark.parametrize("name", golden_files("pattern_"))
+def test_assembly_matches_reference(name):
+    from slope_stability_petsc4py_gb300 import (assemble_overlap_strain, assemble_owned_force_from_local_stress,
+                                                assemble_owned_tangent_values)
+
+    g = golden(name)
+    pat = _pattern(g)
+    for kernel in ("rows", "legacy", "rows_gather"):
+        vals = assemble_owned_tangent_values(pat, g["ds"], kernel=kernel)
+        assert rel_err(vals, g["rows_c"]) <= PLAIN_RTOL, kernel
+        assert np.all(vals[pat.constrained_diag_positions] == 1.0)
+    assert rel_err(assemble_overlap_strain(pat, g["U"]), g["strain_c"]) <= PLAIN_RTOL
+    assert rel_err(assemble_owned_force_from_local_stress(pat, g["stress"]), g["force_c"]) <= PLAIN_RTOL
+
+
+@pytest.mark.parametrize("name", golden_files("pattern_"))
+def test_symmetric_tangent_kernel(name, oracle):
+    import torch
+
+    from slope_stability_petsc4py_gb300.distributed_tangent import tangent_values_device
+
+    g = golden(name)
+    pat = _pattern(g)
+    ds = g["ds"].T.reshape(-1, 6, 6)
+    ds = 0.5 * (ds + np.transpose(ds, (0, 2, 1)))
+    ds_aos = np.ascontiguousarray(ds.reshape(-1, 36))
+    want = oracle.tangent_scatter(3, g["dphi1"], g["dphi2"], g["dphi3"], ds_aos, g["weight"], g["scatter_map"],
+                                  int(g["n_q"]), pat.nnz)
+    want[pat.constrained_diag_positions] = 1.0
+    got_sym = tangent_values_device(pat, _dev(ds_aos), symmetric=True).cpu().numpy()
+    got_gen = tangent_values_device(pat, _dev(ds_aos), symmetric=False).cpu().numpy()
+    assert rel_err(got_sym, want) <= PLAIN_RTOL
+    assert rel_err(got_gen, want) <= PLAIN_RTOL
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("name", golden_files("pattern_"))
+def test_constitutive_operator_matches_reference(name):
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator
+
+    g = golden(name)
+    pat = _pattern(g)
+    n_int = g["mat_c0"].size
+    op = ConstitutiveOperator(B=None, c0=g["mat_c0"], phi=g["mat_phi"], psi=g["mat_psi"], Davis_type="B",
+                              shear=g["mat_shear"], bulk=g["mat_bulk"], lame=g["mat_lame"], WEIGHT=np.ones(n_int),
+                              n_strain=6, n_int=n_int, dim=3, q_mask=g["q_mask"])
+    op.set_owned_tangent_pattern(pat, tangent_kernel="rows", constitutive_mode="overlap")
+    op.reduction(float(g["op_lambda"]))
+    S = op.constitutive_problem_stress_tangent(g["op_U"])
+    assert S.shape == g["op_S"].shape
+    assert rel_err(np.asarray(S), g["op_S"]) <= PLAIN_RTOL
+    assert rel_err(np.asarray(op._owned_local_DS), g["op_DS"]) <= PLAIN_RTOL
+    assert rel_err(op.build_F_local(), g["op_F"]) <= PLAIN_RTOL
+    assert rel_err(op.build_F_free_local(), g["op_F_free"]) <= PLAIN_RTOL
+    K = op._build_owned_tangent_matrix()
+    _, _, kv = K.getValuesCSR()
+    assert rel_err(kv, g["op_K"]) <= PLAIN_RTOL
+    Kr = op.build_K_regularized(float(g["op_r"]))
+    _, cols, kr = Kr.getValuesCSR()
+    assert np.array_equal(cols, g["indices"])
+    assert rel_err(kr, g["op_Kr"]) <= PLAIN_RTOL
+    h1 = Kr.handle
+    assert op.build_K_regularized(float(g["op_r"])).handle == h1  # in-place update, stable handle
+    S_only = op.constitutive_problem_stress(g["op_U"])
+    assert rel_err(np.asarray(S_only), g["op_S_only"]) <= PLAIN_RTOL
+    assert set(op.get_total_time()) >= {"reduction", "stress", "stress_tangent", "build_F", "build_tangent_local"}
+
+
+def test_operator_accepts_caller_tangent_like_reference():
+    """A caller may assign _owned_local_DS directly (tests/test_distributed_tangent_rows.py:308-321)."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, assemble_owned_tangent_matrix
+
+    g = golden("pattern_tet2_P2.npz")
+    pat = _pattern(g)
+    n_int = pat.n_local_int
+    op = ConstitutiveOperator(B=None, c0=np.zeros(n_int), phi=np.zeros(n_int), psi=np.zeros(n_int), Davis_type="B",
+                              shear=np.ones(n_int), bulk=np.ones(n_int), lame=np.ones(n_int), WEIGHT=np.ones(n_int),
+                              n_strain=6, n_int=n_int, dim=3, q_mask=g["q_mask"])
+    op.set_owned_tangent_pattern(pat, tangent_kernel="rows", constitutive_mode="overlap")
+    rng = np.random.default_rng(404)
+    ds1, ds2 = rng.standard_normal((36, n_int)), rng.standard_normal((36, n_int))
+    op._owned_local_DS = ds1
+    m1 = op._build_owned_tangent_matrix()
+    op._owned_local_DS = ds2
+    m2 = op._build_owned_tangent_matrix()
+    assert m1.handle == m2.handle
+    rows, cols, vals = m2.getValuesCSR()
+    ref = assemble_owned_tangent_matrix(pat, ds2)
+    assert np.array_equal(rows, ref.indptr) and np.array_equal(cols, ref.indices)
+    assert rel_err(vals, ref.data) <= 1e-11
+
+
+@pytest.mark.parametrize("name", golden_files("pattern2d_"))
+def test_2d_assembly_matches_reference(name, oracle):
+    from slope_stability_petsc4py_gb300 import (assemble_overlap_strain, assemble_owned_force_from_local_stress,
+                                                assemble_owned_tangent_values)
+
+    g = golden(name)
+    pat = _pattern(g)
+    assert np.array_equal(pat.scatter_map, g["scatter_map"])
+    assert rel_err(pat.dphi1, g["dphi1"]) <= PLAIN_RTOL
+    assert rel_err(pat.elastic_values, g["elastic_values"]) <= PLAIN_RTOL
+    assert rel_err(assemble_owned_tangent_values(pat, g["ds"], kernel="legacy"), g["legacy_py"]) <= PLAIN_RTOL
+    assert rel_err(assemble_overlap_strain(pat, g["U"]), g["strain_py"]) <= PLAIN_RTOL
+    assert rel_err(assemble_owned_force_from_local_stress(pat, g["stress"]), g["force_py"]) <= PLAIN_RTOL
+
+
+def _slope_operator(et, nx, ny, nz, materials=None, lam=1.1):
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
+
+    mesh = synthetic.slope_mesh_3d(nx, ny, nz, elem_type=et, n_layers=4 if materials is not None else 1)
+    mats = materials or synthetic.MaterialSet.homogeneous()
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type=et)
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.05, seed=3)
+    return mesh, op, U
+
+
+@pytest.mark.parametrize("et,dims", [("P2", (12, 5, 6)), ("P4", (4, 2, 2))])
+def test_operator_against_oracle_on_slope(oracle, et, dims):
+    """Strain -> S/DS -> F -> K on a heterogeneous synthetic slope, against the oracle chain."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    mesh, op, U = _slope_operator(et, *dims, materials=synthetic.MaterialSet.layered(4, seed=1))
+    pat = op.owned_tangent_pattern
+    op.reduction(1.1)
+    op.constitutive_problem_stress_tangent(U)
+    idx = pat.local_int_indices
+    cb, sp = oracle.reduction(op.c0[idx], op.phi[idx], op.psi[idx], 1.1, "B")
+    u_ov = U.reshape(-1, order="F")[pat.overlap_global_dofs]
+    n_q = pat.n_q
+    E = oracle.strain_3d(pat.dphi1, pat.dphi2, pat.dphi3, u_ov, pat.overlap_element_dof_lids, n_q)
+    S, DS = oracle.constitutive_3d(E, cb, sp, op.shear[idx], op.bulk[idx], op.lame[idx])
+    plastic = np.mean(np.abs(DS[:, 1] - op.lame[idx]) > 1e-9 * op.lame[idx])
+    assert 0.05 < plastic < 0.6
+    assert rel_err(np.asarray(op._owned_local_S), S.T) <= PLAIN_RTOL
+    assert rel_err(np.asarray(op._owned_local_DS), DS.T) <= PLAIN_RTOL
+    F = op.build_F_local()
+    from slope_stability_petsc4py_gb300.distributed_tangent import _PatternBuild
+
+    pb = _PatternBuild(mesh.elem, mesh.q_mask, (0, mesh.n_nodes))
+    slots = {k: pb.get(k) for k in ("row_slot_ptr", "slot_elem", "slot_lrow", "slot_pos", "scatter_map")}
+    pb.close()
+    F_o = oracle.force_rows_3d(pat.dphi1, pat.dphi2, pat.dphi3, S, pat.overlap_assembly_weight, slots["row_slot_ptr"],
+                               slots["slot_elem"], slots["slot_lrow"], n_q)
+    F_o[~pat.owned_free_mask] = 0.0
+    assert rel_err(F, F_o) <= PLAIN_RTOL
+    r = 0.25
+    _, _, kv = op.build_K_regularized(r).getValuesCSR()
+    K_o = oracle.tangent_rows_3d(pat.dphi1, pat.dphi2, pat.dphi3, DS, pat.overlap_assembly_weight, slots["row_slot_ptr"],
+                                 slots["slot_elem"], slots["slot_lrow"], slots["slot_pos"], n_q, pat.nnz)
+    K_o[pat.constrained_diag_positions] = 1.0
+    K_o = (1.0 - r) * K_o + r * pat.elastic_values
+    assert rel_err(kv, K_o) <= PLAIN_RTOL
+
+
+def test_large_mesh_properties():
+    """At a benchmark-like size: symmetric == general kernel, K symmetric, linear in DS."""
+    import torch
+
+    from slope_stability_petsc4py_gb300.distributed_tangent import tangent_values_device
+
+    mesh, op, U = _slope_operator("P2", 30, 10, 20)  # ~36k tets, ~400k points
+    pat = op.owned_tangent_pattern
+    op.reduction(1.0)
+    op.constitutive_problem_stress_tangent(U)
+    ds = op._DS_aos
+    k_sym = tangent_values_device(pat, ds, symmetric=True)
+    k_gen = tangent_values_device(pat, ds, symmetric=False)
+    assert rel_err(k_sym.cpu().numpy(), k_gen.cpu().numpy()) <= 1e-13
+    # K restricted to free rows/cols is symmetric (every row is owned here)
+    Kf = op._build_owned_tangent_matrix().to_scipy()
+    free = np.flatnonzero(pat.owned_free_mask)
+    Kff = Kf[free][:, free]
+    assert abs(Kff - Kff.T).max() <= 1e-12 * abs(Kff).max()
+    # linearity in DS
+    ds2 = ds * 0.5 + 1.0
+    lhs = tangent_values_device(pat, (ds + 2.0 * ds2).contiguous(), finish=False)
+    rhs = tangent_values_device(pat, ds, finish=False) + 2.0 * tangent_values_device(pat, ds2.contiguous(), finish=False)
+    assert rel_err(lhs.cpu().numpy(), rhs.cpu().numpy()) <= 1e-12
+    torch.cuda.synchronize()
+
+
+def test_device_resident_operator_path():
+    """CUDA-tensor inputs keep every result on the device."""
+    import torch
+
+    mesh, op, U = _slope_operator("P2", 6, 3, 3)
+    op.host_outputs = False
+    Ud = torch.as_tensor(U, device="cuda")
+    op.reduction(1.2)
+    F_free, K = op.build_F_K_regularized_reduced_free(Ud, 0.1)
+    assert isinstance(F_free, torch.Tensor) and F_free.is_cuda
+    assert K.values.is_cuda
+    op.host_outputs = True
+    F_free_h = op.build_F_free_local()
+    assert rel_err(F_free.cpu().numpy(), F_free_h) == 0.0
