@@ -210,6 +210,57 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def kernel_profile(torch, lib, step, reps=3):
+    lib.TRACE = []
+    for _ in range(reps):
+        step()
+    torch.cuda.synchronize()
+    per = {}
+    for name, a, b in lib.TRACE:
+        per.setdefault(name, []).append(a.elapsed_time(b))
+    lib.TRACE = None
+    total = sum(sum(v) for v in per.values()) / reps
+    return {k: {"ms_per_launch": float(np.mean(v)), "launches_per_step": len(v) / reps,
+                "ms_per_step": float(np.sum(v)) / reps, "share": float(np.sum(v)) / reps / total}
+            for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]))}
+
+
+def workload_stats(op):
+    pat = op.owned_tangent_pattern
+    n_q = pat.n_q
+    br = op._branch.view(-1, n_q)
+    plastic = br != 0
+    return {"n": pat.n_local_int, "n_el": int(pat.overlap_elements.size), "n_p": pat.n_p, "n_q": n_q, "dim": pat.dim,
+            "ns": pat.n_strain, "nnz": pat.nnz, "n_rows": int(pat.local_matrix_pattern.shape[0]),
+            "n_u": int(pat.overlap_global_dofs.size), "n_plastic": int(plastic.sum().item()),
+            "n_plastic_el": int(plastic.any(dim=1).sum().item()),
+            "working_set": sum(v.numel() * v.element_size() for v in pat.device.values())}
+
+
+def algorithmic(name, st):
+    """Algorithmic HBM bytes and FP64 flops of one launch (each datum read or written once)."""
+    n, n_el, n_p, n_q, dim, ns = st["n"], st["n_el"], st["n_p"], st["n_q"], st["dim"], st["ns"]
+    nld = dim * n_p
+    s_out = 6 if dim == 3 else 4
+    if name == "ssp_constitutive_sds_branch":
+        return {"bytes": n * (8 * ns + 4 * 8 + 8 * s_out + 8 * ns * ns + 1), "flops": 0}
+    if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d"):
+        return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": n * 2 * 9 * n_p}
+    if name == "ssp_assemble_force_element":
+        return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": n * nld * 8}
+    if name == "ssp_blend_values":
+        return {"bytes": 3 * 8 * st["nnz"], "flops": 0}
+    if name == "ssp_reduction":
+        return {"bytes": 40 * n, "flops": 0}
+    if name == "ssp_gather":
+        return {"bytes": 20 * st["n_u"], "flops": 0}
+    if name == "ssp_tangent_plastic_correction":
+        npl, npe = st["n_plastic"], st["n_plastic_el"]
+        return {"bytes": n + npl * (8 * ns * ns + 8 * dim * n_p + 24) + npe * (4 * nld * nld + 16 * nld * nld),
+                "flops": npl * 2.0 * (nld * ns * dim + nld * (nld + 1) // 2 * dim)}
+    return {"bytes": 0, "flops": 0}
+
+
 def run_gpu(args):
     import torch
 
@@ -244,7 +295,6 @@ def run_gpu(args):
     _lib.raise_on_device_status()
 
     clocks = ClockSampler(local) if not args.no_clocks else None
-    op.tangent_events = []
     launches0 = _lib.LAUNCHES["count"]
     if dist is not None:
         dist.barrier()
@@ -263,23 +313,24 @@ def run_gpu(args):
         dist.barrier()
     launches = _lib.LAUNCHES["count"] - launches0
     ms = e0.elapsed_time(e1) / args.steps
-    tang_ms = float(np.mean([a.elapsed_time(b) for a, b in op.tangent_events]))
-    op.tangent_events = None
     _lib.raise_on_device_status()
     if dist is not None:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # roofline of the dominant kernel (tangent values; algorithmic bytes and flops per launch)
-    dim, n_p, n_q = pat.dim, pat.n_p, pat.n_q
-    ns, n_ld, n_el = pat.n_strain, pat.dim * pat.n_p, int(pat.overlap_elements.size)
-    bytes_launch = n_el * (n_q * (8 * ns * ns + 8 * dim * n_p + 8) + 4 * n_ld * n_ld) + 8 * nnz
-    flops_launch = n_el * 2.0 * n_q * (n_ld * ns * dim + n_ld * (n_ld + 1) // 2 * dim)
+    # per-kernel durations from a separate traced pass (CUDA events on the launch stream)
+    kernels = kernel_profile(torch, _lib, step, reps=3)
+    stats = workload_stats(op)
     hbm_peak, hbm_src = peaks()
-    achieved_gbs = bytes_launch / (tang_ms * 1e-3) / 1e9
     fp64_tf = fp64_peak(torch, _lib)
-    achieved_tf = flops_launch / (tang_ms * 1e-3) / 1e12
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
+    alg = algorithmic(dominant, stats)
+    k_ms = kernels[dominant]["ms_per_launch"]
+    achieved_gbs = alg["bytes"] / (k_ms * 1e-3) / 1e9
+    corr = "ssp_tangent_plastic_correction"
+    fl = algorithmic(corr, stats)["flops"]
+    corr_ms = kernels.get(corr, {}).get("ms_per_launch")
     line = {
         "metric": METRIC, "value": world * n_int / (ms * 1e-3), "unit": "quad-pts/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
@@ -287,16 +338,19 @@ def run_gpu(args):
         "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": "plain",
                    "step": "reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + "
                            "constrained diagonals + regularised blend",
-                   "l2": f"inputs larger than L2 (tangent-kernel working set {bytes_launch / 1e9:.2f} GB > 129 MB)",
+                   "plastic_fraction": stats["n_plastic"] / n_int,
+                   "l2": f"inputs larger than L2 (per-step HBM working set {stats['working_set'] / 1e9:.2f} GB > 129 MB)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "assembled_nnz_per_s": world * nnz / (ms * 1e-3),
-        "roofline": {"bound": "hbm", "kernel": "ssp_tangent_element (symmetric FP64)", "achieved": achieved_gbs,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
-                     "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else hbm_src,
-                     "traffic": None, "ms_per_launch": tang_ms, "algorithmic_bytes": bytes_launch},
-        "roofline_fp64": {"bound": "fp64", "achieved": achieved_tf, "peak": fp64_tf, "unit": "TFLOP/s",
-                          "frac": achieved_tf / fp64_tf, "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)",
-                          "algorithmic_flops": flops_launch},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else hbm_src,
+                     "traffic": None, "ms_per_launch": k_ms, "algorithmic_bytes": alg["bytes"]},
+        "roofline_fp64": ({"bound": "fp64", "kernel": corr, "achieved": fl / (corr_ms * 1e-3) / 1e12, "peak": fp64_tf,
+                           "unit": "TFLOP/s", "frac": fl / (corr_ms * 1e-3) / 1e12 / fp64_tf,
+                           "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)", "algorithmic_flops": fl,
+                           "ms_per_launch": corr_ms} if corr_ms else None),
+        "kernels": kernels,
         "gpu_launches": launches,
         "clocks": clock_info,
     }

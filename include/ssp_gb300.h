@@ -61,6 +61,13 @@ int ssp_constitutive_3d_sds(const double *E, const double *c_bar, const double *
 int ssp_constitutive_3d_branch(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                                const double *lame, int n_int, double *S_out, int8_t *branch_out, void *stream);
 
+/* S, DS and the branch code of every point (2D or 3D); the branch codes drive the plastic-only
+ * tangent correction (ssp_tangent_plastic_correction).  Same arithmetic as ssp_constitutive_3d_sds /
+ * ssp_constitutive_2d. */
+int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, const double *sin_phi,
+                                const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
+                                int8_t *branch_out, void *stream);
+
 /* Replaces constitutive_problem_2D (src/slope_stability/constitutive/problem.py:143-475), which the
  * reference has only in NumPy: E [n_int][3] -> S [n_int][4] ([s11,s22,s12,s33]), DS [n_int][9]
  * (DS_out may be NULL for stress only). */
@@ -132,6 +139,26 @@ int ssp_assemble_tangent_values_3d_p2(const double *dphi1, const double *dphi2, 
 int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const double *dphi2, const double *dphi3,
                         const double *ds, const double *weight, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
                         long long nnz_out, double *out_values, int accumulate, void *stream);
+
+/* Tangent by elastic predictor and plastic correction: adds
+ *     sum over points with branch != 0 of  B^T (w * scale * (DS - D_el)) B
+ * to out_values (no zeroing), where D_el is the elastic tangent the return mapping emits for
+ * (shear, lame).  Added to the elastic tangent of the same mesh (assembled once from
+ * ssp_elastic_tangent_blocks), this equals the element sum of the reference's tangent kernels
+ * (assemble_tangent_values_3d.c:13-214) up to rounding, with FP64 work only for plastic points. */
+int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                                   const double *ds, const double *weight, const int8_t *branch, const double *shear,
+                                   const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
+                                   long long nnz_out, double scale, double *out_values, void *stream);
+
+/* Per-point elastic tangent blocks [n_int][n_s*n_s] of the return mapping's elastic branch. */
+int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
+                               void *stream);
+
+/* out = (1-r) base + r elastic_values (the regularised blend of problem.py:1614-1615 applied to
+ * a precomputed base). */
+int ssp_blend_values(double *out_values, const double *base, const double *elastic_values, double r, long long nnz,
+                     void *stream);
 
 /* Constrained diagonals := 1.0 (distributed_tangent.py:1606-1607), then, when elastic_values is
  * not NULL, values := (1-r) values + r elastic_values (constitutive/problem.py:1614-1615). */

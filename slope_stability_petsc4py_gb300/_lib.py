@@ -26,6 +26,10 @@ _SIGS = {
     "ssp_constitutive_3d_sds": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_3d_branch": [_vp] * 5 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
+    "ssp_tangent_plastic_correction": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp, _vp],
+    "ssp_elastic_tangent_blocks": [_c_int, _vp, _vp, _c_int, _vp, _vp],
+    "ssp_blend_values": [_vp, _vp, _vp, _c_dbl, _c_ll, _vp],
     "ssp_reduction": [_vp, _vp, _vp, _c_int, _c_dbl, ctypes.c_char, _vp, _vp, _vp],
     "ssp_geometry": [_c_int, _vp, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_assemble_overlap_strain_3d": [_vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
@@ -88,16 +92,30 @@ _KERNELS_PER_CALL = {
     "ssp_constitutive_2d": 1, "ssp_reduction": 1, "ssp_geometry": 1, "ssp_assemble_overlap_strain_3d": 1,
     "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
-    "ssp_gather": 1, "ssp_probe_dfma": 1,
+    "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_constitutive_sds_branch": 1, "ssp_tangent_plastic_correction": 1,
+    "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
 }
 LAUNCHES = {"count": 0}
+# When set to a list, every kernel-launching call appends (name, start_event, end_event), recorded
+# on torch's current stream (the stream the kernels run on).  Used by the benchmark's per-kernel
+# timing; None (the default) adds no work.
+TRACE = None
 
 
 def call(name: str, *args) -> None:
-    check(getattr(load(), name)(*args), name)
     k = _KERNELS_PER_CALL.get(name, 0)
-    LAUNCHES["count"] += k(args) if callable(k) else k
+    n_k = k(args) if callable(k) else k
+    if TRACE is not None and n_k:
+        t = torch()
+        e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        e0.record()
+        check(getattr(load(), name)(*args), name)
+        e1.record()
+        TRACE.append((name, e0, e1))
+    else:
+        check(getattr(load(), name)(*args), name)
+    LAUNCHES["count"] += n_k
 
 
 def device_status(clear: bool = True) -> int:

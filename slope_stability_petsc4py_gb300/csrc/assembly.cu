@@ -249,6 +249,28 @@ __global__ void tangent_rows3_kernel(const double *__restrict__ d1, const double
 
 // ---------------------------------------------------------------------------- tangent (element)
 
+struct ElemArgs {
+    const double *d1, *d2, *d3, *DS, *w;
+    const int32_t *emap;
+    int n_elem;
+    long long nnz;
+    double *values;
+    // correction mode only
+    const int8_t *branch;
+    const double *shear, *lame;
+    double scale;
+};
+
+// Entry (i, j) of the elastic tangent the return mapping emits for an elastic point
+// (constitutive.cu, mc3d_point / mc2d_point elastic branches), with the same arithmetic.
+template <int DIM>
+__device__ __forceinline__ double elastic_d(int i, int j, double G, double lam) {
+    constexpr int NN = DIM == 3 ? 3 : 2;  // normal components
+    if (i < NN && j < NN) return i == j ? 2.0 * G + lam : lam;
+    if (i == j) return G;
+    return 0.0;
+}
+
 // One CTA per element (grid-stride).  K_e = sum_q B_q^T (w_q D_q) B_q is formed in two
 // stages per quadrature point through shared memory:
 //   H[alpha][m] = (B^T (w D))[alpha][m]      (n_ld x n_s, split over the CTA)
@@ -256,11 +278,13 @@ __global__ void tangent_rows3_kernel(const double *__restrict__ d1, const double
 // and scattered with FP64 atomics through the element->CSR map (the reference's legacy
 // scatter_map).  SYM evaluates only alpha <= beta and writes both mirror positions; it is
 // valid when every D_q is symmetric (tangents produced by ssp_constitutive_*).
-template <int DIM, int NP, int NQ, int THREADS, bool SYM>
-__global__ void __launch_bounds__(THREADS) tangent_element_kernel(
-    const double *__restrict__ d1, const double *__restrict__ d2, const double *__restrict__ d3,
-    const double *__restrict__ DS, const double *__restrict__ w, const int32_t *__restrict__ emap, int n_elem,
-    long long nnz, double *__restrict__ values) {
+//
+// CORR (correction mode): only points whose branch is not elastic contribute, with
+// D_q := scale * (DS_q - D_el,q).  Added to the elastic tangent assembled once, this gives the
+// full tangent with the FP64 work of the plastic points only: for an elastic point DS_q equals
+// D_el,q exactly, so its term vanishes.
+template <int DIM, int NP, int NQ, int THREADS, bool SYM, bool CORR>
+__global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
@@ -268,6 +292,8 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(
     __shared__ double sg[NQ][DIM][NP];
     __shared__ double sD[NQ][NS * NS];
     __shared__ double sH[NLD * NS];
+    __shared__ int sq[NQ];
+    __shared__ int snq;
 
     const int tid = threadIdx.x;
     // per-thread entry descriptors: alpha | beta << 8 (alpha, beta < 256), or -1
@@ -296,24 +322,38 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(
         code[i] = c;
     }
 
-    for (int e = blockIdx.x; e < n_elem; e += gridDim.x) {
+    for (int e = blockIdx.x; e < A.n_elem; e += gridDim.x) {
         const long long g0 = (long long)e * NQ;
-        for (int i = tid; i < NQ * NP; i += THREADS) {
-            const int q = i / NP, a = i % NP;
-            sg[q][0][a] = d1[g0 * NP + i];
-            sg[q][1][a] = d2[g0 * NP + i];
-            if (DIM == 3) sg[q][DIM - 1][a] = d3[g0 * NP + i];
+        __syncthreads();  // the previous element is done with the shared buffers
+        if (tid == 0) {
+            int k = 0;
+            for (int q = 0; q < NQ; ++q)
+                if (!CORR || A.branch[g0 + q] != 0) sq[k++] = q;
+            snq = k;
         }
-        for (int i = tid; i < NQ * NS * NS; i += THREADS) {
-            const int q = i / (NS * NS), k = i % (NS * NS);
-            sD[q][k] = w[g0 + q] * DS[(g0 + q) * (NS * NS) + k];
+        __syncthreads();
+        const int nq = snq;
+        if (nq == 0) continue;  // uniform across the CTA
+        for (int i = tid; i < nq * NP; i += THREADS) {
+            const int k = i / NP, a = i % NP;
+            const long long src = (g0 + sq[k]) * NP + a;
+            sg[k][0][a] = A.d1[src];
+            sg[k][1][a] = A.d2[src];
+            if (DIM == 3) sg[k][DIM - 1][a] = A.d3[src];
+        }
+        for (int i = tid; i < nq * NS * NS; i += THREADS) {
+            const int k = i / (NS * NS), kk = i % (NS * NS);
+            const long long g = g0 + sq[k];
+            double v = A.DS[g * (NS * NS) + kk];
+            if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, A.shear[g], A.lame[g]));
+            sD[k][kk] = A.w[g] * v;
         }
         double acc[PER];
 #pragma unroll
         for (int i = 0; i < PER; ++i) acc[i] = 0.0;
         __syncthreads();
 
-        for (int q = 0; q < NQ; ++q) {
+        for (int q = 0; q < nq; ++q) {
             for (int it = tid; it < NLD * NS; it += THREADS) {
                 const int alpha = it / NS, m = it % NS;
                 const int a = alpha / DIM, c = alpha % DIM;
@@ -344,7 +384,7 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(
             __syncthreads();
         }
 
-        const int32_t *em = emap + (long long)e * NLD * NLD;
+        const int32_t *em = A.emap + (long long)e * NLD * NLD;
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int c = code[i];
@@ -352,18 +392,30 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(
             const int alpha = c & 0xff, beta = c >> 8;
             const int32_t p = em[alpha * NLD + beta];
             if (p >= 0) {
-                if (p < nnz) atomicAdd(values + p, acc[i]);
+                if (p < A.nnz) atomicAdd(A.values + p, acc[i]);
                 else flag(SSP_DEV_BAD_INDEX);
             }
             if (SYM && alpha != beta) {
                 const int32_t p2 = em[beta * NLD + alpha];
                 if (p2 >= 0) {
-                    if (p2 < nnz) atomicAdd(values + p2, acc[i]);
+                    if (p2 < A.nnz) atomicAdd(A.values + p2, acc[i]);
                     else flag(SSP_DEV_BAD_INDEX);
                 }
             }
         }
     }
+}
+
+// Per-point elastic tangent of the return mapping (for assembling the elastic tangent once).
+template <int DIM>
+__global__ void elastic_blocks_kernel(const double *__restrict__ shear, const double *__restrict__ lame, int n,
+                                      double *__restrict__ DS) {
+    constexpr int NS = DIM == 3 ? 6 : 3;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * NS * NS) return;
+    const long long g = t / (NS * NS);
+    const int kk = static_cast<int>(t % (NS * NS));
+    DS[t] = elastic_d<DIM>(kk % NS, kk / NS, shear[g], lame[g]);
 }
 
 // ---------------------------------------------------------------------------- epilogue
@@ -386,6 +438,13 @@ __global__ void blend_kernel(double *__restrict__ values, const double *__restri
     values[i] = values[i] * (1.0 - r) + r * elastic[i];
 }
 
+__global__ void blend_base_kernel(double *__restrict__ out, const double *__restrict__ base,
+                                  const double *__restrict__ elastic, long long nnz, double r) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nnz) return;
+    out[i] = base[i] * (1.0 - r) + r * elastic[i];
+}
+
 __global__ void gather_rows_kernel(const double *__restrict__ src, const int32_t *__restrict__ idx, int n,
                                    double *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -394,35 +453,28 @@ __global__ void gather_rows_kernel(const double *__restrict__ src, const int32_t
 
 // ---------------------------------------------------------------------------- dispatch
 
-template <int DIM, int NP, int NQ, int THREADS, bool SYM>
-int launch_element(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
-                   const int32_t *emap, int n_elem, long long nnz, double *values, cudaStream_t st) {
+template <int DIM, int NP, int NQ, int THREADS, bool SYM, bool CORR>
+int launch_element(const ElemArgs &a, cudaStream_t st) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tangent_element_kernel<DIM, NP, NQ, THREADS, SYM>, THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tangent_element_kernel<DIM, NP, NQ, THREADS, SYM, CORR>,
+                                                  THREADS, 0);
     if (per_sm < 1) per_sm = 1;
     long long grid = (long long)sms * per_sm;
-    if (grid > n_elem) grid = n_elem;
-    tangent_element_kernel<DIM, NP, NQ, THREADS, SYM>
-        <<<static_cast<unsigned>(grid), THREADS, 0, st>>>(d1, d2, d3, DS, w, emap, n_elem, nnz, values);
+    if (grid > a.n_elem) grid = a.n_elem;
+    tangent_element_kernel<DIM, NP, NQ, THREADS, SYM, CORR><<<static_cast<unsigned>(grid), THREADS, 0, st>>>(a);
     return launch_status();
 }
 
-template <bool SYM>
-int dispatch_element(int dim, int n_p, int n_q, const double *d1, const double *d2, const double *d3, const double *DS,
-                     const double *w, const int32_t *emap, int n_elem, long long nnz, double *values, cudaStream_t st) {
-    if (dim == 3 && n_p == 10 && n_q == 11)
-        return launch_element<3, 10, 11, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
-    if (dim == 3 && n_p == 35 && n_q == 24)
-        return launch_element<3, 35, 24, 256, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
-    if (dim == 3 && n_p == 4 && n_q == 1)
-        return launch_element<3, 4, 1, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
-    if (dim == 2 && n_p == 6 && n_q == 7)
-        return launch_element<2, 6, 7, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
-    if (dim == 2 && n_p == 3 && n_q == 1)
-        return launch_element<2, 3, 1, 32, SYM>(d1, d2, d3, DS, w, emap, n_elem, nnz, values, st);
+template <bool SYM, bool CORR>
+int dispatch_element(int dim, int n_p, int n_q, const ElemArgs &a, cudaStream_t st) {
+    if (dim == 3 && n_p == 10 && n_q == 11) return launch_element<3, 10, 11, 32, SYM, CORR>(a, st);
+    if (dim == 3 && n_p == 35 && n_q == 24) return launch_element<3, 35, 24, 256, SYM, CORR>(a, st);
+    if (dim == 3 && n_p == 4 && n_q == 1) return launch_element<3, 4, 1, 32, SYM, CORR>(a, st);
+    if (dim == 2 && n_p == 6 && n_q == 7) return launch_element<2, 6, 7, 32, SYM, CORR>(a, st);
+    if (dim == 2 && n_p == 3 && n_q == 1) return launch_element<2, 3, 1, 32, SYM, CORR>(a, st);
     return SSP_ERR_UNSUPPORTED;
 }
 
@@ -534,10 +586,43 @@ int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const doubl
         return SSP_ERR_CUDA;
     if (n_elem == 0) return SSP_OK;
     if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !scatter_map) return SSP_ERR_INVALID;
-    return symmetric ? dispatch_element<true>(dim, n_p, n_q, dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out,
-                                              out_values, st)
-                     : dispatch_element<false>(dim, n_p, n_q, dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out,
-                                               out_values, st);
+    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, nullptr, nullptr, nullptr, 1.0};
+    return symmetric ? dispatch_element<true, false>(dim, n_p, n_q, a, st) : dispatch_element<false, false>(dim, n_p, n_q, a, st);
+}
+
+int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                                   const double *ds, const double *weight, const int8_t *branch, const double *shear,
+                                   const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
+                                   long long nnz_out, double scale, double *out_values, void *stream) {
+    if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !branch || !shear || !lame || !scatter_map ||
+        (nnz_out > 0 && !out_values))
+        return SSP_ERR_INVALID;
+    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale};
+    return dispatch_element<true, true>(dim, n_p, n_q, a, as_stream(stream));
+}
+
+int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
+                               void *stream) {
+    if ((dim != 2 && dim != 3) || n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!shear || !lame || !ds_out) return SSP_ERR_INVALID;
+    const long long n = (long long)n_int * (dim == 3 ? 36 : 9);
+    if (dim == 3)
+        elastic_blocks_kernel<3><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(shear, lame, n_int, ds_out);
+    else
+        elastic_blocks_kernel<2><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(shear, lame, n_int, ds_out);
+    return launch_status();
+}
+
+int ssp_blend_values(double *out_values, const double *base, const double *elastic_values, double r, long long nnz,
+                     void *stream) {
+    if (nnz < 0) return SSP_ERR_INVALID;
+    if (nnz == 0) return SSP_OK;
+    if (!out_values || !base || !elastic_values) return SSP_ERR_INVALID;
+    blend_base_kernel<<<grid_for(nnz, 256), 256, 0, as_stream(stream)>>>(out_values, base, elastic_values, nnz, r);
+    return launch_status();
 }
 
 int ssp_assemble_tangent_values_3d_p2(const double *dphi1, const double *dphi2, const double *dphi3, const double *ds,

@@ -459,12 +459,13 @@ template <bool TANGENT>
 __global__ void __launch_bounds__(128) mc2d_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                    const double *__restrict__ sin_phi, const double *__restrict__ shear,
                                                    const double *__restrict__ lame, int n, double *__restrict__ S,
-                                                   double *__restrict__ DS) {
+                                                   double *__restrict__ DS, int8_t *__restrict__ branch) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const double e[3] = {E[3ll * p], E[3ll * p + 1], E[3ll * p + 2]};
     double s[4], ds[9];
-    mc2d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, TANGENT ? ds : nullptr);
+    const int b = mc2d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, TANGENT ? ds : nullptr);
+    if (branch) branch[p] = static_cast<int8_t>(b);
 #pragma unroll
     for (int k = 0; k < 4; ++k) S[4ll * p + k] = s[k];
     if (TANGENT) {
@@ -552,10 +553,25 @@ int ssp_constitutive_2d(const double *E, const double *c_bar, const double *sin_
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out) return SSP_ERR_INVALID;
     if (DS_out)
         mc2d_kernel<true><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
-                                                                                DS_out);
+                                                                                DS_out, nullptr);
     else
         mc2d_kernel<false><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
-                                                                                 nullptr);
+                                                                                 nullptr, nullptr);
+    return launch_status();
+}
+
+int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, const double *sin_phi,
+                                const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
+                                int8_t *branch_out, void *stream) {
+    if ((dim != 2 && dim != 3) || n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out) return SSP_ERR_INVALID;
+    if (dim == 3)
+        mc3d_kernel<true><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                                DS_out, branch_out);
+    else
+        mc2d_kernel<true><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                                DS_out, branch_out);
     return launch_status();
 }
 

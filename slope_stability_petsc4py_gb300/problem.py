@@ -135,6 +135,9 @@ class ConstitutiveOperator:
         self._S_aos = None
         self._DS_aos = None
         self._ds_symmetric = False
+        self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
+        self._K_el = None  # elastic tangent CSR values (device), built on first use
+        self._dev = None
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
         self._owned_unique_c_bar = None
@@ -175,6 +178,8 @@ class ConstitutiveOperator:
         self.owned_constitutive_mode = str(constitutive_mode).lower()
         self.release_petsc_caches()
         self._dev = None
+        self._K_el = None
+        self._clear_owned_local_cache()
         if pattern is not None:
             t = _lib.require_cuda()
             idx = np.asarray(pattern.local_int_indices, dtype=np.int64)
@@ -211,6 +216,7 @@ class ConstitutiveOperator:
     def _owned_local_DS(self, value):
         self._DS_aos = self._ingest_field(value, self.n_strain * self.n_strain)
         self._ds_symmetric = False  # a caller-provided tangent is not known to be symmetric
+        self._branch = None
 
     def _ingest_field(self, value, rows):
         if value is None:
@@ -229,6 +235,7 @@ class ConstitutiveOperator:
         self._S_aos = None
         self._DS_aos = None
         self._ds_symmetric = False
+        self._branch = None
 
     # -------------------------------------------------------------------- hot path
 
@@ -272,16 +279,20 @@ class ConstitutiveOperator:
         st = _lib.stream_handle()
         args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                 _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
-        if pat.dim == 3:
-            if tangent:
-                _lib.call("ssp_constitutive_3d_sds", *args, _lib.ptr(S), _lib.ptr(DS), st)
-            else:
-                _lib.call("ssp_constitutive_3d_s", *args, _lib.ptr(S), st)
+        branch = None
+        if tangent:
+            branch = t.empty(n, dtype=t.int8, device="cuda")
+            _lib.call("ssp_constitutive_sds_branch", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
+                      _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
+                      _lib.ptr(DS), _lib.ptr(branch), st)
+        elif pat.dim == 3:
+            _lib.call("ssp_constitutive_3d_s", *args, _lib.ptr(S), st)
         else:
-            _lib.call("ssp_constitutive_2d", *args, _lib.ptr(S), _lib.ptr(DS) if tangent else None, st)
+            _lib.call("ssp_constitutive_2d", *args, _lib.ptr(S), None, st)
         self.time_local_constitutive.append(perf_counter() - t1)
         self._S_aos = S
         self._DS_aos = DS
+        self._branch = branch
         self._ds_symmetric = bool(tangent)
         self.S = None
         self.DS = None
@@ -347,6 +358,21 @@ class ConstitutiveOperator:
         self._single_rank_check()
         return self.build_F_free_local()
 
+    def _elastic_tangent_values(self):
+        """CSR values of the tangent with every point elastic (constrained diagonals = 1), assembled
+        once per pattern; the base of the elastic-predictor / plastic-correction assembly."""
+        if self._K_el is None:
+            t = _lib.require_cuda()
+            pat = self._require_pattern()
+            n = pat.n_local_int
+            d = self._dev
+            blocks = t.empty((n, self.n_strain * self.n_strain), dtype=t.float64, device="cuda")
+            _lib.call("ssp_elastic_tangent_blocks", pat.dim, _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n,
+                      _lib.ptr(blocks), _lib.stream_handle())
+            self._K_el = tangent_values_device(pat, blocks, symmetric=True)
+            del blocks
+        return self._K_el
+
     def _tangent_into(self, values, r=None):
         pat = self._require_pattern()
         if self._DS_aos is None:
@@ -356,15 +382,39 @@ class ConstitutiveOperator:
         if ev is not None:  # optional CUDA-event bracket of the tangent kernel (measurement)
             t = _lib.torch()
             e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
-            e0.record()
-        tangent_values_device(pat, self._DS_aos, kernel=self.owned_tangent_kernel, symmetric=self._ds_symmetric,
-                              out=values)
-        if ev is not None:
-            e1.record()
-            ev.append((e0, e1))
-        if r is not None:
-            _lib.call("ssp_finish_values", _lib.ptr(values), pat.nnz, None, 0, _lib.ptr(pat.device["elastic_values"]),
-                      float(r), _lib.stream_handle())
+        st = _lib.stream_handle()
+        d = pat.device
+        if self._ds_symmetric and self._branch is not None and self.owned_tangent_kernel in ("rows", "legacy"):
+            # tangent = elastic tangent + plastic-point corrections (FP64 work on plastic points only)
+            base = self._elastic_tangent_values()
+            if r is None:
+                values.copy_(base)
+                scale = 1.0
+            else:
+                _lib.call("ssp_blend_values", _lib.ptr(values), _lib.ptr(base), _lib.ptr(d["elastic_values"]), float(r),
+                          pat.nnz, st)
+                scale = 1.0 - float(r)
+            if ev is not None:
+                e0.record()
+            _lib.call("ssp_tangent_plastic_correction", pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
+                      _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
+                      _lib.ptr(self._branch), _lib.ptr(self._dev["shear"]), _lib.ptr(self._dev["lame"]),
+                      _lib.ptr(d["scatter_map"]), int(pat.overlap_elements.size), pat.n_p, pat.n_q, pat.nnz, scale,
+                      _lib.ptr(values), st)
+            if ev is not None:
+                e1.record()
+                ev.append((e0, e1))
+        else:
+            if ev is not None:
+                e0.record()
+            tangent_values_device(pat, self._DS_aos, kernel=self.owned_tangent_kernel, symmetric=self._ds_symmetric,
+                                  out=values)
+            if ev is not None:
+                e1.record()
+                ev.append((e0, e1))
+            if r is not None:
+                _lib.call("ssp_finish_values", _lib.ptr(values), pat.nnz, None, 0, _lib.ptr(d["elastic_values"]),
+                          float(r), st)
         self.time_build_tangent_local.append(perf_counter() - t0)
 
     def _matrix(self, which: str, values):

@@ -334,8 +334,15 @@ def test_large_mesh_properties():
     k_sym = tangent_values_device(pat, ds, symmetric=True)
     k_gen = tangent_values_device(pat, ds, symmetric=False)
     assert rel_err(k_sym.cpu().numpy(), k_gen.cpu().numpy()) <= 1e-13
-    # K restricted to free rows/cols is symmetric (every row is owned here)
+    # elastic predictor + plastic correction (the operator's path) == direct sum over all points
+    k_direct = tangent_values_device(pat, ds, symmetric=True).cpu().numpy()
     Kf = op._build_owned_tangent_matrix().to_scipy()
+    assert op._branch is not None and int((op._branch != 0).sum()) > 0
+    assert rel_err(Kf.data, k_direct) <= 1e-13
+    r = 0.3
+    _, _, kr = op.build_K_regularized(r).getValuesCSR()
+    assert rel_err(kr, (1.0 - r) * k_direct + r * pat.elastic_values) <= 1e-13
+    # K restricted to free rows/cols is symmetric (every row is owned here)
     free = np.flatnonzero(pat.owned_free_mask)
     Kff = Kf[free][:, free]
     assert abs(Kff - Kff.T).max() <= 1e-12 * abs(Kff).max()
@@ -360,4 +367,5 @@ def test_device_resident_operator_path():
     assert K.values.is_cuda
     op.host_outputs = True
     F_free_h = op.build_F_free_local()
-    assert rel_err(F_free.cpu().numpy(), F_free_h) == 0.0
+    # the element force kernel sums with atomics, so repeated calls agree to rounding only
+    assert rel_err(F_free.cpu().numpy(), F_free_h) <= 1e-14
