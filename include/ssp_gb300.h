@@ -68,6 +68,16 @@ int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, c
                                 const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
                                 int8_t *branch_out, void *stream);
 
+/* The 3D return mapping in two passes over the same arithmetic (replaces
+ * constitutive_problem_3d_sds_batch_c, constitutive_3d_batch.h:15-25): pass A decides every point's
+ * branch and finishes elastic and apex points; the smooth-face, left-edge and right-edge points are
+ * collected into three lists and finished by pass B, so each warp runs one branch's code.
+ * scratch is caller-allocated device memory of 3*n_int + 4 int32 (counters and point lists); it
+ * is overwritten.  Outputs as ssp_constitutive_sds_branch. */
+int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                                   int32_t *scratch, void *stream);
+
 /* Replaces constitutive_problem_2D (src/slope_stability/constitutive/problem.py:143-475), which the
  * reference has only in NumPy: E [n_int][3] -> S [n_int][4] ([s11,s22,s12,s33]), DS [n_int][9]
  * (DS_out may be NULL for stress only). */

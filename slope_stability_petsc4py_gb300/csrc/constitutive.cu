@@ -60,9 +60,13 @@ __device__ __forceinline__ void principal3(const double *E, Principal3 &p) {
     }
     const double third = I1 / 3.0;
     p.I1 = I1;
-    p.e1 = -2.0 * rq * cos(theta + 2.0 * kPi / 3.0) + third;
-    p.e2 = -2.0 * rq * cos(theta - 2.0 * kPi / 3.0) + third;
-    p.e3 = -2.0 * rq * cos(theta) + third;
+    // cos(theta -+ 2 pi/3) = -cos(theta)/2 +- (sqrt(3)/2) sin(theta): one sincos instead of three cos
+    double st, ct;
+    sincos(theta, &st, &ct);
+    const double r3 = 1.7320508075688772 * st;
+    p.e1 = rq * (ct + r3) + third;
+    p.e2 = rq * (ct - r3) + third;
+    p.e3 = -2.0 * rq * ct + third;
 }
 
 // d(t*t)_i / dE_j (symmetric), entry for i <= j only.
@@ -98,16 +102,65 @@ __device__ __forceinline__ void store_sym(double *DS, int i, int j, double v) {
     DS[j + 6 * i] = v;
 }
 
-// Returns the branch code.  DS may be null (stress only).
-__device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
-                          double *DS) {
-    const double sp = sin_phi;
-    Principal3 p;
-    principal3(E, p);
-    const double e1 = p.e1, e2 = p.e2, e3 = p.e3, I1 = p.I1;
-    const double f_tr = 2.0 * shear * ((1.0 + sin_phi) * e1 - (1.0 - sin_phi) * e3) + 2.0 * lame * sin_phi * I1 - c_bar;
+struct Decision3 {
+    int branch;
+    double lam;  // plastic multiplier of the selected branch (elastic / apex: unused)
+    double den;  // its denominator
+};
 
-    if (f_tr <= 0.0) {
+struct Mat3 {
+    double c_bar, sin_phi, shear, lame;
+};
+
+// Plastic multipliers of the three return branches (constitutive_3D_kernel.h:144-147, 213-215, 277-279).
+__device__ __forceinline__ void smooth_lam(const Principal3 &p, const Mat3 &m, double f_tr, double &lam, double &den) {
+    const double sp = m.sin_phi;
+    den = 4.0 * m.lame * m.sin_phi * sp + 4.0 * m.shear * (1.0 + m.sin_phi * sp);
+    lam = f_tr / den;
+}
+__device__ __forceinline__ void left_lam(const Principal3 &p, const Mat3 &m, double &lam, double &den) {
+    const double sp = m.sin_phi, sf = m.sin_phi, G = m.shear, L = m.lame;
+    den = 4.0 * L * sf * sp + G * (1.0 + sf) * (1.0 + sp) + 2.0 * G * (1.0 - sf) * (1.0 - sp);
+    lam = (G * ((1.0 + sf) * (p.e1 + p.e2) - 2.0 * (1.0 - sf) * p.e3) + 2.0 * L * sf * p.I1 - m.c_bar) / den;
+}
+__device__ __forceinline__ void right_lam(const Principal3 &p, const Mat3 &m, double &lam, double &den) {
+    const double sp = m.sin_phi, sf = m.sin_phi, G = m.shear, L = m.lame;
+    den = 4.0 * L * sf * sp + 2.0 * G * (1.0 + sf) * (1.0 + sp) + G * (1.0 - sf) * (1.0 - sp);
+    lam = (G * (2.0 * (1.0 + sf) * p.e1 - (1.0 - sf) * (p.e2 + p.e3)) + 2.0 * L * sf * p.I1 - m.c_bar) / den;
+}
+__device__ __forceinline__ double trial_yield(const Principal3 &p, const Mat3 &m) {
+    return 2.0 * m.shear * ((1.0 + m.sin_phi) * p.e1 - (1.0 - m.sin_phi) * p.e3) + 2.0 * m.lame * m.sin_phi * p.I1 -
+           m.c_bar;
+}
+
+// Branch selection (constitutive_3D_kernel.h:114-338).
+__device__ __forceinline__ Decision3 decide3(const Principal3 &p, const Mat3 &m) {
+    const double sp = m.sin_phi;
+    const double f_tr = trial_yield(p, m);
+    if (f_tr <= 0.0) return {kElastic, 0.0, 1.0};
+    const double g_sl = (p.e1 - p.e2) / (1.0 + sp);
+    const double g_sr = (p.e2 - p.e3) / (1.0 - sp);
+    double lam, den;
+    smooth_lam(p, m, f_tr, lam, den);
+    if (lam <= g_sl && lam <= g_sr) return {kSmooth, lam, den};
+    if (g_sl < g_sr) {
+        left_lam(p, m, lam, den);
+        const double g_la = (p.e1 + p.e2 - 2.0 * p.e3) / (3.0 - sp);
+        if (lam >= g_sl && lam <= g_la) return {kLeft, lam, den};
+    }
+    if (g_sl > g_sr) {
+        right_lam(p, m, lam, den);
+        const double g_ra = (2.0 * p.e1 - p.e2 - p.e3) / (3.0 + sp);
+        if (lam >= g_sr && lam <= g_ra) return {kRight, lam, den};
+    }
+    return {kApex, 0.0, 1.0};
+}
+
+// Stress and (when DS != null) consistent tangent of the decided branch.
+__device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, double *S, double *DS) {
+    const double sp = m.sin_phi, sin_phi = m.sin_phi, shear = m.shear, lame = m.lame;
+    const double e1 = p.e1, e2 = p.e2, e3 = p.e3, I1 = p.I1;
+    if (d.branch == kElastic) {
         const double lI1 = lame * I1, s2 = 2.0 * shear;
 #pragma unroll
         for (int i = 0; i < 3; ++i) S[i] = lI1 + s2 * p.t[i];
@@ -125,15 +178,10 @@ __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double 
             store_sym(DS, 0, 2, lame);
             store_sym(DS, 1, 2, lame);
         }
-        return kElastic;
+        return;
     }
-
-    const double g_sl = (e1 - e2) / (1.0 + sp);
-    const double g_sr = (e2 - e3) / (1.0 - sp);
-    const double den_s = 4.0 * lame * sin_phi * sp + 4.0 * shear * (1.0 + sin_phi * sp);
-    const double lam_s = f_tr / den_s;
-
-    if (lam_s <= g_sl && lam_s <= g_sr) {
+    if (d.branch == kSmooth) {
+        const double lam_s = d.lam;
         const double inv1 = 1.0 / ((e1 - e2) * (e1 - e3));
         const double inv2 = 1.0 / ((e2 - e1) * (e2 - e3));
         const double inv3 = 1.0 / ((e3 - e1) * (e3 - e2));
@@ -155,7 +203,7 @@ __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double 
             const double c1a = 2.0 * e1 - e2 - e3, c1b = e2 - e3;
             const double c2a = 2.0 * e2 - e1 - e3, c2b = e1 - e3;
             const double c3a = 2.0 * e3 - e1 - e2, c3b = e1 - e2;
-            const double inv_den = 1.0 / den_s;
+            const double inv_den = 1.0 / d.den;
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -172,92 +220,77 @@ __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double 
                 }
             }
         }
-        return kSmooth;
+        return;
     }
-
-    if (g_sl < g_sr) {
-        const double den_l = 4.0 * lame * sin_phi * sp + shear * (1.0 + sin_phi) * (1.0 + sp) +
-                             2.0 * shear * (1.0 - sin_phi) * (1.0 - sp);
-        const double lam_l =
-            (shear * ((1.0 + sin_phi) * (e1 + e2) - 2.0 * (1.0 - sin_phi) * e3) + 2.0 * lame * sin_phi * I1 - c_bar) / den_l;
-        const double g_la = (e1 + e2 - 2.0 * e3) / (3.0 - sp);
-        if (lam_l >= g_sl && lam_l <= g_la) {
-            const double inv3 = 1.0 / ((e3 - e1) * (e3 - e2));
-            double P3[6], P12[6];
-            projection(p, e1 + e2, e1 * e2, inv3, P3);
+    if (d.branch == kLeft) {
+        const double lam_l = d.lam;
+        const double inv3 = 1.0 / ((e3 - e1) * (e3 - e2));
+        double P3[6], P12[6];
+        projection(p, e1 + e2, e1 * e2, inv3, P3);
 #pragma unroll
-            for (int i = 0; i < 6; ++i) P12[i] = vol_iota(i) - P3[i];
-            const double s1 = lame * I1 + shear * (e1 + e2) - lam_l * (2.0 * lame * sp + shear * (1.0 + sp));
-            const double s3 = lame * I1 + 2.0 * shear * e3 - lam_l * (2.0 * lame * sp - 2.0 * shear * (1.0 - sp));
+        for (int i = 0; i < 6; ++i) P12[i] = vol_iota(i) - P3[i];
+        const double s1 = lame * I1 + shear * (e1 + e2) - lam_l * (2.0 * lame * sp + shear * (1.0 + sp));
+        const double s3 = lame * I1 + 2.0 * shear * e3 - lam_l * (2.0 * lame * sp - 2.0 * shear * (1.0 - sp));
 #pragma unroll
-            for (int i = 0; i < 6; ++i) S[i] = s1 * P12[i] + s3 * P3[i];
-            if (DS) {
-                double Dp[6];
+        for (int i = 0; i < 6; ++i) S[i] = s1 * P12[i] + s3 * P3[i];
+        if (DS) {
+            double Dp[6];
 #pragma unroll
-                for (int i = 0; i < 6; ++i)
-                    Dp[i] = shear * ((1.0 + sin_phi) * P12[i] - 2.0 * (1.0 - sin_phi) * P3[i]) + 2.0 * lame * sin_phi * vol_iota(i);
-                const double em12 = e1 + e2;
-                const double inv_den = 1.0 / den_l;
+            for (int i = 0; i < 6; ++i)
+                Dp[i] = shear * ((1.0 + sin_phi) * P12[i] - 2.0 * (1.0 - sin_phi) * P3[i]) + 2.0 * lame * sin_phi * vol_iota(i);
+            const double em12 = e1 + e2;
+            const double inv_den = 1.0 / d.den;
 #pragma unroll
-                for (int j = 0; j < 6; ++j) {
+            for (int j = 0; j < 6; ++j) {
 #pragma unroll
-                    for (int i = 0; i <= j; ++i) {
-                        const double idk = (i == j) ? half_ident(i) : 0.0;
-                        const double o33 = P3[i] * P3[j], oAA = P12[i] * P12[j];
-                        const double d3 = inv3 * (square_jac(p.t, i, j) - idk * em12 - (P12[i] * p.t[j] + p.t[i] * P12[j]) +
-                                                  em12 * oAA + (em12 - 2.0 * e3) * o33 + e3 * (P12[i] * P3[j] + P3[i] * P12[j]));
-                        const double v = (s3 - s1) * d3 + lame * vol_iota(i) * vol_iota(j) + shear * (oAA + 2.0 * o33) -
-                                         Dp[i] * Dp[j] * inv_den;
-                        store_sym(DS, i, j, v);
-                    }
+                for (int i = 0; i <= j; ++i) {
+                    const double idk = (i == j) ? half_ident(i) : 0.0;
+                    const double o33 = P3[i] * P3[j], oAA = P12[i] * P12[j];
+                    const double d3 = inv3 * (square_jac(p.t, i, j) - idk * em12 - (P12[i] * p.t[j] + p.t[i] * P12[j]) +
+                                              em12 * oAA + (em12 - 2.0 * e3) * o33 + e3 * (P12[i] * P3[j] + P3[i] * P12[j]));
+                    const double v = (s3 - s1) * d3 + lame * vol_iota(i) * vol_iota(j) + shear * (oAA + 2.0 * o33) -
+                                     Dp[i] * Dp[j] * inv_den;
+                    store_sym(DS, i, j, v);
                 }
             }
-            return kLeft;
         }
+        return;
     }
-
-    if (g_sl > g_sr) {
-        const double den_r = 4.0 * lame * sin_phi * sp + 2.0 * shear * (1.0 + sin_phi) * (1.0 + sp) +
-                             shear * (1.0 - sin_phi) * (1.0 - sp);
-        const double lam_r =
-            (shear * (2.0 * (1.0 + sin_phi) * e1 - (1.0 - sin_phi) * (e2 + e3)) + 2.0 * lame * sin_phi * I1 - c_bar) / den_r;
-        const double g_ra = (2.0 * e1 - e2 - e3) / (3.0 + sp);
-        if (lam_r >= g_sr && lam_r <= g_ra) {
-            const double inv1 = 1.0 / ((e1 - e2) * (e1 - e3));
-            double P1[6], P23[6];
-            projection(p, e2 + e3, e2 * e3, inv1, P1);
+    if (d.branch == kRight) {
+        const double lam_r = d.lam;
+        const double inv1 = 1.0 / ((e1 - e2) * (e1 - e3));
+        double P1[6], P23[6];
+        projection(p, e2 + e3, e2 * e3, inv1, P1);
 #pragma unroll
-            for (int i = 0; i < 6; ++i) P23[i] = vol_iota(i) - P1[i];
-            const double s1 = lame * I1 + 2.0 * shear * e1 - lam_r * (2.0 * lame * sp + 2.0 * shear * (1.0 + sp));
-            const double s3 = lame * I1 + shear * (e2 + e3) - lam_r * (2.0 * lame * sp - shear * (1.0 - sp));
+        for (int i = 0; i < 6; ++i) P23[i] = vol_iota(i) - P1[i];
+        const double s1 = lame * I1 + 2.0 * shear * e1 - lam_r * (2.0 * lame * sp + 2.0 * shear * (1.0 + sp));
+        const double s3 = lame * I1 + shear * (e2 + e3) - lam_r * (2.0 * lame * sp - shear * (1.0 - sp));
 #pragma unroll
-            for (int i = 0; i < 6; ++i) S[i] = s1 * P1[i] + s3 * P23[i];
-            if (DS) {
-                double Dp[6];
+        for (int i = 0; i < 6; ++i) S[i] = s1 * P1[i] + s3 * P23[i];
+        if (DS) {
+            double Dp[6];
 #pragma unroll
-                for (int i = 0; i < 6; ++i)
-                    Dp[i] = shear * (2.0 * (1.0 + sin_phi) * P1[i] - (1.0 - sin_phi) * P23[i]) + 2.0 * lame * sin_phi * vol_iota(i);
-                const double em23 = e2 + e3;
-                const double inv_den = 1.0 / den_r;
+            for (int i = 0; i < 6; ++i)
+                Dp[i] = shear * (2.0 * (1.0 + sin_phi) * P1[i] - (1.0 - sin_phi) * P23[i]) + 2.0 * lame * sin_phi * vol_iota(i);
+            const double em23 = e2 + e3;
+            const double inv_den = 1.0 / d.den;
 #pragma unroll
-                for (int j = 0; j < 6; ++j) {
+            for (int j = 0; j < 6; ++j) {
 #pragma unroll
-                    for (int i = 0; i <= j; ++i) {
-                        const double idk = (i == j) ? half_ident(i) : 0.0;
-                        const double o11 = P1[i] * P1[j], oBB = P23[i] * P23[j];
-                        const double d1 = inv1 * (square_jac(p.t, i, j) - idk * em23 - (P23[i] * p.t[j] + p.t[i] * P23[j]) +
-                                                  em23 * oBB + (em23 - 2.0 * e1) * o11 + e1 * (P23[i] * P1[j] + P1[i] * P23[j]));
-                        const double v = (s1 - s3) * d1 + lame * vol_iota(i) * vol_iota(j) + shear * (2.0 * o11 + oBB) -
-                                         Dp[i] * Dp[j] * inv_den;
-                        store_sym(DS, i, j, v);
-                    }
+                for (int i = 0; i <= j; ++i) {
+                    const double idk = (i == j) ? half_ident(i) : 0.0;
+                    const double o11 = P1[i] * P1[j], oBB = P23[i] * P23[j];
+                    const double d1 = inv1 * (square_jac(p.t, i, j) - idk * em23 - (P23[i] * p.t[j] + p.t[i] * P23[j]) +
+                                              em23 * oBB + (em23 - 2.0 * e1) * o11 + e1 * (P23[i] * P1[j] + P1[i] * P23[j]));
+                    const double v = (s1 - s3) * d1 + lame * vol_iota(i) * vol_iota(j) + shear * (2.0 * o11 + oBB) -
+                                     Dp[i] * Dp[j] * inv_den;
+                    store_sym(DS, i, j, v);
                 }
             }
-            return kRight;
         }
+        return;
     }
-
-    const double sa = c_bar / (2.0 * sin_phi);
+    const double sa = m.c_bar / (2.0 * sin_phi);
 #pragma unroll
     for (int i = 0; i < 3; ++i) S[i] = sa;
 #pragma unroll
@@ -266,7 +299,37 @@ __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double 
 #pragma unroll
         for (int k = 0; k < 36; ++k) DS[k] = 0.0;
     }
-    return kApex;
+}
+
+// Returns the branch code.  DS may be null (stress only).
+__device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
+                          double *DS) {
+    Principal3 p;
+    principal3(E, p);
+    const Mat3 m{c_bar, sin_phi, shear, lame};
+    const Decision3 d = decide3(p, m);
+    finish3(p, d, m, S, DS);
+    return d.branch;
+}
+
+__device__ __forceinline__ void load6(const double *A, long long p, double *e) {
+    const double2 *A2 = reinterpret_cast<const double2 *>(A + 6 * p);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double2 v = A2[k];
+        e[2 * k] = v.x;
+        e[2 * k + 1] = v.y;
+    }
+}
+__device__ __forceinline__ void store6(double *A, long long p, const double *s) {
+    double2 *A2 = reinterpret_cast<double2 *>(A + 6 * p);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) A2[k] = make_double2(s[2 * k], s[2 * k + 1]);
+}
+__device__ __forceinline__ void store36(double *A, long long p, const double *s) {
+    double2 *A2 = reinterpret_cast<double2 *>(A + 36 * p);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) A2[k] = make_double2(s[2 * k], s[2 * k + 1]);
 }
 
 template <bool TANGENT>
@@ -276,29 +339,94 @@ __global__ void __launch_bounds__(128) mc3d_kernel(const double *__restrict__ E,
                                                    double *__restrict__ DS, int8_t *__restrict__ branch) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    double e[6];
-    const double2 *E2 = reinterpret_cast<const double2 *>(E + 6ll * p);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double2 v = E2[k];
-        e[2 * k] = v.x;
-        e[2 * k + 1] = v.y;
-    }
-    double s[6];
+    double e[6], s[6];
+    load6(E, p, e);
     int b;
     if (TANGENT) {
         double ds[36];
         b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
-        double2 *D2 = reinterpret_cast<double2 *>(DS + 36ll * p);
-#pragma unroll
-        for (int k = 0; k < 18; ++k) D2[k] = make_double2(ds[2 * k], ds[2 * k + 1]);
+        store36(DS, p, ds);
     } else {
         b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, nullptr);
     }
-    double2 *S2 = reinterpret_cast<double2 *>(S + 6ll * p);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) S2[k] = make_double2(s[2 * k], s[2 * k + 1]);
+    store6(S, p, s);
     if (branch) branch[p] = static_cast<int8_t>(b);
+}
+
+// Two-pass return mapping, pass A: every point's branch is decided; elastic and apex points are
+// finished here (they carry no branch-specific tangent work), and the points of the smooth,
+// left-edge and right-edge branches are appended to three lists in scratch memory
+// (scratch[0..2] = counters, then three lists of n entries) with warp-aggregated atomics.
+__global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
+                                                       const double *__restrict__ sin_phi,
+                                                       const double *__restrict__ shear, const double *__restrict__ lame,
+                                                       int n, double *__restrict__ S, double *__restrict__ DS,
+                                                       int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    int list_id = -1;
+    if (p < n) {
+        double e[6];
+        load6(E, p, e);
+        Principal3 pr;
+        principal3(e, pr);
+        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
+        const Decision3 d = decide3(pr, m);
+        branch[p] = static_cast<int8_t>(d.branch);
+        if (d.branch == kElastic || d.branch == kApex) {
+            double s[6], ds[36];
+            finish3(pr, d, m, s, ds);
+            store6(S, p, s);
+            store36(DS, p, ds);
+        } else {
+            list_id = d.branch - 1;
+        }
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    int32_t *lists = scratch + 4;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const unsigned mask = __ballot_sync(0xffffffffu, list_id == k);
+        if (mask == 0u) continue;
+        const int leader = __ffs(mask) - 1;
+        int base = 0;
+        if ((int)lane == leader) base = atomicAdd(scratch + k, __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (list_id == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
+    }
+}
+
+// Pass B: the points of one plastic branch per blockIdx.y, read from its list, so every warp runs
+// one branch's tangent code.  The branch is taken from pass A, not re-decided.
+__global__ void __launch_bounds__(128) mc3d_plastic_kernel(const double *__restrict__ E,
+                                                           const double *__restrict__ c_bar,
+                                                           const double *__restrict__ sin_phi,
+                                                           const double *__restrict__ shear,
+                                                           const double *__restrict__ lame, int n,
+                                                           double *__restrict__ S, double *__restrict__ DS,
+                                                           const int32_t *__restrict__ scratch) {
+    const int k = blockIdx.y;
+    const int cnt = scratch[k];
+    const int32_t *list = scratch + 4 + (long long)k * n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const int p = list[i];
+        if (p < 0 || p >= n) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        double e[6];
+        load6(E, p, e);
+        Principal3 pr;
+        principal3(e, pr);
+        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
+        Decision3 d{k + 1, 0.0, 1.0};
+        if (k == 0) smooth_lam(pr, m, trial_yield(pr, m), d.lam, d.den);
+        else if (k == 1) left_lam(pr, m, d.lam, d.den);
+        else right_lam(pr, m, d.lam, d.den);
+        double s[6], ds[36];
+        finish3(pr, d, m, s, ds);
+        store6(S, p, s);
+        store36(DS, p, ds);
+    }
 }
 
 // ---------------------------------------------------------------------------- 2D
@@ -481,28 +609,36 @@ __global__ void reduction_kernel(const double *__restrict__ c0, const double *__
                                  double *__restrict__ sin_phi) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const double f = phi[p], y = psi[p], c = c0[p];
-    double c_l, phi_l;
+    // The reference evaluates atan/cos/sin chains; the same quantities follow from tangents
+    // alone: for a = atan(t), cos a = 1/sqrt(1+t^2) and sin a = t/sqrt(1+t^2) (|a| < pi/2).  This
+    // needs two sincos per point instead of seven transcendental calls.
+    const double c = c0[p];
+    double sf, cf, sy, cy;
+    sincos(phi[p], &sf, &cf);
+    sincos(psi[p], &sy, &cy);
+    double c_l, T;  // c_lambda and tan(phi_lambda)
     if (davis == 0) {  // A
-        const double beta = cos(f) * cos(y) / (1.0 - sin(f) * sin(y));
+        const double beta = cf * cy / (1.0 - sf * sy);
         c_l = beta * c / lam;
-        phi_l = atan(beta * tan(f) / lam);
-    } else if (davis == 1) {  // B
-        const double c1 = c / lam;
-        const double f1 = atan(tan(f) / lam);
-        const double y1 = atan(tan(y) / lam);
-        const double beta = cos(f1) * cos(y1) / (1.0 - sin(f1) * sin(y1));
-        c_l = beta * c1;
-        phi_l = atan(beta * tan(f1));
-    } else {  // C
-        const double c1 = c / lam;
-        const double f1 = atan(tan(f) / lam);
-        const double beta = f1 > y ? cos(f1) * cos(y) / (1.0 - sin(f1) * sin(y)) : 1.0;
-        c_l = beta * c1;
-        phi_l = atan(beta * tan(f1));
+        T = beta * (sf / cf) / lam;
+    } else {
+        const double t1 = (sf / cf) / lam;  // tan(phi1)
+        const double rf = rsqrt(1.0 + t1 * t1);
+        const double c1f = rf, s1f = t1 * rf;  // cos, sin of phi1
+        double beta;
+        if (davis == 1) {  // B
+            const double u1 = (sy / cy) / lam;  // tan(psi1)
+            const double ry = rsqrt(1.0 + u1 * u1);
+            beta = c1f * ry / (1.0 - s1f * (u1 * ry));
+        } else {  // C: phi1 > psi  <=>  tan(phi1) > tan(psi) on (-pi/2, pi/2)
+            beta = t1 > sy / cy ? c1f * cy / (1.0 - s1f * sy) : 1.0;
+        }
+        c_l = beta * (c / lam);
+        T = beta * t1;
     }
-    c_bar[p] = 2.0 * c_l * cos(phi_l);
-    sin_phi[p] = sin(phi_l);
+    const double rT = rsqrt(1.0 + T * T);
+    c_bar[p] = 2.0 * c_l * rT;
+    sin_phi[p] = T * rT;
 }
 
 }  // namespace
@@ -542,6 +678,28 @@ int ssp_constitutive_3d_branch(const double *E, const double *c_bar, const doubl
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !branch_out) return SSP_ERR_INVALID;
     mc3d_kernel<false><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
                                                                              nullptr, branch_out);
+    return launch_status();
+}
+
+int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                                   int32_t *scratch, void *stream) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+        return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                          branch_out, scratch);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long gx = (long long)sms * 8;
+    const long long need = (n_int + 127) / 128;
+    if (gx > need) gx = need;
+    mc3d_plastic_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                             DS_out, scratch);
     return launch_status();
 }
 

@@ -138,6 +138,10 @@ class ConstitutiveOperator:
         self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
         self._K_el = None  # elastic tangent CSR values (device), built on first use
         self._dev = None
+        # 3D tangents through the two-pass, branch-binned return mapping (same results as the
+        # single-pass kernel); False selects the single-pass kernel
+        self.binned_return_mapping = True
+        self._scratch = None
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
         self._owned_unique_c_bar = None
@@ -280,7 +284,14 @@ class ConstitutiveOperator:
         args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                 _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
         branch = None
-        if tangent:
+        if tangent and pat.dim == 3 and self.binned_return_mapping:
+            branch = t.empty(n, dtype=t.int8, device="cuda")
+            if self._scratch is None or self._scratch.numel() < 3 * n + 4:
+                self._scratch = t.empty(3 * n + 4, dtype=t.int32, device="cuda")
+            _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
+                      _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
+                      _lib.ptr(DS), _lib.ptr(branch), _lib.ptr(self._scratch), st)
+        elif tangent:
             branch = t.empty(n, dtype=t.int8, device="cuda")
             _lib.call("ssp_constitutive_sds_branch", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
                       _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),

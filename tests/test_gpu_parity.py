@@ -81,6 +81,49 @@ def test_constitutive_3d_matches_oracle_on_many_points(oracle):
     assert rel_err(DS, DS_o) <= PLAIN_RTOL
 
 
+def test_binned_return_mapping_matches_single_pass_and_oracle(oracle):
+    """Two-pass, branch-binned kernel == single-pass kernel == oracle, on points of every branch."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    rng = np.random.default_rng(77)
+    n = 150_000
+    E = rng.standard_normal((n, 6)) * np.repeat(np.array([1e-4, 1e-3, 3e-3]), n // 3)[:, None]
+    g = golden("constitutive_3d.npz")
+    E = np.vstack([E, g["E"]])
+    n = E.shape[0]
+    young, nu = 2.0e4, 0.49
+    shear = np.full(n, young / (2 * (1 + nu)))
+    lame = np.full(n, young / (3 * (1 - 2 * nu))) - 2 * shear / 3
+    c_bar, sin_phi = oracle.reduction(np.full(n, 6.0), np.full(n, np.deg2rad(45.0)), np.zeros(n), 1.1, "B")
+    Ed, cb, sp, G, L = (_dev(a) for a in (E, c_bar, sin_phi, shear, lame))
+    outs = {}
+    for mode in ("single", "binned"):
+        S = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+        DS = torch.empty((n, 36), dtype=torch.float64, device="cuda")
+        br = torch.empty(n, dtype=torch.int8, device="cuda")
+        if mode == "single":
+            _lib.call("ssp_constitutive_sds_branch", 3, _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G), _lib.ptr(L),
+                      n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.stream_handle())
+        else:
+            scratch = torch.full((3 * n + 4,), -7, dtype=torch.int32, device="cuda")
+            _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G),
+                      _lib.ptr(L), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch), _lib.stream_handle())
+            counts = scratch[:3].cpu().numpy()
+            b = br.cpu().numpy()
+            assert list(counts) == [int((b == k).sum()) for k in (1, 2, 3)]
+        outs[mode] = (S.cpu().numpy(), DS.cpu().numpy(), br.cpu().numpy())
+    assert np.array_equal(outs["single"][2], outs["binned"][2])
+    seen = set(np.unique(outs["binned"][2]).tolist())
+    assert {0, 1, 4} <= seen and seen & {2, 3}
+    assert rel_err(outs["binned"][0], outs["single"][0]) <= 1e-15
+    assert rel_err(outs["binned"][1], outs["single"][1]) <= 1e-15
+    S_o, DS_o = oracle.constitutive_3d(E, c_bar, sin_phi, shear, shear, lame)
+    assert rel_err(outs["binned"][0], S_o) <= PLAIN_RTOL
+    assert rel_err(outs["binned"][1], DS_o) <= PLAIN_RTOL
+
+
 def test_branch_labels_match_tangent_structure():
     import torch
 
