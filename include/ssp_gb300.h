@@ -35,7 +35,8 @@ enum ssp_status {
     SSP_ERR_CUDA = 2,        /* a CUDA call or launch failed */
     SSP_ERR_UNSUPPORTED = 3, /* element type / quadrature combination without a kernel */
     SSP_ERR_OVERFLOW = 4,    /* an index does not fit int32 (distributed_tangent.py:122-124) */
-    SSP_ERR_PATTERN = 5      /* structural entry missing from the pattern (distributed_tangent.py:431-432) */
+    SSP_ERR_PATTERN = 5,     /* structural entry missing from the pattern (distributed_tangent.py:431-432) */
+    SSP_ERR_TOO_LARGE = 6    /* more points than the fixed scratch of the no-allocation entry point holds */
 };
 
 /* bits of the device status word */
@@ -77,6 +78,26 @@ int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, c
 int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
                                    int32_t *scratch, void *stream);
+
+/* No counterpart in the reference.  ssp_constitutive_3d_sds_binned for callers that cannot
+ * allocate device memory, e.g. a constitutive hook called from inside another solver's assembly
+ * loop: it is handed device pointers to its inputs and outputs only, the host framework owns and
+ * budgets all device memory, and a cudaMalloc there would also synchronise the device mid-loop.
+ * The caller passes inputs and outputs as for ssp_constitutive_3d_sds_binned, but no scratch:
+ * the point lists live in a fixed array inside this library (static device memory of
+ * 4 + 3*SSP_NOALLOC_MAX_POINTS int32, about 24 MiB, which every GPU that loads the library holds
+ * until the process exits).  Nothing is allocated: no cudaMalloc, cudaFree or allocating library
+ * call.
+ *   - n_int above SSP_NOALLOC_MAX_POINTS returns SSP_ERR_TOO_LARGE before any work.
+ *   - The first call on each device looks up the array's device address (cudaGetSymbolAddress,
+ *     with that device current) and caches it; make that first call before any stream capture.
+ *   - Every call on a device shares the one array and leaves the last call's lists in it; the
+ *     counters are cleared at the start of each call.  Calls that overlap on the GPU (different
+ *     streams, or host threads sharing a device) race on the array: serialise them. */
+#define SSP_NOALLOC_MAX_POINTS 2097152
+int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar, const double *sin_phi,
+                                           const double *shear, const double *lame, int n_int, double *S_out,
+                                           double *DS_out, int8_t *branch_out, void *stream);
 
 /* Replaces constitutive_problem_2D (src/slope_stability/constitutive/problem.py:143-475), which the
  * reference has only in NumPy: E [n_int][3] -> S [n_int][4] ([s11,s22,s12,s33]), DS [n_int][9]

@@ -13,6 +13,8 @@
 // decided before any tangent work starts.
 #include <math.h>
 
+#include <mutex>
+
 #include "ssp_internal.cuh"
 
 namespace ssp {
@@ -641,6 +643,29 @@ __global__ void reduction_kernel(const double *__restrict__ c0, const double *__
     sin_phi[p] = T * rT;
 }
 
+// Fixed scratch of ssp_constitutive_3d_sds_binned_noalloc: four counters, then three point lists
+// of SSP_NOALLOC_MAX_POINTS entries (24 MiB + 16 B per GPU, for the life of the process).
+static __device__ __align__(256) int32_t g_fixed_scratch[4 + 3 * SSP_NOALLOC_MAX_POINTS];
+
+constexpr int kMaxDevices = 128;
+std::mutex g_fixed_mutex;
+int32_t *g_fixed_ptr[kMaxDevices] = {};
+
+// Device address of g_fixed_scratch on the current device.  In host code the symbol's name is a
+// host-side stand-in, not a device address, so it is looked up once per device (with that device
+// current) and cached; nullptr on failure.
+int32_t *fixed_scratch_for_current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_fixed_mutex);
+    if (!g_fixed_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_fixed_scratch) != cudaSuccess || !p) return nullptr;
+        g_fixed_ptr[dev] = static_cast<int32_t *>(p);
+    }
+    return g_fixed_ptr[dev];
+}
+
 }  // namespace
 }  // namespace ssp
 
@@ -689,6 +714,37 @@ int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const d
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
         return SSP_ERR_INVALID;
     cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                          branch_out, scratch);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long gx = (long long)sms * 8;
+    const long long need = (n_int + 127) / 128;
+    if (gx > need) gx = need;
+    mc3d_plastic_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                             DS_out, scratch);
+    return launch_status();
+}
+
+// Same two-pass return mapping for callers that have no way to allocate device memory: a
+// constitutive hook called from inside another solver's assembly loop that is handed device
+// pointers to its inputs and outputs only, with all device memory owned and budgeted by the
+// host framework (an allocation there would also synchronise the device in the middle of the
+// loop).  Its point lists live in the fixed array below, which every GPU that loads this
+// library holds until the process exits.
+int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar, const double *sin_phi,
+                                           const double *shear, const double *lame, int n_int, double *S_out,
+                                           double *DS_out, int8_t *branch_out, void *stream) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int > SSP_NOALLOC_MAX_POINTS) return SSP_ERR_TOO_LARGE;
+    if (n_int == 0) return SSP_OK;
+    if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out) return SSP_ERR_INVALID;
+    int32_t *scratch = fixed_scratch_for_current_device();
+    if (!scratch) return SSP_ERR_CUDA;
+    cudaStream_t st = as_stream(stream);
+    // the counters must start at zero on every call; the lists are written before they are read
     if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
     mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
                                                           branch_out, scratch);
