@@ -331,6 +331,8 @@ CONFIGS = {
     "3d_p2_hetero": dict(dim=3, elem_type="P2", nx=64, ny=26, nz=40, n_layers=4, amplitude=0.003),  # 399,360 tets
     "3d_p4_hetero": dict(dim=3, elem_type="P4", nx=30, ny=12, nz=23, n_layers=4, amplitude=0.003),  # 49,680 tets
     "3d_p2_large": dict(dim=3, elem_type="P2", nx=110, ny=44, nz=70, n_layers=4, amplitude=0.003),  # 2,032,800 tets
+    # a smaller copy of 3d_p2_homo for detailed profiles (still larger than L2 per step)
+    "3d_p2_profile": dict(dim=3, elem_type="P2", nx=20, ny=8, nz=20, n_layers=1, amplitude=0.0157),  # 19,200 tets
 }
 
 
