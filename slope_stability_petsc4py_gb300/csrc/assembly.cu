@@ -406,6 +406,134 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
     }
 }
 
+// Warp-per-element variant for small elements (n_ld * (n_ld + 1) / 2 <= 32 * 16 and n_q <= 32):
+// WARPS independent warps per CTA, each with its own shared-memory slice, grid-striding over
+// elements.  In correction mode a warp reads the element's branch codes with one coalesced load
+// and a ballot, so an all-elastic element costs a few instructions and no shared-memory traffic.
+// Same arithmetic and scatter as tangent_element_kernel.
+template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR>
+__global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(ElemArgs A) {
+    constexpr int NS = DIM == 3 ? 6 : 3;
+    constexpr int NLD = DIM * NP;
+    constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
+    constexpr int PER = (NENT + 31) / 32;
+    static_assert(NQ <= 32, "one branch code per lane");
+    __shared__ double sg_all[WARPS][NQ][DIM][NP];
+    __shared__ double sD_all[WARPS][NQ][NS * NS];
+    __shared__ double sH_all[WARPS][NLD * NS];
+    __shared__ int sq_all[WARPS][NQ];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double(*sg)[DIM][NP] = sg_all[wid];
+    double(*sD)[NS * NS] = sD_all[wid];
+    double *sH = sH_all[wid];
+    int *sq = sq_all[wid];
+
+    int code[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int id = lane + i * 32;
+        int c = -1;
+        if (id < NENT) {
+            int a, b;
+            if (SYM) {
+                int rem = id;
+                a = 0;
+                while (rem >= NLD - a) {
+                    rem -= NLD - a;
+                    ++a;
+                }
+                b = a + rem;
+            } else {
+                a = id / NLD;
+                b = id % NLD;
+            }
+            c = a | (b << 8);
+        }
+        code[i] = c;
+    }
+
+    const long long warp_global = (long long)blockIdx.x * WARPS + wid;
+    const long long warp_count = (long long)gridDim.x * WARPS;
+    for (long long e = warp_global; e < A.n_elem; e += warp_count) {
+        const long long g0 = e * NQ;
+        bool mine = lane < NQ;
+        if (CORR && mine) mine = A.branch[g0 + lane] != 0;
+        const unsigned qmask = __ballot_sync(0xffffffffu, mine);
+        if (qmask == 0u) continue;  // warp-uniform
+        const int nq = __popc(qmask);
+        __syncwarp();  // the previous element of this warp is done with the shared slice
+        if (mine) sq[__popc(qmask & ((1u << lane) - 1u))] = lane;  // compact list of contributing points
+        __syncwarp();
+        for (int i = lane; i < nq * NP; i += 32) {
+            const int k = i / NP, a = i % NP;
+            const long long src = (g0 + sq[k]) * NP + a;
+            sg[k][0][a] = A.d1[src];
+            sg[k][1][a] = A.d2[src];
+            if (DIM == 3) sg[k][DIM - 1][a] = A.d3[src];
+        }
+        for (int i = lane; i < nq * NS * NS; i += 32) {
+            const int k = i / (NS * NS), kk = i % (NS * NS);
+            const long long g = g0 + sq[k];
+            double v = A.DS[g * (NS * NS) + kk];
+            if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, A.shear[g], A.lame[g]));
+            sD[k][kk] = A.w[g] * v;
+        }
+        double acc[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) acc[i] = 0.0;
+        __syncwarp();
+        for (int q = 0; q < nq; ++q) {
+            for (int it = lane; it < NLD * NS; it += 32) {
+                const int alpha = it / NS, m = it % NS;
+                const int a = alpha / DIM, c = alpha % DIM;
+                double h = 0.0;
+#pragma unroll
+                for (int r = 0; r < DIM; ++r) {
+                    const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
+                    h += sg[q][r][a] * sD[q][k + NS * m];
+                }
+                sH[it] = h;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const int c = code[i];
+                if (c >= 0) {
+                    const int alpha = c & 0xff, beta = c >> 8;
+                    const int b = beta / DIM, cp = beta % DIM;
+                    double v = acc[i];
+#pragma unroll
+                    for (int r = 0; r < DIM; ++r) {
+                        const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
+                        v += sH[alpha * NS + m] * sg[q][r][b];
+                    }
+                    acc[i] = v;
+                }
+            }
+            __syncwarp();
+        }
+        const int32_t *em = A.emap + e * NLD * NLD;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int c = code[i];
+            if (c < 0) continue;
+            const int alpha = c & 0xff, beta = c >> 8;
+            const int32_t p = em[alpha * NLD + beta];
+            if (p >= 0) {
+                if (p < A.nnz) atomicAdd(A.values + p, acc[i]);
+                else flag(SSP_DEV_BAD_INDEX);
+            }
+            if (SYM && alpha != beta) {
+                const int32_t p2 = em[beta * NLD + alpha];
+                if (p2 >= 0) {
+                    if (p2 < A.nnz) atomicAdd(A.values + p2, acc[i]);
+                    else flag(SSP_DEV_BAD_INDEX);
+                }
+            }
+        }
+    }
+}
+
 // Per-point elastic tangent of the return mapping (for assembling the elastic tangent once).
 template <int DIM>
 __global__ void elastic_blocks_kernel(const double *__restrict__ shear, const double *__restrict__ lame, int n,
@@ -468,9 +596,26 @@ int launch_element(const ElemArgs &a, cudaStream_t st) {
     return launch_status();
 }
 
+template <int DIM, int NP, int NQ, bool SYM, bool CORR>
+int launch_element_warp(const ElemArgs &a, cudaStream_t st) {
+    constexpr int WARPS = 4;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR>,
+                                                  32 * WARPS, 0);
+    if (per_sm < 1) per_sm = 1;
+    long long grid = (long long)sms * per_sm;
+    const long long need = (a.n_elem + WARPS - 1) / WARPS;
+    if (grid > need) grid = need;
+    tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR><<<static_cast<unsigned>(grid), 32 * WARPS, 0, st>>>(a);
+    return launch_status();
+}
+
 template <bool SYM, bool CORR>
 int dispatch_element(int dim, int n_p, int n_q, const ElemArgs &a, cudaStream_t st) {
-    if (dim == 3 && n_p == 10 && n_q == 11) return launch_element<3, 10, 11, 32, SYM, CORR>(a, st);
+    if (dim == 3 && n_p == 10 && n_q == 11) return launch_element_warp<3, 10, 11, SYM, CORR>(a, st);
     if (dim == 3 && n_p == 35 && n_q == 24) return launch_element<3, 35, 24, 256, SYM, CORR>(a, st);
     if (dim == 3 && n_p == 4 && n_q == 1) return launch_element<3, 4, 1, 32, SYM, CORR>(a, st);
     if (dim == 2 && n_p == 6 && n_q == 7) return launch_element<2, 6, 7, 32, SYM, CORR>(a, st);

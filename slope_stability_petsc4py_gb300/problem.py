@@ -189,6 +189,13 @@ class ConstitutiveOperator:
             idx = np.asarray(pattern.local_int_indices, dtype=np.int64)
             pick = lambda a: _lib.to_device(np.ascontiguousarray(np.asarray(a, dtype=np.float64)[idx]), t.float64)  # noqa
             self._dev = {k: pick(getattr(self, k)) for k in ("c0", "phi", "psi", "shear", "bulk", "lame")}
+            # The reduction of a point depends only on its (c0, phi, psi).  Soils come in a few
+            # materials, so the distinct triples are reduced once and expanded to the points.
+            trip = np.stack([np.asarray(getattr(self, k), dtype=np.float64)[idx] for k in ("c0", "phi", "psi")], axis=1)
+            uniq, inv = np.unique(trip, axis=0, return_inverse=True)
+            if uniq.shape[0] <= 4096:
+                self._dev["red_unique"] = [_lib.to_device(np.ascontiguousarray(uniq[:, k]), t.float64) for k in range(3)]
+                self._dev["red_index"] = _lib.to_device(inv.reshape(-1).astype(np.int32), t.int32)
 
     def set_bddc_subdomain_pattern(self, pattern) -> None:
         raise NotImplementedError("BDDC subdomain assembly is outside the GPU hot path")
@@ -256,8 +263,19 @@ class ConstitutiveOperator:
         cb = t.empty(n, dtype=t.float64, device="cuda")
         sp = t.empty(n, dtype=t.float64, device="cuda")
         d = self._dev
-        _lib.call("ssp_reduction", _lib.ptr(d["c0"]), _lib.ptr(d["phi"]), _lib.ptr(d["psi"]), n, float(lam),
-                  davis.encode(), _lib.ptr(cb), _lib.ptr(sp), _lib.stream_handle())
+        st = _lib.stream_handle()
+        if "red_unique" in d:
+            c0u, phu, psu = d["red_unique"]
+            m = int(c0u.numel())
+            cbu = t.empty(m, dtype=t.float64, device="cuda")
+            spu = t.empty(m, dtype=t.float64, device="cuda")
+            _lib.call("ssp_reduction", _lib.ptr(c0u), _lib.ptr(phu), _lib.ptr(psu), m, float(lam), davis.encode(),
+                      _lib.ptr(cbu), _lib.ptr(spu), st)
+            _lib.call("ssp_gather", _lib.ptr(cbu), _lib.ptr(d["red_index"]), n, _lib.ptr(cb), st)
+            _lib.call("ssp_gather", _lib.ptr(spu), _lib.ptr(d["red_index"]), n, _lib.ptr(sp), st)
+        else:
+            _lib.call("ssp_reduction", _lib.ptr(d["c0"]), _lib.ptr(d["phi"]), _lib.ptr(d["psi"]), n, float(lam),
+                      davis.encode(), _lib.ptr(cb), _lib.ptr(sp), st)
         self._owned_overlap_c_bar, self._owned_overlap_sin_phi = cb, sp
         self._owned_unique_c_bar, self._owned_unique_sin_phi = cb, sp
         self.c_bar = None
