@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="3d_p2_homo")
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"],
+                    help="plain: FP64 tangent (the drop-in); mixed: FP32 plastic-point products")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
@@ -254,10 +256,13 @@ def algorithmic(name, st):
         return {"bytes": 40 * n, "flops": 0}
     if name == "ssp_gather":
         return {"bytes": 20 * st["n_u"], "flops": 0}
-    if name == "ssp_tangent_plastic_correction":
+    if name.startswith("ssp_tangent_plastic_correction"):
         npl, npe = st["n_plastic"], st["n_plastic_el"]
+        fp64 = npl * 2.0 * nld * ns * dim  # H = B^T (w D): FP64 in both forms
+        if not name.endswith("_mixed"):
+            fp64 += npl * 2.0 * nld * (nld + 1) // 2 * dim  # the B^T H products
         return {"bytes": n + npl * (8 * ns * ns + 8 * dim * n_p + 24) + npe * (4 * nld * nld + 16 * nld * nld),
-                "flops": npl * 2.0 * (nld * ns * dim + nld * (nld + 1) // 2 * dim)}
+                "flops": fp64}
     return {"bytes": 0, "flops": 0}
 
 
@@ -282,6 +287,7 @@ def run_gpu(args):
     n_int, nnz = pat.n_local_int, pat.nnz
     U_dev = torch.as_tensor(U, device="cuda")
     op.host_outputs = False
+    op.tangent_form = args.form
 
     def step():
         op.reduction(LAMBDA)
@@ -328,14 +334,24 @@ def run_gpu(args):
     alg = algorithmic(dominant, stats)
     k_ms = kernels[dominant]["ms_per_launch"]
     achieved_gbs = alg["bytes"] / (k_ms * 1e-3) / 1e9
-    corr = "ssp_tangent_plastic_correction"
+    corr = "ssp_tangent_plastic_correction" + ("_mixed" if args.form == "mixed" and pat.n_p <= 10 else "")
+    tangent_err = None
+    if args.form == "mixed":  # tangent error of this form against the FP64 form, same state
+        op.tangent_form = "plain"
+        kp = op.build_K_regularized(R_REG).values.clone()
+        op.tangent_form = "mixed"
+        km = op.build_K_regularized(R_REG).values
+        tangent_err = {"max_norm_rel": float((km - kp).abs().max() / kp.abs().max()),
+                       "frobenius_rel": float(torch.linalg.norm(km - kp) / torch.linalg.norm(kp))}
     fl = algorithmic(corr, stats)["flops"]
     corr_ms = kernels.get(corr, {}).get("ms_per_launch")
     line = {
         "metric": METRIC, "value": world * n_int / (ms * 1e-3), "unit": "quad-pts/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": "plain",
+        "tangent_error_vs_fp64": tangent_err,
+        "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": args.form,
+                   "plastic_elements": stats["n_plastic_el"],
                    "step": "reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + "
                            "constrained diagonals + regularised blend",
                    "plastic_fraction": stats["n_plastic"] / n_int,

@@ -182,6 +182,18 @@ int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *d
                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
                                    long long nnz_out, double scale, double *out_values, void *stream);
 
+/* Mixed-precision form of ssp_tangent_plastic_correction (P1/P2 elements): H = B^T (w * scale *
+ * (DS - D_el)) is formed in FP64 and split into FP32 hi + lo parts; the products B^T H are taken
+ * and accumulated in FP32 per element; the element sums are added to the FP64 CSR values with
+ * FP64 atomics.  The return mapping that produced DS (eigendecomposition, branch tests, plastic
+ * multipliers) is FP64.  Relative error of the assembled tangent against the FP64 form is about
+ * 1e-7 (tested <= 1e-6).  No reference counterpart: the reference assembles in FP64 only. */
+int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                                         const double *ds, const double *weight, const int8_t *branch,
+                                         const double *shear, const double *lame, const int32_t *scatter_map,
+                                         int n_elem, int n_p, int n_q, long long nnz_out, double scale,
+                                         double *out_values, void *stream);
+
 /* Per-point elastic tangent blocks [n_int][n_s*n_s] of the return mapping's elastic branch. */
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
                                void *stream);

@@ -15,6 +15,8 @@
 // Layout (all FP64 unless stated): points are element-major (g = e*n_q + q); dphi arrays are
 // [n_int][n_p]; strains/stresses/tangents are per-point AoS ([n_int][6], [n_int][36]), which is
 // the reference's C layout and makes each element's data one contiguous block.
+#include <type_traits>
+
 #include "ssp_internal.cuh"
 
 namespace ssp {
@@ -406,27 +408,52 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
     }
 }
 
-// Warp-per-element variant for small elements (n_ld * (n_ld + 1) / 2 <= 32 * 16 and n_q <= 32):
-// WARPS independent warps per CTA, each with its own shared-memory slice, grid-striding over
-// elements.  In correction mode a warp reads the element's branch codes with one coalesced load
-// and a ballot, so an all-elastic element costs a few instructions and no shared-memory traffic.
-// Same arithmetic and scatter as tangent_element_kernel.
-template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR>
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Warp-per-element variant for small elements (n_q <= 32): WARPS independent warps per CTA, each
+// with its own shared-memory slice, grid-striding over elements.  In correction mode a warp reads
+// the element's branch codes with one coalesced load and a ballot, so an all-elastic element
+// costs a few instructions and no shared-memory traffic.  The element's row of the element->CSR
+// map is fetched into shared memory asynchronously (cp.async) while the products are formed.
+//
+// MIXED (mixed-precision form; correction mode only): H = B^T (w D) is formed in FP64 as in the
+// plain kernel, split into FP32 hi + lo parts (hi = fl32(H), lo = fl32(H - hi)), and the products
+// B^T H are taken and accumulated in FP32; the per-element sums are added to the FP64 CSR values
+// with FP64 atomics.  Otherwise the arithmetic and scatter are those of tangent_element_kernel.
+template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR, bool MIXED>
 __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
     constexpr int PER = (NENT + 31) / 32;
+    constexpr int MAPV = NLD * NLD / 4;  // 16-byte chunks of one element's map row
     static_assert(NQ <= 32, "one branch code per lane");
+    static_assert((NLD * NLD) % 4 == 0, "map rows are whole 16-byte chunks");
+    using acc_t = typename std::conditional<MIXED, float, double>::type;
     __shared__ double sg_all[WARPS][NQ][DIM][NP];
     __shared__ double sD_all[WARPS][NQ][NS * NS];
-    __shared__ double sH_all[WARPS][NLD * NS];
+    __shared__ double sH_all[WARPS][MIXED ? 1 : NLD * NS];
+    __shared__ float sHh_all[WARPS][MIXED ? NLD * NS : 1];
+    __shared__ float sHl_all[WARPS][MIXED ? NLD * NS : 1];
+    __shared__ float sgf_all[WARPS][MIXED ? NQ : 1][DIM][NP];
+    __shared__ __align__(16) int32_t smap_all[WARPS][NLD * NLD];
+    __shared__ double spt_all[WARPS][3][NQ];  // w, shear, lame of the contributing points
     __shared__ int sq_all[WARPS][NQ];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     double(*sg)[DIM][NP] = sg_all[wid];
     double(*sD)[NS * NS] = sD_all[wid];
     double *sH = sH_all[wid];
+    float *sHh = sHh_all[wid];
+    float *sHl = sHl_all[wid];
+    float(*sgf)[DIM][NP] = sgf_all[wid];
+    int32_t *smap = smap_all[wid];
+    double(*spt)[NQ] = spt_all[wid];
     int *sq = sq_all[wid];
+    const bool map_aligned = (reinterpret_cast<uintptr_t>(A.emap) & 15u) == 0;
 
     int code[PER];
 #pragma unroll
@@ -462,25 +489,48 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
         if (qmask == 0u) continue;  // warp-uniform
         const int nq = __popc(qmask);
         __syncwarp();  // the previous element of this warp is done with the shared slice
-        if (mine) sq[__popc(qmask & ((1u << lane) - 1u))] = lane;  // compact list of contributing points
+        const int32_t *em = A.emap + e * NLD * NLD;
+        if (map_aligned) {
+            for (int i = lane; i < MAPV; i += 32) cp_async16(smap + 4 * i, em + 4 * i);
+        } else {
+            for (int i = lane; i < NLD * NLD; i += 32) smap[i] = em[i];
+        }
+        if (mine) {
+            const int k = __popc(qmask & ((1u << lane) - 1u));  // compact list of contributing points
+            sq[k] = lane;
+            spt[0][k] = A.w[g0 + lane];
+            if (CORR) {
+                spt[1][k] = A.shear[g0 + lane];
+                spt[2][k] = A.lame[g0 + lane];
+            }
+        }
         __syncwarp();
         for (int i = lane; i < nq * NP; i += 32) {
             const int k = i / NP, a = i % NP;
             const long long src = (g0 + sq[k]) * NP + a;
-            sg[k][0][a] = A.d1[src];
-            sg[k][1][a] = A.d2[src];
-            if (DIM == 3) sg[k][DIM - 1][a] = A.d3[src];
+            const double x = A.d1[src], y = A.d2[src];
+            sg[k][0][a] = x;
+            sg[k][1][a] = y;
+            if (MIXED) {
+                sgf[k][0][a] = static_cast<float>(x);
+                sgf[k][1][a] = static_cast<float>(y);
+            }
+            if (DIM == 3) {
+                const double z = A.d3[src];
+                sg[k][DIM - 1][a] = z;
+                if (MIXED) sgf[k][DIM - 1][a] = static_cast<float>(z);
+            }
         }
         for (int i = lane; i < nq * NS * NS; i += 32) {
             const int k = i / (NS * NS), kk = i % (NS * NS);
             const long long g = g0 + sq[k];
             double v = A.DS[g * (NS * NS) + kk];
-            if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, A.shear[g], A.lame[g]));
-            sD[k][kk] = A.w[g] * v;
+            if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, spt[1][k], spt[2][k]));
+            sD[k][kk] = spt[0][k] * v;
         }
-        double acc[PER];
+        acc_t acc[PER];
 #pragma unroll
-        for (int i = 0; i < PER; ++i) acc[i] = 0.0;
+        for (int i = 0; i < PER; ++i) acc[i] = acc_t(0);
         __syncwarp();
         for (int q = 0; q < nq; ++q) {
             for (int it = lane; it < NLD * NS; it += 32) {
@@ -492,7 +542,13 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
                     const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
                     h += sg[q][r][a] * sD[q][k + NS * m];
                 }
-                sH[it] = h;
+                if (MIXED) {
+                    const float hi = static_cast<float>(h);
+                    sHh[it] = hi;
+                    sHl[it] = static_cast<float>(h - static_cast<double>(hi));
+                } else {
+                    sH[it] = h;
+                }
             }
             __syncwarp();
 #pragma unroll
@@ -501,32 +557,40 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
                 if (c >= 0) {
                     const int alpha = c & 0xff, beta = c >> 8;
                     const int b = beta / DIM, cp = beta % DIM;
-                    double v = acc[i];
+                    acc_t v = acc[i];
 #pragma unroll
                     for (int r = 0; r < DIM; ++r) {
                         const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
-                        v += sH[alpha * NS + m] * sg[q][r][b];
+                        if (MIXED) {
+                            const float gb = sgf[q][r][b];
+                            v = fmaf(sHh[alpha * NS + m], gb, v);
+                            v = fmaf(sHl[alpha * NS + m], gb, v);
+                        } else {
+                            v += sH[alpha * NS + m] * sg[q][r][b];
+                        }
                     }
                     acc[i] = v;
                 }
             }
             __syncwarp();
         }
-        const int32_t *em = A.emap + e * NLD * NLD;
+        if (map_aligned) cp_async_wait_all();
+        __syncwarp();
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int c = code[i];
             if (c < 0) continue;
             const int alpha = c & 0xff, beta = c >> 8;
-            const int32_t p = em[alpha * NLD + beta];
+            const double val = static_cast<double>(acc[i]);
+            const int32_t p = smap[alpha * NLD + beta];
             if (p >= 0) {
-                if (p < A.nnz) atomicAdd(A.values + p, acc[i]);
+                if (p < A.nnz) atomicAdd(A.values + p, val);
                 else flag(SSP_DEV_BAD_INDEX);
             }
             if (SYM && alpha != beta) {
-                const int32_t p2 = em[beta * NLD + alpha];
+                const int32_t p2 = smap[beta * NLD + alpha];
                 if (p2 >= 0) {
-                    if (p2 < A.nnz) atomicAdd(A.values + p2, acc[i]);
+                    if (p2 < A.nnz) atomicAdd(A.values + p2, val);
                     else flag(SSP_DEV_BAD_INDEX);
                 }
             }
@@ -596,20 +660,22 @@ int launch_element(const ElemArgs &a, cudaStream_t st) {
     return launch_status();
 }
 
-template <int DIM, int NP, int NQ, bool SYM, bool CORR>
+template <int DIM, int NP, int NQ, bool SYM, bool CORR, bool MIXED = false>
 int launch_element_warp(const ElemArgs &a, cudaStream_t st) {
-    constexpr int WARPS = 4;
+    constexpr int WARPS = MIXED ? 3 : 4;  // static shared memory stays under 48 KB per CTA
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm,
+                                                  tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>,
                                                   32 * WARPS, 0);
     if (per_sm < 1) per_sm = 1;
     long long grid = (long long)sms * per_sm;
     const long long need = (a.n_elem + WARPS - 1) / WARPS;
     if (grid > need) grid = need;
-    tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR><<<static_cast<unsigned>(grid), 32 * WARPS, 0, st>>>(a);
+    tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>
+        <<<static_cast<unsigned>(grid), 32 * WARPS, 0, st>>>(a);
     return launch_status();
 }
 
@@ -746,6 +812,24 @@ int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *d
         return SSP_ERR_INVALID;
     ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale};
     return dispatch_element<true, true>(dim, n_p, n_q, a, as_stream(stream));
+}
+
+int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
+                                         const double *ds, const double *weight, const int8_t *branch,
+                                         const double *shear, const double *lame, const int32_t *scatter_map,
+                                         int n_elem, int n_p, int n_q, long long nnz_out, double scale,
+                                         double *out_values, void *stream) {
+    if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !branch || !shear || !lame || !scatter_map ||
+        (nnz_out > 0 && !out_values))
+        return SSP_ERR_INVALID;
+    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale};
+    cudaStream_t st = as_stream(stream);
+    if (dim == 3 && n_p == 10 && n_q == 11) return launch_element_warp<3, 10, 11, true, true, true>(a, st);
+    if (dim == 3 && n_p == 4 && n_q == 1) return launch_element_warp<3, 4, 1, true, true, true>(a, st);
+    if (dim == 2 && n_p == 6 && n_q == 7) return launch_element_warp<2, 6, 7, true, true, true>(a, st);
+    return SSP_ERR_UNSUPPORTED;
 }
 
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,

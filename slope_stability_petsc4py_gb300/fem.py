@@ -107,6 +107,29 @@ def _tet_lagrange_grads(order: int, xi: np.ndarray) -> tuple[np.ndarray, np.ndar
 
 
 @lru_cache(maxsize=None)
+def reference_values(dim: int, elem_type: str) -> np.ndarray:
+    """Basis values at the quadrature points, shape (n_p, n_q) (basis.py:15-33, 134-157)."""
+    xi, _ = quadrature(dim, elem_type)
+    et = elem_type.upper()
+    if dim == 3 and et in ("P1", "P2"):
+        l1, l2, l3 = xi
+        lam = [1.0 - l1 - l2 - l3, l1, l2, l3]
+        if et == "P1":
+            return np.array(lam)
+        verts = [lv * (2.0 * lv - 1.0) for lv in lam]
+        edges = [4.0 * lam[i] * lam[j] for i, j in ((0, 1), (1, 2), (0, 2), (1, 3), (2, 3), (0, 3))]
+        return np.array(verts + edges)
+    if dim == 2 and et in ("P1", "P2"):
+        l1, l2 = xi
+        lam = [1.0 - l1 - l2, l1, l2]
+        if et == "P1":
+            return np.array(lam)
+        verts = [lv * (2.0 * lv - 1.0) for lv in lam]
+        return np.array(verts + [4.0 * lam[1] * lam[2], 4.0 * lam[0] * lam[2], 4.0 * lam[0] * lam[1]])
+    raise ValueError(f"no basis values for {dim}D {elem_type}")
+
+
+@lru_cache(maxsize=None)
 def reference_gradients(dim: int, elem_type: str) -> np.ndarray:
     """Basis gradients on the reference element at the quadrature points, shape (dim, n_p, n_q)."""
     xi, _ = quadrature(dim, elem_type)

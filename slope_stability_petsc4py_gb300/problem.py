@@ -142,6 +142,10 @@ class ConstitutiveOperator:
         # single-pass kernel); False selects the single-pass kernel
         self.binned_return_mapping = True
         self._scratch = None
+        # "plain": every tangent product in FP64 (the drop-in, parity 1e-12 with the reference);
+        # "mixed": the plastic-point products B^T H in FP32 with H = w D B formed in FP64 and split
+        # into FP32 hi + lo parts, FP64 CSR accumulation (about 1e-7 relative tangent error)
+        self.tangent_form = "plain"
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
         self._owned_unique_c_bar = None
@@ -425,7 +429,10 @@ class ConstitutiveOperator:
                 scale = 1.0 - float(r)
             if ev is not None:
                 e0.record()
-            _lib.call("ssp_tangent_plastic_correction", pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
+            entry = "ssp_tangent_plastic_correction"
+            if self.tangent_form == "mixed" and pat.n_p <= 10:
+                entry = "ssp_tangent_plastic_correction_mixed"
+            _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
                       _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
                       _lib.ptr(self._branch), _lib.ptr(self._dev["shear"]), _lib.ptr(self._dev["lame"]),
                       _lib.ptr(d["scatter_map"]), int(pat.overlap_elements.size), pat.n_p, pat.n_q, pat.nnz, scale,
