@@ -201,7 +201,7 @@ __global__ void force_element_kernel(const double *__restrict__ d1, const double
             acc += w[g] * (comp == 0 ? gx * s[0] + gy * s[2] : gy * s[1] + gx * s[2]);
         }
     }
-    atomicAdd(F + row, acc);
+    red_add(F + row, acc);
 }
 
 // ---------------------------------------------------------------------------- tangent (rows)
@@ -394,13 +394,13 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
             const int alpha = c & 0xff, beta = c >> 8;
             const int32_t p = em[alpha * NLD + beta];
             if (p >= 0) {
-                if (p < A.nnz) atomicAdd(A.values + p, acc[i]);
+                if (p < A.nnz) red_add(A.values + p, acc[i]);
                 else flag(SSP_DEV_BAD_INDEX);
             }
             if (SYM && alpha != beta) {
                 const int32_t p2 = em[beta * NLD + alpha];
                 if (p2 >= 0) {
-                    if (p2 < A.nnz) atomicAdd(A.values + p2, acc[i]);
+                    if (p2 < A.nnz) red_add(A.values + p2, acc[i]);
                     else flag(SSP_DEV_BAD_INDEX);
                 }
             }
@@ -584,13 +584,13 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
             const double val = static_cast<double>(acc[i]);
             const int32_t p = smap[alpha * NLD + beta];
             if (p >= 0) {
-                if (p < A.nnz) atomicAdd(A.values + p, val);
+                if (p < A.nnz) red_add(A.values + p, val);
                 else flag(SSP_DEV_BAD_INDEX);
             }
             if (SYM && alpha != beta) {
                 const int32_t p2 = smap[beta * NLD + alpha];
                 if (p2 >= 0) {
-                    if (p2 < A.nnz) atomicAdd(A.values + p2, val);
+                    if (p2 < A.nnz) red_add(A.values + p2, val);
                     else flag(SSP_DEV_BAD_INDEX);
                 }
             }

@@ -15,6 +15,12 @@ extern __device__ int g_device_status;
 
 __device__ __forceinline__ void flag(int code) { atomicOr(&g_device_status, code); }
 
+// Fire-and-forget FP64 add into global memory (a reduction, not an atomic that returns the old
+// value), so a scattering warp does not wait for each add to complete.
+__device__ __forceinline__ void red_add(double *p, double v) {
+    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline int launch_status() {
