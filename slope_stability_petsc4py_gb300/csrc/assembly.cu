@@ -425,7 +425,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // B^T H are taken and accumulated in FP32; the per-element sums are added to the FP64 CSR values
 // with FP64 atomics.  Otherwise the arithmetic and scatter are those of tangent_element_kernel.
 template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR, bool MIXED>
-__global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(ElemArgs A) {
+__global__ void __launch_bounds__(32 * WARPS, MIXED ? 2 : 3) tangent_element_warp_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;

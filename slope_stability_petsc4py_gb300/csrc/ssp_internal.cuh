@@ -41,14 +41,15 @@ inline unsigned grid_for(long long n, int block) {
 // gradient component multiplies each.  3D comp 0 -> rows {0, 3, 5} with (dx, dy, dz);
 // comp 1 -> rows {3, 1, 4} with (dx, dy, dz); comp 2 -> rows {5, 4, 2} with (dx, dy, dz).
 // 2D comp 0 -> rows {0, 2} with (dx, dy); comp 1 -> rows {2, 1} with (dx, dy).
+// The tables are packed one entry per 4-bit nibble into a constant, so a runtime index costs a
+// shift and a mask (an indexed local array would live in local memory).
 __host__ __device__ __forceinline__ int bt_row3(int comp, int grad) {
-    // grad 0 = d/dx, 1 = d/dy, 2 = d/dz
-    const int tbl[9] = {0, 3, 5, 3, 1, 4, 5, 4, 2};
-    return tbl[comp * 3 + grad];
+    // grad 0 = d/dx, 1 = d/dy, 2 = d/dz; entries {0,3,5, 3,1,4, 5,4,2}
+    return static_cast<int>((0x245413530ull >> (4 * (comp * 3 + grad))) & 0xFull);
 }
 __host__ __device__ __forceinline__ int bt_row2(int comp, int grad) {
-    const int tbl[4] = {0, 2, 2, 1};
-    return tbl[comp * 2 + grad];
+    // entries {0,2, 2,1}
+    return static_cast<int>((0x1220u >> (4 * (comp * 2 + grad))) & 0xFu);
 }
 
 }  // namespace ssp
