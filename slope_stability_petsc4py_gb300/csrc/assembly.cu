@@ -424,8 +424,23 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // plain kernel, split into FP32 hi + lo parts (hi = fl32(H), lo = fl32(H - hi)), and the products
 // B^T H are taken and accumulated in FP32; the per-element sums are added to the FP64 CSR values
 // with FP64 atomics.  Otherwise the arithmetic and scatter are those of tangent_element_kernel.
+// Per-warp shared-memory slice of tangent_element_warp_kernel (dynamic shared memory).
+template <int DIM, int NP, int NQ, bool MIXED>
+struct WarpSlice {
+    static constexpr int NS = DIM == 3 ? 6 : 3;
+    static constexpr int NLD = DIM * NP;
+    double sg[NQ][DIM][NP];                // gradients of the contributing points
+    double sD[NQ][NS * NS];                // w * D of the contributing points
+    double sH[MIXED ? 1 : NLD * NS];       // B^T (w D) of one point, FP64
+    float2 sHhl[MIXED ? NLD * NS : 1];     // the same split into FP32 hi + lo (mixed form)
+    float sgf[MIXED ? NQ : 1][DIM][NP];    // FP32 gradients (mixed form)
+    alignas(16) int32_t smap[NLD * NLD];   // the element's row of the element->CSR map
+    double spt[3][NQ];                     // w, shear, lame of the contributing points
+    int sq[NQ];                            // contributing point indices
+};
+
 template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR, bool MIXED>
-__global__ void __launch_bounds__(32 * WARPS, MIXED ? 2 : 3) tangent_element_warp_kernel(ElemArgs A) {
+__global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
@@ -434,25 +449,18 @@ __global__ void __launch_bounds__(32 * WARPS, MIXED ? 2 : 3) tangent_element_war
     static_assert(NQ <= 32, "one branch code per lane");
     static_assert((NLD * NLD) % 4 == 0, "map rows are whole 16-byte chunks");
     using acc_t = typename std::conditional<MIXED, float, double>::type;
-    __shared__ double sg_all[WARPS][NQ][DIM][NP];
-    __shared__ double sD_all[WARPS][NQ][NS * NS];
-    __shared__ double sH_all[WARPS][MIXED ? 1 : NLD * NS];
-    __shared__ float sHh_all[WARPS][MIXED ? NLD * NS : 1];
-    __shared__ float sHl_all[WARPS][MIXED ? NLD * NS : 1];
-    __shared__ float sgf_all[WARPS][MIXED ? NQ : 1][DIM][NP];
-    __shared__ __align__(16) int32_t smap_all[WARPS][NLD * NLD];
-    __shared__ double spt_all[WARPS][3][NQ];  // w, shear, lame of the contributing points
-    __shared__ int sq_all[WARPS][NQ];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Slice = WarpSlice<DIM, NP, NQ, MIXED>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double(*sg)[DIM][NP] = sg_all[wid];
-    double(*sD)[NS * NS] = sD_all[wid];
-    double *sH = sH_all[wid];
-    float *sHh = sHh_all[wid];
-    float *sHl = sHl_all[wid];
-    float(*sgf)[DIM][NP] = sgf_all[wid];
-    int32_t *smap = smap_all[wid];
-    double(*spt)[NQ] = spt_all[wid];
-    int *sq = sq_all[wid];
+    Slice &S = reinterpret_cast<Slice *>(smem_raw)[wid];
+    double(*sg)[DIM][NP] = S.sg;
+    double(*sD)[NS * NS] = S.sD;
+    double *sH = S.sH;
+    float2 *sHhl = S.sHhl;
+    float(*sgf)[DIM][NP] = S.sgf;
+    int32_t *smap = S.smap;
+    double(*spt)[NQ] = S.spt;
+    int *sq = S.sq;
     const bool map_aligned = (reinterpret_cast<uintptr_t>(A.emap) & 15u) == 0;
 
     int code[PER];
@@ -544,8 +552,7 @@ __global__ void __launch_bounds__(32 * WARPS, MIXED ? 2 : 3) tangent_element_war
                 }
                 if (MIXED) {
                     const float hi = static_cast<float>(h);
-                    sHh[it] = hi;
-                    sHl[it] = static_cast<float>(h - static_cast<double>(hi));
+                    sHhl[it] = make_float2(hi, static_cast<float>(h - static_cast<double>(hi)));
                 } else {
                     sH[it] = h;
                 }
@@ -563,8 +570,9 @@ __global__ void __launch_bounds__(32 * WARPS, MIXED ? 2 : 3) tangent_element_war
                         const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
                         if (MIXED) {
                             const float gb = sgf[q][r][b];
-                            v = fmaf(sHh[alpha * NS + m], gb, v);
-                            v = fmaf(sHl[alpha * NS + m], gb, v);
+                            const float2 hl = sHhl[alpha * NS + m];
+                            v = fmaf(hl.x, gb, v);
+                            v = fmaf(hl.y, gb, v);
                         } else {
                             v += sH[alpha * NS + m] * sg[q][r][b];
                         }
@@ -662,20 +670,22 @@ int launch_element(const ElemArgs &a, cudaStream_t st) {
 
 template <int DIM, int NP, int NQ, bool SYM, bool CORR, bool MIXED = false>
 int launch_element_warp(const ElemArgs &a, cudaStream_t st) {
-    constexpr int WARPS = MIXED ? 3 : 4;  // static shared memory stays under 48 KB per CTA
+    constexpr int WARPS = 4;
+    constexpr size_t smem = WARPS * sizeof(WarpSlice<DIM, NP, NQ, MIXED>);
+    auto kernel = tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+        cudaSuccess)
+        return SSP_ERR_CUDA;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm,
-                                                  tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>,
-                                                  32 * WARPS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * WARPS, smem);
     if (per_sm < 1) per_sm = 1;
     long long grid = (long long)sms * per_sm;
     const long long need = (a.n_elem + WARPS - 1) / WARPS;
     if (grid > need) grid = need;
-    tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>
-        <<<static_cast<unsigned>(grid), 32 * WARPS, 0, st>>>(a);
+    kernel<<<static_cast<unsigned>(grid), 32 * WARPS, smem, st>>>(a);
     return launch_status();
 }
 
