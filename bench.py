@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--config", default="3d_p2_homo")
     ap.add_argument("--form", default="plain", choices=["plain", "mixed"],
                     help="plain: FP64 tangent (the drop-in); mixed: FP32 plastic-point products")
+    ap.add_argument("--return-mapping", default="binned", choices=["binned", "unsorted", "learned"],
+                    help="binned: two-pass exact binning; unsorted: one divergent pass; learned: bins proposed "
+                         "by the branch network (trained on the GPU before the timed region)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
@@ -244,7 +247,7 @@ def algorithmic(name, st):
     n, n_el, n_p, n_q, dim, ns = st["n"], st["n_el"], st["n_p"], st["n_q"], st["dim"], st["ns"]
     nld = dim * n_p
     s_out = 6 if dim == 3 else 4
-    if name == "ssp_constitutive_sds_branch":
+    if name in ("ssp_constitutive_sds_branch", "ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_learned"):
         return {"bytes": n * (8 * ns + 4 * 8 + 8 * s_out + 8 * ns * ns + 1), "flops": 0}
     if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d"):
         return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": n * 2 * 9 * n_p}
@@ -264,6 +267,26 @@ def algorithmic(name, st):
         return {"bytes": n + npl * (8 * ns * ns + 8 * dim * n_p + 24) + npe * (4 * nld * nld + 16 * nld * nld),
                 "flops": fp64}
     return {"bytes": 0, "flops": 0}
+
+
+def train_branch_model(torch, op, mesh, mats, name):
+    """Train the branch-proposal network on continuation states other than the timed one
+    (strength-reduction factors 1.0..1.4, shear-band amplitudes 0.4..1.6 x the workload's)."""
+    from slope_stability_petsc4py_gb300 import learned, synthetic
+
+    amp0 = synthetic.CONFIGS[name]["amplitude"]
+    t0 = time.perf_counter()
+    states = [(float(lam), torch.as_tensor(synthetic.displacement_field(mesh, mats, amplitude=amp0 * f, seed=100 + k),
+                                           device="cuda"))
+              for k, (lam, f) in enumerate(zip(np.linspace(1.0, 1.4, 6), np.linspace(0.4, 1.6, 6)))]
+    X, y = learned.collect_training_data(op, states)
+    model = learned.BranchProposal(seed=0)
+    hist = model.train(X, y, epochs=4, batch=65536, lr=3e-3)
+    torch.cuda.synchronize()
+    op.branch_model = model
+    return {"training_samples": int(X.shape[0]), "epochs": 4, "final_loss": hist[-1][0],
+            "final_train_accuracy": hist[-1][1], "training_s": time.perf_counter() - t0,
+            "training_states": "6 states, lambda 1.0..1.4, amplitude 0.4..1.6x (the timed state is held out)"}
 
 
 def run_gpu(args):
@@ -288,6 +311,10 @@ def run_gpu(args):
     U_dev = torch.as_tensor(U, device="cuda")
     op.host_outputs = False
     op.tangent_form = args.form
+    learned_info = None
+    if args.return_mapping == "learned":
+        learned_info = train_branch_model(torch, op, mesh, mats, args.config)
+    op.return_mapping = args.return_mapping
 
     def step():
         op.reduction(LAMBDA)
@@ -351,6 +378,7 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "tangent_error_vs_fp64": tangent_err,
         "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": args.form,
+                   "return_mapping": args.return_mapping,
                    "plastic_elements": stats["n_plastic_el"],
                    "step": "reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + "
                            "constrained diagonals + regularised blend",
@@ -370,6 +398,19 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clock_info,
     }
+    if learned_info is not None:
+        from slope_stability_petsc4py_gb300 import learned
+
+        br = op._branch
+        n = br.numel()
+        cnt = op._scratch[:5].cpu().numpy()
+        order = torch.cat([op._scratch[8 + k * n: 8 + k * n + int(cnt[k])] for k in range(5)]).long()
+        learned_info["bench_state_accuracy"] = float(
+            sum(int((br.index_select(0, op._scratch[8 + k * n: 8 + k * n + int(cnt[k])].long()) == k).sum().item())
+                for k in range(5)) / n)
+        learned_info["distinct_branches_per_warp"] = {"point_order": learned.warp_branch_mix(br),
+                                                      "learned_bins": learned.warp_branch_mix(br, order)}
+        line["learned"] = learned_info
 
     if rank == 0 and not args.no_e2e:
         op.host_outputs = True

@@ -219,6 +219,41 @@ int ssp_device_status(int *status_out, int clear);
  * out[blocks*threads].  Timing it gives the device's FP64 FMA rate. */
 int ssp_probe_dfma(int iters, int blocks, int threads, double *out, void *stream);
 
+/* ------------------------------------------------------------------ learned branch proposal */
+
+/* No counterpart in the reference (it has no learned component).  A 6 -> 32 -> 32 -> 5 ReLU MLP
+ * proposes each point's return branch from FP32 trial-strain features; points are binned by the
+ * proposal and the exact FP64 return mapping runs bin by bin.  The parameters are one FP32 vector
+ * of SSP_MLP_PARAMS values: W1[32][6], b1[32], W2[32][32], b2[32], W3[5][32], b3[5]. */
+#define SSP_MLP_PARAMS 1445
+
+/* Features X [n][6] (FP32) of the trial strains E [n][6]. */
+int ssp_branch_features(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                        const double *lame, int n, float *X, void *stream);
+
+/* Predicted branch (argmax) of every feature row; bf16 != 0 rounds weights and activations to
+ * BF16 (the inference precision the binning uses). */
+int ssp_mlp_predict(const float *params, const float *X, int n, int bf16, int8_t *pred, void *stream);
+
+/* Softmax cross-entropy of a batch against labels [n] (branch codes 0..4): grad [SSP_MLP_PARAMS]
+ * receives the gradient summed over the batch, loss_sum the summed loss, correct the number of
+ * argmax hits (all three are zeroed first). */
+int ssp_mlp_loss_grad(const float *params, const float *X, const int8_t *labels, int n, float *grad,
+                      float *loss_sum, int *correct, void *stream);
+
+/* One Adam step on params with moments m, v (all SSP_MLP_PARAMS long); the gradient is scaled by
+ * grad_scale first (e.g. 1/batch); step counts from 1. */
+int ssp_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, float beta1, float beta2,
+                 float eps, float grad_scale, void *stream);
+
+/* The 3D return mapping with learned binning: propose + bin, then the exact FP64 return mapping
+ * over the bins.  Same outputs as ssp_constitutive_sds_branch.  scratch is caller-allocated device
+ * memory of 5*n_int + 8 int32 (counters and bins), overwritten. */
+int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const double *c_bar,
+                                    const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                    double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                    void *stream);
+
 /* ------------------------------------------------------------------ pattern (host) */
 
 /* Fixed owned-row CSR pattern and element->CSR maps, built on the host in C++; replaces the

@@ -415,5 +415,71 @@ def owned_pattern(elem, q_mask, owned_node_range):
     }
 
 
+# --------------------------------------------------------------------------- learned branch proposal
+# (no reference counterpart: the checker of the product's MLP kernels, in float64)
+
+MLP_SHAPES = (("W1", (32, 6)), ("b1", (32,)), ("W2", (32, 32)), ("b2", (32,)), ("W3", (5, 32)), ("b3", (5,)))
+
+
+def mlp_unpack(p):
+    p = np.asarray(p, dtype=np.float64)
+    out, o = {}, 0
+    for name, shape in MLP_SHAPES:
+        k = int(np.prod(shape))
+        out[name] = p[o:o + k].reshape(shape)
+        o += k
+    return out
+
+
+def mlp_forward(p, X):
+    w = mlp_unpack(p)
+    X = np.asarray(X, dtype=np.float64)
+    a1 = X @ w["W1"].T + w["b1"]
+    h1 = np.maximum(a1, 0.0)
+    a2 = h1 @ w["W2"].T + w["b2"]
+    h2 = np.maximum(a2, 0.0)
+    z = h2 @ w["W3"].T + w["b3"]
+    return z, (X, a1, h1, a2, h2)
+
+
+def mlp_loss_grad(p, X, y):
+    """Summed softmax cross-entropy, its gradient (flat, kernel layout) and the argmax hits."""
+    w = mlp_unpack(p)
+    z, (X, a1, h1, a2, h2) = mlp_forward(p, X)
+    y = np.asarray(y, dtype=np.int64)
+    zmax = z.max(axis=1, keepdims=True)
+    ez = np.exp(z - zmax)
+    prob = ez / ez.sum(axis=1, keepdims=True)
+    loss = float(np.sum(np.log(ez.sum(axis=1)) + zmax[:, 0] - z[np.arange(len(y)), y]))
+    g3 = prob.copy()
+    g3[np.arange(len(y)), y] -= 1.0
+    g2 = (g3 @ w["W3"]) * (a2 > 0)
+    g1 = (g2 @ w["W2"]) * (a1 > 0)
+    grads = {"W3": g3.T @ h2, "b3": g3.sum(0), "W2": g2.T @ h1, "b2": g2.sum(0), "W1": g1.T @ X, "b1": g1.sum(0)}
+    flat = np.concatenate([grads[name].ravel() for name, _ in MLP_SHAPES])
+    hits = int(np.sum(np.argmax(z, axis=1) == y))
+    return loss, flat, hits
+
+
+def branch_features(E, c_bar, sin_phi, shear, lame):
+    """Float64 restatement of the proposal network's input features (for checking the kernel)."""
+    E = np.asarray(E, dtype=np.float64)
+    t = E.copy()
+    t[:, 3:] *= 0.5
+    I1 = t[:, 0] + t[:, 1] + t[:, 2]
+    d = t[:, :3] - I1[:, None] / 3.0
+    J2 = 0.5 * np.sum(d * d, axis=1) + np.sum(t[:, 3:] ** 2, axis=1)
+    J3 = (d[:, 0] * d[:, 1] * d[:, 2] + 2 * t[:, 3] * t[:, 4] * t[:, 5] - d[:, 0] * t[:, 4] ** 2
+          - d[:, 1] * t[:, 5] ** 2 - d[:, 2] * t[:, 3] ** 2)
+    k = 2.0 * shear / c_bar
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lode = np.where(J2 > 0, 2.598076211 * J3 / (J2 * np.sqrt(J2)), 0.0)
+    lode = np.clip(lode, -1.0, 1.0)
+    lr = lame / shear
+    slog = lambda x: np.sign(x) * np.log1p(np.abs(x))  # noqa: E731
+    return np.stack([slog(k * np.sqrt(J2)), slog(k * I1), slog(lr * sin_phi * k * I1), lode, sin_phi,
+                     lr / (lr + 2.0)], axis=1)
+
+
 def have_reference_checkout() -> bool:
     return os.path.isdir("/root/reference/src/slope_stability")

@@ -47,6 +47,12 @@ _SIGS = {
     "ssp_gather": [_vp, _vp, _c_int, _vp, _vp],
     "ssp_device_status": [ctypes.POINTER(_c_int), _c_int],
     "ssp_probe_dfma": [_c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_branch_features": [_vp] * 5 + [_c_int, _vp, _vp],
+    "ssp_mlp_predict": [_vp, _vp, _c_int, _c_int, _vp, _vp],
+    "ssp_mlp_loss_grad": [_vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
+    "ssp_mlp_adam": [_vp, _vp, _vp, _vp, _c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, _vp],
+    "ssp_constitutive_3d_sds_learned": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_pattern_build": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _c_int, _c_int, ctypes.POINTER(_vp)],
     "ssp_pattern_sizes": [_vp, _vp],
     "ssp_pattern_copy": [_vp, ctypes.c_char_p, _vp],
@@ -98,7 +104,8 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
     "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_constitutive_sds_branch": 1, "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 2, "ssp_constitutive_3d_sds_binned_noalloc": 2,
-    "ssp_tangent_plastic_correction_mixed": 1,
+    "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
+    "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 2,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
 }

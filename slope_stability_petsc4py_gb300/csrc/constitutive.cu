@@ -23,8 +23,6 @@ __device__ int g_device_status = 0;
 
 namespace {
 
-constexpr double kPi = 3.14159265358979323846;
-
 __device__ __forceinline__ double vol_iota(int i) { return i < 3 ? 1.0 : 0.0; }
 __device__ __forceinline__ double half_ident(int i) { return i < 3 ? 1.0 : 0.5; }
 
@@ -667,6 +665,13 @@ int32_t *fixed_scratch_for_current_device() {
 }
 
 }  // namespace
+
+// The single-pass return mapping of one point, for kernels in other translation units.
+__device__ int mc3d_point_ext(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
+                              double *DS) {
+    return mc3d_point(E, c_bar, sin_phi, shear, lame, S, DS);
+}
+
 }  // namespace ssp
 
 using namespace ssp;

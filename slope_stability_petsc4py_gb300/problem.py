@@ -138,9 +138,11 @@ class ConstitutiveOperator:
         self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
         self._K_el = None  # elastic tangent CSR values (device), built on first use
         self._dev = None
-        # 3D tangents through the two-pass, branch-binned return mapping (same results as the
-        # single-pass kernel); False selects the single-pass kernel
-        self.binned_return_mapping = True
+        # How 3D tangents are evaluated (all give the same results): "binned" -- two passes with
+        # exact branch binning; "unsorted" -- one pass in point order; "learned" -- points binned
+        # by the branch_model's proposal, then the exact return mapping bin by bin.
+        self.return_mapping = "binned"
+        self.branch_model = None
         self._scratch = None
         # "plain": every tangent product in FP64 (the drop-in, parity 1e-12 with the reference);
         # "mixed": the plastic-point products B^T H in FP32 with H = w D B formed in FP64 and split
@@ -306,13 +308,21 @@ class ConstitutiveOperator:
         args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                 _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
         branch = None
-        if tangent and pat.dim == 3 and self.binned_return_mapping:
+        mode = self.return_mapping if pat.dim == 3 else "unsorted"
+        if tangent and mode in ("binned", "learned"):
             branch = t.empty(n, dtype=t.int8, device="cuda")
-            if self._scratch is None or self._scratch.numel() < 3 * n + 4:
-                self._scratch = t.empty(3 * n + 4, dtype=t.int32, device="cuda")
-            _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
-                      _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
-                      _lib.ptr(DS), _lib.ptr(branch), _lib.ptr(self._scratch), st)
+            need = (5 if mode == "learned" else 3) * n + 8
+            if self._scratch is None or self._scratch.numel() < need:
+                self._scratch = t.empty(need, dtype=t.int32, device="cuda")
+            mat = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
+                   _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(branch),
+                   _lib.ptr(self._scratch), st)
+            if mode == "learned":
+                if self.branch_model is None:
+                    raise ValueError("return_mapping='learned' needs a trained branch_model")
+                _lib.call("ssp_constitutive_3d_sds_learned", _lib.ptr(self.branch_model.params), *mat)
+            else:
+                _lib.call("ssp_constitutive_3d_sds_binned", *mat)
         elif tangent:
             branch = t.empty(n, dtype=t.int8, device="cuda")
             _lib.call("ssp_constitutive_sds_branch", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
