@@ -361,7 +361,7 @@ def run_gpu(args):
     alg = algorithmic(dominant, stats)
     k_ms = kernels[dominant]["ms_per_launch"]
     achieved_gbs = alg["bytes"] / (k_ms * 1e-3) / 1e9
-    corr = "ssp_tangent_plastic_correction" + ("_mixed" if args.form == "mixed" and pat.n_p <= 10 else "")
+    corr = "ssp_tangent_plastic_correction" + ("_mixed" if args.form == "mixed" else "")
     tangent_err = None
     if args.form == "mixed":  # tangent error of this form against the FP64 form, same state
         op.tangent_form = "plain"

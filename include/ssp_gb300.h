@@ -42,6 +42,7 @@ enum ssp_status {
 /* bits of the device status word */
 #define SSP_DEV_BAD_INDEX 1
 #define SSP_DEV_NONFINITE 2
+#define SSP_DEV_TIMEOUT 4 /* a bounded wait on the tensor cores expired; the kernel stopped */
 
 /* ------------------------------------------------------------------ constitutive */
 
@@ -182,10 +183,12 @@ int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *d
                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
                                    long long nnz_out, double scale, double *out_values, void *stream);
 
-/* Mixed-precision form of ssp_tangent_plastic_correction (P1/P2 elements): H = B^T (w * scale *
- * (DS - D_el)) is formed in FP64 and split into FP32 hi + lo parts; the products B^T H are taken
- * and accumulated in FP32 per element; the element sums are added to the FP64 CSR values with
- * FP64 atomics.  The return mapping that produced DS (eigendecomposition, branch tests, plastic
+/* Mixed-precision form of ssp_tangent_plastic_correction.  H = B^T (w * scale * (DS - D_el)) is
+ * formed in FP64 and split into hi + lo parts.  P1/P2 elements: the products B^T H are taken and
+ * accumulated in FP32 on the CUDA cores.  P4 elements (3D, 35 nodes, 24 points): the element's
+ * contraction over (point, strain component) runs on the tensor cores (tcgen05.mma kind::tf32,
+ * H and B both split into TF32 hi + lo, hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor
+ * memory).  The element sums are added to the FP64 CSR values with FP64 atomics.  The return mapping that produced DS (eigendecomposition, branch tests, plastic
  * multipliers) is FP64.  Relative error of the assembled tangent against the FP64 form is about
  * 1e-7 (tested <= 1e-6).  No reference counterpart: the reference assembles in FP64 only. */
 int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
@@ -195,6 +198,12 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
                                          double *out_values, void *stream);
 
 /* Per-point elastic tangent blocks [n_int][n_s*n_s] of the return mapping's elastic branch. */
+/* Test support for the tensor-core tangent: D[128][112] = A[128][K] * B[112][K]^T (row-major FP32,
+ * inputs rounded to TF32) through the shared-memory layout, descriptors and tensor-memory read-back
+ * of the P4 kernel, one CTA; K in {8, 16, 24}; convention 1 swaps the descriptor's leading and
+ * stride byte offsets (0 is the kernel's).  No reference counterpart. */
+int ssp_tc_tf32_probe(const float *A, const float *B, int K, int convention, float *D, void *stream);
+
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
                                void *stream);
 

@@ -26,6 +26,7 @@ _SIGS = {
     "ssp_constitutive_3d_sds": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_3d_branch": [_vp] * 5 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_tc_tf32_probe": [_vp, _vp, _c_int, _c_int, _vp, _vp],
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned_noalloc": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
@@ -102,7 +103,8 @@ _KERNELS_PER_CALL = {
     "ssp_constitutive_2d": 1, "ssp_reduction": 1, "ssp_geometry": 1, "ssp_assemble_overlap_strain_3d": 1,
     "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
-    "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_constitutive_sds_branch": 1, "ssp_tangent_plastic_correction": 1,
+    "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
+    "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 2, "ssp_constitutive_3d_sds_binned_noalloc": 2,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
     "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 2,

@@ -839,6 +839,9 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
     if (dim == 3 && n_p == 10 && n_q == 11) return launch_element_warp<3, 10, 11, true, true, true>(a, st);
     if (dim == 3 && n_p == 4 && n_q == 1) return launch_element_warp<3, 4, 1, true, true, true>(a, st);
     if (dim == 2 && n_p == 6 && n_q == 7) return launch_element_warp<2, 6, 7, true, true, true>(a, st);
+    if (dim == 3 && n_p == 35 && n_q == 24)
+        return correction_tc_p4(dphi1, dphi2, dphi3, ds, weight, branch, shear, lame, scatter_map, n_elem, nnz_out, scale,
+                                out_values, st);
     return SSP_ERR_UNSUPPORTED;
 }
 

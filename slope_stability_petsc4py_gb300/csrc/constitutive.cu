@@ -156,28 +156,56 @@ __device__ __forceinline__ Decision3 decide3(const Principal3 &p, const Mat3 &m)
     return {kApex, 0.0, 1.0};
 }
 
+// Elastic branch: S = lambda tr(E) I + 2 G t (t = E with halved shears), DS = the elastic matrix.
+__device__ __forceinline__ void finish_elastic(const double *t, double I1, const Mat3 &m, double *S, double *DS) {
+    const double shear = m.shear, lame = m.lame;
+    const double lI1 = lame * I1, s2 = 2.0 * shear;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) S[i] = lI1 + s2 * t[i];
+#pragma unroll
+    for (int i = 3; i < 6; ++i) S[i] = s2 * t[i];
+    if (DS) {
+#pragma unroll
+        for (int k = 0; k < 36; ++k) DS[k] = 0.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            DS[i * 7] = s2 + lame;
+            DS[(i + 3) * 7] = shear;
+        }
+        store_sym(DS, 0, 1, lame);
+        store_sym(DS, 0, 2, lame);
+        store_sym(DS, 1, 2, lame);
+    }
+}
+
+// Elastic screen from invariants, before any eigen-decomposition.  With principal trial strains
+// e1 >= e2 >= e3, Q = J2/3 and Lode angle a, the trial yield function is
+//   f = 2G[(e1 - e3) + s(e1 + e3)] + 2 lambda s I1 - c_bar,
+//   (e1 - e3) + s(e1 + e3) = 2 sqrt(Q) (sqrt(3) sin a + s cos a) + 2 s I1 / 3,
+// and sqrt(3) sin a + s cos a <= sqrt(3 + s^2) for every a (Cauchy-Schwarz).  A point whose bound
+// is below -1e-6 of the size of f's terms is elastic however its eigenvalues round (their error
+// is at most ~1e-8 sqrt(Q), near repeated roots), so the branch test of the full path would say
+// elastic too; such a point is finished from t and I1 alone, with the arithmetic of the elastic
+// branch, so S and DS are bitwise those of the full path.
+__device__ __forceinline__ bool screen_elastic(const double *E, const Mat3 &m, double *t, double &I1) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i] = half_ident(i) * E[i];
+    I1 = t[0] + t[1] + t[2];
+    const double I2 = t[0] * t[1] + t[0] * t[2] + t[1] * t[2] - t[3] * t[3] - t[4] * t[4] - t[5] * t[5];
+    const double Q = fmax((I1 * I1 - 3.0 * I2) / 9.0, 0.0);
+    const double s = m.sin_phi;
+    const double dev = 2.0 * sqrt(Q) * sqrt(3.0 + s * s);
+    const double bound = 2.0 * m.shear * (dev + (2.0 / 3.0) * s * I1) + 2.0 * m.lame * s * I1 - m.c_bar;
+    const double size = 2.0 * fabs(m.shear) * (dev + fabs(I1)) + 2.0 * fabs(m.lame * s * I1) + fabs(m.c_bar);
+    return bound <= -1e-6 * size;
+}
+
 // Stress and (when DS != null) consistent tangent of the decided branch.
 __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, double *S, double *DS) {
     const double sp = m.sin_phi, sin_phi = m.sin_phi, shear = m.shear, lame = m.lame;
     const double e1 = p.e1, e2 = p.e2, e3 = p.e3, I1 = p.I1;
     if (d.branch == kElastic) {
-        const double lI1 = lame * I1, s2 = 2.0 * shear;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) S[i] = lI1 + s2 * p.t[i];
-#pragma unroll
-        for (int i = 3; i < 6; ++i) S[i] = s2 * p.t[i];
-        if (DS) {
-#pragma unroll
-            for (int k = 0; k < 36; ++k) DS[k] = 0.0;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                DS[i * 7] = s2 + lame;
-                DS[(i + 3) * 7] = shear;
-            }
-            store_sym(DS, 0, 1, lame);
-            store_sym(DS, 0, 2, lame);
-            store_sym(DS, 1, 2, lame);
-        }
+        finish_elastic(p.t, I1, m, S, DS);
         return;
     }
     if (d.branch == kSmooth) {
@@ -304,9 +332,16 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
 // Returns the branch code.  DS may be null (stress only).
 __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
                           double *DS) {
+    const Mat3 m{c_bar, sin_phi, shear, lame};
+    {
+        double t[6], I1;
+        if (screen_elastic(E, m, t, I1)) {
+            finish_elastic(t, I1, m, S, DS);
+            return kElastic;
+        }
+    }
     Principal3 p;
     principal3(E, p);
-    const Mat3 m{c_bar, sin_phi, shear, lame};
     const Decision3 d = decide3(p, m);
     finish3(p, d, m, S, DS);
     return d.branch;
@@ -353,8 +388,8 @@ __global__ void __launch_bounds__(128) mc3d_kernel(const double *__restrict__ E,
     if (branch) branch[p] = static_cast<int8_t>(b);
 }
 
-// Two-pass return mapping, pass A: every point's branch is decided; elastic and apex points are
-// finished here (they carry no branch-specific tangent work), and the points of the smooth,
+// Two-pass return mapping, pass A: every point's branch is decided (points that pass the elastic
+// screen without an eigen-decomposition); elastic and apex points are finished here (they carry no branch-specific tangent work), and the points of the smooth,
 // left-edge and right-edge branches are appended to three lists in scratch memory
 // (scratch[0..2] = counters, then three lists of n entries) with warp-aggregated atomics.
 __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
@@ -367,18 +402,25 @@ __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict_
     if (p < n) {
         double e[6];
         load6(E, p, e);
-        Principal3 pr;
-        principal3(e, pr);
         const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
-        const Decision3 d = decide3(pr, m);
-        branch[p] = static_cast<int8_t>(d.branch);
-        if (d.branch == kElastic || d.branch == kApex) {
-            double s[6], ds[36];
-            finish3(pr, d, m, s, ds);
+        double t[6], I1, s[6], ds[36];
+        int b;
+        if (screen_elastic(e, m, t, I1)) {
+            finish_elastic(t, I1, m, s, ds);
+            b = kElastic;
+        } else {
+            Principal3 pr;
+            principal3(e, pr);
+            const Decision3 d = decide3(pr, m);
+            b = d.branch;
+            if (b == kElastic || b == kApex) finish3(pr, d, m, s, ds);
+        }
+        branch[p] = static_cast<int8_t>(b);
+        if (b == kElastic || b == kApex) {
             store6(S, p, s);
             store36(DS, p, ds);
         } else {
-            list_id = d.branch - 1;
+            list_id = b - 1;
         }
     }
     const unsigned lane = threadIdx.x & 31u;

@@ -1,0 +1,459 @@
+// Mixed-precision plastic-correction tangent of P4 tetrahedra on the tensor cores (tcgen05).
+//
+// For an element whose plastic points are q (branch != elastic), the correction of the
+// elastic-predictor tangent (assembly.cu, tangent_element_kernel in correction mode) is
+//   K_e = sum_q B_q^T dD_q B_q,   dD_q = s w_q (DS_q - D_el,q),   B_q: 6 x 105,
+// which is one dense contraction over kappa = (q, m), m a strain component:
+//   K_e[alpha][beta] = sum_kappa H[alpha][kappa] Bk[kappa][beta],
+//   H[alpha][(q, m)] = (B_q^T dD_q)[alpha][m]          (formed in FP64 on the CUDA cores),
+//   Bk[(q, m)][beta] = B_q[m][beta]                     (the gradients, FP64 in memory).
+// Both operands are split into TF32 pairs, x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and
+// the tensor cores form hi*hi and hi*lo + lo*hi (the three-product TF32 scheme: about 22
+// significant bits per product) in two FP32 accumulators in tensor memory.
+//
+// Accuracy.  A tensor-core MMA rounds its FP32 result once per instruction, so errors grow with
+// the number of MMAs that feed one accumulator.  The points of an element are taken in groups of
+// four (K = 24, three K = 8 steps); each group has its own pair of accumulators (hi*hi: three
+// MMAs, cross terms: six, 2^-11 smaller), and the CUDA cores add every group's two partial sums
+// into FP64 registers.  Two accumulator pairs alternate between groups (ping-pong), so the tensor
+// cores multiply group g while the CUDA cores drain group g - 1 and build group g + 1.  The FP64
+// element sums are added to the CSR values with FP64 reductions through the element->CSR map, on
+// both mirror positions of alpha <= beta, so the correction is exactly symmetric.
+//
+// Tile: M = 128 rows (alpha, 105 used), N = 112 columns (beta, 105 used).  One CTA of 512 threads
+// per SM, grid-striding over elements; it owns all 512 tensor-memory columns (two accumulator
+// pairs at columns 0 / 128 and 256 / 384).  One thread issues the MMAs and commits each group to
+// the mbarrier of its buffer.  Warp w drains accumulator lanes 32 (w % 4) .. + 31 (its lane
+// quarter), columns 28 (w / 4) .. + 27.
+//
+// Operand layout in shared memory: K-major, no swizzle, in 8-row x 16-byte core matrices:
+// byte offset(row, kappa) = ((kappa / 4) * (rows / 8) + row / 8) * 128 + (row % 8) * 16 + (kappa % 4) * 4,
+// so the core matrices of one row group are 128 B apart along M/N (the descriptor's stride byte
+// offset) and rows/8 * 128 B apart along K (its leading byte offset).
+//
+// Every wait on an mbarrier is bounded (about one second of SM clocks); on expiry the CTA sets
+// SSP_DEV_TIMEOUT, stops, and still releases its tensor memory.
+#include "ssp_internal.cuh"
+
+namespace ssp {
+namespace {
+
+constexpr int kNP = 35, kNQ = 24, kNLD = 105, kNS = 6;
+constexpr int kM = 128, kN = 112, kPts = 4, kK = kPts * kNS;  // 24 = three K steps of 8
+constexpr int kThreads = 512;
+constexpr int kTmemCols = 512;                                 // two (hi*hi, cross) accumulator pairs
+constexpr int kColsPerWarp = kN / 4;                           // 28 accumulator columns per drain warp
+constexpr uint32_t kLboA = (kM / 8) * 128, kLboB = (kN / 8) * 128, kSbo = 128;
+constexpr int kABytes = kM * kK * 4, kBBytes = kN * kK * 4;
+static_assert(kABytes % 1024 == 0 && kBBytes % 128 == 0, "operand tiles keep 128-byte alignment");
+static_assert(kColsPerWarp % 4 == 0, "drain loads four columns at a time");
+
+// Instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits 4-5 = 1), A and B TF32
+// (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(kN >> 3) << 17) | (uint32_t(kM >> 4) << 24);
+
+struct Stage {  // one group of four points, operands split hi / lo
+    uint32_t a_hi[kABytes / 4];
+    uint32_t a_lo[kABytes / 4];
+    uint32_t b_hi[kBBytes / 4];
+    uint32_t b_lo[kBBytes / 4];
+};
+struct PointData {  // FP64 inputs of the group being built
+    double g[kPts][3][kNP];
+    double dD[kPts][kNS * kNS];
+};
+struct Smem {
+    Stage stage[2];
+    PointData pts;
+    unsigned long long mbar[2];
+    uint32_t tmem_slot;
+    int abort;
+    int nq[2];
+    int sq[kNQ];
+};
+// Dynamic shared memory requested: more than half of an SM's, so one CTA (which owns all of the
+// SM's tensor memory) is resident per SM.
+constexpr size_t kSmemBytes = sizeof(Smem) > 120 * 1024 ? sizeof(Smem) : 120 * 1024;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ int kmaj_off(int row, int kap, int rows) {
+    return ((kap >> 2) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (kap & 3) * 4;
+}
+
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading byte offset >> 4
+// (bits 16-29), stride byte offset >> 4 (bits 32-45), descriptor version 1 (bit 46), base offset 0,
+// no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) | (static_cast<uint64_t>(lbo >> 4) << 16) |
+           (static_cast<uint64_t>(sbo >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void split_tf32(double x, uint32_t &hi, uint32_t &lo) {
+    hi = to_tf32(static_cast<float>(x));
+    lo = to_tf32(static_cast<float>(x - static_cast<double>(__uint_as_float(hi))));
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t mbar_addr) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint32_t addr) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(addr) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the completion of the phase with the given parity (about 1 s of SM clocks).
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(addr, parity)) {
+        if (clock64() - t0 > 2000000000ll) return false;
+    }
+    return true;
+}
+
+// 32 lanes x 16 consecutive FP32 columns of the accumulator (this warp's lane quarter).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+// 32 lanes x 4 consecutive FP32 columns (no wait: the caller waits once for a batch).
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// acc[j] += accumulator column (col0 + j) of this thread's lane, j < 28, in FP64.
+__device__ __forceinline__ void drain_add(uint32_t taddr0, double *acc) {
+    uint32_t r[kColsPerWarp];
+#pragma unroll
+    for (int i = 0; i < kColsPerWarp / 4; ++i) tmem_ld4(taddr0 + 4 * i, r + 4 * i);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < kColsPerWarp; ++j) acc[j] += static_cast<double>(__uint_as_float(r[j]));
+}
+
+__device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam) {
+    if (i < 3 && j < 3) return i == j ? 2.0 * G + lam : lam;
+    if (i == j) return G;
+    return 0.0;
+}
+
+// Every thread waits for the commit of group parity b (bounded), then reads that group's two
+// accumulators into its FP64 sums.
+__device__ __forceinline__ void drain_group(Smem &S, uint32_t tmem, int b, uint32_t &phase_bits, uint32_t lane_col,
+                                            double *acc) {
+    if (!mbar_wait(smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u)) {
+        S.abort = 1;
+        flag(SSP_DEV_TIMEOUT);
+    }
+    phase_bits ^= 1u << b;
+    fence_after_sync();
+    const uint32_t base = tmem + lane_col + 256u * b;
+    drain_add(base, acc);         // hi * hi
+    drain_add(base + 128u, acc);  // hi * lo + lo * hi
+    fence_before_sync();          // these reads precede the next MMAs into this pair
+}
+
+__global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
+    const double *__restrict__ d1, const double *__restrict__ d2, const double *__restrict__ d3,
+    const double *__restrict__ DS, const double *__restrict__ w, const int8_t *__restrict__ branch,
+    const double *__restrict__ shear, const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem,
+    long long nnz, double scale, double *__restrict__ values) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem &S = *reinterpret_cast<Smem *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int lq = warp & 3, cq = warp >> 2;  // drain lane quarter and column quarter
+    const uint32_t lane_col = (static_cast<uint32_t>(32 * lq) << 16) + static_cast<uint32_t>(kColsPerWarp * cq);
+
+    // zero both stages once: the padding rows (alpha >= 105, beta >= 105) are never written again
+    for (int i = tid; i < (int)(sizeof(Stage) * 2 / 4); i += kThreads) reinterpret_cast<uint32_t *>(S.stage)[i] = 0u;
+    if (tid == 0) {
+        mbar_init(smem_u32(&S.mbar[0]));
+        mbar_init(smem_u32(&S.mbar[1]));
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = S.tmem_slot;
+    uint32_t phase_bits = 0;
+    int parity = 0;
+
+    for (int e = blockIdx.x; e < n_elem; e += gridDim.x, parity ^= 1) {
+        const long long g0 = (long long)e * kNQ;
+        if (warp == 0) {
+            const bool pl = lane < kNQ && branch[g0 + lane] != 0;
+            const unsigned mask = __ballot_sync(0xffffffffu, pl);
+            if (pl) S.sq[__popc(mask & ((1u << lane) - 1u))] = lane;
+            if (lane == 0) S.nq[parity] = __popc(mask);
+        }
+        __syncthreads();
+        const int nq = S.nq[parity];
+        if (nq == 0) continue;  // uniform across the CTA
+        const int groups = (nq + kPts - 1) / kPts;
+        double acc[kColsPerWarp];
+#pragma unroll
+        for (int j = 0; j < kColsPerWarp; ++j) acc[j] = 0.0;
+        for (int grp = 0; grp < groups; ++grp) {
+            const int b = grp & 1;  // stage buffer and accumulator pair; both were released by drain(grp - 2)
+            // FP64 inputs of the group's points (absent slots are zero)
+            for (int i = tid; i < kPts * 3 * kNP; i += kThreads) {
+                const int pi = i / (3 * kNP), rem = i % (3 * kNP), r = rem / kNP, a = rem % kNP;
+                const int k = grp * kPts + pi;
+                double v = 0.0;
+                if (k < nq) {
+                    const long long src = (g0 + S.sq[k]) * kNP + a;
+                    v = r == 0 ? d1[src] : (r == 1 ? d2[src] : d3[src]);
+                }
+                S.pts.g[pi][r][a] = v;
+            }
+            for (int i = tid; i < kPts * kNS * kNS; i += kThreads) {
+                const int pi = i / (kNS * kNS), kk = i % (kNS * kNS);
+                const int k = grp * kPts + pi;
+                double v = 0.0;
+                if (k < nq) {
+                    const long long gq = g0 + S.sq[k];
+                    v = w[gq] * (scale * (DS[gq * (kNS * kNS) + kk] - elastic_d3(kk % kNS, kk / kNS, shear[gq], lame[gq])));
+                }
+                S.pts.dD[pi][kk] = v;
+            }
+            __syncthreads();
+            Stage &st = S.stage[b];
+            unsigned char *a_hi = reinterpret_cast<unsigned char *>(st.a_hi);
+            unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
+            unsigned char *b_hi = reinterpret_cast<unsigned char *>(st.b_hi);
+            unsigned char *b_lo = reinterpret_cast<unsigned char *>(st.b_lo);
+            // H = B^T dD (FP64), alpha = 3 * node + component
+            for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
+                const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), alpha = rem / kNS, m = rem % kNS;
+                const int a = alpha / 3, c = alpha % 3;
+                double h = 0.0;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) h += S.pts.g[pi][r][a] * S.pts.dD[pi][bt_row3(c, r) + kNS * m];
+                uint32_t hi, lo;
+                split_tf32(h, hi, lo);
+                const int off = kmaj_off(alpha, pi * kNS + m, kM);
+                *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
+                *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
+            }
+            // Bk[(q, m)][beta] = B_q[m][beta]: the gradient component r with bt_row3(comp, r) == m
+            for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
+                const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), beta = rem / kNS, m = rem % kNS;
+                const int bn = beta / 3, cp = beta % 3;
+                double v = 0.0;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    if (bt_row3(cp, r) == m) v = S.pts.g[pi][r][bn];
+                uint32_t hi, lo;
+                split_tf32(v, hi, lo);
+                const int off = kmaj_off(beta, pi * kNS + m, kN);
+                *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
+                *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
+            }
+            fence_async_smem();  // generic-proxy writes -> visible to the tensor cores
+            __syncthreads();
+            if (S.abort) break;
+            if (tid == 0) {
+                fence_after_sync();
+                const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+                const uint32_t t_hh = tmem + 256u * b, t_x = t_hh + 128u;
+#pragma unroll
+                for (int s = 0; s < kK / 8; ++s) {
+                    const uint32_t oa = s * 2 * kLboA, ob = s * 2 * kLboB;
+                    mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), s != 0 ? 1u : 0u);
+                    mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), s != 0 ? 1u : 0u);
+                    mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), 1u);
+                }
+                mma_commit(smem_u32(&S.mbar[b]));
+            }
+            if (grp >= 1) drain_group(S, tmem, b ^ 1, phase_bits, lane_col, acc);
+        }
+        if (S.abort) break;
+        drain_group(S, tmem, (groups - 1) & 1, phase_bits, lane_col, acc);
+        __syncthreads();  // also orders this element's shared-memory reads before the next element's writes
+        if (S.abort) break;
+        // scatter alpha <= beta to both mirror positions
+        const int row = 32 * lq + lane;
+        if (row < kNLD) {
+            const int32_t *em = emap + (long long)e * kNLD * kNLD;
+#pragma unroll
+            for (int j = 0; j < kColsPerWarp; ++j) {
+                const int beta = kColsPerWarp * cq + j;
+                if (beta < row || beta >= kNLD) continue;
+                const double val = acc[j];
+                const int32_t p = em[row * kNLD + beta];
+                if (p >= 0) {
+                    if (p < nnz) red_add(values + p, val);
+                    else flag(SSP_DEV_BAD_INDEX);
+                }
+                if (beta != row) {
+                    const int32_t p2 = em[beta * kNLD + row];
+                    if (p2 >= 0) {
+                        if (p2 < nnz) red_add(values + p2, val);
+                        else flag(SSP_DEV_BAD_INDEX);
+                    }
+                }
+            }
+        }
+    }
+    // all tensor-core work of this CTA has been waited for (or abandoned after a timeout)
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// Layout / descriptor check: D[128][112] = A[128][K] B[112][K]^T through the same shared-memory
+// layout, descriptors and tensor-memory read-back as the kernel above (one CTA, K = 8, 16 or 24).
+// convention 0 passes (leading, stride) byte offsets as (K-direction, row-direction) core-matrix
+// strides, convention 1 swaps them.  Operands sit in a 64 KiB buffer so either reading stays
+// inside it.
+__global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restrict__ A, const float *__restrict__ B,
+                                                          int K, int convention, float *__restrict__ D) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *sa = smem_raw, *sb = smem_raw + 32768;
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(smem_raw + 65536);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem_raw + 65536 + 8);
+    int *abort_flag = reinterpret_cast<int *>(smem_raw + 65536 + 12);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < 65536 / 4; i += 128) reinterpret_cast<uint32_t *>(smem_raw)[i] = 0u;
+    __syncthreads();
+    for (int i = tid; i < kM * K; i += 128) {
+        const int r = i / K, k = i % K;
+        *reinterpret_cast<uint32_t *>(sa + kmaj_off(r, k, kM)) = to_tf32(A[i]);
+    }
+    for (int i = tid; i < kN * K; i += 128) {
+        const int r = i / K, k = i % K;
+        *reinterpret_cast<uint32_t *>(sb + kmaj_off(r, k, kN)) = to_tf32(B[i]);
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(mbar));
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *slot;
+    if (tid == 0) {
+        const uint32_t la = convention == 0 ? kLboA : kSbo, sa_ = convention == 0 ? kSbo : kLboA;
+        const uint32_t lb = convention == 0 ? kLboB : kSbo, sb_ = convention == 0 ? kSbo : kLboB;
+        for (int s = 0; s < K / 8; ++s)
+            mma_tf32(tmem, smem_desc(smem_u32(sa) + s * 2 * kLboA, la, sa_), smem_desc(smem_u32(sb) + s * 2 * kLboB, lb, sb_),
+                     s != 0 ? 1u : 0u);
+        mma_commit(smem_u32(mbar));
+        if (!mbar_wait(smem_u32(mbar), 0)) {
+            *abort_flag = 1;
+            flag(SSP_DEV_TIMEOUT);
+        }
+    }
+    __syncthreads();
+    fence_after_sync();
+    if (*abort_flag == 0) {
+        for (int ch = 0; ch < kN / 16; ++ch) {
+            float v[16];
+            tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + ch * 16, v);
+            const int row = 32 * warp + lane;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) D[row * kN + ch * 16 + j] = v[j];
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+}  // namespace
+
+int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
+                     const int8_t *branch, const double *shear, const double *lame, const int32_t *emap, int n_elem,
+                     long long nnz, double scale, double *values, cudaStream_t st) {
+    const size_t smem = kSmemBytes;
+    if (cudaFuncSetAttribute(correction_tc_p4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = sms;  // one CTA per SM: each owns the SM's 512 tensor-memory columns
+    if (grid > n_elem) grid = n_elem;
+    correction_tc_p4_kernel<<<static_cast<unsigned>(grid), kThreads, smem, st>>>(d1, d2, d3, DS, w, branch, shear, lame,
+                                                                                   emap, n_elem, nnz, scale, values);
+    return launch_status();
+}
+
+}  // namespace ssp
+
+using namespace ssp;
+
+extern "C" int ssp_tc_tf32_probe(const float *A, const float *B, int K, int convention, float *D, void *stream) {
+    if ((K != 8 && K != 16 && K != 24) || (convention != 0 && convention != 1) || !A || !B || !D)
+        return SSP_ERR_INVALID;
+    const int smem = 65536 + 64;
+    if (cudaFuncSetAttribute(tc_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    tc_probe_kernel<<<1, 128, smem, as_stream(stream)>>>(A, B, K, convention, D);
+    return launch_status();
+}

@@ -278,6 +278,9 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
     overlap_global_dofs = (dim * np.repeat(ov_nodes, dim) + np.tile(np.arange(dim), ov_nodes.size)).astype(np.int64)
     _ensure_int32_capacity("global dofs", dim * n_nodes)
     dev["overlap_global_dofs32"] = _lib.to_device(overlap_global_dofs.astype(np.int32), t.int32)
+    # the same dofs as indices into U stored (dim, n_nodes) row-major: comp * n_nodes + node
+    dev["overlap_dofs_rowmajor32"] = _lib.to_device(
+        ((overlap_global_dofs % dim) * n_nodes + overlap_global_dofs // dim).astype(np.int32), t.int32)
     if keep_slot_metadata and dim == 3:
         dev["row_slot_ptr"] = _lib.to_device(g["row_slot_ptr"], t.int32)
         dev["slot_elem"] = _lib.to_device(g["slot_elem"], t.int32)
@@ -361,13 +364,18 @@ def _is_torch(a) -> bool:
 def _u_overlap_device(pattern, U):
     """U as (dim, n_nodes) array / tensor (or flat Fortran vector) -> overlap dof values on device."""
     t = _lib.require_cuda()
+    # a (dim, n_nodes) field is uploaded as stored (row-major, asynchronously when it is pinned)
+    # and gathered by row-major indices on the device; a flat vector is in dof order
     if _is_torch(U):
-        u = U.to(t.float64)
-        u_flat = u.T.reshape(-1) if u.dim() == 2 else u.reshape(-1)
-        u_flat = u_flat.cuda()
+        u = U if U.dtype == t.float64 else U.to(t.float64)
+        rowmajor = u.dim() == 2
+        u = u.contiguous()
+        u_flat = u.to("cuda", non_blocking=True).reshape(-1)
     else:
-        u_flat = _lib.to_device(np.asarray(U, dtype=np.float64).reshape(-1, order="F"), t.float64)
-    idx = pattern.device["overlap_global_dofs32"]
+        a = np.asarray(U, dtype=np.float64)
+        rowmajor = a.ndim == 2
+        u_flat = _lib.to_device(a if rowmajor else a.reshape(-1), t.float64).reshape(-1)
+    idx = pattern.device["overlap_dofs_rowmajor32" if rowmajor else "overlap_global_dofs32"]
     u_ov = t.empty(idx.numel(), dtype=t.float64, device="cuda")
     _lib.call("ssp_gather", _lib.ptr(u_flat.contiguous()), _lib.ptr(idx), int(idx.numel()), _lib.ptr(u_ov),
               _lib.stream_handle())

@@ -126,6 +126,15 @@ def reference_values(dim: int, elem_type: str) -> np.ndarray:
             return np.array(lam)
         verts = [lv * (2.0 * lv - 1.0) for lv in lam]
         return np.array(verts + [4.0 * lam[1] * lam[2], 4.0 * lam[0] * lam[2], 4.0 * lam[0] * lam[1]])
+    if dim == 3 and et == "P4":
+        bary = (1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2])
+        out = np.empty((N_NODES[(3, "P4")], xi.shape[1]))
+        for idx, counts in enumerate(tet_node_tuples(4)):
+            val = np.ones(xi.shape[1])
+            for lv, c in zip(bary, counts):
+                val = val * _lagrange_factor(4, c, lv)[0]
+            out[idx] = val
+        return out
     raise ValueError(f"no basis values for {dim}D {elem_type}")
 
 

@@ -137,6 +137,7 @@ class ConstitutiveOperator:
         self._ds_symmetric = False
         self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
         self._K_el = None  # elastic tangent CSR values (device), built on first use
+        self._blend_base = None  # (r, (1-r) K_el,t + r K_el) for the last regularisation factor
         self._dev = None
         # How 3D tangents are evaluated (all give the same results): "binned" -- two passes with
         # exact branch binning; "unsorted" -- one pass in point order; "learned" -- points binned
@@ -150,6 +151,7 @@ class ConstitutiveOperator:
         self.tangent_form = "plain"
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
+        self._red_key = None
         self._owned_unique_c_bar = None
         self._owned_unique_sin_phi = None
         self._dev_mat = None
@@ -189,6 +191,8 @@ class ConstitutiveOperator:
         self.release_petsc_caches()
         self._dev = None
         self._K_el = None
+        self._blend_base = None
+        self._red_key = None
         self._clear_owned_local_cache()
         if pattern is not None:
             t = _lib.require_cuda()
@@ -265,6 +269,12 @@ class ConstitutiveOperator:
         davis = str(self.Davis_type).upper()
         if davis not in ("A", "B", "C"):
             raise ValueError("Incorrect choice of the Davis approach")
+        key = (float(lam), davis)
+        if self._red_key == key and self._owned_overlap_c_bar is not None:
+            # c_bar and sin_phi depend on (lambda, Davis type) and the materials only: Newton
+            # iterations at one lambda reuse the arrays of the first
+            self.time_reduction.append(perf_counter() - t0)
+            return
         n = pat.n_local_int
         cb = t.empty(n, dtype=t.float64, device="cuda")
         sp = t.empty(n, dtype=t.float64, device="cuda")
@@ -284,6 +294,7 @@ class ConstitutiveOperator:
                       davis.encode(), _lib.ptr(cb), _lib.ptr(sp), st)
         self._owned_overlap_c_bar, self._owned_overlap_sin_phi = cb, sp
         self._owned_unique_c_bar, self._owned_unique_sin_phi = cb, sp
+        self._red_key = key
         self.c_bar = None
         self.sin_phi = None
         self.time_reduction.append(perf_counter() - t0)
@@ -434,13 +445,20 @@ class ConstitutiveOperator:
                 values.copy_(base)
                 scale = 1.0
             else:
-                _lib.call("ssp_blend_values", _lib.ptr(values), _lib.ptr(base), _lib.ptr(d["elastic_values"]), float(r),
-                          pat.nnz, st)
-                scale = 1.0 - float(r)
+                # (1-r) K_el,t + r K_el depends on r and the pattern only: blended once per r, then
+                # each build starts from a copy of it
+                rr = float(r)
+                if self._blend_base is None or self._blend_base[0] != rr:
+                    buf = self._blend_base[1] if self._blend_base is not None else _lib.torch().empty_like(base)
+                    _lib.call("ssp_blend_values", _lib.ptr(buf), _lib.ptr(base), _lib.ptr(d["elastic_values"]), rr,
+                              pat.nnz, st)
+                    self._blend_base = (rr, buf)
+                values.copy_(self._blend_base[1])
+                scale = 1.0 - rr
             if ev is not None:
                 e0.record()
             entry = "ssp_tangent_plastic_correction"
-            if self.tangent_form == "mixed" and pat.n_p <= 10:
+            if self.tangent_form == "mixed" and (pat.n_p <= 10 or (pat.dim == 3 and pat.n_p == 35)):
                 entry = "ssp_tangent_plastic_correction_mixed"
             _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
                       _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),

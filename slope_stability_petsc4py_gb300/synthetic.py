@@ -333,6 +333,8 @@ CONFIGS = {
     "3d_p2_large": dict(dim=3, elem_type="P2", nx=110, ny=44, nz=70, n_layers=4, amplitude=0.003),  # 2,032,800 tets
     # a smaller copy of 3d_p2_homo for detailed profiles (still larger than L2 per step)
     "3d_p2_profile": dict(dim=3, elem_type="P2", nx=20, ny=8, nz=20, n_layers=1, amplitude=0.0157),  # 19,200 tets
+    # a smaller copy of 3d_p4_hetero for detailed profiles
+    "3d_p4_profile": dict(dim=3, elem_type="P4", nx=14, ny=6, nz=10, n_layers=4, amplitude=0.003),  # 5,040 tets
 }
 
 

@@ -17,22 +17,25 @@ pytestmark = pytest.mark.gpu
 MIXED_RTOL = 1.0e-6
 
 
-def _operator(nx, ny, nz, layered=True, seed=1):
+def _operator(nx, ny, nz, layered=True, seed=1, elem_type="P2"):
     from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
 
     mats = synthetic.MaterialSet.layered(4, seed=seed) if layered else synthetic.MaterialSet.homogeneous()
-    mesh = synthetic.slope_mesh_3d(nx, ny, nz, elem_type="P2", n_layers=4 if layered else 1)
+    mesh = synthetic.slope_mesh_3d(nx, ny, nz, elem_type=elem_type, n_layers=4 if layered else 1)
     specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=0.0, young=float(mats.young[i]),
                   poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
-    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs,
+                                        elem_type=elem_type)
     return mesh, mats, op
 
 
-def test_mixed_tangent_error_bound(cuda_device):
+@pytest.mark.parametrize("elem_type,dims,amp", [("P2", (20, 8, 10), 0.02), ("P4", (10, 4, 5), 0.01)])
+def test_mixed_tangent_error_bound(cuda_device, elem_type, dims, amp):
+    """P2: FP32 CUDA-core products; P4: the tensor-core (tcgen05 TF32 split) contraction."""
     from slope_stability_petsc4py_gb300 import synthetic
 
-    mesh, mats, op = _operator(20, 8, 10)
-    U = synthetic.displacement_field(mesh, mats, amplitude=0.02, seed=4)
+    mesh, mats, op = _operator(*dims, elem_type=elem_type)
+    U = synthetic.displacement_field(mesh, mats, amplitude=amp, seed=4)
     op.reduction(1.1)
     op.constitutive_problem_stress_tangent(U)
     plastic = int((op._branch != 0).sum())
@@ -44,20 +47,21 @@ def test_mixed_tangent_error_bound(cuda_device):
         op.tangent_form = "mixed"
         _, _, km = op.build_K_regularized(r).getValuesCSR()
         err = rel_err(km, kp)
-        print(f"r={r}: mixed tangent max-norm relative error {err:.3e} ({plastic} plastic points)")
+        print(f"{elem_type} r={r}: mixed tangent max-norm relative error {err:.3e} ({plastic} plastic points)")
         assert 0.0 < err <= MIXED_RTOL
         fro = np.linalg.norm(km - kp) / np.linalg.norm(kp)
         assert fro <= MIXED_RTOL
 
 
-def test_mixed_form_newton_iterations_unchanged(cuda_device):
+@pytest.mark.parametrize("elem_type,dims", [("P2", (8, 4, 4)), ("P4", (4, 2, 2))])
+def test_mixed_form_newton_iterations_unchanged(cuda_device, elem_type, dims):
     from slope_stability_petsc4py_gb300.newton_check import newton_compare, newton_iterations
 
-    mesh, _mats, op = _operator(8, 4, 4)
+    mesh, _mats, op = _operator(*dims, elem_type=elem_type)
     lam = 1.0
     it_plain, res_plain, U_plain = newton_iterations(op, mesh, form="plain", lam=lam)
     it_mixed, res_mixed, U_mixed = newton_iterations(op, mesh, form="mixed", lam=lam)
-    print(f"Newton iterations plain {it_plain} (res {res_plain:.2e}), mixed {it_mixed} (res {res_mixed:.2e})")
+    print(f"{elem_type}: Newton iterations plain {it_plain} (res {res_plain:.2e}), mixed {it_mixed} (res {res_mixed:.2e})")
     assert res_plain < 1e-9 and res_mixed < 1e-9
     assert it_mixed == it_plain
     assert np.linalg.norm(U_mixed - U_plain) <= 1e-8 * np.linalg.norm(U_plain)

@@ -412,3 +412,89 @@ def test_device_resident_operator_path():
     F_free_h = op.build_F_free_local()
     # the element force kernel sums with atomics, so repeated calls agree to rounding only
     assert rel_err(F_free.cpu().numpy(), F_free_h) <= 1e-14
+
+
+def _yield_parts(E, shear, lame, sin_phi):
+    """g with f = g - c_bar (exact eigenvalues), the invariant bound h >= g and the size of f's terms."""
+    t = E.copy()
+    t[:, 3:] *= 0.5
+    M = np.zeros((E.shape[0], 3, 3))
+    for (i, j), k in {(0, 0): 0, (1, 1): 1, (2, 2): 2, (0, 1): 3, (1, 2): 4, (0, 2): 5}.items():
+        M[:, i, j] = M[:, j, i] = t[:, k]
+    ev = np.linalg.eigvalsh(M)
+    I1 = t[:, :3].sum(axis=1)
+    s = sin_phi
+    g = 2 * shear * ((1 + s) * ev[:, 2] - (1 - s) * ev[:, 0]) + 2 * lame * s * I1
+    dev = 2 * np.sqrt(((ev[:, :, None] - ev[:, None, :]) ** 2).sum(axis=(1, 2)) / 36.0) * np.sqrt(3 + s * s)  # 2 sqrt(J2/3)
+    h = 2 * shear * (dev + 2 * s * I1 / 3) + 2 * lame * s * I1
+    size = 2 * shear * (dev + np.abs(I1)) + 2 * np.abs(lame * s * I1)
+    return g, h, size
+
+
+def test_elastic_screen_near_yield_and_screen_threshold(oracle):
+    """Points straddling the yield surface and the invariant screen's threshold: every point the
+    kernels call elastic is elastic for the reference formula, and results match the oracle away
+    from the yield surface itself (|f| > 1e-9 of its terms, where any two FP64 evaluations agree)."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    rng = np.random.default_rng(5)
+    young, nu, c0, phi = 2.0e4, 0.3, 10.0, np.deg2rad(32.0)
+    shear, lame = young / (2 * (1 + nu)), young * nu / ((1 + nu) * (1 - 2 * nu))
+    sin_phi = np.sin(phi)
+    c_bar = 2 * c0 * np.cos(phi)
+    dirs = [rng.standard_normal((3000, 6))]
+    # deviators at the Lode angle that maximises the trial yield function (where the bound is tight)
+    a = np.arctan2(np.sqrt(3.0), sin_phi)
+    th = a - np.pi / 3
+    d = np.array([np.cos(th), np.cos(th - 2 * np.pi / 3), np.cos(th + 2 * np.pi / 3)])
+    for k in range(600):
+        Rq, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        T = Rq @ np.diag(d + rng.uniform(-0.5, 0.5)) @ Rq.T
+        dirs.append(np.array([[T[0, 0], T[1, 1], T[2, 2], 2 * T[0, 1], 2 * T[1, 2], 2 * T[0, 2]]]))
+    rep = rng.standard_normal((300, 2))  # repeated eigenvalues
+    dirs.append(np.column_stack([rep[:, 0], rep[:, 0], rep[:, 1], np.zeros((300, 3))]))
+    D = np.vstack(dirs)
+    g1, h1, size1 = _yield_parts(D, shear, lame, sin_phi)
+    pts = []
+    mult = np.array([1 - 1e-2, 1 - 1e-5, 1 - 1e-8, 1 + 1e-8, 1 + 1e-5, 1 + 1e-2])
+    ok = g1 > 0
+    for m in mult:  # around the yield surface
+        pts.append(D[ok] * (c_bar / g1[ok] * m)[:, None])
+    ok = h1 + 1e-6 * size1 > 0
+    alpha_s = c_bar * (1 - 1e-6) / (h1[ok] + 1e-6 * size1[ok])  # the screen's threshold
+    for m in (1 - 1e-9, 1 - 1e-12, 1.0, 1 + 1e-12, 1 + 1e-9):
+        pts.append(D[ok] * (alpha_s * m)[:, None])
+    E = np.vstack(pts)
+    n = E.shape[0]
+    full = lambda v: np.full(n, v)  # noqa: E731
+    args = (full(c_bar), full(sin_phi), full(shear), full(lame))
+    Ed, cb, sp, G, L = (_dev(x) for x in (E,) + args)
+    outs = {}
+    for mode in ("single", "binned"):
+        S = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+        DS = torch.empty((n, 36), dtype=torch.float64, device="cuda")
+        br = torch.empty(n, dtype=torch.int8, device="cuda")
+        if mode == "single":
+            _lib.call("ssp_constitutive_sds_branch", 3, _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G),
+                      _lib.ptr(L), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.stream_handle())
+        else:
+            scratch = torch.empty(3 * n + 4, dtype=torch.int32, device="cuda")
+            _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G),
+                      _lib.ptr(L), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch), _lib.stream_handle())
+        outs[mode] = (S.cpu().numpy(), DS.cpu().numpy(), br.cpu().numpy())
+    assert np.array_equal(outs["single"][2], outs["binned"][2])
+    assert np.array_equal(outs["single"][0], outs["binned"][0]) and np.array_equal(outs["single"][1], outs["binned"][1])
+    g, h, size = _yield_parts(E, shear, lame, sin_phi)
+    f = g - c_bar
+    tol = 1e-9 * (size + c_bar)
+    br = outs["binned"][2]
+    assert np.all(f[br == 0] <= tol[br == 0])  # never elastic where the reference yields
+    assert np.all(br[f < -tol] == 0) and np.all(br[f > tol] != 0)
+    clear = np.abs(f) > tol
+    S_o, DS_o = oracle.constitutive_3d(E, *args[:3], args[2], args[3])
+    assert rel_err(outs["binned"][0][clear], S_o[clear]) <= PLAIN_RTOL
+    assert rel_err(outs["binned"][1][clear], DS_o[clear]) <= PLAIN_RTOL
+    # the threshold points are elastic and far enough from the surface to be unambiguous
+    print(f"{n} points, {int(clear.sum())} away from the surface, elastic {float(np.mean(br == 0)):.3f}")
