@@ -220,6 +220,15 @@ int ssp_finish_values(double *values, long long nnz, const int32_t *constrained_
 /* dst[i] = src[idx[i]] (owned free rows of a force vector, problem.py:1008-1015). */
 int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *stream);
 
+/* 1 if host_ptr is host memory that kernels can address with the same pointer (pinned and
+ * device-mapped, as cudaHostAlloc / cudaMallocHost memory is under unified addressing), else 0. */
+int ssp_host_writable(const void *host_ptr);
+
+/* dst_host[0..n) = src[0..n) written by the SMs into pinned, device-mapped host memory
+ * (ssp_host_writable(dst_host) must hold, else SSP_ERR_INVALID); asynchronous on the stream.
+ * The operator's host hand-off of the CSR values; no reference counterpart. */
+int ssp_copy_out(const double *src, long long n, double *dst_host, void *stream);
+
 /* Reads the device status word (SSP_DEV_* bits); clear != 0 resets it.  Synchronous. */
 int ssp_device_status(int *status_out, int clear);
 

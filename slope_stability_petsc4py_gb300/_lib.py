@@ -26,6 +26,8 @@ _SIGS = {
     "ssp_constitutive_3d_sds": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_3d_branch": [_vp] * 5 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_host_writable": [_vp],
+    "ssp_copy_out": [_vp, _c_ll, _vp, _vp],
     "ssp_tc_tf32_probe": [_vp, _vp, _c_int, _c_int, _vp, _vp],
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
@@ -104,6 +106,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
     "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
+    "ssp_copy_out": 1, "ssp_host_writable": 0,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 2, "ssp_constitutive_3d_sds_binned_noalloc": 2,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
@@ -131,6 +134,11 @@ def call(name: str, *args) -> None:
     else:
         check(getattr(load(), name)(*args), name)
     LAUNCHES["count"] += n_k
+
+
+def host_writable(ptr_value) -> bool:
+    """True if kernels can store to this host address directly (pinned, device-mapped memory)."""
+    return bool(load().ssp_host_writable(ptr_value))
 
 
 def device_status(clear: bool = True) -> int:

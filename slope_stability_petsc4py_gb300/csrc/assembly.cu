@@ -429,11 +429,17 @@ template <int DIM, int NP, int NQ, bool MIXED>
 struct WarpSlice {
     static constexpr int NS = DIM == 3 ? 6 : 3;
     static constexpr int NLD = DIM * NP;
-    double sg[NQ][DIM][NP];                // gradients of the contributing points
-    double sD[NQ][NS * NS];                // w * D of the contributing points
-    double sH[MIXED ? 1 : NLD * NS];       // B^T (w D) of one point, FP64
-    float2 sHhl[MIXED ? NLD * NS : 1];     // the same split into FP32 hi + lo (mixed form)
-    float sgf[MIXED ? NQ : 1][DIM][NP];    // FP32 gradients (mixed form)
+    struct Work {
+        double sg[NQ][DIM][NP];            // gradients of the contributing points
+        double sD[NQ][NS * NS];            // w * D of the contributing points
+        double sH[MIXED ? 1 : NLD * NS];   // B^T (w D) of one point, FP64
+        float2 sHhl[MIXED ? NLD * NS : 1]; // the same split into FP32 hi + lo (mixed form)
+        float sgf[MIXED ? NQ : 1][DIM][NP];// FP32 gradients (mixed form)
+    };
+    union {
+        Work w;                            // while the products are formed
+        double sK[NLD * NLD];              // then the element's sums, staged for the row-wise scatter
+    } u;
     alignas(16) int32_t smap[NLD * NLD];   // the element's row of the element->CSR map
     double spt[3][NQ];                     // w, shear, lame of the contributing points
     int sq[NQ];                            // contributing point indices
@@ -453,11 +459,12 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
     using Slice = WarpSlice<DIM, NP, NQ, MIXED>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Slice &S = reinterpret_cast<Slice *>(smem_raw)[wid];
-    double(*sg)[DIM][NP] = S.sg;
-    double(*sD)[NS * NS] = S.sD;
-    double *sH = S.sH;
-    float2 *sHhl = S.sHhl;
-    float(*sgf)[DIM][NP] = S.sgf;
+    double(*sg)[DIM][NP] = S.u.w.sg;
+    double(*sD)[NS * NS] = S.u.w.sD;
+    double *sH = S.u.w.sH;
+    float2 *sHhl = S.u.w.sHhl;
+    float(*sgf)[DIM][NP] = S.u.w.sgf;
+    double *sK = S.u.sK;
     int32_t *smap = S.smap;
     double(*spt)[NQ] = S.spt;
     int *sq = S.sq;
@@ -583,24 +590,22 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
             __syncwarp();
         }
         if (map_aligned) cp_async_wait_all();
-        __syncwarp();
+        // stage the sums (the products are done with the work buffers), then scatter every entry
+        // row by row: consecutive lanes take consecutive columns of one CSR row, so a warp's
+        // reductions share cache lines; SYM reads alpha > beta from the mirrored entry
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int c = code[i];
-            if (c < 0) continue;
-            const int alpha = c & 0xff, beta = c >> 8;
-            const double val = static_cast<double>(acc[i]);
-            const int32_t p = smap[alpha * NLD + beta];
+            if (c >= 0) sK[(c & 0xff) * NLD + (c >> 8)] = static_cast<double>(acc[i]);
+        }
+        __syncwarp();
+        for (int idx = lane; idx < NLD * NLD; idx += 32) {
+            const int alpha = idx / NLD, beta = idx - alpha * NLD;
+            const double val = (!SYM || beta >= alpha) ? sK[idx] : sK[beta * NLD + alpha];
+            const int32_t p = smap[idx];
             if (p >= 0) {
                 if (p < A.nnz) red_add(A.values + p, val);
                 else flag(SSP_DEV_BAD_INDEX);
-            }
-            if (SYM && alpha != beta) {
-                const int32_t p2 = smap[beta * NLD + alpha];
-                if (p2 >= 0) {
-                    if (p2 < A.nnz) red_add(A.values + p2, val);
-                    else flag(SSP_DEV_BAD_INDEX);
-                }
             }
         }
     }
@@ -643,6 +648,23 @@ __global__ void blend_base_kernel(double *__restrict__ out, const double *__rest
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= nnz) return;
     out[i] = base[i] * (1.0 - r) + r * elastic[i];
+}
+
+// Device -> host copy by the SMs (16-byte stores when both ends are 16-byte aligned) into pinned,
+// device-mapped host memory: on a part whose host link is coherent the stores stream straight over
+// it, and several SMs keep more of it busy than one copy engine.
+__global__ void copy_out_kernel(const double *__restrict__ src, long long n, double *__restrict__ dst, int vec) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (vec) {
+        const long long n2 = n / 2;
+        const double2 *s2 = reinterpret_cast<const double2 *>(src);
+        double2 *d2 = reinterpret_cast<double2 *>(dst);
+        for (long long k = i; k < n2; k += stride) d2[k] = s2[k];
+        if (i == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+    } else {
+        for (long long k = i; k < n; k += stride) dst[k] = src[k];
+    }
 }
 
 __global__ void gather_rows_kernel(const double *__restrict__ src, const int32_t *__restrict__ idx, int n,
@@ -895,6 +917,28 @@ int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *
     if (n == 0) return SSP_OK;
     if (!src || !idx || !dst) return SSP_ERR_INVALID;
     gather_rows_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(src, idx, n, dst);
+    return launch_status();
+}
+
+int ssp_host_writable(const void *host_ptr) {
+    if (!host_ptr) return 0;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host_ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer == host_ptr ? 1 : 0;
+}
+
+int ssp_copy_out(const double *src, long long n, double *dst_host, void *stream) {
+    if (n < 0) return SSP_ERR_INVALID;
+    if (n == 0) return SSP_OK;
+    if (!src || !dst_host || !ssp_host_writable(dst_host)) return SSP_ERR_INVALID;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst_host)) & 15u) == 0;
+    copy_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, n, dst_host, vec ? 1 : 0);
     return launch_status();
 }
 

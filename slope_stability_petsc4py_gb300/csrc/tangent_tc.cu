@@ -24,7 +24,8 @@
 // per SM, grid-striding over elements; it owns all 512 tensor-memory columns (two accumulator
 // pairs at columns 0 / 128 and 256 / 384).  One thread issues the MMAs and commits each group to
 // the mbarrier of its buffer.  Warp w drains accumulator lanes 32 (w % 4) .. + 31 (its lane
-// quarter), columns 28 (w / 4) .. + 27.
+// quarter), columns 28 (w / 4) .. + 27.  The element's FP64 sums are staged in shared memory and
+// scattered row by row, so the reductions of a warp fall on neighbouring entries of one CSR row.
 //
 // Operand layout in shared memory: K-major, no swizzle, in 8-row x 16-byte core matrices:
 // byte offset(row, kappa) = ((kappa / 4) * (rows / 8) + row / 8) * 128 + (row % 8) * 16 + (kappa % 4) * 4,
@@ -66,6 +67,7 @@ struct PointData {  // FP64 inputs of the group being built
 struct Smem {
     Stage stage[2];
     PointData pts;
+    double ke[kNLD * kNLD];  // the element's FP64 sums (upper triangle used), staged for a row-wise scatter
     unsigned long long mbar[2];
     uint32_t tmem_slot;
     int abort;
@@ -75,6 +77,7 @@ struct Smem {
 // Dynamic shared memory requested: more than half of an SM's, so one CTA (which owns all of the
 // SM's tensor memory) is resident per SM.
 constexpr size_t kSmemBytes = sizeof(Smem) > 120 * 1024 ? sizeof(Smem) : 120 * 1024;
+static_assert(sizeof(Smem) <= 227 * 1024, "shared memory of one CTA");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -322,27 +325,25 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
         drain_group(S, tmem, (groups - 1) & 1, phase_bits, lane_col, acc);
         __syncthreads();  // also orders this element's shared-memory reads before the next element's writes
         if (S.abort) break;
-        // scatter alpha <= beta to both mirror positions
+        // stage the upper triangle, then scatter every entry row by row (consecutive threads ->
+        // consecutive columns of one CSR row, so the reductions of a warp share cache lines)
         const int row = 32 * lq + lane;
         if (row < kNLD) {
-            const int32_t *em = emap + (long long)e * kNLD * kNLD;
 #pragma unroll
             for (int j = 0; j < kColsPerWarp; ++j) {
                 const int beta = kColsPerWarp * cq + j;
-                if (beta < row || beta >= kNLD) continue;
-                const double val = acc[j];
-                const int32_t p = em[row * kNLD + beta];
-                if (p >= 0) {
-                    if (p < nnz) red_add(values + p, val);
-                    else flag(SSP_DEV_BAD_INDEX);
-                }
-                if (beta != row) {
-                    const int32_t p2 = em[beta * kNLD + row];
-                    if (p2 >= 0) {
-                        if (p2 < nnz) red_add(values + p2, val);
-                        else flag(SSP_DEV_BAD_INDEX);
-                    }
-                }
+                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = acc[j];
+            }
+        }
+        __syncthreads();
+        const int32_t *em = emap + (long long)e * kNLD * kNLD;
+        for (int idx = tid; idx < kNLD * kNLD; idx += kThreads) {
+            const int a = idx / kNLD, bcol = idx - a * kNLD;
+            const double val = bcol >= a ? S.ke[idx] : S.ke[bcol * kNLD + a];
+            const int32_t p = em[idx];
+            if (p >= 0) {
+                if (p < nnz) red_add(values + p, val);
+                else flag(SSP_DEV_BAD_INDEX);
             }
         }
     }
