@@ -420,21 +420,25 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // costs a few instructions and no shared-memory traffic.  The element's row of the element->CSR
 // map is fetched into shared memory asynchronously (cp.async) while the products are formed.
 //
-// MIXED (mixed-precision form; correction mode only): H = B^T (w D) is formed in FP64 as in the
-// plain kernel, split into FP32 hi + lo parts (hi = fl32(H), lo = fl32(H - hi)), and the products
-// B^T H are taken and accumulated in FP32; the per-element sums are added to the FP64 CSR values
-// with FP64 atomics.  Otherwise the arithmetic and scatter are those of tangent_element_kernel.
+// MIXED (mixed-precision form; correction mode only): the gradients and w s (DS - D_el) are split
+// into hi + lo float pairs by bit operations, H = B^T (w D) is formed in compensated double-float
+// arithmetic on the FP32 pipe (about 48 significant bits; the only FP64 instructions left are the
+// D_el subtractions and w s), the products B^T H are taken as Hh gh + Hl gh + Hh gl and
+// accumulated in FP32, and the per-element sums are widened exactly and added to the FP64 CSR
+// values with FP64 reductions.  Otherwise the arithmetic and scatter are those of
+// tangent_element_kernel.
 // Per-warp shared-memory slice of tangent_element_warp_kernel (dynamic shared memory).
 template <int DIM, int NP, int NQ, bool MIXED>
 struct WarpSlice {
     static constexpr int NS = DIM == 3 ? 6 : 3;
     static constexpr int NLD = DIM * NP;
     struct Work {
-        double sg[NQ][DIM][NP];            // gradients of the contributing points
-        double sD[NQ][NS * NS];            // w * D of the contributing points
-        double sH[MIXED ? 1 : NLD * NS];   // B^T (w D) of one point, FP64
-        float2 sHhl[MIXED ? NLD * NS : 1]; // the same split into FP32 hi + lo (mixed form)
-        float sgf[MIXED ? NQ : 1][DIM][NP];// FP32 gradients (mixed form)
+        double sg[MIXED ? 1 : NQ][DIM][NP];  // gradients of the contributing points (FP64 form)
+        double sD[MIXED ? 1 : NQ][NS * NS];  // w * D of the contributing points (FP64 form)
+        double sH[MIXED ? 1 : NLD * NS];     // B^T (w D) of one point (FP64 form)
+        df32 sgm[MIXED ? NQ : 1][DIM][NP];   // gradients as hi + lo (mixed form)
+        df32 sDm[MIXED ? NQ : 1][NS * NS];   // w * D as hi + lo (mixed form)
+        float2 sHhl[MIXED ? NLD * NS : 1];   // B^T (w D) of one point as hi + lo (mixed form)
     };
     union {
         Work w;                            // while the products are formed
@@ -462,8 +466,9 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
     double(*sg)[DIM][NP] = S.u.w.sg;
     double(*sD)[NS * NS] = S.u.w.sD;
     double *sH = S.u.w.sH;
+    df32(*sgm)[DIM][NP] = S.u.w.sgm;
+    df32(*sDm)[NS * NS] = S.u.w.sDm;
     float2 *sHhl = S.u.w.sHhl;
-    float(*sgf)[DIM][NP] = S.u.w.sgf;
     double *sK = S.u.sK;
     int32_t *smap = S.smap;
     double(*spt)[NQ] = S.spt;
@@ -524,24 +529,31 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
             const int k = i / NP, a = i % NP;
             const long long src = (g0 + sq[k]) * NP + a;
             const double x = A.d1[src], y = A.d2[src];
-            sg[k][0][a] = x;
-            sg[k][1][a] = y;
+            const double z = DIM == 3 ? A.d3[src] : 0.0;
             if (MIXED) {
-                sgf[k][0][a] = static_cast<float>(x);
-                sgf[k][1][a] = static_cast<float>(y);
-            }
-            if (DIM == 3) {
-                const double z = A.d3[src];
-                sg[k][DIM - 1][a] = z;
-                if (MIXED) sgf[k][DIM - 1][a] = static_cast<float>(z);
+                sgm[k][0][a] = df_from_f64(x);
+                sgm[k][1][a] = df_from_f64(y);
+                if (DIM == 3) sgm[k][DIM - 1][a] = df_from_f64(z);
+            } else {
+                sg[k][0][a] = x;
+                sg[k][1][a] = y;
+                if (DIM == 3) sg[k][DIM - 1][a] = z;
             }
         }
         for (int i = lane; i < nq * NS * NS; i += 32) {
             const int k = i / (NS * NS), kk = i % (NS * NS);
             const long long g = g0 + sq[k];
             double v = A.DS[g * (NS * NS) + kk];
-            if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, spt[1][k], spt[2][k]));
-            sD[k][kk] = spt[0][k] * v;
+            if (MIXED) {
+                // w s (DS - D_el): the FP64 subtraction only where D_el is nonzero, the scaling by
+                // w s as a double-float product
+                const double de = elastic_d<DIM>(kk % NS, kk / NS, spt[1][k], spt[2][k]);
+                if (de != 0.0) v -= de;
+                sDm[k][kk] = df_mul(df_from_f64(v), df_from_f64(A.scale * spt[0][k]));
+            } else {
+                if (CORR) v = A.scale * (v - elastic_d<DIM>(kk % NS, kk / NS, spt[1][k], spt[2][k]));
+                sD[k][kk] = spt[0][k] * v;
+            }
         }
         acc_t acc[PER];
 #pragma unroll
@@ -551,16 +563,21 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
             for (int it = lane; it < NLD * NS; it += 32) {
                 const int alpha = it / NS, m = it % NS;
                 const int a = alpha / DIM, c = alpha % DIM;
-                double h = 0.0;
+                if (MIXED) {  // H = B^T (w D) in double-float arithmetic on the FP32 pipe
+                    df32 h = df_mul(sgm[q][0][a], sDm[q][(DIM == 3 ? bt_row3(c, 0) : bt_row2(c, 0)) + NS * m]);
 #pragma unroll
-                for (int r = 0; r < DIM; ++r) {
-                    const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
-                    h += sg[q][r][a] * sD[q][k + NS * m];
-                }
-                if (MIXED) {
-                    const float hi = static_cast<float>(h);
-                    sHhl[it] = make_float2(hi, static_cast<float>(h - static_cast<double>(hi)));
+                    for (int r = 1; r < DIM; ++r) {
+                        const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
+                        h = df_fma(h, sgm[q][r][a], sDm[q][k + NS * m]);
+                    }
+                    sHhl[it] = make_float2(h.hi, h.lo);
                 } else {
+                    double h = 0.0;
+#pragma unroll
+                    for (int r = 0; r < DIM; ++r) {
+                        const int k = DIM == 3 ? bt_row3(c, r) : bt_row2(c, r);
+                        h += sg[q][r][a] * sD[q][k + NS * m];
+                    }
                     sH[it] = h;
                 }
             }
@@ -575,11 +592,12 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
 #pragma unroll
                     for (int r = 0; r < DIM; ++r) {
                         const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
-                        if (MIXED) {
-                            const float gb = sgf[q][r][b];
+                        if (MIXED) {  // (Hh + Hl)(gh + gl) without the Hl gl term, FP32 accumulation
+                            const df32 gb = sgm[q][r][b];
                             const float2 hl = sHhl[alpha * NS + m];
-                            v = fmaf(hl.x, gb, v);
-                            v = fmaf(hl.y, gb, v);
+                            v = fmaf(hl.x, gb.hi, v);
+                            v = fmaf(hl.y, gb.hi, v);
+                            v = fmaf(hl.x, gb.lo, v);
                         } else {
                             v += sH[alpha * NS + m] * sg[q][r][b];
                         }
@@ -596,7 +614,12 @@ __global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(Ele
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int c = code[i];
-            if (c >= 0) sK[(c & 0xff) * NLD + (c >> 8)] = static_cast<double>(acc[i]);
+            if (c >= 0) {
+                double v;
+                if constexpr (MIXED) v = f32_widen(acc[i]);  // exact, on the integer pipe
+                else v = acc[i];
+                sK[(c & 0xff) * NLD + (c >> 8)] = v;
+            }
         }
         __syncwarp();
         for (int idx = lane; idx < NLD * NLD; idx += 32) {

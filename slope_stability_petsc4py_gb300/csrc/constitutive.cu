@@ -178,26 +178,40 @@ __device__ __forceinline__ void finish_elastic(const double *t, double I1, const
     }
 }
 
-// Elastic screen from invariants, before any eigen-decomposition.  With principal trial strains
-// e1 >= e2 >= e3, Q = J2/3 and Lode angle a, the trial yield function is
+// Elastic screen from invariants, before any eigen-decomposition, in FP32.  With principal trial
+// strains e1 >= e2 >= e3, Q = J2/3 and Lode angle a, the trial yield function is
 //   f = 2G[(e1 - e3) + s(e1 + e3)] + 2 lambda s I1 - c_bar,
 //   (e1 - e3) + s(e1 + e3) = 2 sqrt(Q) (sqrt(3) sin a + s cos a) + 2 s I1 / 3,
-// and sqrt(3) sin a + s cos a <= sqrt(3 + s^2) for every a (Cauchy-Schwarz).  A point whose bound
-// is below -1e-6 of the size of f's terms is elastic however its eigenvalues round (their error
-// is at most ~1e-8 sqrt(Q), near repeated roots), so the branch test of the full path would say
-// elastic too; such a point is finished from t and I1 alone, with the arithmetic of the elastic
-// branch, so S and DS are bitwise those of the full path.
-__device__ __forceinline__ bool screen_elastic(const double *E, const Mat3 &m, double *t, double &I1) {
+// and sqrt(3) sin a + s cos a <= sqrt(3 + s^2) for every a (Cauchy-Schwarz), so
+//   f <= bound = 2G[2 sqrt(Q) sqrt(3 + s^2) + 2 s I1 / 3] + 2 lambda s I1 - c_bar.
+// The bound is evaluated in FP32 from inputs truncated to 24 bits (J2 from differences of the
+// normal components, so no cancellation against I1): its absolute error stays below ~4e-6 of
+//   size = 2|G| (2 sqrt(Q) sqrt(3 + s^2) + 3 max|t_i|) + 2|lambda s I1| + |c_bar|.
+// A point with bound <= -1e-4 size is therefore elastic however the FP64 eigenvalues of the full
+// path round (their error is at most ~1e-8 sqrt(Q), near repeated roots): the full path's branch
+// test would say elastic too.  Such a point is finished from t and I1 in FP64 with the elastic
+// branch's own arithmetic, so S and DS are bitwise those of the full path, and it costs about a
+// dozen FP64 instructions instead of an eigen-decomposition.
+__device__ __forceinline__ bool screen_elastic(const double *E, const Mat3 &m) {
+    float t[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i] = df_from_f64(E[i]).hi * (i < 3 ? 1.0f : 0.5f);
+    const float G = df_from_f64(m.shear).hi, L = df_from_f64(m.lame).hi;
+    const float s = df_from_f64(m.sin_phi).hi, c = df_from_f64(m.c_bar).hi;
+    const float d01 = t[0] - t[1], d12 = t[1] - t[2], d20 = t[2] - t[0];
+    const float J2 = (d01 * d01 + d12 * d12 + d20 * d20) * (1.0f / 6.0f) + t[3] * t[3] + t[4] * t[4] + t[5] * t[5];
+    const float I1 = t[0] + t[1] + t[2];
+    const float dev = 2.0f * sqrtf(J2 * (1.0f / 3.0f)) * sqrtf(3.0f + s * s);
+    const float bound = 2.0f * G * (dev + (2.0f / 3.0f) * s * I1) + 2.0f * L * s * I1 - c;
+    const float tmax = fmaxf(fmaxf(fabsf(t[0]), fabsf(t[1])), fmaxf(fabsf(t[2]), fmaxf(fabsf(t[3]), fmaxf(fabsf(t[4]), fabsf(t[5])))));
+    const float size = 2.0f * fabsf(G) * (dev + 3.0f * tmax) + 2.0f * fabsf(L * s * I1) + fabsf(c);
+    return bound <= -1e-4f * size;
+}
+// t (shears halved) and I1 of the trial strain, in FP64, as principal3 forms them.
+__device__ __forceinline__ void elastic_trial(const double *E, double *t, double &I1) {
 #pragma unroll
     for (int i = 0; i < 6; ++i) t[i] = half_ident(i) * E[i];
     I1 = t[0] + t[1] + t[2];
-    const double I2 = t[0] * t[1] + t[0] * t[2] + t[1] * t[2] - t[3] * t[3] - t[4] * t[4] - t[5] * t[5];
-    const double Q = fmax((I1 * I1 - 3.0 * I2) / 9.0, 0.0);
-    const double s = m.sin_phi;
-    const double dev = 2.0 * sqrt(Q) * sqrt(3.0 + s * s);
-    const double bound = 2.0 * m.shear * (dev + (2.0 / 3.0) * s * I1) + 2.0 * m.lame * s * I1 - m.c_bar;
-    const double size = 2.0 * fabs(m.shear) * (dev + fabs(I1)) + 2.0 * fabs(m.lame * s * I1) + fabs(m.c_bar);
-    return bound <= -1e-6 * size;
 }
 
 // Stress and (when DS != null) consistent tangent of the decided branch.
@@ -333,12 +347,11 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
 __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
                           double *DS) {
     const Mat3 m{c_bar, sin_phi, shear, lame};
-    {
+    if (screen_elastic(E, m)) {
         double t[6], I1;
-        if (screen_elastic(E, m, t, I1)) {
-            finish_elastic(t, I1, m, S, DS);
-            return kElastic;
-        }
+        elastic_trial(E, t, I1);
+        finish_elastic(t, I1, m, S, DS);
+        return kElastic;
     }
     Principal3 p;
     principal3(E, p);
@@ -388,67 +401,54 @@ __global__ void __launch_bounds__(128) mc3d_kernel(const double *__restrict__ E,
     if (branch) branch[p] = static_cast<int8_t>(b);
 }
 
-// Two-pass return mapping, pass A: every point's branch is decided (points that pass the elastic
-// screen without an eigen-decomposition); elastic and apex points are finished here (they carry no branch-specific tangent work), and the points of the smooth,
-// left-edge and right-edge branches are appended to three lists in scratch memory
-// (scratch[0..2] = counters, then three lists of n entries) with warp-aggregated atomics.
+// Two-pass return mapping.  Pass A screens every point (screen_elastic, FP32): screened points
+// are finished here as elastic (a dozen FP64 instructions); the others are appended to one list
+// in scratch memory (scratch[0] = count, the list from scratch + 4) with a warp-aggregated
+// atomic.  Pass B runs the full FP64 return mapping (eigen-decomposition, branch decision,
+// stress and tangent) on the list, so its warps are dense in the points that need it instead of
+// idling beside screened lanes.
 __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                        const double *__restrict__ sin_phi,
                                                        const double *__restrict__ shear, const double *__restrict__ lame,
                                                        int n, double *__restrict__ S, double *__restrict__ DS,
                                                        int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int list_id = -1;
+    bool listed = false;
     if (p < n) {
         double e[6];
         load6(E, p, e);
         const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
-        double t[6], I1, s[6], ds[36];
-        int b;
-        if (screen_elastic(e, m, t, I1)) {
+        if (screen_elastic(e, m)) {
+            double t[6], I1, s[6], ds[36];
+            elastic_trial(e, t, I1);
             finish_elastic(t, I1, m, s, ds);
-            b = kElastic;
-        } else {
-            Principal3 pr;
-            principal3(e, pr);
-            const Decision3 d = decide3(pr, m);
-            b = d.branch;
-            if (b == kElastic || b == kApex) finish3(pr, d, m, s, ds);
-        }
-        branch[p] = static_cast<int8_t>(b);
-        if (b == kElastic || b == kApex) {
             store6(S, p, s);
             store36(DS, p, ds);
+            branch[p] = static_cast<int8_t>(kElastic);
         } else {
-            list_id = b - 1;
+            listed = true;
         }
     }
     const unsigned lane = threadIdx.x & 31u;
-    int32_t *lists = scratch + 4;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const unsigned mask = __ballot_sync(0xffffffffu, list_id == k);
-        if (mask == 0u) continue;
-        const int leader = __ffs(mask) - 1;
-        int base = 0;
-        if ((int)lane == leader) base = atomicAdd(scratch + k, __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (list_id == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
-    }
+    const unsigned mask = __ballot_sync(0xffffffffu, listed);
+    if (mask == 0u) return;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if ((int)lane == leader) base = atomicAdd(scratch, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (listed) scratch[4 + base + __popc(mask & ((1u << lane) - 1u))] = p;
 }
 
-// Pass B: the points of one plastic branch per blockIdx.y, read from its list, so every warp runs
-// one branch's tangent code.  The branch is taken from pass A, not re-decided.
-__global__ void __launch_bounds__(128) mc3d_plastic_kernel(const double *__restrict__ E,
-                                                           const double *__restrict__ c_bar,
-                                                           const double *__restrict__ sin_phi,
-                                                           const double *__restrict__ shear,
-                                                           const double *__restrict__ lame, int n,
-                                                           double *__restrict__ S, double *__restrict__ DS,
-                                                           const int32_t *__restrict__ scratch) {
-    const int k = blockIdx.y;
-    const int cnt = scratch[k];
-    const int32_t *list = scratch + 4 + (long long)k * n;
+// Pass B: the full return mapping of the listed points.
+__global__ void __launch_bounds__(128) mc3d_list_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
+                                                        const double *__restrict__ sin_phi,
+                                                        const double *__restrict__ shear,
+                                                        const double *__restrict__ lame, int n,
+                                                        double *__restrict__ S, double *__restrict__ DS,
+                                                        int8_t *__restrict__ branch,
+                                                        const int32_t *__restrict__ scratch) {
+    const int cnt = scratch[0];
+    const int32_t *list = scratch + 4;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         const int p = list[i];
         if (p < 0 || p >= n) {
@@ -457,17 +457,15 @@ __global__ void __launch_bounds__(128) mc3d_plastic_kernel(const double *__restr
         }
         double e[6];
         load6(E, p, e);
+        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
         Principal3 pr;
         principal3(e, pr);
-        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
-        Decision3 d{k + 1, 0.0, 1.0};
-        if (k == 0) smooth_lam(pr, m, trial_yield(pr, m), d.lam, d.den);
-        else if (k == 1) left_lam(pr, m, d.lam, d.den);
-        else right_lam(pr, m, d.lam, d.den);
+        const Decision3 d = decide3(pr, m);
         double s[6], ds[36];
         finish3(pr, d, m, s, ds);
         store6(S, p, s);
         store36(DS, p, ds);
+        branch[p] = static_cast<int8_t>(d.branch);
     }
 }
 
@@ -770,8 +768,8 @@ int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const d
     long long gx = (long long)sms * 8;
     const long long need = (n_int + 127) / 128;
     if (gx > need) gx = need;
-    mc3d_plastic_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
-                                                                             DS_out, scratch);
+    mc3d_list_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                                 branch_out, scratch);
     return launch_status();
 }
 
@@ -801,8 +799,8 @@ int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar,
     long long gx = (long long)sms * 8;
     const long long need = (n_int + 127) / 128;
     if (gx > need) gx = need;
-    mc3d_plastic_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
-                                                                             DS_out, scratch);
+    mc3d_list_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                                 branch_out, scratch);
     return launch_status();
 }
 

@@ -58,3 +58,83 @@ int correction_tc_p4(const double *d1, const double *d2, const double *d3, const
                      long long nnz, double scale, double *values, cudaStream_t st);
 
 }  // namespace ssp
+
+namespace ssp {
+
+// ---------------------------------------------------------------------------------------------
+// Double-float arithmetic on the FP32 pipe (a value is an unevaluated sum hi + lo of two floats,
+// about 48 significant bits).  GB300 issues FP64 at a small fraction of the FP32 rate, so the
+// mixed-precision kernels form their compensated products this way.  Error-free transformations
+// after Knuth (TwoSum) and Dekker (TwoProduct, here with a fused multiply-add), in the form of
+// Hida, Li and Bailey's double-double library.  Conversions to and from FP64 use integer bit
+// operations only, so they take no FP64 issue slots.
+
+struct df32 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df32 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ df32 df_fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+    df32 s = df_two_sum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return df_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df32 df_add_f(df32 a, float b) {
+    df32 s = df_two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return df_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_fast_two_sum(p, e);
+}
+// a + b * c
+__device__ __forceinline__ df32 df_fma(df32 a, df32 b, df32 c) { return df_add(a, df_mul(b, c)); }
+
+// FP64 -> hi + lo: hi = x truncated to 24 significant bits, lo = the remaining 29 bits rounded to
+// a float.  Integer operations and one integer->float conversion only.  Zero, FP64 values below
+// the FP32 normal range and non-finite values give (0, 0), (0, 0) and (+-inf or nan, 0); lo is
+// flushed to 0 when it would be subnormal (|x| < 2^-73), where hi alone keeps 2^-24.
+__device__ __forceinline__ df32 df_from_f64(double x) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned sign = static_cast<unsigned>(u >> 32) & 0x80000000u;
+    const int e = static_cast<int>((u >> 52) & 0x7FFull);
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    if (e == 0x7FF) return {__uint_as_float(sign | 0x7F800000u | (m ? 0x400000u : 0u)), 0.0f};
+    const int ef = e - 1023 + 127;  // biased FP32 exponent
+    if (ef <= 0) return {__uint_as_float(sign), 0.0f};
+    if (ef >= 255) return {__uint_as_float(sign | 0x7F800000u), 0.0f};
+    const float hi = __uint_as_float(sign | (static_cast<unsigned>(ef) << 23) | static_cast<unsigned>(m >> 29));
+    const unsigned r = static_cast<unsigned>(m & 0x1FFFFFFFull);  // 29 bits below hi
+    // lo = r * 2^(e - 1023 - 52); the power of two as a float when it is normal
+    const int es = e - 1023 - 52 + 127;
+    float lo = 0.0f;
+    if (r != 0u && es > 0) lo = __uint2float_rn(r) * __uint_as_float(static_cast<unsigned>(es) << 23);
+    return {hi, sign ? -lo : lo};
+}
+// Exact float -> double by bit operations (subnormal floats flush to a signed zero).
+__device__ __forceinline__ double f32_widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+    if (e == 0u) return __longlong_as_double(static_cast<long long>(sign));
+    const unsigned long long ed = e == 0xFFu ? 0x7FFull : static_cast<unsigned long long>(e + 896u);
+    return __longlong_as_double(
+        static_cast<long long>(sign | (ed << 52) | (static_cast<unsigned long long>(u & 0x7FFFFFu) << 29)));
+}
+// hi + lo as one double (one FP64 add).
+__device__ __forceinline__ double df_to_f64(df32 a) { return f32_widen(a.hi) + f32_widen(a.lo); }
+
+}  // namespace ssp

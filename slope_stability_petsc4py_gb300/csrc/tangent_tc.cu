@@ -5,17 +5,19 @@
 //   K_e = sum_q B_q^T dD_q B_q,   dD_q = s w_q (DS_q - D_el,q),   B_q: 6 x 105,
 // which is one dense contraction over kappa = (q, m), m a strain component:
 //   K_e[alpha][beta] = sum_kappa H[alpha][kappa] Bk[kappa][beta],
-//   H[alpha][(q, m)] = (B_q^T dD_q)[alpha][m]          (formed in FP64 on the CUDA cores),
-//   Bk[(q, m)][beta] = B_q[m][beta]                     (the gradients, FP64 in memory).
-// Both operands are split into TF32 pairs, x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and
-// the tensor cores form hi*hi and hi*lo + lo*hi (the three-product TF32 scheme: about 22
-// significant bits per product) in two FP32 accumulators in tensor memory.
+//   H[alpha][(q, m)] = (B_q^T dD_q)[alpha][m],   Bk[(q, m)][beta] = B_q[m][beta].
+// The compensated D*B term: the gradients and dD are split into hi + lo float pairs by bit
+// operations and H is formed in double-float arithmetic on the FP32 pipe (about 48 significant
+// bits; GB300's FP64 pipe is a small fraction of its FP32 rate).  Both operands are then split
+// into TF32 pairs, x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and the tensor cores form
+// hi*hi and hi*lo + lo*hi (the three-product TF32 scheme: about 22 significant bits per product)
+// in two FP32 accumulators in tensor memory.
 //
 // Accuracy.  A tensor-core MMA rounds its FP32 result once per instruction, so errors grow with
 // the number of MMAs that feed one accumulator.  The points of an element are taken in groups of
 // four (K = 24, three K = 8 steps); each group has its own pair of accumulators (hi*hi: three
 // MMAs, cross terms: six, 2^-11 smaller), and the CUDA cores add every group's two partial sums
-// into FP64 registers.  Two accumulator pairs alternate between groups (ping-pong), so the tensor
+// into double-float registers (widened exactly to FP64 once per element).  Two accumulator pairs alternate between groups (ping-pong), so the tensor
 // cores multiply group g while the CUDA cores drain group g - 1 and build group g + 1.  The FP64
 // element sums are added to the CSR values with FP64 reductions through the element->CSR map, on
 // both mirror positions of alpha <= beta, so the correction is exactly symmetric.
@@ -60,9 +62,9 @@ struct Stage {  // one group of four points, operands split hi / lo
     uint32_t b_hi[kBBytes / 4];
     uint32_t b_lo[kBBytes / 4];
 };
-struct PointData {  // FP64 inputs of the group being built
-    double g[kPts][3][kNP];
-    double dD[kPts][kNS * kNS];
+struct PointData {  // inputs of the group being built, as double-float (hi + lo) pairs
+    df32 g[kPts][3][kNP];
+    df32 dD[kPts][kNS * kNS];
 };
 struct Smem {
     Stage stage[2];
@@ -100,9 +102,11 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
 }
-__device__ __forceinline__ void split_tf32(double x, uint32_t &hi, uint32_t &lo) {
-    hi = to_tf32(static_cast<float>(x));
-    lo = to_tf32(static_cast<float>(x - static_cast<double>(__uint_as_float(hi))));
+// A double-float value as two TF32 parts: hi = tf32(x.hi), lo = tf32((x.hi - hi) + x.lo); the
+// subtraction is exact (hi is x.hi rounded to 10 mantissa bits).
+__device__ __forceinline__ void split_tf32(df32 x, uint32_t &hi, uint32_t &lo) {
+    hi = to_tf32(x.hi);
+    lo = to_tf32(__fadd_rn(__fsub_rn(x.hi, __uint_as_float(hi)), x.lo));
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
@@ -167,14 +171,14 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t *r) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// acc[j] += accumulator column (col0 + j) of this thread's lane, j < 28, in FP64.
-__device__ __forceinline__ void drain_add(uint32_t taddr0, double *acc) {
+// acc[j] += accumulator column (col0 + j) of this thread's lane, j < 28, in double-float.
+__device__ __forceinline__ void drain_add(uint32_t taddr0, df32 *acc) {
     uint32_t r[kColsPerWarp];
 #pragma unroll
     for (int i = 0; i < kColsPerWarp / 4; ++i) tmem_ld4(taddr0 + 4 * i, r + 4 * i);
     tmem_wait_ld();
 #pragma unroll
-    for (int j = 0; j < kColsPerWarp; ++j) acc[j] += static_cast<double>(__uint_as_float(r[j]));
+    for (int j = 0; j < kColsPerWarp; ++j) acc[j] = df_add_f(acc[j], __uint_as_float(r[j]));
 }
 
 __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam) {
@@ -183,10 +187,10 @@ __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam)
     return 0.0;
 }
 
-// Every thread waits for the commit of group parity b (bounded), then reads that group's two
-// accumulators into its FP64 sums.
+// Every thread waits for the commit of group parity b (bounded), then adds that group's two
+// accumulators to its double-float sums.
 __device__ __forceinline__ void drain_group(Smem &S, uint32_t tmem, int b, uint32_t &phase_bits, uint32_t lane_col,
-                                            double *acc) {
+                                            df32 *acc) {
     if (!mbar_wait(smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u)) {
         S.abort = 1;
         flag(SSP_DEV_TIMEOUT);
@@ -244,29 +248,33 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
         const int nq = S.nq[parity];
         if (nq == 0) continue;  // uniform across the CTA
         const int groups = (nq + kPts - 1) / kPts;
-        double acc[kColsPerWarp];
+        df32 acc[kColsPerWarp];
 #pragma unroll
-        for (int j = 0; j < kColsPerWarp; ++j) acc[j] = 0.0;
+        for (int j = 0; j < kColsPerWarp; ++j) acc[j] = {0.0f, 0.0f};
         for (int grp = 0; grp < groups; ++grp) {
             const int b = grp & 1;  // stage buffer and accumulator pair; both were released by drain(grp - 2)
-            // FP64 inputs of the group's points (absent slots are zero)
+            // inputs of the group's points as hi + lo pairs (absent slots are zero): the gradients,
+            // and w s (DS - D_el) with the FP64 subtraction only where D_el is nonzero
             for (int i = tid; i < kPts * 3 * kNP; i += kThreads) {
                 const int pi = i / (3 * kNP), rem = i % (3 * kNP), r = rem / kNP, a = rem % kNP;
                 const int k = grp * kPts + pi;
-                double v = 0.0;
+                df32 v{0.0f, 0.0f};
                 if (k < nq) {
                     const long long src = (g0 + S.sq[k]) * kNP + a;
-                    v = r == 0 ? d1[src] : (r == 1 ? d2[src] : d3[src]);
+                    v = df_from_f64(r == 0 ? d1[src] : (r == 1 ? d2[src] : d3[src]));
                 }
                 S.pts.g[pi][r][a] = v;
             }
             for (int i = tid; i < kPts * kNS * kNS; i += kThreads) {
                 const int pi = i / (kNS * kNS), kk = i % (kNS * kNS);
                 const int k = grp * kPts + pi;
-                double v = 0.0;
+                df32 v{0.0f, 0.0f};
                 if (k < nq) {
                     const long long gq = g0 + S.sq[k];
-                    v = w[gq] * (scale * (DS[gq * (kNS * kNS) + kk] - elastic_d3(kk % kNS, kk / kNS, shear[gq], lame[gq])));
+                    double d = DS[gq * (kNS * kNS) + kk];
+                    const double de = elastic_d3(kk % kNS, kk / kNS, shear[gq], lame[gq]);
+                    if (de != 0.0) d -= de;
+                    v = df_mul(df_from_f64(d), df_from_f64(scale * w[gq]));
                 }
                 S.pts.dD[pi][kk] = v;
             }
@@ -276,13 +284,13 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
             unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
             unsigned char *b_hi = reinterpret_cast<unsigned char *>(st.b_hi);
             unsigned char *b_lo = reinterpret_cast<unsigned char *>(st.b_lo);
-            // H = B^T dD (FP64), alpha = 3 * node + component
+            // H = B^T dD in double-float arithmetic on the FP32 pipe, alpha = 3 * node + component
             for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
                 const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), alpha = rem / kNS, m = rem % kNS;
                 const int a = alpha / 3, c = alpha % 3;
-                double h = 0.0;
-#pragma unroll
-                for (int r = 0; r < 3; ++r) h += S.pts.g[pi][r][a] * S.pts.dD[pi][bt_row3(c, r) + kNS * m];
+                df32 h = df_mul(S.pts.g[pi][0][a], S.pts.dD[pi][bt_row3(c, 0) + kNS * m]);
+                h = df_fma(h, S.pts.g[pi][1][a], S.pts.dD[pi][bt_row3(c, 1) + kNS * m]);
+                h = df_fma(h, S.pts.g[pi][2][a], S.pts.dD[pi][bt_row3(c, 2) + kNS * m]);
                 uint32_t hi, lo;
                 split_tf32(h, hi, lo);
                 const int off = kmaj_off(alpha, pi * kNS + m, kM);
@@ -293,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
             for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
                 const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), beta = rem / kNS, m = rem % kNS;
                 const int bn = beta / 3, cp = beta % 3;
-                double v = 0.0;
+                df32 v{0.0f, 0.0f};
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
                     if (bt_row3(cp, r) == m) v = S.pts.g[pi][r][bn];
@@ -332,7 +340,7 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
 #pragma unroll
             for (int j = 0; j < kColsPerWarp; ++j) {
                 const int beta = kColsPerWarp * cq + j;
-                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = acc[j];
+                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = df_to_f64(acc[j]);
             }
         }
         __syncthreads();

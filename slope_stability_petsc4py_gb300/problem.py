@@ -55,7 +55,10 @@ class OwnedCSRMatrix:
     """Owned-row CSR matrix on the fixed pattern, updated in place (stable ``handle``).
 
     ``values`` is the CUDA tensor the kernels write; ``data`` is a pinned host mirror refreshed by
-    ``sync_host()`` (what a PETSc ``setValuesCSR`` would read, utils.py:288-306)."""
+    ``sync_host()`` (what a PETSc ``setValuesCSR`` would read, utils.py:288-306).  The device ->
+    host copy runs on a side stream, so the caller's stream can go on (the operator computes the
+    internal force meanwhile); ``getValuesCSR`` / ``to_scipy`` wait for it, and ``fence()`` makes
+    the current stream wait for it before the values are overwritten."""
 
     _next_handle = 1
 
@@ -67,19 +70,39 @@ class OwnedCSRMatrix:
         t = _lib.torch()
         self._host = t.empty(values.numel(), dtype=t.float64, pin_memory=True)
         self.data = self._host.numpy()
+        self._copy_stream = t.cuda.Stream()
+        self._copied = None  # event recorded after the last host copy
         self.handle = OwnedCSRMatrix._next_handle
         OwnedCSRMatrix._next_handle += 1
 
     def sync_host(self, stream=None):
-        self._host.copy_(self.values, non_blocking=True)
+        t = _lib.torch()
+        cur = t.cuda.current_stream()
+        self._copy_stream.wait_stream(cur)
+        with t.cuda.stream(self._copy_stream):
+            self._host.copy_(self.values, non_blocking=True)
+            self._copied = t.cuda.Event()
+            self._copied.record(self._copy_stream)
+        self.values.record_stream(self._copy_stream)
         return self
 
+    def fence(self):
+        """Make the current stream wait until the last host copy has read the values."""
+        if self._copied is not None:
+            _lib.torch().cuda.current_stream().wait_event(self._copied)
+
+    def _wait(self):
+        t = _lib.torch()
+        t.cuda.current_stream().synchronize()
+        if self._copied is not None:
+            self._copied.synchronize()
+
     def getValuesCSR(self):
-        _lib.torch().cuda.current_stream().synchronize()
+        self._wait()
         return self.indptr, self.indices, self.data
 
     def to_scipy(self) -> csr_matrix:
-        _lib.torch().cuda.current_stream().synchronize()
+        self._wait()
         return csr_matrix((self.data.copy(), self.indices.copy(), self.indptr.copy()), shape=self.shape)
 
     def destroy(self):
@@ -510,6 +533,8 @@ class ConstitutiveOperator:
         pat = self._require_pattern()
         if self._tangent_values is None:
             self._tangent_values = t.empty(pat.nnz, dtype=t.float64, device="cuda")
+        if self._owned_tangent_mat is not None and hasattr(self._owned_tangent_mat, "fence"):
+            self._owned_tangent_mat.fence()
         self._tangent_into(self._tangent_values)
         return self._matrix("tangent", self._tangent_values)
 
@@ -518,6 +543,8 @@ class ConstitutiveOperator:
         pat = self._require_pattern()
         if self._regularized_values is None:
             self._regularized_values = t.empty(pat.nnz, dtype=t.float64, device="cuda")
+        if self._owned_regularized_mat is not None and hasattr(self._owned_regularized_mat, "fence"):
+            self._owned_regularized_mat.fence()
         self._tangent_into(self._regularized_values, r=r)
         return self._matrix("regularized", self._regularized_values)
 
@@ -591,9 +618,10 @@ class ConstitutiveOperator:
         return self.build_F_free(), self._build_owned_tangent_matrix()
 
     def _regularized_pair(self, F_fn, r):
+        # K first: its device -> host copy (the bulk of the hand-off) then overlaps the force
         t0 = perf_counter()
-        F = F_fn()
         K = self.build_K_regularized(r)
+        F = F_fn()
         self.time_build_F_K_tangent.append(perf_counter() - t0)
         return F, K
 

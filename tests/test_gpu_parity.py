@@ -110,15 +110,18 @@ def test_binned_return_mapping_matches_single_pass_and_oracle(oracle):
             scratch = torch.full((3 * n + 4,), -7, dtype=torch.int32, device="cuda")
             _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G),
                       _lib.ptr(L), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch), _lib.stream_handle())
-            counts = scratch[:3].cpu().numpy()
+            listed = int(scratch[0].item())
             b = br.cpu().numpy()
-            assert list(counts) == [int((b == k).sum()) for k in (1, 2, 3)]
+            lst = scratch[4:4 + listed].cpu().numpy()
+            assert int((b != 0).sum()) <= listed <= n  # every plastic point went through the full path
+            assert np.unique(lst).size == listed and set(np.flatnonzero(b != 0)) <= set(lst.tolist())
         outs[mode] = (S.cpu().numpy(), DS.cpu().numpy(), br.cpu().numpy())
     assert np.array_equal(outs["single"][2], outs["binned"][2])
     seen = set(np.unique(outs["binned"][2]).tolist())
     assert {0, 1, 4} <= seen and seen & {2, 3}
-    assert rel_err(outs["binned"][0], outs["single"][0]) <= 1e-15
-    assert rel_err(outs["binned"][1], outs["single"][1]) <= 1e-15
+    # the same FP64 formulas compiled in two kernels (FMA contraction may differ): a few ulps
+    assert rel_err(outs["binned"][0], outs["single"][0]) <= 1e-14
+    assert rel_err(outs["binned"][1], outs["single"][1]) <= 1e-14
     S_o, DS_o = oracle.constitutive_3d(E, c_bar, sin_phi, shear, shear, lame)
     assert rel_err(outs["binned"][0], S_o) <= PLAIN_RTOL
     assert rel_err(outs["binned"][1], DS_o) <= PLAIN_RTOL
@@ -465,9 +468,16 @@ def test_elastic_screen_near_yield_and_screen_threshold(oracle):
     for m in mult:  # around the yield surface
         pts.append(D[ok] * (c_bar / g1[ok] * m)[:, None])
         rep_tag.append(repeated_dir[ok])
-    ok = h1 + 1e-6 * size1 > 0
-    alpha_s = c_bar * (1 - 1e-6) / (h1[ok] + 1e-6 * size1[ok])  # the screen's threshold
-    for m in (1 - 1e-9, 1 - 1e-12, 1.0, 1 + 1e-12, 1 + 1e-9):
+    # the screen's threshold: bound = -1e-4 size with the kernel's size = 2G (dev + 3 max|t|) +
+    # 2|lambda s I1| + c_bar (dev and I1 scale with the strain, c_bar does not)
+    tD = D.copy()
+    tD[:, 3:] *= 0.5
+    dev1 = (h1 - 2 * lame * sin_phi * tD[:, :3].sum(1)) / (2 * shear) - 2 * sin_phi * tD[:, :3].sum(1) / 3
+    size_k = 2 * shear * (dev1 + 3 * np.abs(tD).max(1)) + 2 * np.abs(lame * sin_phi * tD[:, :3].sum(1))
+    ok = h1 + 1e-4 * size_k > 0
+    alpha_s = c_bar * (1 - 1e-4) / (h1[ok] + 1e-4 * size_k[ok])
+    # the screen's FP32 noise is ~4e-6 of size; beyond 1e-4 the yield surface is reached
+    for m in (1 - 3e-5, 1 - 1e-6, 1 - 1e-7, 1.0, 1 + 1e-7, 1 + 1e-6, 1 + 3e-5):
         pts.append(D[ok] * (alpha_s * m)[:, None])
         rep_tag.append(repeated_dir[ok])
     E = np.vstack(pts)
@@ -497,7 +507,7 @@ def test_elastic_screen_near_yield_and_screen_threshold(oracle):
     g, h, size = _yield_parts(E, shear, lame, sin_phi)
     f = g - c_bar
     # the reference's trigonometric eigenvalues carry up to ~1e-8 sqrt(Q) of rounding near repeated
-    # roots, so decisions are compared where |f| exceeds 1e-7 of its terms (the screen's margin is 1e-6)
+    # roots, so decisions are compared where |f| exceeds 1e-7 of its terms (the screen's margin is 1e-4)
     tol = 1e-7 * (size + c_bar)
     assert np.all(f[el] <= tol[el])  # never elastic where the reference yields
     assert np.all(br[f < -tol] == 0) and np.all(br[f > tol] != 0)
@@ -510,6 +520,6 @@ def test_elastic_screen_near_yield_and_screen_threshold(oracle):
         assert rel_err(outs[mode][0][well], S_o[well]) <= PLAIN_RTOL
         assert rel_err(outs[mode][1][well], DS_o[well]) <= PLAIN_RTOL
     thr = np.zeros(n, dtype=bool)
-    thr[-5 * int((h1 + 1e-6 * size1 > 0).sum()):] = True  # the points at the screen's threshold
+    thr[-7 * int(ok.sum()):] = True  # the points around the screen's threshold
     assert np.all(br[thr] == 0)
     print(f"{n} points, {int(well.sum())} compared with the oracle, elastic {float(np.mean(el)):.3f}")
