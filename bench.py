@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--return-mapping", default="binned", choices=["binned", "unsorted", "learned"],
                     help="binned: two-pass exact binning; unsorted: one divergent pass; learned: bins proposed "
                          "by the branch network (trained on the GPU before the timed region)")
+    ap.add_argument("--no-forms", action="store_true", help="skip timing the mixed / learned / unsorted forms")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
@@ -269,6 +270,44 @@ def algorithmic(name, st):
     return {"bytes": 0, "flops": 0}
 
 
+def time_steps(torch, step, warmup, steps):
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def compare_forms(torch, lib, op, mesh, mats, args, step, ms_plain):
+    """The same step in the other forms, on the same state and timed the same way: the mixed
+    tangent, the mixed tangent with the learned branch proposal, and the unsorted single-pass
+    return mapping (the method without binning).  Restores the plain form afterwards."""
+    n_int = op.owned_tangent_pattern.n_local_int
+    out = {"plain": {"value": n_int / (ms_plain * 1e-3), "ms_per_step": ms_plain}}
+    w = max(args.warmup, 3)
+    op.tangent_form = "plain"
+    kp = op.build_K_regularized(R_REG).values.clone()
+    for name, form, mapping in (("mixed", "mixed", "binned"), ("mixed+learned", "mixed", "learned"),
+                                ("plain+unsorted", "plain", "unsorted"), ("plain+learned", "plain", "learned")):
+        if mapping == "learned" and op.branch_model is None:
+            out["learned_training"] = train_branch_model(torch, op, mesh, mats, args.config)
+        op.tangent_form, op.return_mapping = form, mapping
+        ms = time_steps(torch, step, w, args.steps)
+        entry = {"value": n_int / (ms * 1e-3), "ms_per_step": ms, "speedup_vs_plain": ms_plain / ms}
+        if form == "mixed":
+            km = op.build_K_regularized(R_REG).values
+            entry["tangent_error_vs_fp64"] = float((km - kp).abs().max() / kp.abs().max())
+        out[name] = entry
+    op.tangent_form, op.return_mapping = "plain", "binned"
+    lib.raise_on_device_status()
+    return out
+
+
 def train_branch_model(torch, op, mesh, mats, name):
     """Train the branch-proposal network on continuation states other than the timed one
     (strength-reduction factors 1.0..1.4, shear-band amplitudes 0.4..1.6 x the workload's)."""
@@ -411,6 +450,9 @@ def run_gpu(args):
         learned_info["distinct_branches_per_warp"] = {"point_order": learned.warp_branch_mix(br),
                                                       "learned_bins": learned.warp_branch_mix(br, order)}
         line["learned"] = learned_info
+
+    if args.form == "plain" and args.return_mapping == "binned" and pat.dim == 3 and not args.no_forms:
+        line["forms"] = compare_forms(torch, _lib, op, mesh, mats, args, step, ms)
 
     if rank == 0 and not args.no_e2e:
         op.host_outputs = True

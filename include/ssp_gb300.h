@@ -70,15 +70,16 @@ int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, c
                                 const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
                                 int8_t *branch_out, void *stream);
 
-/* The 3D return mapping in two passes over the same arithmetic (replaces
+/* The 3D return mapping in three passes over the same arithmetic (replaces
  * constitutive_problem_3d_sds_batch_c, constitutive_3d_batch.h:15-25): pass A bounds every point's
  * trial yield function from its invariants (FP32, with a margin that covers FP32 and eigenvalue
  * rounding) and finishes the points it proves elastic with the elastic branch's FP64 arithmetic;
- * the other points are collected into a list and pass B runs the full FP64 return mapping on it,
- * so its warps are dense.  Results equal ssp_constitutive_sds_branch's (same branch codes; S and DS
- * of elastic points bitwise).  scratch is caller-allocated device memory of 3*n_int + 4 int32
- * (scratch[0] = listed points, the list from scratch + 4); it is overwritten.  Outputs as
- * ssp_constitutive_sds_branch. */
+ * pass B runs the FP64 eigen-decomposition and branch decision on the other points (a dense list)
+ * and finishes elastic and apex ones; pass C finishes the smooth-face, left-edge and right-edge
+ * points one branch per warp from the decision record pass B leaves in their DS rows.  Results
+ * equal ssp_constitutive_sds_branch's (same branch codes; the same FP64 operations).  scratch is
+ * caller-allocated device memory of 3*n_int + 4 int32 (counters and point lists); it is
+ * overwritten.  Outputs as ssp_constitutive_sds_branch. */
 int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
                                    int32_t *scratch, void *stream);

@@ -108,7 +108,7 @@ _KERNELS_PER_CALL = {
     "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
     "ssp_copy_out": 1, "ssp_host_writable": 0,
     "ssp_tangent_plastic_correction": 1,
-    "ssp_constitutive_3d_sds_binned": 2, "ssp_constitutive_3d_sds_binned_noalloc": 2,
+    "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
     "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 2,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,

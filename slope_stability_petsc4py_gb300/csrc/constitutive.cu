@@ -401,12 +401,71 @@ __global__ void __launch_bounds__(128) mc3d_kernel(const double *__restrict__ E,
     if (branch) branch[p] = static_cast<int8_t>(b);
 }
 
-// Two-pass return mapping.  Pass A screens every point (screen_elastic, FP32): screened points
-// are finished here as elastic (a dozen FP64 instructions); the others are appended to one list
-// in scratch memory (scratch[0] = count, the list from scratch + 4) with a warp-aggregated
-// atomic.  Pass B runs the full FP64 return mapping (eigen-decomposition, branch decision,
-// stress and tangent) on the list, so its warps are dense in the points that need it instead of
-// idling beside screened lanes.
+// Binned return mapping in three passes.  scratch = 4 counters, then three regions of n int32.
+//   A: every point is screened (screen_elastic, FP32); screened points are finished as elastic
+//      (a dozen FP64 instructions), the others are appended to list L (counter 0, region 0).
+//   B: over L, the FP64 eigen-decomposition and branch decision (dense warps); elastic and apex
+//      points are finished here; a smooth / left-edge / right-edge point leaves its decision record
+//      (principal values, t, t*t, I1, multiplier, denominator: 18 doubles) in the first entries of
+//      its own DS row, which pass C overwrites, and is appended to its branch's list (smooth:
+//      region 1 from the front; left: region 2 from the front; right: region 2 from the back;
+//      counters 1, 2, 3).
+//   C: one branch per blockIdx.y: the stress and consistent tangent from the record, so every
+//      warp runs one branch's code and nothing is computed twice.
+// Every result equals the single-pass kernel's (the same operations on the same values).
+constexpr int kRecord = 18;
+__device__ __forceinline__ void store_record(double *DS, long long p, const Principal3 &pr, const Decision3 &d) {
+    double r[kRecord];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        r[i] = pr.t[i];
+        r[6 + i] = pr.sq[i];
+    }
+    r[12] = pr.I1;
+    r[13] = pr.e1;
+    r[14] = pr.e2;
+    r[15] = pr.e3;
+    r[16] = d.lam;
+    r[17] = d.den;
+    double2 *D2 = reinterpret_cast<double2 *>(DS + 36 * p);
+#pragma unroll
+    for (int k = 0; k < kRecord / 2; ++k) D2[k] = make_double2(r[2 * k], r[2 * k + 1]);
+}
+__device__ __forceinline__ void load_record(const double *DS, long long p, Principal3 &pr, Decision3 &d) {
+    double r[kRecord];
+    const double2 *D2 = reinterpret_cast<const double2 *>(DS + 36 * p);
+#pragma unroll
+    for (int k = 0; k < kRecord / 2; ++k) {
+        const double2 v = D2[k];
+        r[2 * k] = v.x;
+        r[2 * k + 1] = v.y;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        pr.t[i] = r[i];
+        pr.sq[i] = r[6 + i];
+    }
+    pr.I1 = r[12];
+    pr.e1 = r[13];
+    pr.e2 = r[14];
+    pr.e3 = r[15];
+    d.lam = r[16];
+    d.den = r[17];
+}
+
+// warp-aggregated append of the lanes with want == true to list[...] through counter *ctr;
+// returns this lane's slot
+__device__ __forceinline__ int warp_append(bool want, int32_t *ctr) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(__activemask(), want);
+    if (mask == 0u) return -1;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if ((int)lane == leader) base = atomicAdd(ctr, __popc(mask));
+    base = __shfl_sync(__activemask(), base, leader);
+    return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
 __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                        const double *__restrict__ sin_phi,
                                                        const double *__restrict__ shear, const double *__restrict__ lame,
@@ -429,44 +488,104 @@ __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict_
             listed = true;
         }
     }
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned mask = __ballot_sync(0xffffffffu, listed);
-    if (mask == 0u) return;
-    const int leader = __ffs(mask) - 1;
-    int base = 0;
-    if ((int)lane == leader) base = atomicAdd(scratch, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (listed) scratch[4 + base + __popc(mask & ((1u << lane) - 1u))] = p;
+    const int slot = warp_append(listed, scratch);
+    if (listed) scratch[4 + slot] = p;
 }
 
-// Pass B: the full return mapping of the listed points.
-__global__ void __launch_bounds__(128) mc3d_list_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
-                                                        const double *__restrict__ sin_phi,
-                                                        const double *__restrict__ shear,
-                                                        const double *__restrict__ lame, int n,
-                                                        double *__restrict__ S, double *__restrict__ DS,
-                                                        int8_t *__restrict__ branch,
-                                                        const int32_t *__restrict__ scratch) {
+__global__ void __launch_bounds__(128) mc3d_decide_kernel(const double *__restrict__ E,
+                                                          const double *__restrict__ c_bar,
+                                                          const double *__restrict__ sin_phi,
+                                                          const double *__restrict__ shear,
+                                                          const double *__restrict__ lame, int n,
+                                                          double *__restrict__ S, double *__restrict__ DS,
+                                                          int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
     const int cnt = scratch[0];
-    const int32_t *list = scratch + 4;
+    const int32_t *L = scratch + 4;
+    int32_t *smooth = scratch + 4 + n, *edges = scratch + 4 + 2ll * n;
+    const int stride = gridDim.x * blockDim.x;
+    // whole warps iterate together (the appends are warp-collective)
+    const int iters = (cnt + stride - 1) / stride;
+    for (int it = 0; it < iters; ++it) {
+        const int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        int p = -1, b = -1;
+        if (i < cnt) {
+            p = L[i];
+            if (p < 0 || p >= n) {
+                flag(SSP_DEV_BAD_INDEX);
+                p = -1;
+            }
+        }
+        if (p >= 0) {
+            double e[6];
+            load6(E, p, e);
+            const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
+            Principal3 pr;
+            principal3(e, pr);
+            const Decision3 d = decide3(pr, m);
+            b = d.branch;
+            branch[p] = static_cast<int8_t>(b);
+            if (b == kElastic || b == kApex) {
+                double s[6], ds[36];
+                finish3(pr, d, m, s, ds);
+                store6(S, p, s);
+                store36(DS, p, ds);
+            } else {
+                store_record(DS, p, pr, d);
+            }
+        }
+        const int js = warp_append(b == kSmooth, scratch + 1);
+        if (b == kSmooth) smooth[js] = p;
+        const int jl = warp_append(b == kLeft, scratch + 2);
+        if (b == kLeft) edges[jl] = p;
+        const int jr = warp_append(b == kRight, scratch + 3);
+        if (b == kRight) edges[n - 1 - jr] = p;
+    }
+}
+
+__global__ void __launch_bounds__(128) mc3d_finish_kernel(const double *__restrict__ c_bar,
+                                                          const double *__restrict__ sin_phi,
+                                                          const double *__restrict__ shear,
+                                                          const double *__restrict__ lame, int n,
+                                                          double *__restrict__ S, double *__restrict__ DS,
+                                                          const int32_t *__restrict__ scratch) {
+    const int k = blockIdx.y;  // 0 smooth, 1 left edge, 2 right edge
+    const int cnt = scratch[1 + k];
+    const int32_t *smooth = scratch + 4 + n, *edges = scratch + 4 + 2ll * n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-        const int p = list[i];
+        const int p = k == 0 ? smooth[i] : (k == 1 ? edges[i] : edges[n - 1 - i]);
         if (p < 0 || p >= n) {
             flag(SSP_DEV_BAD_INDEX);
             continue;
         }
-        double e[6];
-        load6(E, p, e);
-        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
         Principal3 pr;
-        principal3(e, pr);
-        const Decision3 d = decide3(pr, m);
+        Decision3 d{k + 1, 0.0, 1.0};
+        load_record(DS, p, pr, d);
+        const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
         double s[6], ds[36];
         finish3(pr, d, m, s, ds);
         store6(S, p, s);
         store36(DS, p, ds);
-        branch[p] = static_cast<int8_t>(d.branch);
     }
+}
+
+// The three passes on one stream.  scratch: 4 + 3 n int32.
+int launch_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                  const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                  cudaStream_t st) {
+    if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                          branch_out, scratch);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long gx = (long long)sms * 8;
+    const long long need = (n_int + 127) / 128;
+    if (gx > need) gx = need;
+    mc3d_decide_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                                   branch_out, scratch);
+    mc3d_finish_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                           DS_out, scratch);
+    return launch_status();
 }
 
 // ---------------------------------------------------------------------------- 2D
@@ -758,19 +877,8 @@ int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const d
     if (n_int == 0) return SSP_OK;
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
         return SSP_ERR_INVALID;
-    cudaStream_t st = as_stream(stream);
-    if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                          branch_out, scratch);
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long gx = (long long)sms * 8;
-    const long long need = (n_int + 127) / 128;
-    if (gx > need) gx = need;
-    mc3d_list_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                                 branch_out, scratch);
-    return launch_status();
+    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                         as_stream(stream));
 }
 
 // Same two-pass return mapping for callers that have no way to allocate device memory: a
@@ -788,20 +896,8 @@ int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar,
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out) return SSP_ERR_INVALID;
     int32_t *scratch = fixed_scratch_for_current_device();
     if (!scratch) return SSP_ERR_CUDA;
-    cudaStream_t st = as_stream(stream);
-    // the counters must start at zero on every call; the lists are written before they are read
-    if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                          branch_out, scratch);
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long gx = (long long)sms * 8;
-    const long long need = (n_int + 127) / 128;
-    if (gx > need) gx = need;
-    mc3d_list_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                                 branch_out, scratch);
-    return launch_status();
+    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                         as_stream(stream));
 }
 
 int ssp_constitutive_2d(const double *E, const double *c_bar, const double *sin_phi, const double *shear,

@@ -102,6 +102,21 @@ __device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
 }
 // a + b * c
 __device__ __forceinline__ df32 df_fma(df32 a, df32 b, df32 c) { return df_add(a, df_mul(b, c)); }
+// a0 b0 + a1 b1 + a2 b2 as a compensated dot product (Ogita, Rump and Oishi's Dot2 on the hi
+// parts, with the hi*lo cross terms and the rounding errors gathered in one float).
+__device__ __forceinline__ df32 df_dot3(df32 a0, df32 b0, df32 a1, df32 b1, df32 a2, df32 b2) {
+    const float p0 = __fmul_rn(a0.hi, b0.hi), p1 = __fmul_rn(a1.hi, b1.hi), p2 = __fmul_rn(a2.hi, b2.hi);
+    float e = __fmaf_rn(a0.hi, b0.hi, -p0);
+    e = __fadd_rn(e, __fmaf_rn(a1.hi, b1.hi, -p1));
+    e = __fadd_rn(e, __fmaf_rn(a2.hi, b2.hi, -p2));
+    const df32 s1 = df_two_sum(p0, p1);
+    const df32 s2 = df_two_sum(s1.hi, p2);
+    e = __fadd_rn(e, __fadd_rn(s1.lo, s2.lo));
+    e = __fmaf_rn(a0.hi, b0.lo, __fmaf_rn(a0.lo, b0.hi, e));
+    e = __fmaf_rn(a1.hi, b1.lo, __fmaf_rn(a1.lo, b1.hi, e));
+    e = __fmaf_rn(a2.hi, b2.lo, __fmaf_rn(a2.lo, b2.hi, e));
+    return df_fast_two_sum(s2.hi, e);
+}
 
 // FP64 -> hi + lo: hi = x truncated to 24 significant bits, lo = the remaining 29 bits rounded to
 // a float.  Integer operations and one integer->float conversion only.  Zero, FP64 values below

@@ -7,8 +7,8 @@
 //   K_e[alpha][beta] = sum_kappa H[alpha][kappa] Bk[kappa][beta],
 //   H[alpha][(q, m)] = (B_q^T dD_q)[alpha][m],   Bk[(q, m)][beta] = B_q[m][beta].
 // The compensated D*B term: the gradients and dD are split into hi + lo float pairs by bit
-// operations and H is formed in double-float arithmetic on the FP32 pipe (about 48 significant
-// bits; GB300's FP64 pipe is a small fraction of its FP32 rate).  Both operands are then split
+// operations and every H entry is a compensated dot product of three double-float terms on the
+// FP32 pipe (about 46 significant bits; GB300's FP64 pipe is a small fraction of its FP32 rate).  Both operands are then split
 // into TF32 pairs, x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and the tensor cores form
 // hi*hi and hi*lo + lo*hi (the three-product TF32 scheme: about 22 significant bits per product)
 // in two FP32 accumulators in tensor memory.
@@ -17,7 +17,7 @@
 // the number of MMAs that feed one accumulator.  The points of an element are taken in groups of
 // four (K = 24, three K = 8 steps); each group has its own pair of accumulators (hi*hi: three
 // MMAs, cross terms: six, 2^-11 smaller), and the CUDA cores add every group's two partial sums
-// into double-float registers (widened exactly to FP64 once per element).  Two accumulator pairs alternate between groups (ping-pong), so the tensor
+// into compensated (Kahan) FP32 sums in registers (widened exactly to FP64 once per element).  Two accumulator pairs alternate between groups (ping-pong), so the tensor
 // cores multiply group g while the CUDA cores drain group g - 1 and build group g + 1.  The FP64
 // element sums are added to the CSR values with FP64 reductions through the element->CSR map, on
 // both mirror positions of alpha <= beta, so the correction is exactly symmetric.
@@ -171,14 +171,45 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t *r) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// acc[j] += accumulator column (col0 + j) of this thread's lane, j < 28, in double-float.
-__device__ __forceinline__ void drain_add(uint32_t taddr0, df32 *acc) {
-    uint32_t r[kColsPerWarp];
-#pragma unroll
-    for (int i = 0; i < kColsPerWarp / 4; ++i) tmem_ld4(taddr0 + 4 * i, r + 4 * i);
+// 32 lanes x 8 consecutive FP32 columns (no wait).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+}
+// 32 lanes x 16 consecutive FP32 columns (no wait).
+__device__ __forceinline__ void tmem_ld16nw(uint32_t taddr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+// The 28 accumulator columns col0 .. col0 + 27 of this thread's lane.
+__device__ __forceinline__ void tmem_ld28(uint32_t taddr0, uint32_t *r) {
+    tmem_ld16nw(taddr0, r);
+    tmem_ld8(taddr0 + 16, r + 16);
+    tmem_ld4(taddr0 + 24, r + 24);
+}
+
+// Compensated (Kahan) running sums of the groups' partials: sum[j] - comp[j] is the element's
+// value of column j; each group adds its hi*hi and cross partials.
+__device__ __forceinline__ void drain_add(uint32_t taddr_hh, uint32_t taddr_x, float *sum, float *comp) {
+    uint32_t rh[kColsPerWarp], rx[kColsPerWarp];
+    tmem_ld28(taddr_hh, rh);
+    tmem_ld28(taddr_x, rx);
     tmem_wait_ld();
 #pragma unroll
-    for (int j = 0; j < kColsPerWarp; ++j) acc[j] = df_add_f(acc[j], __uint_as_float(r[j]));
+    for (int j = 0; j < kColsPerWarp; ++j) {
+        const float x = __fadd_rn(__uint_as_float(rh[j]), __uint_as_float(rx[j]));
+        const float y = __fsub_rn(x, comp[j]);
+        const float t = __fadd_rn(sum[j], y);
+        comp[j] = __fsub_rn(__fsub_rn(t, sum[j]), y);
+        sum[j] = t;
+    }
 }
 
 __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam) {
@@ -188,9 +219,9 @@ __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam)
 }
 
 // Every thread waits for the commit of group parity b (bounded), then adds that group's two
-// accumulators to its double-float sums.
+// accumulators to its compensated sums.
 __device__ __forceinline__ void drain_group(Smem &S, uint32_t tmem, int b, uint32_t &phase_bits, uint32_t lane_col,
-                                            df32 *acc) {
+                                            float *sum, float *comp) {
     if (!mbar_wait(smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u)) {
         S.abort = 1;
         flag(SSP_DEV_TIMEOUT);
@@ -198,9 +229,8 @@ __device__ __forceinline__ void drain_group(Smem &S, uint32_t tmem, int b, uint3
     phase_bits ^= 1u << b;
     fence_after_sync();
     const uint32_t base = tmem + lane_col + 256u * b;
-    drain_add(base, acc);         // hi * hi
-    drain_add(base + 128u, acc);  // hi * lo + lo * hi
-    fence_before_sync();          // these reads precede the next MMAs into this pair
+    drain_add(base, base + 128u, sum, comp);  // hi * hi, hi * lo + lo * hi
+    fence_before_sync();                      // these reads precede the next MMAs into this pair
 }
 
 __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
@@ -248,9 +278,9 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
         const int nq = S.nq[parity];
         if (nq == 0) continue;  // uniform across the CTA
         const int groups = (nq + kPts - 1) / kPts;
-        df32 acc[kColsPerWarp];
+        float sum[kColsPerWarp], comp[kColsPerWarp];
 #pragma unroll
-        for (int j = 0; j < kColsPerWarp; ++j) acc[j] = {0.0f, 0.0f};
+        for (int j = 0; j < kColsPerWarp; ++j) sum[j] = comp[j] = 0.0f;
         for (int grp = 0; grp < groups; ++grp) {
             const int b = grp & 1;  // stage buffer and accumulator pair; both were released by drain(grp - 2)
             // inputs of the group's points as hi + lo pairs (absent slots are zero): the gradients,
@@ -284,32 +314,34 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
             unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
             unsigned char *b_hi = reinterpret_cast<unsigned char *>(st.b_hi);
             unsigned char *b_lo = reinterpret_cast<unsigned char *>(st.b_lo);
-            // H = B^T dD in double-float arithmetic on the FP32 pipe, alpha = 3 * node + component
-            for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
-                const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), alpha = rem / kNS, m = rem % kNS;
-                const int a = alpha / 3, c = alpha % 3;
-                df32 h = df_mul(S.pts.g[pi][0][a], S.pts.dD[pi][bt_row3(c, 0) + kNS * m]);
-                h = df_fma(h, S.pts.g[pi][1][a], S.pts.dD[pi][bt_row3(c, 1) + kNS * m]);
-                h = df_fma(h, S.pts.g[pi][2][a], S.pts.dD[pi][bt_row3(c, 2) + kNS * m]);
-                uint32_t hi, lo;
-                split_tf32(h, hi, lo);
-                const int off = kmaj_off(alpha, pi * kNS + m, kM);
-                *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
-                *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
-            }
-            // Bk[(q, m)][beta] = B_q[m][beta]: the gradient component r with bt_row3(comp, r) == m
-            for (int i = tid; i < kPts * kNLD * kNS; i += kThreads) {
-                const int pi = i / (kNLD * kNS), rem = i % (kNLD * kNS), beta = rem / kNS, m = rem % kNS;
-                const int bn = beta / 3, cp = beta % 3;
-                df32 v{0.0f, 0.0f};
+            if (tid < kPts * kNLD) {
+                // H = B^T dD for one (point, alpha), all six strain components: compensated dot
+                // products of three terms on the FP32 pipe; alpha = 3 * node + component
+                const int pi = tid / kNLD, alpha = tid - pi * kNLD;
+                const int a = alpha / 3, c = alpha - 3 * a;
+                const df32 ga = S.pts.g[pi][0][a], gb = S.pts.g[pi][1][a], gc = S.pts.g[pi][2][a];
+                const int k0 = bt_row3(c, 0), k1 = bt_row3(c, 1), k2 = bt_row3(c, 2);
+                const df32 *D = S.pts.dD[pi];
 #pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    if (bt_row3(cp, r) == m) v = S.pts.g[pi][r][bn];
-                uint32_t hi, lo;
-                split_tf32(v, hi, lo);
-                const int off = kmaj_off(beta, pi * kNS + m, kN);
-                *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
-                *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
+                for (int m = 0; m < kNS; ++m) {
+                    const df32 h = df_dot3(ga, D[k0 + kNS * m], gb, D[k1 + kNS * m], gc, D[k2 + kNS * m]);
+                    uint32_t hi, lo;
+                    split_tf32(h, hi, lo);
+                    const int off = kmaj_off(alpha, pi * kNS + m, kM);
+                    *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
+                    *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
+                }
+            } else {
+                // the nonzeros of Bk: g[pi][r][bn] at beta = 3 bn + cp, kappa = 6 pi + bt_row3(cp, r); the
+                // other entries are zero in every group and were zeroed once
+                for (int i = tid - kPts * kNLD; i < kPts * 3 * kNP * 3; i += kThreads - kPts * kNLD) {
+                    const int cp = i % 3, rest = i / 3, bn = rest % kNP, pr = rest / kNP, r = pr % 3, pi = pr / 3;
+                    uint32_t hi, lo;
+                    split_tf32(S.pts.g[pi][r][bn], hi, lo);
+                    const int off = kmaj_off(3 * bn + cp, pi * kNS + bt_row3(cp, r), kN);
+                    *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
+                    *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
+                }
             }
             fence_async_smem();  // generic-proxy writes -> visible to the tensor cores
             __syncthreads();
@@ -327,10 +359,10 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
                 }
                 mma_commit(smem_u32(&S.mbar[b]));
             }
-            if (grp >= 1) drain_group(S, tmem, b ^ 1, phase_bits, lane_col, acc);
+            if (grp >= 1) drain_group(S, tmem, b ^ 1, phase_bits, lane_col, sum, comp);
         }
         if (S.abort) break;
-        drain_group(S, tmem, (groups - 1) & 1, phase_bits, lane_col, acc);
+        drain_group(S, tmem, (groups - 1) & 1, phase_bits, lane_col, sum, comp);
         __syncthreads();  // also orders this element's shared-memory reads before the next element's writes
         if (S.abort) break;
         // stage the upper triangle, then scatter every entry row by row (consecutive threads ->
@@ -340,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
 #pragma unroll
             for (int j = 0; j < kColsPerWarp; ++j) {
                 const int beta = kColsPerWarp * cq + j;
-                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = df_to_f64(acc[j]);
+                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = df_to_f64({sum[j], -comp[j]});
             }
         }
         __syncthreads();

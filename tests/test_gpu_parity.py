@@ -110,11 +110,12 @@ def test_binned_return_mapping_matches_single_pass_and_oracle(oracle):
             scratch = torch.full((3 * n + 4,), -7, dtype=torch.int32, device="cuda")
             _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(Ed), _lib.ptr(cb), _lib.ptr(sp), _lib.ptr(G),
                       _lib.ptr(L), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch), _lib.stream_handle())
-            listed = int(scratch[0].item())
+            listed, n_smooth, n_left, n_right = (int(v) for v in scratch[:4].cpu().numpy())
             b = br.cpu().numpy()
             lst = scratch[4:4 + listed].cpu().numpy()
             assert int((b != 0).sum()) <= listed <= n  # every plastic point went through the full path
             assert np.unique(lst).size == listed and set(np.flatnonzero(b != 0)) <= set(lst.tolist())
+            assert [n_smooth, n_left, n_right] == [int((b == k).sum()) for k in (1, 2, 3)]
         outs[mode] = (S.cpu().numpy(), DS.cpu().numpy(), br.cpu().numpy())
     assert np.array_equal(outs["single"][2], outs["binned"][2])
     seen = set(np.unique(outs["binned"][2]).tolist())
