@@ -33,6 +33,25 @@ sys.path.insert(0, str(REPO))
 METRIC = "quad-pts/s constitutive+tangent; FP64 plain vs mixed+learned at ≤1e-6 err"
 LAMBDA, R_REG = 1.1, 0.1
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the step kernels, from one
+# ncu capture of the full-size workload on a GB300 (one pass per launch, the second Newton step of
+# `bench.py --steps 3 --warmup 3`); keyed by workload and C-ABI entry point.
+NCU_TRAFFIC = {
+    "3d_p2_homo": {
+        "ssp_tangent_plastic_correction": 283.76e6 + 60.25e6,
+        "ssp_tangent_plastic_correction_mixed": 283.38e6 + 59.38e6,
+        "ssp_assemble_overlap_strain_3d": 285.23e6 + 36.26e6,
+        "ssp_assemble_force_element": 343.75e6 + 2.65e6,
+        "ssp_constitutive_3d_sds_binned": (124.71 + 302.00 + 22.34 + 1.75 + 34.33 + 1.11) * 1e6,
+    },
+    "3d_p4_hetero": {
+        "ssp_tangent_plastic_correction_mixed": 1121.05e6 + 524.74e6,
+        "ssp_assemble_overlap_strain_3d": 1784.86e6 + 50.96e6,
+        "ssp_assemble_force_element": 1102.46e6 + 11.75e6,
+        "ssp_constitutive_3d_sds_binned": (121.29 + 245.19 + 39.91 + 39.69 + 41.21 + 1.96) * 1e6,
+    },
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -428,7 +447,8 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else hbm_src,
-                     "traffic": None, "ms_per_launch": k_ms, "algorithmic_bytes": alg["bytes"]},
+                     "traffic": NCU_TRAFFIC.get(args.config, {}).get(dominant), "ms_per_launch": k_ms,
+                     "algorithmic_bytes": alg["bytes"]},
         "roofline_fp64": ({"bound": "fp64", "kernel": corr, "achieved": fl / (corr_ms * 1e-3) / 1e12, "peak": fp64_tf,
                            "unit": "TFLOP/s", "frac": fl / (corr_ms * 1e-3) / 1e12 / fp64_tf,
                            "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)", "algorithmic_flops": fl,

@@ -450,7 +450,7 @@ struct WarpSlice {
 };
 
 template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR, bool MIXED>
-__global__ void __launch_bounds__(32 * WARPS, 3) tangent_element_warp_kernel(ElemArgs A) {
+__global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;

@@ -466,12 +466,22 @@ __device__ __forceinline__ int warp_append(bool want, int32_t *ctr) {
     return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
+// The DS rows of a warp's 32 points are one contiguous 9 KiB block: pass A stages them in shared
+// memory (row stride 37 doubles, so the per-lane row writes are at most 2-way bank conflicts) and
+// the warp writes the block with consecutive 8-byte stores (full cache lines) instead of 32
+// strided rows.  Rows of listed points are written with whatever the stage holds; passes B and C
+// overwrite them.
+constexpr int kDsStride = 37;
 __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                        const double *__restrict__ sin_phi,
                                                        const double *__restrict__ shear, const double *__restrict__ lame,
                                                        int n, double *__restrict__ S, double *__restrict__ DS,
                                                        int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
+    __shared__ double stage[4][32 * kDsStride];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p0 = blockIdx.x * blockDim.x + warp * 32;
+    double *w = stage[warp];
     bool listed = false;
     if (p < n) {
         double e[6];
@@ -482,10 +492,20 @@ __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict_
             elastic_trial(e, t, I1);
             finish_elastic(t, I1, m, s, ds);
             store6(S, p, s);
-            store36(DS, p, ds);
+#pragma unroll
+            for (int k = 0; k < 36; ++k) w[lane * kDsStride + k] = ds[k];
             branch[p] = static_cast<int8_t>(kElastic);
         } else {
             listed = true;
+        }
+    }
+    __syncwarp();
+    if (p0 < n) {
+        const int nw = n - p0 < 32 ? n - p0 : 32;
+        double *dst = DS + 36ll * p0;
+        for (int idx = lane; idx < nw * 36; idx += 32) {
+            const int pt = idx / 36;
+            dst[idx] = w[pt * kDsStride + (idx - pt * 36)];
         }
     }
     const int slot = warp_append(listed, scratch);

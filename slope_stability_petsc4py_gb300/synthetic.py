@@ -168,21 +168,31 @@ def elevate_tets(vcoord: np.ndarray, tet4: np.ndarray, order: int) -> tuple[np.n
     elem[:4] = tet4
     if order == 1:
         return vcoord.copy(), elem
-    keys: dict[tuple, int] = {}
-    new_pts: list[np.ndarray] = []
-    for e in range(n_e):
-        verts = tet4[:, e]
-        for li in range(4, len(tuples)):
-            t = tuples[li]
-            key = tuple(sorted((int(verts[v]), t[v]) for v in range(4) if t[v] > 0))
-            gid = keys.get(key)
-            if gid is None:
-                gid = n_v + len(new_pts)
-                keys[key] = gid
-                bary = np.asarray(t, dtype=np.float64) / order
-                new_pts.append(vcoord[:, verts] @ bary)
-            elem[li, e] = gid
-    coord = np.concatenate((vcoord, np.stack(new_pts, axis=1)), axis=1) if new_pts else vcoord.copy()
+    # key of a higher-order node: its (vertex, count) pairs sorted by vertex, padded with (-1, 0)
+    hi = np.asarray(tuples[4:], dtype=np.int64)  # (n_hi, 4) barycentric counts
+    width = int((hi > 0).sum(axis=1).max())
+    verts = tet4.T  # (n_e, 4)
+    key_v = np.full((n_e, hi.shape[0], width), -1, dtype=np.int64)
+    key_c = np.zeros((n_e, hi.shape[0], width), dtype=np.int64)
+    for li, t in enumerate(hi):
+        nz = np.flatnonzero(t > 0)
+        vv = verts[:, nz]
+        order_ = np.argsort(vv, axis=1, kind="stable")
+        key_v[:, li, : nz.size] = np.take_along_axis(vv, order_, axis=1)
+        key_c[:, li, : nz.size] = t[nz][order_]
+    keys = np.concatenate((key_v, key_c), axis=2).reshape(n_e * hi.shape[0], 2 * width)
+    uniq, first, inverse = np.unique(keys, axis=0, return_index=True, return_inverse=True)
+    # number new nodes in order of first appearance (element-major, then local node)
+    rank = np.empty(uniq.shape[0], dtype=np.int64)
+    rank[np.argsort(first, kind="stable")] = np.arange(uniq.shape[0])
+    gid = n_v + rank[inverse.reshape(-1)]
+    elem[4:] = gid.reshape(n_e, hi.shape[0]).T
+    # coordinates of the new nodes from their first element
+    occ = np.sort(first)
+    e_of, li_of = occ // hi.shape[0], occ % hi.shape[0]
+    bary = hi[li_of].astype(np.float64) / order  # (n_new, 4)
+    new_pts = np.einsum("dkn,nk->dn", vcoord[:, tet4[:, e_of]], bary)
+    coord = np.concatenate((vcoord, new_pts), axis=1)
     return coord, elem
 
 
