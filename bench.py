@@ -38,11 +38,11 @@ LAMBDA, R_REG = 1.1, 0.1
 # `bench.py --steps 3 --warmup 3`); keyed by workload and C-ABI entry point.
 NCU_TRAFFIC = {
     "3d_p2_homo": {
-        "ssp_tangent_plastic_correction": 283.76e6 + 60.25e6,
-        "ssp_tangent_plastic_correction_mixed": 283.38e6 + 59.38e6,
-        "ssp_assemble_overlap_strain_3d": 285.23e6 + 36.26e6,
-        "ssp_assemble_force_element": 343.75e6 + 2.65e6,
-        "ssp_constitutive_3d_sds_binned": (124.71 + 302.00 + 22.34 + 1.75 + 34.33 + 1.11) * 1e6,
+        "ssp_tangent_plastic_correction": 286.20e6 + 63.73e6,
+        "ssp_tangent_plastic_correction_mixed": 283.71e6 + 59.34e6,
+        "ssp_assemble_overlap_strain_3d": 284.63e6 + 36.25e6,
+        "ssp_assemble_force_element": 343.75e6 + 2.57e6,
+        "ssp_constitutive_3d_sds_binned": (90.67 + 304.28 + 22.35 + 1.76 + 34.33 + 1.12) * 1e6,
     },
     "3d_p4_hetero": {
         "ssp_tangent_plastic_correction_mixed": 1121.05e6 + 524.74e6,

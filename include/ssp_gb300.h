@@ -185,7 +185,15 @@ int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const doubl
 int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
                                    const double *ds, const double *weight, const int8_t *branch, const double *shear,
                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
-                                   long long nnz_out, double scale, double *out_values, void *stream);
+                                   long long nnz_out, double scale, double *out_values, const int32_t *elem_list,
+                                   const int32_t *elem_count, void *stream);
+
+/* The elements with at least one point whose branch is not elastic: list_out[0 .. *count_out)
+ * (device memory; count_out is zeroed first; the order is unspecified).  Passed as elem_list /
+ * elem_count to the plastic-correction entry points, which then visit only those elements (both
+ * NULL: every element). */
+int ssp_plastic_elements(const int8_t *branch, int n_elem, int n_q, int32_t *list_out, int32_t *count_out,
+                         void *stream);
 
 /* Mixed-precision form of ssp_tangent_plastic_correction.  H = B^T (w * scale * (DS - D_el)) is
  * formed in FP64 and split into hi + lo parts.  P1/P2 elements: the products B^T H are taken and
@@ -199,7 +207,8 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
                                          const double *ds, const double *weight, const int8_t *branch,
                                          const double *shear, const double *lame, const int32_t *scatter_map,
                                          int n_elem, int n_p, int n_q, long long nnz_out, double scale,
-                                         double *out_values, void *stream);
+                                         double *out_values, const int32_t *elem_list,
+                                         const int32_t *elem_count, void *stream);
 
 /* Per-point elastic tangent blocks [n_int][n_s*n_s] of the return mapping's elastic branch. */
 /* Test support for the tensor-core tangent: D[128][112] = A[128][K] * B[112][K]^T (row-major FP32,
@@ -253,9 +262,11 @@ int ssp_probe_dfma(int iters, int blocks, int threads, double *out, void *stream
 int ssp_branch_features(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                         const double *lame, int n, float *X, void *stream);
 
-/* Predicted branch (argmax) of every feature row; bf16 != 0 rounds weights and activations to
- * BF16 (the inference precision the binning uses). */
-int ssp_mlp_predict(const float *params, const float *X, int n, int bf16, int8_t *pred, void *stream);
+/* Predicted branch (argmax) of every feature row.  mode 0: FP32 on the CUDA cores; 1: weights and
+ * activations rounded to BF16, FP32 accumulation, CUDA cores; 2: the same BF16 network on the tensor
+ * cores (tcgen05.mma kind::f16, FP32 accumulation in tensor memory; the inference the binning of
+ * ssp_constitutive_3d_sds_learned uses). */
+int ssp_mlp_predict(const float *params, const float *X, int n, int mode, int8_t *pred, void *stream);
 
 /* Softmax cross-entropy of a batch against labels [n] (branch codes 0..4): grad [SSP_MLP_PARAMS]
  * receives the gradient summed over the batch, loss_sum the summed loss, correct the number of

@@ -32,9 +32,11 @@ _SIGS = {
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned_noalloc": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
-    "ssp_tangent_plastic_correction": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp, _vp],
+    "ssp_tangent_plastic_correction": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp, _vp, _vp,
+                                       _vp],
+    "ssp_plastic_elements": [_vp, _c_int, _c_int, _vp, _vp, _vp],
     "ssp_tangent_plastic_correction_mixed": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp,
-                                                                    _vp],
+                                             _vp, _vp, _vp],
     "ssp_elastic_tangent_blocks": [_c_int, _vp, _vp, _c_int, _vp, _vp],
     "ssp_blend_values": [_vp, _vp, _vp, _c_dbl, _c_ll, _vp],
     "ssp_reduction": [_vp, _vp, _vp, _c_int, _c_dbl, ctypes.c_char, _vp, _vp, _vp],
@@ -106,7 +108,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
     "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
-    "ssp_copy_out": 1, "ssp_host_writable": 0,
+    "ssp_copy_out": 1, "ssp_host_writable": 0, "ssp_plastic_elements": 1,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,

@@ -261,7 +261,25 @@ struct ElemArgs {
     const int8_t *branch;
     const double *shear, *lame;
     double scale;
+    // optional list of the elements to visit (elist[0 .. *elist_count)), else every element
+    const int32_t *elist = nullptr;
+    const int32_t *elist_count = nullptr;
 };
+
+// Element of iteration it: from the list when one is given (bounds-checked), else it itself;
+// -1 for an out-of-range list entry.
+__device__ __forceinline__ long long element_of(const ElemArgs &A, long long it) {
+    if (!A.elist) return it;
+    const int32_t e = A.elist[it];
+    if (e < 0 || e >= A.n_elem) {
+        flag(SSP_DEV_BAD_INDEX);
+        return -1;
+    }
+    return e;
+}
+__device__ __forceinline__ long long element_iterations(const ElemArgs &A) {
+    return A.elist ? static_cast<long long>(*A.elist_count) : static_cast<long long>(A.n_elem);
+}
 
 // Entry (i, j) of the elastic tangent the return mapping emits for an elastic point
 // (constitutive.cu, mc3d_point / mc2d_point elastic branches), with the same arithmetic.
@@ -324,8 +342,11 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
         code[i] = c;
     }
 
-    for (int e = blockIdx.x; e < A.n_elem; e += gridDim.x) {
-        const long long g0 = (long long)e * NQ;
+    const long long n_iter = element_iterations(A);
+    for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
+        const long long e = element_of(A, it);
+        if (e < 0) continue;  // uniform across the CTA
+        const long long g0 = e * NQ;
         __syncthreads();  // the previous element is done with the shared buffers
         if (tid == 0) {
             int k = 0;
@@ -501,7 +522,10 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
 
     const long long warp_global = (long long)blockIdx.x * WARPS + wid;
     const long long warp_count = (long long)gridDim.x * WARPS;
-    for (long long e = warp_global; e < A.n_elem; e += warp_count) {
+    const long long n_iter = element_iterations(A);
+    for (long long it = warp_global; it < n_iter; it += warp_count) {
+        const long long e = element_of(A, it);
+        if (e < 0) continue;  // warp-uniform
         const long long g0 = e * NQ;
         bool mine = lane < NQ;
         if (CORR && mine) mine = A.branch[g0 + lane] != 0;
@@ -632,6 +656,26 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
             }
         }
     }
+}
+
+// Elements with at least one plastic point (branch != 0), appended to list with warp-aggregated
+// atomics (count[0]); the order is unspecified.
+__global__ void plastic_elements_kernel(const int8_t *__restrict__ branch, int n_elem, int n_q, int32_t *__restrict__ list,
+                                        int32_t *__restrict__ count) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    bool pl = false;
+    if (e < n_elem) {
+        const int8_t *b = branch + (long long)e * n_q;
+        for (int q = 0; q < n_q && !pl; ++q) pl = b[q] != 0;
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(0xffffffffu, pl);
+    if (mask == 0u) return;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pl) list[base + __popc(mask & ((1u << lane) - 1u))] = e;
 }
 
 // Per-point elastic tangent of the return mapping (for assembling the elastic tangent once).
@@ -859,13 +903,16 @@ int ssp_tangent_element(int dim, int symmetric, const double *dphi1, const doubl
 int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *dphi2, const double *dphi3,
                                    const double *ds, const double *weight, const int8_t *branch, const double *shear,
                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_p, int n_q,
-                                   long long nnz_out, double scale, double *out_values, void *stream) {
+                                   long long nnz_out, double scale, double *out_values, const int32_t *elem_list,
+                                   const int32_t *elem_count, void *stream) {
     if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0) return SSP_ERR_INVALID;
     if (n_elem == 0) return SSP_OK;
     if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !branch || !shear || !lame || !scatter_map ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale};
+    if ((elem_list == nullptr) != (elem_count == nullptr)) return SSP_ERR_INVALID;
+    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale,
+               elem_list, elem_count};
     return dispatch_element<true, true>(dim, n_p, n_q, a, as_stream(stream));
 }
 
@@ -873,21 +920,35 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
                                          const double *ds, const double *weight, const int8_t *branch,
                                          const double *shear, const double *lame, const int32_t *scatter_map,
                                          int n_elem, int n_p, int n_q, long long nnz_out, double scale,
-                                         double *out_values, void *stream) {
+                                         double *out_values, const int32_t *elem_list, const int32_t *elem_count,
+                                         void *stream) {
     if ((dim != 2 && dim != 3) || n_elem < 0 || n_p <= 0 || n_q <= 0 || nnz_out < 0) return SSP_ERR_INVALID;
     if (n_elem == 0) return SSP_OK;
     if (!dphi1 || !dphi2 || (dim == 3 && !dphi3) || !ds || !weight || !branch || !shear || !lame || !scatter_map ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale};
+    if ((elem_list == nullptr) != (elem_count == nullptr)) return SSP_ERR_INVALID;
+    ElemArgs a{dphi1, dphi2, dphi3, ds, weight, scatter_map, n_elem, nnz_out, out_values, branch, shear, lame, scale,
+               elem_list, elem_count};
     cudaStream_t st = as_stream(stream);
     if (dim == 3 && n_p == 10 && n_q == 11) return launch_element_warp<3, 10, 11, true, true, true>(a, st);
     if (dim == 3 && n_p == 4 && n_q == 1) return launch_element_warp<3, 4, 1, true, true, true>(a, st);
     if (dim == 2 && n_p == 6 && n_q == 7) return launch_element_warp<2, 6, 7, true, true, true>(a, st);
     if (dim == 3 && n_p == 35 && n_q == 24)
         return correction_tc_p4(dphi1, dphi2, dphi3, ds, weight, branch, shear, lame, scatter_map, n_elem, nnz_out, scale,
-                                out_values, st);
+                                out_values, elem_list, elem_count, st);
     return SSP_ERR_UNSUPPORTED;
+}
+
+int ssp_plastic_elements(const int8_t *branch, int n_elem, int n_q, int32_t *list_out, int32_t *count_out,
+                         void *stream) {
+    if (n_elem < 0 || n_q <= 0 || !count_out) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(count_out, 0, sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!branch || !list_out) return SSP_ERR_INVALID;
+    plastic_elements_kernel<<<grid_for(n_elem, 256), 256, 0, st>>>(branch, n_elem, n_q, list_out, count_out);
+    return launch_status();
 }
 
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,

@@ -13,6 +13,7 @@
 #include <cuda_bf16.h>
 
 #include "ssp_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace ssp {
 
@@ -246,36 +247,210 @@ __global__ void adam_kernel(float *__restrict__ params, const float *__restrict_
     params[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// Proposal + binning: features, BF16 MLP, argmax, and a warp-aggregated append of the point to
-// the list of its proposed branch.  scratch = 8 counters, then five lists of n entries.
-__global__ void __launch_bounds__(128) propose_bin_kernel(const float *__restrict__ params,
-                                                          const double *__restrict__ E,
-                                                          const double *__restrict__ c_bar,
-                                                          const double *__restrict__ sin_phi,
-                                                          const double *__restrict__ shear,
-                                                          const double *__restrict__ lame, int n,
-                                                          int32_t *__restrict__ scratch) {
-    __shared__ float P[kParams];
-    load_params(params, P, true);
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int b = -1;
-    if (p < n) {
-        float x[kIn];
-        features(E + 6ll * p, c_bar[p], sin_phi[p], shear[p], lame[p], x);
-        b = forward_argmax<true>(P, x);
-    }
-    const unsigned lane = threadIdx.x & 31u;
-    int32_t *lists = scratch + 8;
+// The network on the tensor cores: a CTA of 128 threads takes tiles of 128 points; each layer is
+// one tcgen05.mma kind::f16 chain (BF16 operands in shared memory, FP32 accumulator in tensor
+// memory): [128 x 16] x [16 x 32] (the 6 features, zero-padded), [128 x 32] x [32 x 32],
+// [128 x 32] x [32 x 16] (5 logits, zero-padded).  Thread t owns point row t: it writes its
+// operand row, and after each MMA reads its accumulator row (tcgen05.ld, lane t), adds the bias,
+// applies ReLU and rounds to BF16 for the next layer.  The same BF16 rounding of weights and
+// activations as forward_argmax<true>; the accumulation order is the tensor core's.
+// FROM_STRAIN: features from the trial strain, the argmax appended to its branch list (the
+// learned return mapping's proposal); otherwise features from X and the argmax stored in pred.
+constexpr int kTcTile = 128, kTcCols = 128;
+struct MlpSmem {
+    alignas(128) unsigned char w1[32 * 16 * 2];
+    alignas(128) unsigned char w2[32 * 32 * 2];
+    alignas(128) unsigned char w3[16 * 32 * 2];
+    alignas(128) unsigned char a1[kTcTile * 16 * 2];
+    alignas(128) unsigned char a2[kTcTile * 32 * 2];
+    alignas(128) unsigned char a3[kTcTile * 32 * 2];
+    float b1[kH], b2[kH], b3[8];
+    unsigned long long mbar;
+    uint32_t tmem_slot;
+    int abort;
+};
+// more than a quarter of an SM's shared memory, so at most four CTAs (4 x 128 tensor-memory
+// columns) are resident on an SM
+constexpr size_t kMlpSmemBytes = 58 * 1024;
+static_assert(sizeof(MlpSmem) <= kMlpSmemBytes, "MLP shared memory");
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+// One row of 8 * chunks BF16 values (from v) into the K-major tile at row r.
+template <int CHUNKS>
+__device__ __forceinline__ void store_row_bf16(unsigned char *tile, int r, const float *v) {
 #pragma unroll
-    for (int k = 0; k < kOut; ++k) {
-        const unsigned mask = __ballot_sync(0xffffffffu, b == k);
-        if (mask == 0u) continue;
-        const int leader = __ffs(mask) - 1;
-        int base = 0;
-        if ((int)lane == leader) base = atomicAdd(scratch + k, __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (b == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
+    for (int c = 0; c < CHUNKS; ++c) {
+        uint4 q;
+        q.x = pack_bf16(v[8 * c + 0], v[8 * c + 1]);
+        q.y = pack_bf16(v[8 * c + 2], v[8 * c + 3]);
+        q.z = pack_bf16(v[8 * c + 4], v[8 * c + 5]);
+        q.w = pack_bf16(v[8 * c + 6], v[8 * c + 7]);
+        *reinterpret_cast<uint4 *>(tile + tc::kmaj_off<2>(r, 8 * c, kTcTile)) = q;
     }
+}
+// Issue one layer (K / 16 MMAs), commit, wait for it (bounded; on expiry flag and return false).
+__device__ __forceinline__ bool mlp_layer(MlpSmem &S, const unsigned char *a, const unsigned char *b, int n_rows_b,
+                                          int K, uint32_t tmem_d, uint32_t id, uint32_t &phase) {
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        const uint32_t lbo_a = (kTcTile / 8) * 128, lbo_b = (n_rows_b / 8) * 128;
+        for (int s = 0; s < K / 16; ++s)
+            tc::mma_f16(tmem_d, tc::smem_desc(tc::smem_u32(a) + s * 2 * lbo_a, lbo_a, 128),
+                        tc::smem_desc(tc::smem_u32(b) + s * 2 * lbo_b, lbo_b, 128), id, s != 0 ? 1u : 0u);
+        tc::mma_commit(tc::smem_u32(&S.mbar));
+    }
+    if (!tc::mbar_wait(tc::smem_u32(&S.mbar), phase)) {
+        S.abort = 1;
+        flag(SSP_DEV_TIMEOUT);
+    }
+    phase ^= 1u;
+    __syncthreads();  // every thread leaves on the same decision
+    tc::fence_after_sync();
+    return S.abort == 0;
+}
+
+template <bool FROM_STRAIN>
+__global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict__ params, const float *__restrict__ X,
+                                                         const double *__restrict__ E,
+                                                         const double *__restrict__ c_bar,
+                                                         const double *__restrict__ sin_phi,
+                                                         const double *__restrict__ shear,
+                                                         const double *__restrict__ lame, int n,
+                                                         int8_t *__restrict__ pred, int32_t *__restrict__ scratch) {
+    extern __shared__ __align__(128) unsigned char mlp_raw[];
+    MlpSmem &S = *reinterpret_cast<MlpSmem *>(mlp_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights as BF16 B operands (N x K, K-major), zero-padded; biases as FP32
+    for (int i = tid; i < 32 * 16; i += kTcTile) {
+        const int nn = i / 16, k = i % 16;
+        *reinterpret_cast<__nv_bfloat16 *>(S.w1 + tc::kmaj_off<2>(nn, k, 32)) =
+            __float2bfloat16_rn(k < kIn ? params[oW1 + nn * kIn + k] : 0.0f);
+    }
+    for (int i = tid; i < 32 * 32; i += kTcTile) {
+        const int nn = i / 32, k = i % 32;
+        *reinterpret_cast<__nv_bfloat16 *>(S.w2 + tc::kmaj_off<2>(nn, k, 32)) = __float2bfloat16_rn(params[oW2 + i]);
+    }
+    for (int i = tid; i < 16 * 32; i += kTcTile) {
+        const int nn = i / 32, k = i % 32;
+        *reinterpret_cast<__nv_bfloat16 *>(S.w3 + tc::kmaj_off<2>(nn, k, 16)) =
+            __float2bfloat16_rn(nn < kOut ? params[oW3 + nn * kH + k] : 0.0f);
+    }
+    if (tid < kH) {
+        S.b1[tid] = params[ob1 + tid];
+        S.b2[tid] = params[ob2 + tid];
+    }
+    if (tid < 8) S.b3[tid] = tid < kOut ? params[ob3 + tid] : 0.0f;
+    if (tid == 0) {
+        tc::mbar_init(tc::smem_u32(&S.mbar));
+        S.abort = 0;
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) tc::tmem_alloc(&S.tmem_slot, kTcCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = S.tmem_slot;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
+    constexpr uint32_t id32 = tc::idesc(tc::kFmtBF16, kTcTile, 32), id16 = tc::idesc(tc::kFmtBF16, kTcTile, 16);
+    uint32_t phase = 0;
+    const int tiles = (n + kTcTile - 1) / kTcTile;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int p = tile * kTcTile + tid;
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+        if (p < n) {
+            if (FROM_STRAIN) {
+                features(E + 6ll * p, c_bar[p], sin_phi[p], shear[p], lame[p], v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < kIn; ++i) v[i] = X[(long long)p * kIn + i];
+            }
+        }
+        store_row_bf16<2>(S.a1, tid, v);
+        if (!mlp_layer(S, S.a1, S.w1, 32, 16, tmem, id32, phase)) break;
+        {
+            uint32_t r[32];
+            tc::tmem_ld16(tmem + lane_base, r);
+            tc::tmem_ld16(tmem + lane_base + 16, r + 16);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(__uint_as_float(r[j]) + S.b1[j], 0.0f);
+        }
+        store_row_bf16<4>(S.a2, tid, v);
+        if (!mlp_layer(S, S.a2, S.w2, 32, 32, tmem + 32, id32, phase)) break;
+        {
+            uint32_t r[32];
+            tc::tmem_ld16(tmem + lane_base + 32, r);
+            tc::tmem_ld16(tmem + lane_base + 48, r + 16);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = fmaxf(__uint_as_float(r[j]) + S.b2[j], 0.0f);
+        }
+        store_row_bf16<4>(S.a3, tid, v);
+        if (!mlp_layer(S, S.a3, S.w3, 16, 32, tmem + 64, id16, phase)) break;
+        int best = 0;
+        {
+            uint32_t r[16];
+            tc::tmem_ld16(tmem + lane_base + 64, r);
+            tc::tmem_wait_ld();
+            float bz = -3.0e38f;
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) {
+                const float a = __uint_as_float(r[o]) + S.b3[o];
+                if (a > bz) {
+                    bz = a;
+                    best = o;
+                }
+            }
+        }
+        if (FROM_STRAIN) {
+            const int b = p < n ? best : -1;
+            int32_t *lists = scratch + 8;
+#pragma unroll
+            for (int k = 0; k < kOut; ++k) {
+                const unsigned mask = __ballot_sync(0xffffffffu, b == k);
+                if (mask == 0u) continue;
+                const int leader = __ffs(mask) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(scratch + k, __popc(mask));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (b == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
+            }
+        } else if (p < n) {
+            pred[p] = static_cast<int8_t>(best);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kTcCols);
+    }
+}
+
+template <bool FROM_STRAIN>
+int launch_mlp_tc(const float *params, const float *X, const double *E, const double *c_bar, const double *sin_phi,
+                  const double *shear, const double *lame, int n, int8_t *pred, int32_t *scratch, cudaStream_t st) {
+    auto kernel = mlp_tc_kernel<FROM_STRAIN>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kMlpSmemBytes)) !=
+        cudaSuccess)
+        return SSP_ERR_CUDA;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (long long)sms * 4;
+    const long long tiles = (n + kTcTile - 1) / kTcTile;
+    if (grid > tiles) grid = tiles;
+    kernel<<<static_cast<unsigned>(grid), kTcTile, kMlpSmemBytes, st>>>(params, X, E, c_bar, sin_phi, shear, lame, n, pred,
+                                                                        scratch);
+    return launch_status();
 }
 
 // The exact FP64 return mapping over the five proposal lists (blockIdx.y = list).
@@ -326,11 +501,14 @@ int ssp_branch_features(const double *E, const double *c_bar, const double *sin_
     return launch_status();
 }
 
-int ssp_mlp_predict(const float *params, const float *X, int n, int bf16, int8_t *pred, void *stream) {
-    if (n < 0) return SSP_ERR_INVALID;
+int ssp_mlp_predict(const float *params, const float *X, int n, int mode, int8_t *pred, void *stream) {
+    if (n < 0 || mode < 0 || mode > 2) return SSP_ERR_INVALID;
     if (n == 0) return SSP_OK;
     if (!params || !X || !pred) return SSP_ERR_INVALID;
-    predict_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(params, X, n, bf16, pred);
+    if (mode == 2)
+        return launch_mlp_tc<false>(params, X, nullptr, nullptr, nullptr, nullptr, nullptr, n, pred, nullptr,
+                                    as_stream(stream));
+    predict_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(params, X, n, mode, pred);
     return launch_status();
 }
 
@@ -370,7 +548,8 @@ int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const 
         return SSP_ERR_INVALID;
     cudaStream_t st = as_stream(stream);
     if (cudaMemsetAsync(scratch, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    propose_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(params, E, c_bar, sin_phi, shear, lame, n_int, scratch);
+    const int rc = launch_mlp_tc<true>(params, nullptr, E, c_bar, sin_phi, shear, lame, n_int, nullptr, scratch, st);
+    if (rc != SSP_OK) return rc;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

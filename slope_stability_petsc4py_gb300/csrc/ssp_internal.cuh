@@ -55,7 +55,8 @@ __host__ __device__ __forceinline__ int bt_row2(int comp, int grad) {
 // Mixed-precision plastic-correction tangent of 3D P4 elements on the tensor cores (tangent_tc.cu).
 int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
                      const int8_t *branch, const double *shear, const double *lame, const int32_t *emap, int n_elem,
-                     long long nnz, double scale, double *values, cudaStream_t st);
+                     long long nnz, double scale, double *values, const int32_t *elist, const int32_t *elist_count,
+                     cudaStream_t st);
 
 }  // namespace ssp
 

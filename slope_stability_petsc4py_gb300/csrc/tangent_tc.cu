@@ -37,9 +37,12 @@
 // Every wait on an mbarrier is bounded (about one second of SM clocks); on expiry the CTA sets
 // SSP_DEV_TIMEOUT, stops, and still releases its tensor memory.
 #include "ssp_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace ssp {
 namespace {
+
+using namespace tc;
 
 constexpr int kNP = 35, kNQ = 24, kNLD = 105, kNS = 6;
 constexpr int kM = 128, kN = 112, kPts = 4, kK = kPts * kNS;  // 24 = three K steps of 8
@@ -54,7 +57,7 @@ static_assert(kColsPerWarp % 4 == 0, "drain loads four columns at a time");
 // Instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits 4-5 = 1), A and B TF32
 // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
 // bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(kN >> 3) << 17) | (uint32_t(kM >> 4) << 24);
+constexpr uint32_t kIdesc = tc::idesc(tc::kFmtTF32, kM, kN);
 
 struct Stage {  // one group of four points, operands split hi / lo
     uint32_t a_hi[kABytes / 4];
@@ -81,22 +84,6 @@ struct Smem {
 constexpr size_t kSmemBytes = sizeof(Smem) > 120 * 1024 ? sizeof(Smem) : 120 * 1024;
 static_assert(sizeof(Smem) <= 227 * 1024, "shared memory of one CTA");
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ int kmaj_off(int row, int kap, int rows) {
-    return ((kap >> 2) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (kap & 3) * 4;
-}
-
-// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading byte offset >> 4
-// (bits 16-29), stride byte offset >> 4 (bits 32-45), descriptor version 1 (bit 46), base offset 0,
-// no swizzle (bits 61-63 = 0).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) | (static_cast<uint64_t>(lbo >> 4) << 16) |
-           (static_cast<uint64_t>(sbo >> 4) << 32) | (1ull << 46);
-}
-
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -109,88 +96,17 @@ __device__ __forceinline__ void split_tf32(df32 x, uint32_t &hi, uint32_t &lo) {
     lo = to_tf32(__fadd_rn(__fsub_rn(x.hi, __uint_as_float(hi)), x.lo));
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t mbar_addr) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
-                 : "memory");
-}
-__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_init(uint32_t addr) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(addr) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the completion of the phase with the given parity (about 1 s of SM clocks).
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(addr, parity)) {
-        if (clock64() - t0 > 2000000000ll) return false;
-    }
-    return true;
-}
-
-// 32 lanes x 16 consecutive FP32 columns of the accumulator (this warp's lane quarter).
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+// 32 lanes x 16 consecutive FP32 columns of the accumulator (this warp's lane quarter), waited for.
+__device__ __forceinline__ void tmem_ld16f(uint32_t taddr, float *v) {
     uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    tmem_ld16(taddr, r);
+    tmem_wait_ld();
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
-// 32 lanes x 4 consecutive FP32 columns (no wait: the caller waits once for a batch).
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(taddr)
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-// 32 lanes x 8 consecutive FP32 columns (no wait).
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr)
-                 : "memory");
-}
-// 32 lanes x 16 consecutive FP32 columns (no wait).
-__device__ __forceinline__ void tmem_ld16nw(uint32_t taddr, uint32_t *r) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-}
 // The 28 accumulator columns col0 .. col0 + 27 of this thread's lane.
 __device__ __forceinline__ void tmem_ld28(uint32_t taddr0, uint32_t *r) {
-    tmem_ld16nw(taddr0, r);
+    tmem_ld16(taddr0, r);
     tmem_ld8(taddr0 + 16, r + 16);
     tmem_ld4(taddr0 + 24, r + 24);
 }
@@ -237,7 +153,8 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
     const double *__restrict__ d1, const double *__restrict__ d2, const double *__restrict__ d3,
     const double *__restrict__ DS, const double *__restrict__ w, const int8_t *__restrict__ branch,
     const double *__restrict__ shear, const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem,
-    long long nnz, double scale, double *__restrict__ values) {
+    long long nnz, double scale, double *__restrict__ values, const int32_t *__restrict__ elist,
+    const int32_t *__restrict__ elist_count) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem &S = *reinterpret_cast<Smem *>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -266,8 +183,17 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
     uint32_t phase_bits = 0;
     int parity = 0;
 
-    for (int e = blockIdx.x; e < n_elem; e += gridDim.x, parity ^= 1) {
-        const long long g0 = (long long)e * kNQ;
+    const long long n_iter = elist ? static_cast<long long>(*elist_count) : static_cast<long long>(n_elem);
+    for (long long it = blockIdx.x; it < n_iter; it += gridDim.x, parity ^= 1) {
+        long long e = it;
+        if (elist) {
+            e = elist[it];
+            if (e < 0 || e >= n_elem) {  // uniform across the CTA
+                if (tid == 0) flag(SSP_DEV_BAD_INDEX);
+                continue;
+            }
+        }
+        const long long g0 = e * kNQ;
         if (warp == 0) {
             const bool pl = lane < kNQ && branch[g0 + lane] != 0;
             const unsigned mask = __ballot_sync(0xffffffffu, pl);
@@ -327,7 +253,7 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
                     const df32 h = df_dot3(ga, D[k0 + kNS * m], gb, D[k1 + kNS * m], gc, D[k2 + kNS * m]);
                     uint32_t hi, lo;
                     split_tf32(h, hi, lo);
-                    const int off = kmaj_off(alpha, pi * kNS + m, kM);
+                    const int off = kmaj_off<4>(alpha, pi * kNS + m, kM);
                     *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
                     *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
                 }
@@ -338,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
                     const int cp = i % 3, rest = i / 3, bn = rest % kNP, pr = rest / kNP, r = pr % 3, pi = pr / 3;
                     uint32_t hi, lo;
                     split_tf32(S.pts.g[pi][r][bn], hi, lo);
-                    const int off = kmaj_off(3 * bn + cp, pi * kNS + bt_row3(cp, r), kN);
+                    const int off = kmaj_off<4>(3 * bn + cp, pi * kNS + bt_row3(cp, r), kN);
                     *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
                     *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
                 }
@@ -353,9 +279,9 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
 #pragma unroll
                 for (int s = 0; s < kK / 8; ++s) {
                     const uint32_t oa = s * 2 * kLboA, ob = s * 2 * kLboB;
-                    mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), s != 0 ? 1u : 0u);
-                    mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), s != 0 ? 1u : 0u);
-                    mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), 1u);
+                    mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, s != 0 ? 1u : 0u);
+                    mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), kIdesc, s != 0 ? 1u : 0u);
+                    mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, 1u);
                 }
                 mma_commit(smem_u32(&S.mbar[b]));
             }
@@ -413,11 +339,11 @@ __global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restric
     __syncthreads();
     for (int i = tid; i < kM * K; i += 128) {
         const int r = i / K, k = i % K;
-        *reinterpret_cast<uint32_t *>(sa + kmaj_off(r, k, kM)) = to_tf32(A[i]);
+        *reinterpret_cast<uint32_t *>(sa + kmaj_off<4>(r, k, kM)) = to_tf32(A[i]);
     }
     for (int i = tid; i < kN * K; i += 128) {
         const int r = i / K, k = i % K;
-        *reinterpret_cast<uint32_t *>(sb + kmaj_off(r, k, kN)) = to_tf32(B[i]);
+        *reinterpret_cast<uint32_t *>(sb + kmaj_off<4>(r, k, kN)) = to_tf32(B[i]);
     }
     if (tid == 0) {
         mbar_init(smem_u32(mbar));
@@ -440,7 +366,7 @@ __global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restric
         const uint32_t lb = convention == 0 ? kLboB : kSbo, sb_ = convention == 0 ? kSbo : kLboB;
         for (int s = 0; s < K / 8; ++s)
             mma_tf32(tmem, smem_desc(smem_u32(sa) + s * 2 * kLboA, la, sa_), smem_desc(smem_u32(sb) + s * 2 * kLboB, lb, sb_),
-                     s != 0 ? 1u : 0u);
+                     kIdesc, s != 0 ? 1u : 0u);
         mma_commit(smem_u32(mbar));
         if (!mbar_wait(smem_u32(mbar), 0)) {
             *abort_flag = 1;
@@ -452,7 +378,7 @@ __global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restric
     if (*abort_flag == 0) {
         for (int ch = 0; ch < kN / 16; ++ch) {
             float v[16];
-            tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + ch * 16, v);
+            tmem_ld16f(tmem + (static_cast<uint32_t>(32 * warp) << 16) + ch * 16, v);
             const int row = 32 * warp + lane;
 #pragma unroll
             for (int j = 0; j < 16; ++j) D[row * kN + ch * 16 + j] = v[j];
@@ -470,7 +396,8 @@ __global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restric
 
 int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
                      const int8_t *branch, const double *shear, const double *lame, const int32_t *emap, int n_elem,
-                     long long nnz, double scale, double *values, cudaStream_t st) {
+                     long long nnz, double scale, double *values, const int32_t *elist, const int32_t *elist_count,
+                     cudaStream_t st) {
     const size_t smem = kSmemBytes;
     if (cudaFuncSetAttribute(correction_tc_p4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
@@ -481,7 +408,8 @@ int correction_tc_p4(const double *d1, const double *d2, const double *d3, const
     long long grid = sms;  // one CTA per SM: each owns the SM's 512 tensor-memory columns
     if (grid > n_elem) grid = n_elem;
     correction_tc_p4_kernel<<<static_cast<unsigned>(grid), kThreads, smem, st>>>(d1, d2, d3, DS, w, branch, shear, lame,
-                                                                                   emap, n_elem, nnz, scale, values);
+                                                                                   emap, n_elem, nnz, scale, values,
+                                                                                   elist, elist_count);
     return launch_status();
 }
 

@@ -119,11 +119,14 @@ class BranchProposal:
             self.history.append((float(tot_loss.item()) / n, float(tot_hits.item()) / n))
         return self.history
 
-    def predict(self, X, *, bf16: bool = True):
+    def predict(self, X, *, bf16: bool = True, tensor_cores: bool = True):
+        """Argmax branch of every feature row: BF16 on the tensor cores (the binning's inference),
+        BF16 or FP32 on the CUDA cores."""
         t = _lib.require_cuda()
         pred = t.empty(int(X.shape[0]), dtype=t.int8, device="cuda")
-        _lib.call("ssp_mlp_predict", _lib.ptr(self.params), _lib.ptr(X), int(X.shape[0]), 1 if bf16 else 0,
-                  _lib.ptr(pred), _lib.stream_handle())
+        mode = (2 if tensor_cores else 1) if bf16 else 0
+        _lib.call("ssp_mlp_predict", _lib.ptr(self.params), _lib.ptr(X), int(X.shape[0]), mode, _lib.ptr(pred),
+                  _lib.stream_handle())
         return pred
 
     def accuracy(self, X, y, *, bf16: bool = True) -> float:

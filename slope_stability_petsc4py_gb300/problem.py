@@ -483,11 +483,20 @@ class ConstitutiveOperator:
             entry = "ssp_tangent_plastic_correction"
             if self.tangent_form == "mixed" and (pat.n_p <= 10 or (pat.dim == 3 and pat.n_p == 35)):
                 entry = "ssp_tangent_plastic_correction_mixed"
+            n_el = int(pat.overlap_elements.size)
+            dv = self._dev
+            if "plastic_elems" not in dv:
+                t = _lib.torch()
+                dv["plastic_elems"] = t.empty(max(n_el, 1), dtype=t.int32, device="cuda")
+                dv["plastic_count"] = t.empty(1, dtype=t.int32, device="cuda")
+            # the correction visits the plastic elements only (an even share per warp)
+            _lib.call("ssp_plastic_elements", _lib.ptr(self._branch), n_el, pat.n_q, _lib.ptr(dv["plastic_elems"]),
+                      _lib.ptr(dv["plastic_count"]), st)
             _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
                       _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
-                      _lib.ptr(self._branch), _lib.ptr(self._dev["shear"]), _lib.ptr(self._dev["lame"]),
-                      _lib.ptr(d["scatter_map"]), int(pat.overlap_elements.size), pat.n_p, pat.n_q, pat.nnz, scale,
-                      _lib.ptr(values), st)
+                      _lib.ptr(self._branch), _lib.ptr(dv["shear"]), _lib.ptr(dv["lame"]), _lib.ptr(d["scatter_map"]),
+                      n_el, pat.n_p, pat.n_q, pat.nnz, scale, _lib.ptr(values), _lib.ptr(dv["plastic_elems"]),
+                      _lib.ptr(dv["plastic_count"]), st)
             if ev is not None:
                 e1.record()
                 ev.append((e0, e1))

@@ -59,10 +59,19 @@ def test_mlp_gradient_matches_oracle(cuda_device, oracle):
     assert int(hits.item()) == hits_o
     # the FP32 prediction is the oracle's argmax
     z, _ = oracle.mlp_forward(params, X)
-    pred = model.predict(torch.as_tensor(X, device="cuda"), bf16=False).cpu().numpy()
+    Xd = torch.as_tensor(X, device="cuda")
+    pred = model.predict(Xd, bf16=False).cpu().numpy()
     margin = np.sort(z, axis=1)[:, -1] - np.sort(z, axis=1)[:, -2]
     sure = margin > 1e-4
     assert np.array_equal(pred[sure], np.argmax(z, axis=1)[sure])
+    # BF16 inference: CUDA cores and tensor cores (tcgen05 kind::f16) agree except where BF16
+    # rounding makes the top two logits tie (their accumulation orders differ)
+    p_cc = model.predict(Xd, bf16=True, tensor_cores=False).cpu().numpy()
+    p_tc = model.predict(Xd, bf16=True, tensor_cores=True).cpu().numpy()
+    clear = margin > 0.05 * np.maximum(1.0, np.abs(z).max(axis=1))
+    assert np.array_equal(p_cc[clear], p_tc[clear])
+    assert np.mean(p_cc == p_tc) > 0.99
+    assert np.mean(p_tc[clear] == np.argmax(z, axis=1)[clear]) > 0.99
 
 
 def _trained_model(op, mesh, mats):
