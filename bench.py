@@ -269,10 +269,12 @@ def algorithmic(name, st):
     s_out = 6 if dim == 3 else 4
     if name in ("ssp_constitutive_sds_branch", "ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_learned"):
         return {"bytes": n * (8 * ns + 4 * 8 + 8 * s_out + 8 * ns * ns + 1), "flops": 0}
-    if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d"):
-        return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": n * 2 * 9 * n_p}
-    if name == "ssp_assemble_force_element":
-        return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": n * nld * 8}
+    if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d", "ssp_assemble_overlap_strain_3d_mixed"):
+        fp64 = 0 if name.endswith("_mixed") else n * 2 * 9 * n_p  # the mixed kernel's products are FP32
+        return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": fp64}
+    if name in ("ssp_assemble_force_element", "ssp_assemble_force_element_mixed"):
+        fp64 = 0 if name.endswith("_mixed") else n * nld * 8
+        return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": fp64}
     if name == "ssp_blend_values":
         return {"bytes": 3 * 8 * st["nnz"], "flops": 0}
     if name == "ssp_reduction":

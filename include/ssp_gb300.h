@@ -138,6 +138,26 @@ int ssp_assemble_overlap_strain_2d(const double *dphi1, const double *dphi2, con
                                    const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
                                    double *out_values, void *stream);
 
+/* hi + lo float pairs of FP64 values: out_pairs[2 i], out_pairs[2 i + 1] = split of
+ * x[i] * (scale ? scale[i / group] : 1) (the product in FP64; hi = the value truncated to 24 bits,
+ * lo = the rest rounded to a float).  The inputs of the compensated kernels below. */
+int ssp_split_f64(const double *x, const double *scale, long long n, int group, float *out_pairs, void *stream);
+
+/* Mixed-precision form of ssp_assemble_overlap_strain_3d and ssp_assemble_force_element (3D): the
+ * same sums in compensated double-float arithmetic on the FP32 pipe (product rounding errors
+ * recovered with FMAs, sums kept as hi + lo pairs), widened to FP64 once per output.  Inputs are
+ * hi + lo pairs from ssp_split_f64: the gradients (strain), w * gradient (force; scale = weight,
+ * group = n_p), the overlap displacements and the stresses.  The strain is formed from displacement
+ * differences to the element's first node (sum of the basis gradients = 0), so no digits cancel.
+ * Relative error against the FP64 kernels ~1e-13; the force is still accumulated into out_values
+ * with FP64 reductions.  No reference counterpart. */
+int ssp_assemble_overlap_strain_3d_mixed(const float *dphi1_hl, const float *dphi2_hl, const float *dphi3_hl,
+                                         const float *u_hl, int n_u, const int32_t *elem_dof_lids, int n_int,
+                                         int n_elem, int n_p, int n_q, double *out_values, void *stream);
+int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2_hl, const float *wdphi3_hl,
+                                     const float *stress_hl, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                     int n_rows, double *out_values, void *stream);
+
 /* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
  * Deterministic row gather; rows without slots come out 0. */
 int ssp_assemble_force_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *stress,

@@ -45,6 +45,9 @@ _SIGS = {
     "ssp_assemble_overlap_strain_2d": [_vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_force_3d_rows": [_vp] * 8 + [_c_int] * 6 + [_vp, _vp],
     "ssp_assemble_force_element": [_c_int] + [_vp] * 6 + [_c_int] * 4 + [_vp, _vp],
+    "ssp_assemble_overlap_strain_3d_mixed": [_vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_force_element_mixed": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
+    "ssp_split_f64": [_vp, _vp, _c_ll, _c_int, _vp, _vp],
     "ssp_assemble_tangent_values_3d_rows": [_vp] * 9 + [_c_int] * 6 + [_vp, _vp],
     "ssp_assemble_tangent_values_3d_p2": [_vp] * 6 + [_c_int] * 5 + [_vp, _vp],
     "ssp_tangent_element": [_c_int, _c_int] + [_vp] * 6 + [_c_int, _c_int, _c_int, _c_ll, _vp, _c_int, _vp],
@@ -109,6 +112,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
     "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
     "ssp_copy_out": 1, "ssp_host_writable": 0, "ssp_plastic_elements": 1,
+    "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,

@@ -1,0 +1,177 @@
+// Strain and internal force of the mixed-precision form in compensated FP32 arithmetic.
+//
+// GB300 issues FP64 at a small fraction of its FP32 rate, and the FP64 strain E = B u and force
+// F = B^T (w S) kernels (assembly.cu) run at 82-86 % of the FP64 pipe.  Here the same sums are
+// formed in double-float arithmetic on the FP32 pipe (inputs split into hi + lo float pairs by bit
+// operations; every product's rounding error recovered with an FMA, the sums kept as an unevaluated
+// hi + lo pair), about 46 significant bits, and widened to FP64 once per output.
+//
+// The FP64 inputs are split once where they are constant (the gradients dphi and w * dphi, once per
+// pattern) and once per call otherwise (the overlap displacements, the stresses): ssp_split_f64.
+//
+// Strain: with sum_a grad N_a = 0, E = sum_a dphi_a (x) (u_a - u_0), node 0 of the element as the
+// reference displacement.  The differences remove the rigid translation of the element, so the
+// products are of the size of the strain itself and the compensated sum keeps its relative
+// accuracy (a plain FP32 sum of dphi_a u_a would cancel three or more digits).
+//
+// Force: one thread per (element, local dof) as force_element_kernel; the element sum over the
+// quadrature points is compensated and added to the FP64 force vector with one FP64 reduction.
+#include "ssp_internal.cuh"
+
+namespace ssp {
+namespace {
+
+// Compensated accumulator: value = s + c, s accumulates the leading parts with TwoSum, c the
+// rounding errors and the low-order product terms.
+struct CSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add_prod(df32 x, df32 y) {
+        const float p = __fmul_rn(x.hi, y.hi);
+        float e = __fmaf_rn(x.hi, y.hi, -p);
+        e = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, e));
+        const df32 t = df_two_sum(s, p);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
+    __device__ __forceinline__ double value() const { return df_to_f64(df_fast_two_sum(s, c)); }
+};
+
+__device__ __forceinline__ df32 df_neg(df32 a) { return {-a.hi, -a.lo}; }
+
+// out[i] = hi + lo split of x[i] * (scale ? scale[i / group] : 1), the product in FP64.
+__global__ void split_kernel(const double *__restrict__ x, const double *__restrict__ scale, long long n, int group,
+                             float2 *__restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = scale ? x[i] * scale[i / group] : x[i];
+    const df32 d = df_from_f64(v);
+    out[i] = make_float2(d.hi, d.lo);
+}
+
+__device__ __forceinline__ df32 ld(const float2 *p) {
+    const float2 v = *p;
+    return {v.x, v.y};
+}
+
+// Strain from hi + lo pairs of the gradients (split once per pattern) and of the overlap
+// displacements (split once per call).
+__global__ void __launch_bounds__(128) strain3_mixed_kernel(const float2 *__restrict__ g1, const float2 *__restrict__ g2,
+                                                            const float2 *__restrict__ g3,
+                                                            const float2 *__restrict__ u,
+                                                            const int32_t *__restrict__ dof, long long n_u, int n_elem,
+                                                            int n_p, int n_q, double *__restrict__ E) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const long long e = g / n_q;
+    const int32_t *dl = dof + e * 3 * n_p;
+    const int32_t r0 = dl[0], r1 = dl[1], r2 = dl[2];
+    if (r0 < 0 || r1 < 0 || r2 < 0 || r0 >= n_u || r1 >= n_u || r2 >= n_u) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    const df32 u0x = df_neg(ld(u + r0)), u0y = df_neg(ld(u + r1)), u0z = df_neg(ld(u + r2));
+    CSum a0, a1, a2, a3, a4, a5;
+    for (int a = 1; a < n_p; ++a) {
+        const int32_t i0 = dl[3 * a], i1 = dl[3 * a + 1], i2 = dl[3 * a + 2];
+        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= n_u || i1 >= n_u || i2 >= n_u) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const df32 gx = ld(g1 + g * n_p + a), gy = ld(g2 + g * n_p + a), gz = ld(g3 + g * n_p + a);
+        const df32 ux = df_add(ld(u + i0), u0x), uy = df_add(ld(u + i1), u0y), uz = df_add(ld(u + i2), u0z);
+        a0.add_prod(gx, ux);
+        a1.add_prod(gy, uy);
+        a2.add_prod(gz, uz);
+        a3.add_prod(gy, ux);
+        a3.add_prod(gx, uy);
+        a4.add_prod(gz, uy);
+        a4.add_prod(gy, uz);
+        a5.add_prod(gz, ux);
+        a5.add_prod(gx, uz);
+    }
+    double2 *o = reinterpret_cast<double2 *>(E + 6 * g);
+    o[0] = make_double2(a0.value(), a1.value());
+    o[1] = make_double2(a2.value(), a3.value());
+    o[2] = make_double2(a4.value(), a5.value());
+}
+
+// Force from hi + lo pairs of w * dphi (split once per pattern) and of the stress (split once per
+// call).
+__global__ void __launch_bounds__(128) force3_mixed_kernel(const float2 *__restrict__ wg1,
+                                                           const float2 *__restrict__ wg2,
+                                                           const float2 *__restrict__ wg3,
+                                                           const float2 *__restrict__ S,
+                                                           const int32_t *__restrict__ elem_row, int n_rows,
+                                                           int n_elem, int n_p, int n_q, double *__restrict__ F) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int nld = 3 * n_p;
+    if (t >= (long long)n_elem * nld) return;
+    const long long e = t / nld;
+    const int alpha = static_cast<int>(t % nld);
+    const int row = elem_row[t];
+    if (row < 0) return;
+    if (row >= n_rows) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    const int node = alpha / 3, comp = alpha % 3;
+    // the stress components multiplying d/dx, d/dy, d/dz for this displacement component
+    const int k0 = bt_row3(comp, 0), k1 = bt_row3(comp, 1), k2 = bt_row3(comp, 2);
+    CSum acc;
+    for (int q = 0; q < n_q; ++q) {
+        const long long g = e * n_q + q;
+        const float2 *s = S + 6 * g;
+        acc.add_prod(ld(wg1 + g * n_p + node), ld(s + k0));
+        acc.add_prod(ld(wg2 + g * n_p + node), ld(s + k1));
+        acc.add_prod(ld(wg3 + g * n_p + node), ld(s + k2));
+    }
+    red_add(F + row, acc.value());
+}
+
+}  // namespace
+}  // namespace ssp
+
+using namespace ssp;
+
+extern "C" {
+
+int ssp_split_f64(const double *x, const double *scale, long long n, int group, float *out_pairs, void *stream) {
+    if (n < 0 || (scale && group <= 0)) return SSP_ERR_INVALID;
+    if (n == 0) return SSP_OK;
+    if (!x || !out_pairs) return SSP_ERR_INVALID;
+    split_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(x, scale, n, group, reinterpret_cast<float2 *>(out_pairs));
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_3d_mixed(const float *dphi1_hl, const float *dphi2_hl, const float *dphi3_hl,
+                                         const float *u_hl, int n_u, const int32_t *elem_dof_lids, int n_int,
+                                         int n_elem, int n_p, int n_q, double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!dphi1_hl || !dphi2_hl || !dphi3_hl || !u_hl || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    const float2 *g1 = reinterpret_cast<const float2 *>(dphi1_hl), *g2 = reinterpret_cast<const float2 *>(dphi2_hl),
+                 *g3 = reinterpret_cast<const float2 *>(dphi3_hl);
+    strain3_mixed_kernel<<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(
+        g1, g2, g3, reinterpret_cast<const float2 *>(u_hl), elem_dof_lids, n_u, n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2_hl, const float *wdphi3_hl,
+                                     const float *stress_hl, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                     int n_rows, double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!wdphi1_hl || !wdphi2_hl || !wdphi3_hl || !stress_hl || !elem_row) return SSP_ERR_INVALID;
+    const long long n = (long long)n_elem * 3 * n_p;
+    force3_mixed_kernel<<<grid_for(n, 128), 128, 0, st>>>(
+        reinterpret_cast<const float2 *>(wdphi1_hl), reinterpret_cast<const float2 *>(wdphi2_hl),
+        reinterpret_cast<const float2 *>(wdphi3_hl), reinterpret_cast<const float2 *>(stress_hl), elem_row, n_rows,
+        n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+}  // extern "C"

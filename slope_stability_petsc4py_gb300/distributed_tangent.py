@@ -382,8 +382,29 @@ def _u_overlap_device(pattern, U):
     return u_ov
 
 
-def overlap_strain_device(pattern, U):
-    """E of every overlap point as an AoS (n_int, n_strain) CUDA tensor."""
+def _split_pairs(x, scale=None, group: int = 1):
+    """hi + lo float pairs of an FP64 CUDA tensor (ssp_split_f64), flat float32 (2 per value)."""
+    t = _lib.require_cuda()
+    out = t.empty(2 * x.numel(), dtype=t.float32, device="cuda")
+    _lib.call("ssp_split_f64", _lib.ptr(x), _lib.ptr(scale) if scale is not None else None, int(x.numel()), int(group),
+              _lib.ptr(out), _lib.stream_handle())
+    return out
+
+
+def _mixed_inputs(pattern):
+    """Per-pattern hi + lo pairs of the gradients and of w * gradient (the mixed form's constant
+    inputs), split once and kept with the pattern's device arrays."""
+    d = pattern.device
+    if "dphi1_hl" not in d:
+        for k in ("dphi1", "dphi2", "dphi3"):
+            d[k + "_hl"] = _split_pairs(d[k])
+            d["w" + k + "_hl"] = _split_pairs(d[k], d["weight"], pattern.n_p)
+    return d
+
+
+def overlap_strain_device(pattern, U, *, mixed: bool = False):
+    """E of every overlap point as an AoS (n_int, n_strain) CUDA tensor; mixed (3D): the
+    compensated FP32 kernel of the mixed-precision form."""
     t = _lib.require_cuda()
     u_ov = _u_overlap_device(pattern, U)
     n_int = pattern.n_local_int
@@ -391,7 +412,13 @@ def overlap_strain_device(pattern, U):
     d = pattern.device
     E = t.empty((n_int, pattern.n_strain), dtype=t.float64, device="cuda")
     st = _lib.stream_handle()
-    if pattern.dim == 3:
+    if pattern.dim == 3 and mixed:
+        d = _mixed_inputs(pattern)
+        u_hl = _split_pairs(u_ov)
+        _lib.call("ssp_assemble_overlap_strain_3d_mixed", _lib.ptr(d["dphi1_hl"]), _lib.ptr(d["dphi2_hl"]),
+                  _lib.ptr(d["dphi3_hl"]), _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el,
+                  pattern.n_p, pattern.n_q, _lib.ptr(E), st)
+    elif pattern.dim == 3:
         _lib.call("ssp_assemble_overlap_strain_3d", _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
                   _lib.ptr(u_ov), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p, pattern.n_q,
                   _lib.ptr(E), st)
@@ -429,12 +456,20 @@ def _local_field_aos(pattern, field, rows: int):
     return _lib.to_device(np.ascontiguousarray(f.T), t.float64)
 
 
-def owned_force_device(pattern, S_aos):
-    """Owned internal force B^T (w S) on owned rows (constrained rows = 0), CUDA tensor (n_rows,)."""
+def owned_force_device(pattern, S_aos, *, mixed: bool = False):
+    """Owned internal force B^T (w S) on owned rows (constrained rows = 0), CUDA tensor (n_rows,);
+    mixed (3D): the compensated FP32 kernel of the mixed-precision form."""
     t = _lib.require_cuda()
     d = pattern.device
     n_rows = int(pattern.local_matrix_pattern.shape[0])
     F = t.empty(n_rows, dtype=t.float64, device="cuda")
+    if mixed and pattern.dim == 3:
+        d = _mixed_inputs(pattern)
+        s_hl = _split_pairs(S_aos)
+        _lib.call("ssp_assemble_force_element_mixed", _lib.ptr(d["wdphi1_hl"]), _lib.ptr(d["wdphi2_hl"]),
+                  _lib.ptr(d["wdphi3_hl"]), _lib.ptr(s_hl), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
+                  pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
+        return F
     _lib.call("ssp_assemble_force_element", pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
               _lib.ptr(d["dphi3"]) if pattern.dim == 3 else None, _lib.ptr(S_aos), _lib.ptr(d["weight"]),
               _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size), pattern.n_p, pattern.n_q, n_rows,

@@ -39,7 +39,8 @@ def _free_system(op, K_mat):
 
 def newton_compare(op, mesh, *, lam: float, gamma: float = 20.0, r: float = 0.0, tol: float = 1e-9,
                    max_it: int = 30) -> dict:
-    """Plain-FP64 Newton solve; at each iterate also the mixed-tangent update, compared."""
+    """Plain-FP64 Newton solve; at each iterate also the mixed form's force, tangent and update,
+    compared with the FP64 ones (relative errors per Newton step)."""
     free = np.flatnonzero(op.q_mask.reshape(-1, order="F"))
     F_ext = gravity_load(op, mesh, gamma)[free]
     norm_ext = float(np.linalg.norm(F_ext))
@@ -63,9 +64,10 @@ def newton_compare(op, mesh, *, lam: float, gamma: float = 20.0, r: float = 0.0,
             break
         Kp = _free_system(op, K)
         dU = spsolve(Kp, -R)
-        # the mixed tangent at the same iterate
+        # the mixed form (compensated strain and force, mixed tangent) at the same iterate
         op.tangent_form = "mixed"
-        _, Km = op.build_F_K_regularized_all_free(lam, Ushape, r)
+        F_m, Km = op.build_F_K_regularized_all_free(lam, Ushape, r)
+        f_err = float(np.linalg.norm(np.asarray(F_m) - np.asarray(F_free)) / max(np.linalg.norm(F_free), 1e-300))
         Kmx = _free_system(op, Km)
         dUm = spsolve(Kmx, -R)
         op.tangent_form = "plain"
@@ -79,7 +81,8 @@ def newton_compare(op, mesh, *, lam: float, gamma: float = 20.0, r: float = 0.0,
                 break
             alpha *= 0.5
         U[free] += alpha * dU
-        history.append({"it": it, "residual": rel, "tangent_rel_err": k_err, "update_rel_err": du_err, "alpha": alpha})
+        history.append({"it": it, "residual": rel, "tangent_rel_err": k_err, "force_rel_err": f_err,
+                        "update_rel_err": du_err, "alpha": alpha})
     return {"iterations": len(history) - 1, "converged": history[-1]["residual"] < tol, "history": history, "U": U}
 
 

@@ -168,9 +168,11 @@ class ConstitutiveOperator:
         self.return_mapping = "binned"
         self.branch_model = None
         self._scratch = None
-        # "plain": every tangent product in FP64 (the drop-in, parity 1e-12 with the reference);
-        # "mixed": the plastic-point products B^T H in FP32 with H = w D B formed in FP64 and split
-        # into FP32 hi + lo parts, FP64 CSR accumulation (about 1e-7 relative tangent error)
+        # "plain": FP64 throughout (the drop-in, parity 1e-12 with the reference);
+        # "mixed": the plastic-point tangent products in FP32 (CUDA cores for P1/P2, tensor cores
+        # for P4) with H = w D B formed in compensated double-float arithmetic, and the 3D strain and
+        # force in compensated double-float arithmetic (~1e-13); the return mapping and every CSR /
+        # force accumulation stay FP64 (about 1e-7 relative tangent error)
         self.tangent_form = "plain"
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
@@ -331,7 +333,7 @@ class ConstitutiveOperator:
             raise ValueError(f"Unsupported owned constitutive mode {self.owned_constitutive_mode!r}")
         t = _lib.require_cuda()
         t0 = perf_counter()
-        E = overlap_strain_device(pat, U)
+        E = overlap_strain_device(pat, U, mixed=self.tangent_form == "mixed")
         self.time_local_strain.append(perf_counter() - t0)
         t1 = perf_counter()
         n = pat.n_local_int
@@ -392,7 +394,7 @@ class ConstitutiveOperator:
             raise ValueError("Stress tensor not computed")
         t0 = perf_counter()
         S = self._S_aos[:, : self.n_strain].contiguous() if self._S_aos.shape[1] != self.n_strain else self._S_aos
-        F = owned_force_device(pat, S)
+        F = owned_force_device(pat, S, mixed=self.tangent_form == "mixed")
         self.time_local_force_assembly.append(perf_counter() - t0)
         return F
 

@@ -68,6 +68,33 @@ def test_mixed_form_newton_iterations_unchanged(cuda_device, elem_type, dims):
     cmp = newton_compare(op, mesh, lam=lam)
     for h in cmp["history"][:-1]:
         print(f"  step {h['it']}: residual {h['residual']:.3e} tangent err {h['tangent_rel_err']:.2e} "
-              f"update err {h['update_rel_err']:.2e}")
+              f"force err {h['force_rel_err']:.2e} update err {h['update_rel_err']:.2e}")
         assert h["tangent_rel_err"] <= MIXED_RTOL
+        assert h["force_rel_err"] <= 1e-11
         assert h["update_rel_err"] <= 1e-4
+
+
+@pytest.mark.parametrize("elem_type,dims,amp", [("P2", (20, 8, 10), 0.02), ("P4", (8, 3, 4), 0.01)])
+def test_compensated_strain_and_force_match_fp64(cuda_device, elem_type, dims, amp):
+    """The mixed form's strain and force (compensated double-float on the FP32 pipe) against the
+    FP64 kernels: max-norm relative error ~1e-13, bounded here by 1e-11."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import synthetic
+    from slope_stability_petsc4py_gb300.distributed_tangent import overlap_strain_device, owned_force_device
+
+    mesh, mats, op = _operator(*dims, elem_type=elem_type)
+    pat = op.owned_tangent_pattern
+    U = synthetic.displacement_field(mesh, mats, amplitude=amp, seed=8)
+    E64 = overlap_strain_device(pat, U).cpu().numpy()
+    Emx = overlap_strain_device(pat, U, mixed=True).cpu().numpy()
+    err_e = rel_err(Emx, E64)
+    op.reduction(1.1)
+    op.constitutive_problem_stress_tangent(U)
+    S = op._S_aos
+    F64 = owned_force_device(pat, S).cpu().numpy()
+    Fmx = owned_force_device(pat, S, mixed=True).cpu().numpy()
+    err_f = rel_err(Fmx, F64)
+    print(f"{elem_type}: strain error {err_e:.2e}, force error {err_f:.2e}")
+    assert err_e <= 1e-11 and err_f <= 1e-11
+    torch.cuda.synchronize()
