@@ -17,10 +17,6 @@
 
 namespace ssp {
 
-// defined in constitutive.cu
-__device__ int mc3d_point_ext(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
-                              double *DS);
-
 namespace {
 
 constexpr int kIn = 6, kH = 32, kOut = 5;
@@ -454,37 +450,6 @@ int launch_mlp_tc(const float *params, const float *X, const double *E, const do
 }
 
 // The exact FP64 return mapping over the five proposal lists (blockIdx.y = list).
-__global__ void __launch_bounds__(128) exact_over_bins_kernel(const double *__restrict__ E,
-                                                              const double *__restrict__ c_bar,
-                                                              const double *__restrict__ sin_phi,
-                                                              const double *__restrict__ shear,
-                                                              const double *__restrict__ lame, int n,
-                                                              double *__restrict__ S, double *__restrict__ DS,
-                                                              int8_t *__restrict__ branch,
-                                                              const int32_t *__restrict__ scratch) {
-    const int k = blockIdx.y;
-    const int cnt = scratch[k];
-    const int32_t *list = scratch + 8 + (long long)k * n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-        const int p = list[i];
-        if (p < 0 || p >= n) {
-            flag(SSP_DEV_BAD_INDEX);
-            continue;
-        }
-        double e[6], s[6], ds[36];
-#pragma unroll
-        for (int j = 0; j < 6; ++j) e[j] = E[6ll * p + j];
-        const int b = mc3d_point_ext(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
-        double2 *S2 = reinterpret_cast<double2 *>(S + 6ll * p);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) S2[j] = make_double2(s[2 * j], s[2 * j + 1]);
-        double2 *D2 = reinterpret_cast<double2 *>(DS + 36ll * p);
-#pragma unroll
-        for (int j = 0; j < 18; ++j) D2[j] = make_double2(ds[2 * j], ds[2 * j + 1]);
-        branch[p] = static_cast<int8_t>(b);
-    }
-}
-
 }  // namespace
 }  // namespace ssp
 
@@ -550,15 +515,7 @@ int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const 
     if (cudaMemsetAsync(scratch, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
     const int rc = launch_mlp_tc<true>(params, nullptr, E, c_bar, sin_phi, shear, lame, n_int, nullptr, scratch, st);
     if (rc != SSP_OK) return rc;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long gx = (long long)sms * 8;
-    const long long need = (n_int + 127) / 128;
-    if (gx > need) gx = need;
-    exact_over_bins_kernel<<<dim3(static_cast<unsigned>(gx), kOut), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int,
-                                                                                   S_out, DS_out, branch_out, scratch);
-    return launch_status();
+    return exact_over_bins(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, kOut, st);
 }
 
 }  // extern "C"

@@ -380,25 +380,45 @@ __device__ __forceinline__ void store36(double *A, long long p, const double *s)
     for (int k = 0; k < 18; ++k) A2[k] = make_double2(s[2 * k], s[2 * k + 1]);
 }
 
+// Single pass, one thread per point.  With the tangent, a warp's 32 consecutive DS rows are staged
+// in shared memory (row stride 37 doubles) and written as one contiguous block with full-line
+// stores.
 template <bool TANGENT>
 __global__ void __launch_bounds__(128) mc3d_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                    const double *__restrict__ sin_phi, const double *__restrict__ shear,
                                                    const double *__restrict__ lame, int n, double *__restrict__ S,
                                                    double *__restrict__ DS, int8_t *__restrict__ branch) {
+    constexpr int kStride = 37;
+    __shared__ double stage[TANGENT ? 4 : 1][TANGENT ? 32 * kStride : 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    double e[6], s[6];
-    load6(E, p, e);
-    int b;
-    if (TANGENT) {
-        double ds[36];
-        b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
-        store36(DS, p, ds);
-    } else {
-        b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, nullptr);
+    if (p < n) {
+        double e[6], s[6];
+        load6(E, p, e);
+        int b;
+        if (TANGENT) {
+            double ds[36];
+            b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
+#pragma unroll
+            for (int k = 0; k < 36; ++k) stage[warp][lane * kStride + k] = ds[k];
+        } else {
+            b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, nullptr);
+        }
+        store6(S, p, s);
+        if (branch) branch[p] = static_cast<int8_t>(b);
     }
-    store6(S, p, s);
-    if (branch) branch[p] = static_cast<int8_t>(b);
+    if (TANGENT) {
+        __syncwarp();
+        const int p0 = blockIdx.x * blockDim.x + warp * 32;
+        if (p0 < n) {
+            const int nw = n - p0 < 32 ? n - p0 : 32;
+            double *dst = DS + 36ll * p0;
+            for (int idx = lane; idx < nw * 36; idx += 32) {
+                const int pt = idx / 36;
+                dst[idx] = stage[warp][pt * kStride + (idx - pt * 36)];
+            }
+        }
+    }
 }
 
 // Binned return mapping in three passes.  scratch = 4 counters, then three regions of n int32.
@@ -843,12 +863,82 @@ int32_t *fixed_scratch_for_current_device() {
     return g_fixed_ptr[dev];
 }
 
+// The exact return mapping over lists of points (the learned proposal's bins, blockIdx.y = list;
+// scratch = counters at scratch[list], lists of n entries from scratch + 8).  Each warp takes 32
+// consecutive list entries, runs the exact return mapping lane by lane, stages
+// the results in shared memory and writes them back row by row, the whole warp on one point's
+// 288-byte DS row at a time (full-line stores instead of 32 strided rows).
+constexpr int kRowStride = 37;
+__global__ void __launch_bounds__(128) exact_over_bins_kernel(const double *__restrict__ E,
+                                                              const double *__restrict__ c_bar,
+                                                              const double *__restrict__ sin_phi,
+                                                              const double *__restrict__ shear,
+                                                              const double *__restrict__ lame, int n,
+                                                              double *__restrict__ S, double *__restrict__ DS,
+                                                              int8_t *__restrict__ branch,
+                                                              const int32_t *__restrict__ scratch) {
+    __shared__ double sds[4][32 * kRowStride];
+    __shared__ double ss[4][32 * 7];
+    __shared__ int sp[4][32];
+    const int k = blockIdx.y;
+    const int cnt = scratch[k];
+    const int32_t *list = scratch + 8 + (long long)k * n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double *wd = sds[warp], *ws = ss[warp];
+    int *wp = sp[warp];
+    for (long long base = ((long long)blockIdx.x * 4 + warp) * 32; base < cnt; base += (long long)gridDim.x * 128) {
+        const long long i = base + lane;
+        int p = i < cnt ? list[i] : -1;
+        if (i < cnt && (p < 0 || p >= n)) {
+            flag(SSP_DEV_BAD_INDEX);
+            p = -1;
+        }
+        if (p >= 0) {
+            double e[6], s[6], ds[36];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) e[j] = E[6ll * p + j];
+            const int b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
+            branch[p] = static_cast<int8_t>(b);
+#pragma unroll
+            for (int j = 0; j < 36; ++j) wd[lane * kRowStride + j] = ds[j];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) ws[lane * 7 + j] = s[j];
+        }
+        wp[lane] = p;
+        __syncwarp();
+        for (int r = 0; r < 32; ++r) {
+            const int pr = wp[r];
+            if (pr < 0) continue;  // warp-uniform
+            double *row = DS + 36ll * pr;
+            row[lane] = wd[r * kRowStride + lane];
+            if (lane < 4) row[32 + lane] = wd[r * kRowStride + 32 + lane];
+        }
+#pragma unroll
+        for (int it = 0; it < 6; ++it) {
+            const int idx = it * 32 + lane, r = idx / 6, j = idx - 6 * (idx / 6);
+            const int pr = wp[r];
+            if (pr >= 0) S[6ll * pr + j] = ws[r * 7 + j];
+        }
+        __syncwarp();
+    }
+}
+
 }  // namespace
 
-// The single-pass return mapping of one point, for kernels in other translation units.
-__device__ int mc3d_point_ext(const double *E, double c_bar, double sin_phi, double shear, double lame, double *S,
-                              double *DS) {
-    return mc3d_point(E, c_bar, sin_phi, shear, lame, S, DS);
+
+int exact_over_bins(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                    const int32_t *scratch, int n_lists, cudaStream_t st) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long gx = (long long)sms * 8;
+    const long long need = (n_int + 127) / 128;
+    if (gx > need) gx = need;
+    exact_over_bins_kernel<<<dim3(static_cast<unsigned>(gx), n_lists), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame,
+                                                                                       n_int, S_out, DS_out, branch_out,
+                                                                                       scratch);
+    return launch_status();
 }
 
 }  // namespace ssp

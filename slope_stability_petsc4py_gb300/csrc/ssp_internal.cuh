@@ -52,6 +52,12 @@ __host__ __device__ __forceinline__ int bt_row2(int comp, int grad) {
     return static_cast<int>((0x1220u >> (4 * (comp * 2 + grad))) & 0xFu);
 }
 
+// The exact 3D return mapping over n_lists point lists (constitutive.cu); scratch holds the list
+// sizes at scratch[0 .. n_lists) and the lists of n_int entries from scratch + 8.
+int exact_over_bins(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                    const int32_t *scratch, int n_lists, cudaStream_t st);
+
 // Mixed-precision plastic-correction tangent of 3D P4 elements on the tensor cores (tangent_tc.cu).
 int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
                      const int8_t *branch, const double *shear, const double *lame, const int32_t *emap, int n_elem,

@@ -115,9 +115,10 @@ def test_training_learns_the_branches_and_gains(cuda_device):
         op.reduction(1.25)
         op.constitutive_problem_stress_tangent(U)
         outs[mode] = (op._S_aos.clone(), op._DS_aos.clone(), op._branch.clone())
-    assert torch.equal(outs["learned"][0], outs["unsorted"][0])
-    assert torch.equal(outs["learned"][1], outs["unsorted"][1])
+    # the same FP64 return mapping compiled into two kernels: the same branches, results to a few ulps
     assert torch.equal(outs["learned"][2], outs["unsorted"][2])
+    assert rel_err(outs["learned"][0].cpu().numpy(), outs["unsorted"][0].cpu().numpy()) <= 1e-14
+    assert rel_err(outs["learned"][1].cpu().numpy(), outs["unsorted"][1].cpu().numpy()) <= 1e-14
     assert rel_err(outs["binned"][1].cpu().numpy(), outs["unsorted"][1].cpu().numpy()) <= PLAIN_RTOL
 
     br = outs["unsorted"][2]
