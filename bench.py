@@ -39,7 +39,8 @@ LAMBDA, R_REG = 1.1, 0.1
 NCU_TRAFFIC = {
     "3d_p2_homo": {
         "ssp_tangent_plastic_correction": 286.20e6 + 63.73e6,
-        "ssp_tangent_plastic_correction_mixed": 283.71e6 + 59.34e6,
+        "ssp_tangent_plastic_correction_mixed": 297.67e6 + 70.18e6,
+        "ssp_assemble_overlap_strain_3d_mixed": 281.74e6 + 35.76e6,
         "ssp_assemble_overlap_strain_3d": 284.63e6 + 36.25e6,
         "ssp_assemble_force_element": 343.75e6 + 2.57e6,
         "ssp_constitutive_3d_sds_binned": (90.67 + 304.28 + 22.35 + 1.76 + 34.33 + 1.12) * 1e6,
@@ -235,7 +236,11 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def kernel_profile(torch, lib, step, reps=3):
+def kernel_profile(torch, lib, step, op, reps=3):
+    """Per-entry-point CUDA-event times, the launches serialised on one stream (the concurrent force
+    and the staged values copy would otherwise share the GPU with the kernels inside the brackets)."""
+    op.concurrent_force = False
+    op.stage_values = False
     lib.TRACE = []
     for _ in range(reps):
         step()
@@ -244,6 +249,8 @@ def kernel_profile(torch, lib, step, reps=3):
     for name, a, b in lib.TRACE:
         per.setdefault(name, []).append(a.elapsed_time(b))
     lib.TRACE = None
+    op.concurrent_force = True
+    op.stage_values = True
     total = sum(sum(v) for v in per.values()) / reps
     return {k: {"ms_per_launch": float(np.mean(v)), "launches_per_step": len(v) / reps,
                 "ms_per_step": float(np.sum(v)) / reps, "share": float(np.sum(v)) / reps / total}
@@ -267,7 +274,8 @@ def algorithmic(name, st):
     n, n_el, n_p, n_q, dim, ns = st["n"], st["n_el"], st["n_p"], st["n_q"], st["dim"], st["ns"]
     nld = dim * n_p
     s_out = 6 if dim == 3 else 4
-    if name in ("ssp_constitutive_sds_branch", "ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_learned"):
+    if name in ("ssp_constitutive_sds_branch", "ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_learned",
+                "ssp_constitutive_3d_sds_binned_mixed", "ssp_constitutive_3d_sds_learned_mixed"):
         return {"bytes": n * (8 * ns + 4 * 8 + 8 * s_out + 8 * ns * ns + 1), "flops": 0}
     if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d", "ssp_assemble_overlap_strain_3d_mixed"):
         fp64 = 0 if name.endswith("_mixed") else n * 2 * 9 * n_p  # the mixed kernel's products are FP32
@@ -312,6 +320,7 @@ def compare_forms(torch, lib, op, mesh, mats, args, step, ms_plain):
     out = {"plain": {"value": n_int / (ms_plain * 1e-3), "ms_per_step": ms_plain}}
     w = max(args.warmup, 3)
     op.tangent_form = "plain"
+    step()
     kp = op.build_K_regularized(R_REG).values.clone()
     for name, form, mapping in (("mixed", "mixed", "binned"), ("mixed+learned", "mixed", "learned"),
                                 ("plain+unsorted", "plain", "unsorted"), ("plain+learned", "plain", "learned")):
@@ -341,10 +350,11 @@ def train_branch_model(torch, op, mesh, mats, name):
               for k, (lam, f) in enumerate(zip(np.linspace(1.0, 1.4, 6), np.linspace(0.4, 1.6, 6)))]
     X, y = learned.collect_training_data(op, states)
     model = learned.BranchProposal(seed=0)
-    hist = model.train(X, y, epochs=4, batch=65536, lr=3e-3)
+    hist = model.train(X, y, epochs=6, batch=8192, lr=3e-3)
     torch.cuda.synchronize()
     op.branch_model = model
-    return {"training_samples": int(X.shape[0]), "epochs": 4, "final_loss": hist[-1][0],
+    return {"training_samples": int(X.shape[0]), "samples": "points the elastic screen lists", "epochs": 6,
+            "batch": 8192, "final_loss": hist[-1][0],
             "final_train_accuracy": hist[-1][1], "training_s": time.perf_counter() - t0,
             "training_states": "6 states, lambda 1.0..1.4, amplitude 0.4..1.6x (the timed state is held out)"}
 
@@ -376,11 +386,8 @@ def run_gpu(args):
         learned_info = train_branch_model(torch, op, mesh, mats, args.config)
     op.return_mapping = args.return_mapping
 
-    def step():
-        op.reduction(LAMBDA)
-        op.constitutive_problem_stress_tangent(U_dev)
-        op.build_F_free_local()
-        op.build_K_regularized(R_REG)
+    def step():  # one Newton iteration through the operator's composite entry point
+        op.build_F_K_regularized_all_free(LAMBDA, U_dev, R_REG)
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -397,8 +404,10 @@ def run_gpu(args):
         time.sleep(0.3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
+    h0 = time.perf_counter()
     for _ in range(args.steps):
         step()
+    host_ms = (time.perf_counter() - h0) * 1e3 / args.steps  # the host's enqueue time per step
     e1.record()
     torch.cuda.synchronize()
     clock_info = clocks.stop() if clocks else None
@@ -413,7 +422,7 @@ def run_gpu(args):
         ms = float(t.item())
 
     # per-kernel durations from a separate traced pass (CUDA events on the launch stream)
-    kernels = kernel_profile(torch, _lib, step, reps=3)
+    kernels = kernel_profile(torch, _lib, step, op, reps=3)
     stats = workload_stats(op)
     hbm_peak, hbm_src = peaks()
     fp64_tf = fp64_peak(torch, _lib)
@@ -425,8 +434,10 @@ def run_gpu(args):
     tangent_err = None
     if args.form == "mixed":  # tangent error of this form against the FP64 form, same state
         op.tangent_form = "plain"
+        step()
         kp = op.build_K_regularized(R_REG).values.clone()
         op.tangent_form = "mixed"
+        step()
         km = op.build_K_regularized(R_REG).values
         tangent_err = {"max_norm_rel": float((km - kp).abs().max() / kp.abs().max()),
                        "frobenius_rel": float(torch.linalg.norm(km - kp) / torch.linalg.norm(kp))}
@@ -456,6 +467,7 @@ def run_gpu(args):
                            "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)", "algorithmic_flops": fl,
                            "ms_per_launch": corr_ms} if corr_ms else None),
         "kernels": kernels,
+        "host_enqueue_ms_per_step": host_ms,
         "gpu_launches": launches,
         "clocks": clock_info,
     }
@@ -463,14 +475,14 @@ def run_gpu(args):
         from slope_stability_petsc4py_gb300 import learned
 
         br = op._branch
-        n = br.numel()
-        cnt = op._scratch[:5].cpu().numpy()
-        order = torch.cat([op._scratch[8 + k * n: 8 + k * n + int(cnt[k])] for k in range(5)]).long()
-        learned_info["bench_state_accuracy"] = float(
-            sum(int((br.index_select(0, op._scratch[8 + k * n: 8 + k * n + int(cnt[k])].long()) == k).sum().item())
-                for k in range(5)) / n)
-        learned_info["distinct_branches_per_warp"] = {"point_order": learned.warp_branch_mix(br),
-                                                      "learned_bins": learned.warp_branch_mix(br, order)}
+        listed, bins = learned.proposal_bins(op._scratch, br.numel())
+        n_listed = max(1, listed.numel())
+        learned_info["listed_points"] = int(listed.numel())
+        learned_info["bench_state_accuracy_listed"] = float(
+            sum(int((br.index_select(0, bins[k]) == k).sum().item()) for k in range(5)) / n_listed)
+        learned_info["distinct_branches_per_warp_listed"] = {
+            "screen_order": learned.warp_branch_mix(br, listed),
+            "learned_bins": learned.warp_branch_mix(br, torch.cat(bins))}
         line["learned"] = learned_info
 
     if args.form == "plain" and args.return_mapping == "binned" and pat.dim == 3 and not args.no_forms:

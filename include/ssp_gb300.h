@@ -84,6 +84,15 @@ int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const d
                                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
                                    int32_t *scratch, void *stream);
 
+/* No counterpart in the reference.  ssp_constitutive_3d_sds_binned for the mixed-precision form:
+ * the same branches, multipliers and S (FP64, bitwise the same), the plastic points' DS in
+ * double-float arithmetic on the FP32 pipe (per-point FP64 coefficients, compensated sums of
+ * products per entry, about 2^-46 of the terms' magnitude).  A point whose smallest eigenvalue gap is
+ * below 1e-3 of max|e|, or whose coefficients leave the float range, gets the FP64 DS. */
+int ssp_constitutive_3d_sds_binned_mixed(const double *E, const double *c_bar, const double *sin_phi,
+                                         const double *shear, const double *lame, int n_int, double *S_out,
+                                         double *DS_out, int8_t *branch_out, int32_t *scratch, void *stream);
+
 /* No counterpart in the reference.  ssp_constitutive_3d_sds_binned for callers that cannot
  * allocate device memory, e.g. a constitutive hook called from inside another solver's assembly
  * loop: it is handed device pointers to its inputs and outputs only, the host framework owns and
@@ -147,7 +156,7 @@ int ssp_split_f64(const double *x, const double *scale, long long n, int group, 
  * same sums in compensated double-float arithmetic on the FP32 pipe (product rounding errors
  * recovered with FMAs, sums kept as hi + lo pairs), widened to FP64 once per output.  Inputs are
  * hi + lo pairs from ssp_split_f64: the gradients (strain), w * gradient (force; scale = weight,
- * group = n_p), the overlap displacements and the stresses.  The strain is formed from displacement
+ * group = n_p) and the overlap displacements; the force kernel splits the FP64 stresses itself.  The strain is formed from displacement
  * differences to the element's first node (sum of the basis gradients = 0), so no digits cancel.
  * Relative error against the FP64 kernels ~1e-13; the force is still accumulated into out_values
  * with FP64 reductions.  No reference counterpart. */
@@ -155,7 +164,7 @@ int ssp_assemble_overlap_strain_3d_mixed(const float *dphi1_hl, const float *dph
                                          const float *u_hl, int n_u, const int32_t *elem_dof_lids, int n_int,
                                          int n_elem, int n_p, int n_q, double *out_values, void *stream);
 int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2_hl, const float *wdphi3_hl,
-                                     const float *stress_hl, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                     const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                      int n_rows, double *out_values, void *stream);
 
 /* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
@@ -299,13 +308,21 @@ int ssp_mlp_loss_grad(const float *params, const float *X, const int8_t *labels,
 int ssp_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr, float beta1, float beta2,
                  float eps, float grad_scale, void *stream);
 
-/* The 3D return mapping with learned binning: propose + bin, then the exact FP64 return mapping
- * over the bins.  Same outputs as ssp_constitutive_sds_branch.  scratch is caller-allocated device
- * memory of 5*n_int + 8 int32 (counters and bins), overwritten. */
+/* The 3D return mapping with learned binning: the binned return mapping's elastic screen (pass A),
+ * then a branch proposal by the MLP (tensor-core inference) for the points the screen listed,
+ * which are binned by it; the exact FP64 decision pass runs over the five bins, then the branch
+ * finish pass.  Same outputs as ssp_constitutive_sds_branch.  scratch is caller-allocated device
+ * memory of 8*n_int + 12 int32 (the binned layout of 3*n_int + 4, then 8 bin counters and five
+ * bins of n_int), overwritten. */
 int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const double *c_bar,
                                     const double *sin_phi, const double *shear, const double *lame, int n_int,
                                     double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
                                     void *stream);
+/* The learned return mapping of the mixed-precision form (DS as ssp_constitutive_3d_sds_binned_mixed). */
+int ssp_constitutive_3d_sds_learned_mixed(const float *params, const double *E, const double *c_bar,
+                                          const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                          double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                          void *stream);
 
 /* ------------------------------------------------------------------ pattern (host) */
 

@@ -31,6 +31,7 @@ _SIGS = {
     "ssp_tc_tf32_probe": [_vp, _vp, _c_int, _c_int, _vp, _vp],
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_constitutive_3d_sds_binned_mixed": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned_noalloc": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_tangent_plastic_correction": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp, _vp, _vp,
                                        _vp],
@@ -61,6 +62,7 @@ _SIGS = {
     "ssp_mlp_adam": [_vp, _vp, _vp, _vp, _c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                      ctypes.c_float, _vp],
     "ssp_constitutive_3d_sds_learned": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_constitutive_3d_sds_learned_mixed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_pattern_build": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _c_int, _c_int, ctypes.POINTER(_vp)],
     "ssp_pattern_sizes": [_vp, _vp],
     "ssp_pattern_copy": [_vp, ctypes.c_char_p, _vp],
@@ -115,8 +117,9 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
+    "ssp_constitutive_3d_sds_binned_mixed": 3, "ssp_constitutive_3d_sds_learned_mixed": 4,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
-    "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 2,
+    "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 4,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
 }

@@ -2,9 +2,11 @@
 //
 // A small MLP (6 -> 32 -> 32 -> 5, ReLU) maps cheap FP32 invariants of the trial strain to one of
 // the five return branches of constitutive_3D_kernel.h:116-350 (elastic, smooth face, left edge,
-// right edge, apex).  Points are binned by the proposed branch and the exact FP64 return mapping
-// then runs bin by bin, so each warp mostly executes one branch's code.  The exact kernel decides
-// and computes every result; a wrong proposal only costs time.  The network is trained on the GPU
+// right edge, apex).  In the learned return mapping the points that the exact kernel's FP32 elastic
+// screen cannot settle (those near or past the yield surface) get a proposal, are binned by it, and
+// the exact FP64 decision pass runs bin by bin, so each warp mostly follows one branch's checks.
+// The exact kernel decides and computes every result; a wrong proposal only costs time.  The
+// network is trained on the GPU
 // by the kernels below (forward, backward, Adam), on (features, branch) pairs produced by the
 // exact return mapping.
 //
@@ -250,9 +252,11 @@ __global__ void adam_kernel(float *__restrict__ params, const float *__restrict_
 // operand row, and after each MMA reads its accumulator row (tcgen05.ld, lane t), adds the bias,
 // applies ReLU and rounds to BF16 for the next layer.  The same BF16 rounding of weights and
 // activations as forward_argmax<true>; the accumulation order is the tensor core's.
-// FROM_STRAIN: features from the trial strain, the argmax appended to its branch list (the
-// learned return mapping's proposal); otherwise features from X and the argmax stored in pred.
-constexpr int kTcTile = 128, kTcCols = 128;
+// FROM_LIST: the points listed by the binned return mapping's screen (count scratch[0], indices
+// from scratch + 4), features from their trial strain, each point appended to the list of its
+// proposed branch (counts at scratch + 4 + 3 n, lists of n entries from scratch + 12 + 3 n);
+// otherwise features from X and the argmax stored in pred.
+constexpr int kTcTile = 128, kTcCols = 64;  // layer 1 -> columns 0-31, layer 2 -> 32-63, layer 3 -> 0-15
 struct MlpSmem {
     alignas(128) unsigned char w1[32 * 16 * 2];
     alignas(128) unsigned char w2[32 * 32 * 2];
@@ -265,9 +269,9 @@ struct MlpSmem {
     uint32_t tmem_slot;
     int abort;
 };
-// more than a quarter of an SM's shared memory, so at most four CTAs (4 x 128 tensor-memory
-// columns) are resident on an SM
-constexpr size_t kMlpSmemBytes = 58 * 1024;
+// more than a ninth of an SM's 228 KB of shared memory, so at most eight CTAs (8 x 64 tensor-memory
+// columns, all of the SM's 512) are resident on an SM and every allocation succeeds at once
+constexpr size_t kMlpSmemBytes = 26 * 1024;
 static_assert(sizeof(MlpSmem) <= kMlpSmemBytes, "MLP shared memory");
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -311,8 +315,8 @@ __device__ __forceinline__ bool mlp_layer(MlpSmem &S, const unsigned char *a, co
     return S.abort == 0;
 }
 
-template <bool FROM_STRAIN>
-__global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict__ params, const float *__restrict__ X,
+template <bool FROM_LIST>
+__global__ void __launch_bounds__(kTcTile, 8) mlp_tc_kernel(const float *__restrict__ params, const float *__restrict__ X,
                                                          const double *__restrict__ E,
                                                          const double *__restrict__ c_bar,
                                                          const double *__restrict__ sin_phi,
@@ -355,14 +359,23 @@ __global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict
     const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
     constexpr uint32_t id32 = tc::idesc(tc::kFmtBF16, kTcTile, 32), id16 = tc::idesc(tc::kFmtBF16, kTcTile, 16);
     uint32_t phase = 0;
-    const int tiles = (n + kTcTile - 1) / kTcTile;
+    const int cnt = FROM_LIST ? scratch[0] : n;
+    const int tiles = (cnt + kTcTile - 1) / kTcTile;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int p = tile * kTcTile + tid;
+        const int i_item = tile * kTcTile + tid;
+        int p = i_item < cnt ? i_item : -1;
+        if (FROM_LIST && p >= 0) {
+            p = scratch[4 + p];
+            if (p < 0 || p >= n) {
+                flag(SSP_DEV_BAD_INDEX);
+                p = -1;
+            }
+        }
         float v[32];
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = 0.0f;
-        if (p < n) {
-            if (FROM_STRAIN) {
+        if (p >= 0) {
+            if (FROM_LIST) {
                 features(E + 6ll * p, c_bar[p], sin_phi[p], shear[p], lame[p], v);
             } else {
 #pragma unroll
@@ -390,11 +403,12 @@ __global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict
             for (int j = 0; j < 32; ++j) v[j] = fmaxf(__uint_as_float(r[j]) + S.b2[j], 0.0f);
         }
         store_row_bf16<4>(S.a3, tid, v);
-        if (!mlp_layer(S, S.a3, S.w3, 16, 32, tmem + 64, id16, phase)) break;
+        // layer 1's accumulator columns are free again: every thread has read them
+        if (!mlp_layer(S, S.a3, S.w3, 16, 32, tmem, id16, phase)) break;
         int best = 0;
         {
             uint32_t r[16];
-            tc::tmem_ld16(tmem + lane_base + 64, r);
+            tc::tmem_ld16(tmem + lane_base, r);
             tc::tmem_wait_ld();
             float bz = -3.0e38f;
 #pragma unroll
@@ -406,20 +420,20 @@ __global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict
                 }
             }
         }
-        if (FROM_STRAIN) {
-            const int b = p < n ? best : -1;
-            int32_t *lists = scratch + 8;
+        if (FROM_LIST) {
+            const int b = p >= 0 ? best : -1;
+            int32_t *counts = scratch + 4 + 3ll * n, *lists = scratch + 12 + 3ll * n;
 #pragma unroll
             for (int k = 0; k < kOut; ++k) {
                 const unsigned mask = __ballot_sync(0xffffffffu, b == k);
                 if (mask == 0u) continue;
                 const int leader = __ffs(mask) - 1;
                 int base = 0;
-                if (lane == leader) base = atomicAdd(scratch + k, __popc(mask));
+                if (lane == leader) base = atomicAdd(counts + k, __popc(mask));
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (b == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
             }
-        } else if (p < n) {
+        } else if (p >= 0) {
             pred[p] = static_cast<int8_t>(best);
         }
     }
@@ -431,17 +445,17 @@ __global__ void __launch_bounds__(kTcTile) mlp_tc_kernel(const float *__restrict
     }
 }
 
-template <bool FROM_STRAIN>
+template <bool FROM_LIST>
 int launch_mlp_tc(const float *params, const float *X, const double *E, const double *c_bar, const double *sin_phi,
                   const double *shear, const double *lame, int n, int8_t *pred, int32_t *scratch, cudaStream_t st) {
-    auto kernel = mlp_tc_kernel<FROM_STRAIN>;
+    auto kernel = mlp_tc_kernel<FROM_LIST>;
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kMlpSmemBytes)) !=
         cudaSuccess)
         return SSP_ERR_CUDA;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long grid = (long long)sms * 4;
+    long long grid = (long long)sms * 8;
     const long long tiles = (n + kTcTile - 1) / kTcTile;
     if (grid > tiles) grid = tiles;
     kernel<<<static_cast<unsigned>(grid), kTcTile, kMlpSmemBytes, st>>>(params, X, E, c_bar, sin_phi, shear, lame, n, pred,
@@ -449,7 +463,25 @@ int launch_mlp_tc(const float *params, const float *X, const double *E, const do
     return launch_status();
 }
 
-// The exact FP64 return mapping over the five proposal lists (blockIdx.y = list).
+// Pass A of the binned return mapping, the proposal for its listed points, then passes B (over
+// the five proposal bins) and C.
+int learned_return_mapping(const float *params, const double *E, const double *c_bar, const double *sin_phi,
+                           const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
+                           int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!params || !E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+        return SSP_ERR_INVALID;
+    int32_t *counts = scratch + 4 + 3ll * n_int, *lists = scratch + 12 + 3ll * n_int;
+    if (cudaMemsetAsync(counts, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+    if (rc != SSP_OK) return rc;
+    rc = launch_mlp_tc<true>(params, nullptr, E, c_bar, sin_phi, shear, lame, n_int, nullptr, scratch, st);
+    if (rc != SSP_OK) return rc;
+    return binned_decide_finish(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, lists,
+                                counts, kOut, n_int, compensated_ds, st);
+}
+
 }  // namespace
 }  // namespace ssp
 
@@ -507,15 +539,16 @@ int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const 
                                     const double *sin_phi, const double *shear, const double *lame, int n_int,
                                     double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
                                     void *stream) {
-    if (n_int < 0) return SSP_ERR_INVALID;
-    if (n_int == 0) return SSP_OK;
-    if (!params || !E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
-        return SSP_ERR_INVALID;
-    cudaStream_t st = as_stream(stream);
-    if (cudaMemsetAsync(scratch, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    const int rc = launch_mlp_tc<true>(params, nullptr, E, c_bar, sin_phi, shear, lame, n_int, nullptr, scratch, st);
-    if (rc != SSP_OK) return rc;
-    return exact_over_bins(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, kOut, st);
+    return learned_return_mapping(params, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                                  false, as_stream(stream));
+}
+
+int ssp_constitutive_3d_sds_learned_mixed(const float *params, const double *E, const double *c_bar,
+                                          const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                          double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                          void *stream) {
+    return learned_return_mapping(params, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                                  true, as_stream(stream));
 }
 
 }  // extern "C"

@@ -7,7 +7,8 @@
 // hi + lo pair), about 46 significant bits, and widened to FP64 once per output.
 //
 // The FP64 inputs are split once where they are constant (the gradients dphi and w * dphi, once per
-// pattern) and once per call otherwise (the overlap displacements, the stresses): ssp_split_f64.
+// pattern, ssp_split_f64), once per call otherwise (the overlap displacements), and the stresses
+// by the force kernel's blocks into shared memory.
 //
 // Strain: with sum_a grad N_a = 0, E = sum_a dphi_a (x) (u_a - u_0), node 0 of the element as the
 // reference displacement.  The differences remove the rigid translation of the element, so the
@@ -20,21 +21,6 @@
 
 namespace ssp {
 namespace {
-
-// Compensated accumulator: value = s + c, s accumulates the leading parts with TwoSum, c the
-// rounding errors and the low-order product terms.
-struct CSum {
-    float s = 0.0f, c = 0.0f;
-    __device__ __forceinline__ void add_prod(df32 x, df32 y) {
-        const float p = __fmul_rn(x.hi, y.hi);
-        float e = __fmaf_rn(x.hi, y.hi, -p);
-        e = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, e));
-        const df32 t = df_two_sum(s, p);
-        s = t.hi;
-        c = __fadd_rn(c, __fadd_rn(t.lo, e));
-    }
-    __device__ __forceinline__ double value() const { return df_to_f64(df_fast_two_sum(s, c)); }
-};
 
 __device__ __forceinline__ df32 df_neg(df32 a) { return {-a.hi, -a.lo}; }
 
@@ -95,16 +81,30 @@ __global__ void __launch_bounds__(128) strain3_mixed_kernel(const float2 *__rest
     o[2] = make_double2(a4.value(), a5.value());
 }
 
-// Force from hi + lo pairs of w * dphi (split once per pattern) and of the stress (split once per
-// call).
-__global__ void __launch_bounds__(128) force3_mixed_kernel(const float2 *__restrict__ wg1,
-                                                           const float2 *__restrict__ wg2,
-                                                           const float2 *__restrict__ wg3,
-                                                           const float2 *__restrict__ S,
-                                                           const int32_t *__restrict__ elem_row, int n_rows,
-                                                           int n_elem, int n_p, int n_q, double *__restrict__ F) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// Force from hi + lo pairs of w * dphi (split once per pattern) and of the stresses, which the block
+// splits itself into shared memory for the elements its threads cover (each stress value once).
+constexpr int kForceThreads = 128, kForceMaxStress = 6 * 24 * 8;  // up to 8 elements of 24 points
+__global__ void __launch_bounds__(kForceThreads) force3_mixed_kernel(const float2 *__restrict__ wg1,
+                                                                     const float2 *__restrict__ wg2,
+                                                                     const float2 *__restrict__ wg3,
+                                                                     const double *__restrict__ S,
+                                                                     const int32_t *__restrict__ elem_row, int n_rows,
+                                                                     int n_elem, int n_p, int n_q,
+                                                                     double *__restrict__ F) {
+    __shared__ float2 s_hl[kForceMaxStress];
     const int nld = 3 * n_p;
+    const long long t0 = (long long)blockIdx.x * kForceThreads;
+    const long long e_first = t0 / nld;
+    long long e_last = (t0 + kForceThreads - 1) / nld;
+    if (e_last >= n_elem) e_last = n_elem - 1;
+    const int n_vals = static_cast<int>(e_last - e_first + 1) * n_q * 6;  // <= kForceMaxStress (host check)
+    const double *Sb = S + e_first * n_q * 6;
+    for (int i = threadIdx.x; i < n_vals; i += kForceThreads) {
+        const df32 d = df_from_f64(Sb[i]);
+        s_hl[i] = make_float2(d.hi, d.lo);
+    }
+    __syncthreads();
+    const long long t = t0 + threadIdx.x;
     if (t >= (long long)n_elem * nld) return;
     const long long e = t / nld;
     const int alpha = static_cast<int>(t % nld);
@@ -117,13 +117,14 @@ __global__ void __launch_bounds__(128) force3_mixed_kernel(const float2 *__restr
     const int node = alpha / 3, comp = alpha % 3;
     // the stress components multiplying d/dx, d/dy, d/dz for this displacement component
     const int k0 = bt_row3(comp, 0), k1 = bt_row3(comp, 1), k2 = bt_row3(comp, 2);
+    const float2 *sl = s_hl + (e - e_first) * n_q * 6;
     CSum acc;
     for (int q = 0; q < n_q; ++q) {
         const long long g = e * n_q + q;
-        const float2 *s = S + 6 * g;
-        acc.add_prod(ld(wg1 + g * n_p + node), ld(s + k0));
-        acc.add_prod(ld(wg2 + g * n_p + node), ld(s + k1));
-        acc.add_prod(ld(wg3 + g * n_p + node), ld(s + k2));
+        const float2 *sq = sl + 6 * q;
+        acc.add_prod(ld(wg1 + g * n_p + node), ld(sq + k0));
+        acc.add_prod(ld(wg2 + g * n_p + node), ld(sq + k1));
+        acc.add_prod(ld(wg3 + g * n_p + node), ld(sq + k2));
     }
     red_add(F + row, acc.value());
 }
@@ -158,19 +159,20 @@ int ssp_assemble_overlap_strain_3d_mixed(const float *dphi1_hl, const float *dph
 }
 
 int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2_hl, const float *wdphi3_hl,
-                                     const float *stress_hl, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                     const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                      int n_rows, double *out_values, void *stream) {
     if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    // a block's threads cover at most 128 / (3 n_p) + 2 elements, whose stresses it stages
+    if ((kForceThreads / (3 * n_p) + 2) * n_q * 6 > kForceMaxStress) return SSP_ERR_UNSUPPORTED;
     if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
     cudaStream_t st = as_stream(stream);
     if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
     if (n_elem == 0) return SSP_OK;
-    if (!wdphi1_hl || !wdphi2_hl || !wdphi3_hl || !stress_hl || !elem_row) return SSP_ERR_INVALID;
+    if (!wdphi1_hl || !wdphi2_hl || !wdphi3_hl || !stress || !elem_row) return SSP_ERR_INVALID;
     const long long n = (long long)n_elem * 3 * n_p;
-    force3_mixed_kernel<<<grid_for(n, 128), 128, 0, st>>>(
+    force3_mixed_kernel<<<grid_for(n, kForceThreads), kForceThreads, 0, st>>>(
         reinterpret_cast<const float2 *>(wdphi1_hl), reinterpret_cast<const float2 *>(wdphi2_hl),
-        reinterpret_cast<const float2 *>(wdphi3_hl), reinterpret_cast<const float2 *>(stress_hl), elem_row, n_rows,
-        n_elem, n_p, n_q, out_values);
+        reinterpret_cast<const float2 *>(wdphi3_hl), stress, elem_row, n_rows, n_elem, n_p, n_q, out_values);
     return launch_status();
 }
 

@@ -214,7 +214,140 @@ __device__ __forceinline__ void elastic_trial(const double *E, double *t, double
     I1 = t[0] + t[1] + t[2];
 }
 
-// Stress and (when DS != null) consistent tangent of the decided branch.
+// ---- consistent tangent of the plastic branches in double-float arithmetic (the mixed form)
+//
+// The FP64 formulas below (finish3) are regrouped per point into FP64 coefficients, and each DS
+// entry becomes a short sum of products of per-point vectors, accumulated compensated on the FP32
+// pipe (CSum, about 2^-48 of the sum of |terms|) and widened once.  Smooth face, with
+// a_k = s_k inv_k, A = sum_k a_k, B = sum_k a_k em_k:
+//   DS_ij = A J_ij - I_ij B + sum_k (K_k P_k,i) P_k,j + lambda iota_i iota_j - (Dp_i / den) Dp_j,
+//   K_1 = 2G - (a1 c1a + a2 c2b + a3 c3b), K_2 = 2G - (a1 c1b + a2 c2a - a3 c3b),
+//   K_3 = 2G + (a1 c1b + a2 c2b - a3 c3a);
+// edges (left: Q = P12, R = P3, e = e3, em = e1 + e2, a = (s3 - s1) inv3; right: Q = P23, R = P1,
+// e = e1, em = e2 + e3, a = (s1 - s3) inv1):
+//   DS_ij = a J_ij - I_ij a em - a (Q_i t_j + t_i Q_j) + (a em + G) Q_i Q_j
+//           + (a (em - 2e) + 2G) R_i R_j + a e (Q_i R_j + R_i Q_j) + lambda iota_i iota_j - (Dp_i / den) Dp_j,
+// with J = d(t t)/dE (square_jac) and I_ij = half_ident(i) on the diagonal.  The inverse gaps make
+// the terms larger than the result by about (|e| / gap)^2, so a point whose smallest eigenvalue
+// gap is below 1e-3 of max|e|, or whose coefficients leave the float range, keeps the FP64 loop.
+__device__ __forceinline__ df32 df_pow2(df32 a, float f) { return {a.hi * f, a.lo * f}; }  // f a power of two
+
+// acc += A * d(t t)_ij / dE_j (square_jac's entries)
+__device__ __forceinline__ void add_square_jac(CSum &acc, df32 A, const df32 *t, int i, int j) {
+    const df32 A2 = df_pow2(A, 2.0f), Ah = df_pow2(A, 0.5f);
+    switch (i * 6 + j) {
+        case 0: acc.add_prod(A2, t[0]); break;
+        case 3: case 9: acc.add_prod(A, t[3]); break;
+        case 5: case 17: acc.add_prod(A, t[5]); break;
+        case 7: acc.add_prod(A2, t[1]); break;
+        case 10: case 16: acc.add_prod(A, t[4]); break;
+        case 14: acc.add_prod(A2, t[2]); break;
+        case 21: acc.add_prod(Ah, t[0]); acc.add_prod(Ah, t[1]); break;
+        case 22: acc.add_prod(Ah, t[5]); break;
+        case 23: acc.add_prod(Ah, t[4]); break;
+        case 28: acc.add_prod(Ah, t[1]); acc.add_prod(Ah, t[2]); break;
+        case 29: acc.add_prod(Ah, t[3]); break;
+        case 35: acc.add_prod(Ah, t[0]); acc.add_prod(Ah, t[2]); break;
+        default: break;
+    }
+}
+__device__ __forceinline__ bool in_float_range(double x) { return fabs(x) <= 1e30; }  // false for nan
+
+__device__ __forceinline__ bool smooth_ds_compensated(const Principal3 &p, const Mat3 &m, const double *P1,
+                                                      const double *P2, const double *P3, double inv1, double inv2,
+                                                      double inv3, double s1, double s2, double s3, const double *Dp,
+                                                      double inv_den, double *DS) {
+    const double e1 = p.e1, e2 = p.e2, e3 = p.e3;
+    if (!(fmin(e1 - e2, e2 - e3) >= 1e-3 * fmax(fabs(e1), fabs(e3)))) return false;
+    const double a1 = s1 * inv1, a2 = s2 * inv2, a3 = s3 * inv3;
+    const double c1a = 2.0 * e1 - e2 - e3, c1b = e2 - e3;
+    const double c2a = 2.0 * e2 - e1 - e3, c2b = e1 - e3;
+    const double c3a = 2.0 * e3 - e1 - e2, c3b = e1 - e2;
+    const double A = a1 + a2 + a3, B = a1 * (e2 + e3) + a2 * (e1 + e3) + a3 * (e1 + e2);
+    const double G2 = 2.0 * m.shear;
+    const double K1 = G2 - (a1 * c1a + a2 * c2b + a3 * c3b);
+    const double K2 = G2 - (a1 * c1b + a2 * c2a - a3 * c3b);
+    const double K3 = G2 + (a1 * c1b + a2 * c2b - a3 * c3a);
+    if (!(in_float_range(A) && in_float_range(B) && in_float_range(K1) && in_float_range(K2) && in_float_range(K3)))
+        return false;
+    df32 t[6], r1[6], r2[6], r3[6], q1[6], q2[6], q3[6], dp[6], dq[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        t[i] = df_from_f64(p.t[i]);
+        r1[i] = df_from_f64(P1[i]);
+        r2[i] = df_from_f64(P2[i]);
+        r3[i] = df_from_f64(P3[i]);
+        q1[i] = df_from_f64(K1 * P1[i]);
+        q2[i] = df_from_f64(K2 * P2[i]);
+        q3[i] = df_from_f64(K3 * P3[i]);
+        dp[i] = df_from_f64(Dp[i]);
+        dq[i] = df_from_f64(-Dp[i] * inv_den);
+    }
+    const df32 Ad = df_from_f64(A), Bd = df_from_f64(B), Ld = df_from_f64(m.lame);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+            CSum acc;
+            add_square_jac(acc, Ad, t, i, j);
+            if (i == j) acc.add(df_pow2(Bd, i < 3 ? -1.0f : -0.5f));
+            acc.add_prod(q1[i], r1[j]);
+            acc.add_prod(q2[i], r2[j]);
+            acc.add_prod(q3[i], r3[j]);
+            if (j < 3) acc.add(Ld);
+            acc.add_prod(dq[i], dp[j]);
+            store_sym(DS, i, j, acc.value());
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool edge_ds_compensated(const Principal3 &p, const Mat3 &m, const double *Q,
+                                                    const double *R, double a, double em, double e, double gap,
+                                                    const double *Dp, double inv_den, double *DS) {
+    if (!(gap >= 1e-3 * fmax(fabs(p.e1), fabs(p.e3)))) return false;
+    const double kQ = a * em + m.shear, kR = a * (em - 2.0 * e) + 2.0 * m.shear, ae = a * e, aem = a * em;
+    if (!(in_float_range(a) && in_float_range(kQ) && in_float_range(kR) && in_float_range(ae) && in_float_range(aem)))
+        return false;
+    df32 t[6], qd[6], rd[6], aq[6], kqq[6], krr[6], aeq[6], dp[6], dq[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        t[i] = df_from_f64(p.t[i]);
+        qd[i] = df_from_f64(Q[i]);
+        rd[i] = df_from_f64(R[i]);
+        aq[i] = df_from_f64(-a * Q[i]);
+        kqq[i] = df_from_f64(kQ * Q[i]);
+        krr[i] = df_from_f64(kR * R[i]);
+        aeq[i] = df_from_f64(ae * Q[i]);
+        dp[i] = df_from_f64(Dp[i]);
+        dq[i] = df_from_f64(-Dp[i] * inv_den);
+    }
+    const df32 ad = df_from_f64(a), aemd = df_from_f64(aem), Ld = df_from_f64(m.lame);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+            CSum acc;
+            add_square_jac(acc, ad, t, i, j);
+            if (i == j) acc.add(df_pow2(aemd, i < 3 ? -1.0f : -0.5f));
+            acc.add_prod(aq[i], t[j]);
+            acc.add_prod(t[i], aq[j]);
+            acc.add_prod(kqq[i], qd[j]);
+            acc.add_prod(krr[i], rd[j]);
+            acc.add_prod(aeq[i], rd[j]);
+            acc.add_prod(rd[i], aeq[j]);
+            if (j < 3) acc.add(Ld);
+            acc.add_prod(dq[i], dp[j]);
+            store_sym(DS, i, j, acc.value());
+        }
+    }
+    return true;
+}
+
+// Stress and (when DS != null) consistent tangent of the decided branch.  COMP: the plastic
+// branches' DS in double-float arithmetic where the point allows it (S is always FP64 and the
+// same as without COMP).
+template <bool COMP>
 __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, double *S, double *DS) {
     const double sp = m.sin_phi, sin_phi = m.sin_phi, shear = m.shear, lame = m.lame;
     const double e1 = p.e1, e2 = p.e2, e3 = p.e3, I1 = p.I1;
@@ -241,11 +374,14 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
 #pragma unroll
             for (int i = 0; i < 6; ++i)
                 Dp[i] = 2.0 * shear * ((1.0 + sin_phi) * P1[i] - (1.0 - sin_phi) * P3[i]) + 2.0 * lame * sin_phi * vol_iota(i);
+            const double inv_den = 1.0 / d.den;
+            if constexpr (COMP) {
+                if (smooth_ds_compensated(p, m, P1, P2, P3, inv1, inv2, inv3, s1, s2, s3, Dp, inv_den, DS)) return;
+            }
             const double em23 = e2 + e3, em13 = e1 + e3, em12 = e1 + e2;
             const double c1a = 2.0 * e1 - e2 - e3, c1b = e2 - e3;
             const double c2a = 2.0 * e2 - e1 - e3, c2b = e1 - e3;
             const double c3a = 2.0 * e3 - e1 - e2, c3b = e1 - e2;
-            const double inv_den = 1.0 / d.den;
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -282,6 +418,9 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
                 Dp[i] = shear * ((1.0 + sin_phi) * P12[i] - 2.0 * (1.0 - sin_phi) * P3[i]) + 2.0 * lame * sin_phi * vol_iota(i);
             const double em12 = e1 + e2;
             const double inv_den = 1.0 / d.den;
+            if constexpr (COMP) {
+                if (edge_ds_compensated(p, m, P12, P3, (s3 - s1) * inv3, em12, e3, e2 - e3, Dp, inv_den, DS)) return;
+            }
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -316,6 +455,9 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
                 Dp[i] = shear * (2.0 * (1.0 + sin_phi) * P1[i] - (1.0 - sin_phi) * P23[i]) + 2.0 * lame * sin_phi * vol_iota(i);
             const double em23 = e2 + e3;
             const double inv_den = 1.0 / d.den;
+            if constexpr (COMP) {
+                if (edge_ds_compensated(p, m, P23, P1, (s1 - s3) * inv1, em23, e1, e1 - e2, Dp, inv_den, DS)) return;
+            }
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
 #pragma unroll
@@ -356,7 +498,7 @@ __device__ int mc3d_point(const double *E, double c_bar, double sin_phi, double 
     Principal3 p;
     principal3(E, p);
     const Decision3 d = decide3(p, m);
-    finish3(p, d, m, S, DS);
+    finish3<false>(p, d, m, S, DS);
     return d.branch;
 }
 
@@ -538,9 +680,11 @@ __global__ void __launch_bounds__(128) mc3d_decide_kernel(const double *__restri
                                                           const double *__restrict__ shear,
                                                           const double *__restrict__ lame, int n,
                                                           double *__restrict__ S, double *__restrict__ DS,
-                                                          int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
-    const int cnt = scratch[0];
-    const int32_t *L = scratch + 4;
+                                                          int8_t *__restrict__ branch, int32_t *__restrict__ scratch,
+                                                          const int32_t *__restrict__ lists,
+                                                          const int32_t *__restrict__ counts, long long list_stride) {
+    const int cnt = counts[blockIdx.y];
+    const int32_t *L = lists + blockIdx.y * list_stride;
     int32_t *smooth = scratch + 4 + n, *edges = scratch + 4 + 2ll * n;
     const int stride = gridDim.x * blockDim.x;
     // whole warps iterate together (the appends are warp-collective)
@@ -566,7 +710,7 @@ __global__ void __launch_bounds__(128) mc3d_decide_kernel(const double *__restri
             branch[p] = static_cast<int8_t>(b);
             if (b == kElastic || b == kApex) {
                 double s[6], ds[36];
-                finish3(pr, d, m, s, ds);
+                finish3<false>(pr, d, m, s, ds);
                 store6(S, p, s);
                 store36(DS, p, ds);
             } else {
@@ -582,7 +726,9 @@ __global__ void __launch_bounds__(128) mc3d_decide_kernel(const double *__restri
     }
 }
 
-__global__ void __launch_bounds__(128) mc3d_finish_kernel(const double *__restrict__ c_bar,
+// three CTAs per SM (168 registers): the lists are short and each point a long dependent chain
+template <bool COMP>
+__global__ void __launch_bounds__(128, 3) mc3d_finish_kernel(const double *__restrict__ c_bar,
                                                           const double *__restrict__ sin_phi,
                                                           const double *__restrict__ shear,
                                                           const double *__restrict__ lame, int n,
@@ -602,30 +748,54 @@ __global__ void __launch_bounds__(128) mc3d_finish_kernel(const double *__restri
         load_record(DS, p, pr, d);
         const Mat3 m{c_bar[p], sin_phi[p], shear[p], lame[p]};
         double s[6], ds[36];
-        finish3(pr, d, m, s, ds);
+        finish3<COMP>(pr, d, m, s, ds);
         store6(S, p, s);
         store36(DS, p, ds);
     }
 }
 
-// The three passes on one stream.  scratch: 4 + 3 n int32.
-int launch_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+}  // namespace
+
+// Pass A on one stream (counters zeroed first).  scratch: 4 + 3 n int32.
+int binned_screen(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
                   cudaStream_t st) {
     if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
     mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
                                                           branch_out, scratch);
+    return launch_status();
+}
+
+// Passes B (over n_lists point lists, blockIdx.y = list) and C.
+int binned_decide_finish(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                         const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                         int32_t *scratch, const int32_t *lists, const int32_t *counts, int n_lists,
+                         long long list_stride, bool compensated_ds, cudaStream_t st) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     long long gx = (long long)sms * 8;
     const long long need = (n_int + 127) / 128;
     if (gx > need) gx = need;
-    mc3d_decide_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                                   branch_out, scratch);
-    mc3d_finish_kernel<<<dim3(static_cast<unsigned>(gx), 3), 128, 0, st>>>(c_bar, sin_phi, shear, lame, n_int, S_out,
-                                                                           DS_out, scratch);
+    mc3d_decide_kernel<<<dim3(static_cast<unsigned>(gx), n_lists), 128, 0, st>>>(
+        E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, lists, counts, list_stride);
+    const dim3 grid(static_cast<unsigned>(gx), 3);
+    if (compensated_ds)
+        mc3d_finish_kernel<true><<<grid, 128, 0, st>>>(c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, scratch);
+    else
+        mc3d_finish_kernel<false><<<grid, 128, 0, st>>>(c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, scratch);
     return launch_status();
+}
+
+namespace {
+
+int launch_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                  const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                  bool compensated_ds, cudaStream_t st) {
+    const int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+    if (rc != SSP_OK) return rc;
+    return binned_decide_finish(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                                scratch + 4, scratch, 1, 0, compensated_ds, st);
 }
 
 // ---------------------------------------------------------------------------- 2D
@@ -863,83 +1033,7 @@ int32_t *fixed_scratch_for_current_device() {
     return g_fixed_ptr[dev];
 }
 
-// The exact return mapping over lists of points (the learned proposal's bins, blockIdx.y = list;
-// scratch = counters at scratch[list], lists of n entries from scratch + 8).  Each warp takes 32
-// consecutive list entries, runs the exact return mapping lane by lane, stages
-// the results in shared memory and writes them back row by row, the whole warp on one point's
-// 288-byte DS row at a time (full-line stores instead of 32 strided rows).
-constexpr int kRowStride = 37;
-__global__ void __launch_bounds__(128) exact_over_bins_kernel(const double *__restrict__ E,
-                                                              const double *__restrict__ c_bar,
-                                                              const double *__restrict__ sin_phi,
-                                                              const double *__restrict__ shear,
-                                                              const double *__restrict__ lame, int n,
-                                                              double *__restrict__ S, double *__restrict__ DS,
-                                                              int8_t *__restrict__ branch,
-                                                              const int32_t *__restrict__ scratch) {
-    __shared__ double sds[4][32 * kRowStride];
-    __shared__ double ss[4][32 * 7];
-    __shared__ int sp[4][32];
-    const int k = blockIdx.y;
-    const int cnt = scratch[k];
-    const int32_t *list = scratch + 8 + (long long)k * n;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *wd = sds[warp], *ws = ss[warp];
-    int *wp = sp[warp];
-    for (long long base = ((long long)blockIdx.x * 4 + warp) * 32; base < cnt; base += (long long)gridDim.x * 128) {
-        const long long i = base + lane;
-        int p = i < cnt ? list[i] : -1;
-        if (i < cnt && (p < 0 || p >= n)) {
-            flag(SSP_DEV_BAD_INDEX);
-            p = -1;
-        }
-        if (p >= 0) {
-            double e[6], s[6], ds[36];
-#pragma unroll
-            for (int j = 0; j < 6; ++j) e[j] = E[6ll * p + j];
-            const int b = mc3d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds);
-            branch[p] = static_cast<int8_t>(b);
-#pragma unroll
-            for (int j = 0; j < 36; ++j) wd[lane * kRowStride + j] = ds[j];
-#pragma unroll
-            for (int j = 0; j < 6; ++j) ws[lane * 7 + j] = s[j];
-        }
-        wp[lane] = p;
-        __syncwarp();
-        for (int r = 0; r < 32; ++r) {
-            const int pr = wp[r];
-            if (pr < 0) continue;  // warp-uniform
-            double *row = DS + 36ll * pr;
-            row[lane] = wd[r * kRowStride + lane];
-            if (lane < 4) row[32 + lane] = wd[r * kRowStride + 32 + lane];
-        }
-#pragma unroll
-        for (int it = 0; it < 6; ++it) {
-            const int idx = it * 32 + lane, r = idx / 6, j = idx - 6 * (idx / 6);
-            const int pr = wp[r];
-            if (pr >= 0) S[6ll * pr + j] = ws[r * 7 + j];
-        }
-        __syncwarp();
-    }
-}
-
 }  // namespace
-
-
-int exact_over_bins(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
-                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
-                    const int32_t *scratch, int n_lists, cudaStream_t st) {
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long gx = (long long)sms * 8;
-    const long long need = (n_int + 127) / 128;
-    if (gx > need) gx = need;
-    exact_over_bins_kernel<<<dim3(static_cast<unsigned>(gx), n_lists), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame,
-                                                                                       n_int, S_out, DS_out, branch_out,
-                                                                                       scratch);
-    return launch_status();
-}
 
 }  // namespace ssp
 
@@ -987,7 +1081,20 @@ int ssp_constitutive_3d_sds_binned(const double *E, const double *c_bar, const d
     if (n_int == 0) return SSP_OK;
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
         return SSP_ERR_INVALID;
-    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, false,
+                         as_stream(stream));
+}
+
+// The binned return mapping of the mixed-precision form: branches, multipliers and S in FP64 as
+// above, the plastic points' DS in double-float arithmetic.
+int ssp_constitutive_3d_sds_binned_mixed(const double *E, const double *c_bar, const double *sin_phi,
+                                         const double *shear, const double *lame, int n_int, double *S_out,
+                                         double *DS_out, int8_t *branch_out, int32_t *scratch, void *stream) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+        return SSP_ERR_INVALID;
+    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, true,
                          as_stream(stream));
 }
 
@@ -1006,7 +1113,7 @@ int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar,
     if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out) return SSP_ERR_INVALID;
     int32_t *scratch = fixed_scratch_for_current_device();
     if (!scratch) return SSP_ERR_CUDA;
-    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+    return launch_binned(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, false,
                          as_stream(stream));
 }
 

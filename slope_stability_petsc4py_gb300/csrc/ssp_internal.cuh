@@ -52,11 +52,20 @@ __host__ __device__ __forceinline__ int bt_row2(int comp, int grad) {
     return static_cast<int>((0x1220u >> (4 * (comp * 2 + grad))) & 0xFu);
 }
 
-// The exact 3D return mapping over n_lists point lists (constitutive.cu); scratch holds the list
-// sizes at scratch[0 .. n_lists) and the lists of n_int entries from scratch + 8.
-int exact_over_bins(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
-                    const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
-                    const int32_t *scratch, int n_lists, cudaStream_t st);
+// The binned 3D return mapping (constitutive.cu).  scratch: counters at scratch[0..3] (listed,
+// smooth, left edge, right edge), the listed points from scratch + 4, the smooth list from
+// scratch + 4 + n_int, the edge lists from scratch + 4 + 2 n_int.
+// Pass A: zero the counters, screen every point, finish the screened ones, list the others.
+int binned_screen(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                  const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                  cudaStream_t st);
+// Passes B and C: decide the points of n_lists lists (list k: counts[k] entries from
+// lists + k list_stride), finish elastic and apex points, record and list the others by branch,
+// finish those (compensated_ds: the plastic DS in double-float arithmetic).
+int binned_decide_finish(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                         const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                         int32_t *scratch, const int32_t *lists, const int32_t *counts, int n_lists,
+                         long long list_stride, bool compensated_ds, cudaStream_t st);
 
 // Mixed-precision plastic-correction tangent of 3D P4 elements on the tensor cores (tangent_tc.cu).
 int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
@@ -158,5 +167,25 @@ __device__ __forceinline__ double f32_widen(float f) {
 }
 // hi + lo as one double (one FP64 add).
 __device__ __forceinline__ double df_to_f64(df32 a) { return f32_widen(a.hi) + f32_widen(a.lo); }
+
+// Compensated accumulator: value = s + c, s accumulates the leading parts with TwoSum, c the
+// rounding errors and the low-order product terms (about 2^-48 of the sum of |terms|).
+struct CSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add_prod(df32 x, df32 y) {
+        const float p = __fmul_rn(x.hi, y.hi);
+        float e = __fmaf_rn(x.hi, y.hi, -p);
+        e = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, e));
+        const df32 t = df_two_sum(s, p);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
+    __device__ __forceinline__ void add(df32 x) {
+        const df32 t = df_two_sum(s, x.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, x.lo));
+    }
+    __device__ __forceinline__ double value() const { return df_to_f64(df_fast_two_sum(s, c)); }
+};
 
 }  // namespace ssp

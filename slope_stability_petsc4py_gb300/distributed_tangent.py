@@ -465,9 +465,8 @@ def owned_force_device(pattern, S_aos, *, mixed: bool = False):
     F = t.empty(n_rows, dtype=t.float64, device="cuda")
     if mixed and pattern.dim == 3:
         d = _mixed_inputs(pattern)
-        s_hl = _split_pairs(S_aos)
         _lib.call("ssp_assemble_force_element_mixed", _lib.ptr(d["wdphi1_hl"]), _lib.ptr(d["wdphi2_hl"]),
-                  _lib.ptr(d["wdphi3_hl"]), _lib.ptr(s_hl), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
+                  _lib.ptr(d["wdphi3_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
                   pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
         return F
     _lib.call("ssp_assemble_force_element", pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),

@@ -2,13 +2,14 @@
 
 The reference decides every point's return branch inside one divergent kernel
 (``src/slope_stability/cython/constitutive_3D_kernel.h:116-350``).  Here a 6 -> 32 -> 32 -> 5
-ReLU network proposes the branch from cheap FP32 invariants of the trial strain; points are
-binned by the proposal and the exact FP64 return mapping runs bin by bin, so each warp mostly
-executes one branch.  The exact kernel still decides and computes every result: a wrong
-proposal costs time, never accuracy.
+ReLU network proposes the branch from cheap FP32 invariants of the trial strain for the points
+that the binned return mapping's FP32 elastic screen cannot settle (near or past the yield
+surface); those points are binned by the proposal and the exact FP64 decision pass runs bin by
+bin, so each warp mostly follows one branch's checks.  The exact kernels still decide and compute
+every result: a wrong proposal costs time, never accuracy.
 
-Training data are (features, branch) pairs emitted by the exact return mapping on a sequence of
-continuation states (``collect_training_data``).  Training runs on the GPU through the library's
+Training data are (features, branch) pairs of the screen-listed points, emitted by the exact
+return mapping on a sequence of continuation states (``collect_training_data``).  Training runs on the GPU through the library's
 own kernels: ``ssp_mlp_loss_grad`` (forward and backward of a batch), ``ssp_mlp_adam``.
 """
 
@@ -58,8 +59,24 @@ def exact_branches(E, c_bar, sin_phi, shear, lame):
     return br
 
 
-def collect_training_data(op, states):
-    """(features, labels) from the exact return mapping over continuation states [(lam, U), ...]."""
+def screen_listed(E, c_bar, sin_phi, shear, lame):
+    """(indices of the points the binned return mapping's FP32 elastic screen cannot settle, branch
+    codes of all points), from one ssp_constitutive_3d_sds_binned call."""
+    t = _lib.require_cuda()
+    n = int(E.shape[0])
+    S = t.empty((n, 6), dtype=t.float64, device="cuda")
+    DS = t.empty((n, 36), dtype=t.float64, device="cuda")
+    br = t.empty(n, dtype=t.int8, device="cuda")
+    scratch = t.empty(3 * n + 4, dtype=t.int32, device="cuda")
+    _lib.call("ssp_constitutive_3d_sds_binned", _lib.ptr(E), _lib.ptr(c_bar), _lib.ptr(sin_phi), _lib.ptr(shear),
+              _lib.ptr(lame), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch), _lib.stream_handle())
+    return scratch[4: 4 + int(scratch[0])].long(), br
+
+
+def collect_training_data(op, states, listed_only: bool = True):
+    """(features, labels) from the exact return mapping over continuation states [(lam, U), ...].
+    With listed_only, only the points the elastic screen lists: the ones the learned return
+    mapping asks the network about."""
     t = _lib.require_cuda()
     pat = op.owned_tangent_pattern
     Xs, ys = [], []
@@ -68,8 +85,14 @@ def collect_training_data(op, states):
         E = overlap_strain_device(pat, U)
         d = op._dev
         args = (E, op._owned_overlap_c_bar, op._owned_overlap_sin_phi, d["shear"], d["lame"])
-        Xs.append(features(*args))
-        ys.append(exact_branches(*args))
+        X = features(*args)
+        if listed_only:
+            listed, br = screen_listed(*args)
+            Xs.append(X.index_select(0, listed))
+            ys.append(br.index_select(0, listed))
+        else:
+            Xs.append(X)
+            ys.append(exact_branches(*args))
     return t.cat(Xs), t.cat(ys)
 
 
@@ -134,6 +157,17 @@ class BranchProposal:
 
     def state(self) -> np.ndarray:
         return self.params.cpu().numpy().copy()
+
+
+def proposal_bins(scratch, n: int):
+    """The learned return mapping's point lists, read from its scratch after a call on n points:
+    the points the elastic screen listed (in point order) and the five bins of proposed branches
+    over them (layout of ``ssp_constitutive_3d_sds_learned``)."""
+    listed = scratch[4: 4 + int(scratch[0])].long()
+    cnt = scratch[4 + 3 * n: 9 + 3 * n].cpu().numpy()
+    base = 12 + 3 * n
+    bins = [scratch[base + k * n: base + k * n + int(cnt[k])].long() for k in range(5)]
+    return listed, bins
 
 
 def warp_branch_mix(branches, order=None) -> float:

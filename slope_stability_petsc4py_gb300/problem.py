@@ -162,6 +162,10 @@ class ConstitutiveOperator:
         self._K_el = None  # elastic tangent CSR values (device), built on first use
         self._blend_base = None  # (r, (1-r) K_el,t + r K_el) for the last regularisation factor
         self._dev = None
+        # composite regularised builds copy the tangent's starting values on a second stream while
+        # the strain and return mapping run (_stage_values); (key, values, event) of that copy
+        self.stage_values = True
+        self._staged_values = None
         # How 3D tangents are evaluated (all give the same results): "binned" -- two passes with
         # exact branch binning; "unsorted" -- one pass in point order; "learned" -- points binned
         # by the branch_model's proposal, then the exact return mapping bin by bin.
@@ -174,6 +178,9 @@ class ConstitutiveOperator:
         # force in compensated double-float arithmetic (~1e-13); the return mapping and every CSR /
         # force accumulation stay FP64 (about 1e-7 relative tangent error)
         self.tangent_form = "plain"
+        # composite builds with device outputs run the force concurrently with the tangent
+        self.concurrent_force = True
+        self._force_stream = None
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
         self._red_key = None
@@ -217,6 +224,7 @@ class ConstitutiveOperator:
         self._dev = None
         self._K_el = None
         self._blend_base = None
+        self._staged_values = None
         self._red_key = None
         self._clear_owned_local_cache()
         if pattern is not None:
@@ -347,18 +355,20 @@ class ConstitutiveOperator:
         mode = self.return_mapping if pat.dim == 3 else "unsorted"
         if tangent and mode in ("binned", "learned"):
             branch = t.empty(n, dtype=t.int8, device="cuda")
-            need = (5 if mode == "learned" else 3) * n + 8
+            need = (8 if mode == "learned" else 3) * n + 12
             if self._scratch is None or self._scratch.numel() < need:
                 self._scratch = t.empty(need, dtype=t.int32, device="cuda")
             mat = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                    _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(branch),
                    _lib.ptr(self._scratch), st)
+            # the mixed form: the plastic points' DS in double-float arithmetic (S, branches FP64)
+            sfx = "_mixed" if self.tangent_form == "mixed" else ""
             if mode == "learned":
                 if self.branch_model is None:
                     raise ValueError("return_mapping='learned' needs a trained branch_model")
-                _lib.call("ssp_constitutive_3d_sds_learned", _lib.ptr(self.branch_model.params), *mat)
+                _lib.call("ssp_constitutive_3d_sds_learned" + sfx, _lib.ptr(self.branch_model.params), *mat)
             else:
-                _lib.call("ssp_constitutive_3d_sds_binned", *mat)
+                _lib.call("ssp_constitutive_3d_sds_binned" + sfx, *mat)
         elif tangent:
             branch = t.empty(n, dtype=t.int8, device="cuda")
             _lib.call("ssp_constitutive_sds_branch", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
@@ -452,6 +462,54 @@ class ConstitutiveOperator:
             del blocks
         return self._K_el
 
+    def _regularized_start(self, r):
+        """(1-r) K_el,t + r K_el: it depends on r and the pattern only, so it is blended once per r
+        and each regularised build starts from a copy of it."""
+        pat = self._require_pattern()
+        base = self._elastic_tangent_values()
+        rr = float(r)
+        if self._blend_base is None or self._blend_base[0] != rr:
+            self._drain_staged()  # a staged copy may still read the old blend
+            buf = self._blend_base[1] if self._blend_base is not None else _lib.torch().empty_like(base)
+            _lib.call("ssp_blend_values", _lib.ptr(buf), _lib.ptr(base), _lib.ptr(pat.device["elastic_values"]), rr,
+                      pat.nnz, _lib.stream_handle())
+            self._blend_base = (rr, buf)
+        return self._blend_base[1]
+
+    def _drain_staged(self):
+        """Order the current stream after a staged copy that no build has waited for yet."""
+        staged, self._staged_values = self._staged_values, None
+        if staged is not None:
+            _lib.torch().cuda.current_stream().wait_event(staged[2])
+        return staged
+
+    def _stage_values(self, r):
+        """Issue the copy of the regularised tangent's starting values into its values array on the
+        second stream, ahead of the strain and return-mapping kernels that the build runs first:
+        the copy (nnz doubles read and written, HBM-bound) overlaps those FP64-bound kernels, and
+        the tangent assembly waits for it instead of copying."""
+        self._drain_staged()
+        if not self.stage_values or self.owned_tangent_pattern is None or \
+                self.owned_tangent_kernel not in ("rows", "legacy"):
+            return
+        t = _lib.require_cuda()
+        pat = self.owned_tangent_pattern
+        start = self._regularized_start(r)
+        if self._regularized_values is None:
+            self._regularized_values = t.empty(pat.nnz, dtype=t.float64, device="cuda")
+        values = self._regularized_values
+        if self._owned_regularized_mat is not None and hasattr(self._owned_regularized_mat, "fence"):
+            self._owned_regularized_mat.fence()  # the last host copy of these values has read them
+        main, side = t.cuda.current_stream(), self._aux_stream()
+        side.wait_stream(main)
+        with t.cuda.stream(side):
+            values.copy_(start)
+        values.record_stream(side)
+        start.record_stream(side)
+        done = t.cuda.Event()
+        done.record(side)
+        self._staged_values = (("regularized", float(r)), values, done)
+
     def _tangent_into(self, values, r=None):
         pat = self._require_pattern()
         if self._DS_aos is None:
@@ -467,19 +525,14 @@ class ConstitutiveOperator:
             # tangent = elastic tangent + plastic-point corrections (FP64 work on plastic points only)
             base = self._elastic_tangent_values()
             if r is None:
-                values.copy_(base)
-                scale = 1.0
+                start, key, scale = base, ("tangent",), 1.0
             else:
-                # (1-r) K_el,t + r K_el depends on r and the pattern only: blended once per r, then
-                # each build starts from a copy of it
-                rr = float(r)
-                if self._blend_base is None or self._blend_base[0] != rr:
-                    buf = self._blend_base[1] if self._blend_base is not None else _lib.torch().empty_like(base)
-                    _lib.call("ssp_blend_values", _lib.ptr(buf), _lib.ptr(base), _lib.ptr(d["elastic_values"]), rr,
-                              pat.nnz, st)
-                    self._blend_base = (rr, buf)
-                values.copy_(self._blend_base[1])
-                scale = 1.0 - rr
+                start, key, scale = self._regularized_start(r), ("regularized", float(r)), 1.0 - float(r)
+            staged = self._drain_staged()
+            if staged is None or staged[0] != key or staged[1] is not values:
+                values.copy_(start)
+            # else the copy of start, issued on the second stream ahead of the strain and return
+            # mapping (_stage_values), has overlapped them
             if ev is not None:
                 e0.record()
             entry = "ssp_tangent_plastic_correction"
@@ -628,29 +681,55 @@ class ConstitutiveOperator:
         self.constitutive_problem_stress_tangent(U)
         return self.build_F_free(), self._build_owned_tangent_matrix()
 
+    def _aux_stream(self):
+        if self._force_stream is None:
+            self._force_stream = _lib.torch().cuda.Stream()
+        return self._force_stream
+
     def _regularized_pair(self, F_fn, r):
-        # K first: its device -> host copy (the bulk of the hand-off) then overlaps the force
+        """(F, K_r) of one Newton iteration, the tangent first.  Device outputs: the internal force
+        runs on a second stream at the same time as the tangent and the caller's stream waits for
+        both.  Host outputs: both on the caller's stream, so the force runs while the tangent's
+        values are copied to the host (the copy, not the kernels, bounds that path)."""
         t0 = perf_counter()
-        K = self.build_K_regularized(r)
-        F = F_fn()
+        t = _lib.torch()
+        if self.host_outputs or not self.concurrent_force:
+            K = self.build_K_regularized(r)
+            F = F_fn()
+        else:
+            main = t.cuda.current_stream()
+            stress_ready = t.cuda.Event()
+            stress_ready.record(main)
+            K = self.build_K_regularized(r)
+            side = self._aux_stream()
+            side.wait_event(stress_ready)
+            with t.cuda.stream(side):
+                F = F_fn()
+            main.wait_stream(side)
+            if isinstance(F, t.Tensor):
+                F.record_stream(main)
         self.time_build_F_K_tangent.append(perf_counter() - t0)
         return F, K
 
     def build_F_K_regularized_all(self, lam, U, r):
+        self._stage_values(r)
         self.reduction(lam)
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F, r)
 
     def build_F_K_regularized_all_free(self, lam, U, r):
+        self._stage_values(r)
         self.reduction(lam)
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F_free, r)
 
     def build_F_K_regularized_reduced(self, U, r):
+        self._stage_values(r)
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F, r)
 
     def build_F_K_regularized_reduced_free(self, U, r):
+        self._stage_values(r)
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F_free, r)
 
@@ -674,6 +753,7 @@ class ConstitutiveOperator:
         }
 
     def release_petsc_caches(self) -> None:
+        self._drain_staged()
         for attr in ("_owned_tangent_mat", "_owned_regularized_mat"):
             mat = getattr(self, attr, None)
             if mat is not None and hasattr(mat, "destroy"):
@@ -681,3 +761,4 @@ class ConstitutiveOperator:
             setattr(self, attr, None)
         self._tangent_values = None
         self._regularized_values = None
+        self._staged_values = None

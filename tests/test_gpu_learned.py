@@ -83,7 +83,7 @@ def _trained_model(op, mesh, mats):
         states.append((float(lam), synthetic.displacement_field(mesh, mats, amplitude=amp, seed=11 + k)))
     X, y = learned.collect_training_data(op, states)
     model = learned.BranchProposal(seed=0)
-    hist = model.train(X, y, epochs=6, batch=32768, lr=3e-3)
+    hist = model.train(X, y, epochs=8, batch=2048, lr=3e-3)
     return model, X, y, hist
 
 
@@ -115,19 +115,30 @@ def test_training_learns_the_branches_and_gains(cuda_device):
         op.reduction(1.25)
         op.constitutive_problem_stress_tangent(U)
         outs[mode] = (op._S_aos.clone(), op._DS_aos.clone(), op._branch.clone())
-    # the same FP64 return mapping compiled into two kernels: the same branches, results to a few ulps
+    # the single-pass kernel and the binned passes: the same branches, results to a few ulps
     assert torch.equal(outs["learned"][2], outs["unsorted"][2])
     assert rel_err(outs["learned"][0].cpu().numpy(), outs["unsorted"][0].cpu().numpy()) <= 1e-14
     assert rel_err(outs["learned"][1].cpu().numpy(), outs["unsorted"][1].cpu().numpy()) <= 1e-14
     assert rel_err(outs["binned"][1].cpu().numpy(), outs["unsorted"][1].cpu().numpy()) <= PLAIN_RTOL
+    # the learned path runs the binned path's per-point code in another order: bit-identical results
+    for a, b in zip(outs["learned"], outs["binned"]):
+        assert torch.equal(a, b)
 
     br = outs["unsorted"][2]
     n = br.numel()
     scratch = op._scratch
-    counts_l = scratch[:5].cpu().numpy()
-    order = torch.cat([scratch[8 + k * n: 8 + k * n + int(counts_l[k])] for k in range(5)]).long()
-    assert order.numel() == n
-    mix_natural = learned.warp_branch_mix(br)
+    # the screen's list (point order) and the five proposal bins over it
+    listed, bins = learned.proposal_bins(scratch, n)
+    counts_l = [b.numel() for b in bins]
+    order = torch.cat(bins)
+    assert order.numel() == listed.numel()
+    assert torch.equal(torch.sort(order).values, torch.sort(listed).values)
+    screened = torch.ones(n, dtype=torch.bool, device=br.device)
+    screened[listed] = False
+    assert (br[screened] == 0).all()
+    print(f"listed by the screen {listed.numel()} of {n}, bins {counts_l}")
+    mix_natural = learned.warp_branch_mix(br, listed)
     mix_learned = learned.warp_branch_mix(br, order)
-    print(f"distinct branches per warp: point order {mix_natural:.3f}, learned bins {mix_learned:.3f}")
+    print(f"distinct branches per warp over the listed points: screen order {mix_natural:.3f}, "
+          f"learned bins {mix_learned:.3f}")
     assert mix_learned < mix_natural

@@ -1,8 +1,9 @@
 """Mixed-precision tangent form: error against the FP64 form, per tangent and per Newton step.
 
-The mixed form keeps the return mapping (eigendecomposition, branch tests, plastic multipliers)
-and the CSR accumulation in FP64 and takes the plastic-point products B^T (w D B) in FP32 with an
-FP64-formed, hi/lo-split D B.  Tolerance of the spec mixed form: 1e-6 relative tangent error.
+The mixed form keeps the return mapping's eigendecomposition, branch tests, plastic multipliers
+and stresses and the CSR accumulation in FP64; it forms the plastic points' consistent tangent DS,
+the strain, the force and the plastic-point products B^T (w D B) in compensated FP32
+(double-float) arithmetic.  Tolerance of the spec mixed form: 1e-6 relative tangent error.
 """
 
 from __future__ import annotations
@@ -37,14 +38,17 @@ def test_mixed_tangent_error_bound(cuda_device, elem_type, dims, amp):
     mesh, mats, op = _operator(*dims, elem_type=elem_type)
     U = synthetic.displacement_field(mesh, mats, amplitude=amp, seed=4)
     op.reduction(1.1)
-    op.constitutive_problem_stress_tangent(U)
-    plastic = int((op._branch != 0).sum())
-    assert plastic > 0
+    plastic = None
     for r in (0.0, 0.3):
+        # each form runs its own return mapping (the mixed one forms the plastic DS compensated)
         op.tangent_form = "plain"
+        op.constitutive_problem_stress_tangent(U)
+        plastic = int((op._branch != 0).sum())
+        assert plastic > 0
         _, _, kp = op.build_K_regularized(r).getValuesCSR()
         kp = kp.copy()
         op.tangent_form = "mixed"
+        op.constitutive_problem_stress_tangent(U)
         _, _, km = op.build_K_regularized(r).getValuesCSR()
         err = rel_err(km, kp)
         print(f"{elem_type} r={r}: mixed tangent max-norm relative error {err:.3e} ({plastic} plastic points)")
@@ -98,3 +102,48 @@ def test_compensated_strain_and_force_match_fp64(cuda_device, elem_type, dims, a
     print(f"{elem_type}: strain error {err_e:.2e}, force error {err_f:.2e}")
     assert err_e <= 1e-11 and err_f <= 1e-11
     torch.cuda.synchronize()
+
+
+def test_compensated_plastic_ds_matches_fp64(cuda_device):
+    """ssp_constitutive_3d_sds_binned_mixed against the FP64 binned return mapping on random trial
+    strains over four orders of magnitude: the same branches, bitwise the same stresses, and the
+    plastic DS rows within 1e-10 of each row's size."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    rng = np.random.default_rng(17)
+    n = 400_000
+    E = rng.standard_normal((n, 6)) * np.repeat(np.array([1e-4, 1e-3, 3e-3, 1e-2]), n // 4)[:, None]
+    young = rng.uniform(1e4, 5e4, n)
+    nu = rng.uniform(0.2, 0.45, n)
+    shear = young / (2 * (1 + nu))
+    lame = young / (3 * (1 - 2 * nu)) - 2 * shear / 3
+    phi = np.deg2rad(rng.uniform(20.0, 40.0, n))
+    c_bar = 2 * rng.uniform(5.0, 30.0, n) * np.cos(phi)
+    sin_phi = np.sin(phi)
+    dev = [torch.as_tensor(np.ascontiguousarray(a), device="cuda") for a in (E, c_bar, sin_phi, shear, lame)]
+    out = {}
+    for entry in ("ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_binned_mixed"):
+        S = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+        DS = torch.empty((n, 36), dtype=torch.float64, device="cuda")
+        br = torch.empty(n, dtype=torch.int8, device="cuda")
+        scratch = torch.empty(3 * n + 4, dtype=torch.int32, device="cuda")
+        _lib.call(entry, *[_lib.ptr(a) for a in dev], n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br), _lib.ptr(scratch),
+                  _lib.stream_handle())
+        out[entry] = (S, DS, br)
+    _lib.raise_on_device_status()
+    S0, DS0, b0 = out["ssp_constitutive_3d_sds_binned"]
+    S1, DS1, b1 = out["ssp_constitutive_3d_sds_binned_mixed"]
+    assert torch.equal(b0, b1)
+    assert torch.equal(S0, S1)
+    counts = torch.bincount(b0.long(), minlength=5).cpu().numpy()
+    plastic = (b0 >= 1) & (b0 <= 3)
+    assert int(plastic.sum()) > 10_000
+    err = ((DS1 - DS0).abs().max(dim=1).values / DS0.abs().max(dim=1).values)[plastic]
+    same = (DS1 == DS0).all(dim=1)[plastic]
+    print(f"branches {counts.tolist()}; plastic DS rows: max rel err {float(err.max()):.3e}, "
+          f"median {float(err.median()):.3e}, FP64 fallback (bitwise equal) {float(same.float().mean()):.4f}")
+    assert float(err.max()) <= 1e-10
+    # the other rows are the FP64 path's own
+    assert torch.equal(DS1[~plastic], DS0[~plastic])
