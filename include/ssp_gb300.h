@@ -262,14 +262,27 @@ int ssp_finish_values(double *values, long long nnz, const int32_t *constrained_
 /* dst[i] = src[idx[i]] (owned free rows of a force vector, problem.py:1008-1015). */
 int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *stream);
 
-/* 1 if host_ptr is host memory that kernels can address with the same pointer (pinned and
- * device-mapped, as cudaHostAlloc / cudaMallocHost memory is under unified addressing), else 0. */
+/* 1 if host_ptr is pinned, device-mapped host memory (cudaHostAlloc / cudaMallocHost memory, or
+ * registered memory, under unified addressing) that kernels can store to, else 0.  The copy entry
+ * points below address it through its device mapping (cudaPointerGetAttributes). */
 int ssp_host_writable(const void *host_ptr);
 
 /* dst_host[0..n) = src[0..n) written by the SMs into pinned, device-mapped host memory
  * (ssp_host_writable(dst_host) must hold, else SSP_ERR_INVALID); asynchronous on the stream.
  * The operator's host hand-off of the CSR values; no reference counterpart. */
 int ssp_copy_out(const double *src, long long n, double *dst_host, void *stream);
+
+/* No counterpart in the reference.  row_mark[r] = 1 (not cleared first) for every owned row
+ * r = elem_row[e][a] (a < n_ld, r >= 0) of the elements e of elem_list[0 .. *elem_count): the rows
+ * a plastic correction of those elements writes. */
+int ssp_mark_element_rows(const int32_t *elem_row, int n_elem, int n_ld, const int32_t *elem_list,
+                          const int32_t *elem_count, int n_rows, uint8_t *row_mark, void *stream);
+
+/* No counterpart in the reference.  The CSR rows r with row_mark[r] != 0 of src (device) stored to
+ * the same positions of dst_host (pinned, device-mapped host memory: ssp_host_writable), by the SMs.
+ * Refreshes a host mirror of the tangent values whose other rows are known to be unchanged. */
+int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                      double *dst_host, void *stream);
 
 /* Reads the device status word (SSP_DEV_* bits); clear != 0 resets it.  Synchronous. */
 int ssp_device_status(int *status_out, int clear);

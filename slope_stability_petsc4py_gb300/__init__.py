@@ -17,7 +17,7 @@ from .distributed_tangent import (  # noqa: F401
     prepare_owned_tangent_pattern,
 )
 from .materials import MaterialSpec, heterogenous_materials  # noqa: F401
-from .problem import ConstitutiveOperator, OwnedCSRMatrix  # noqa: F401
+from .problem import CapturedBuild, ConstitutiveOperator, OwnedCSRMatrix  # noqa: F401
 from .reduction import reduction  # noqa: F401
 
 __version__ = "0.1.0"

@@ -734,6 +734,45 @@ __global__ void copy_out_kernel(const double *__restrict__ src, long long n, dou
     }
 }
 
+// row_mark[r] = 1 for every owned row r = elem_row[e][a] of the listed elements e.
+__global__ void mark_rows_kernel(const int32_t *__restrict__ elem_row, int n_elem, int n_ld,
+                                 const int32_t *__restrict__ list, const int32_t *__restrict__ count, int n_rows,
+                                 uint8_t *__restrict__ mark) {
+    const long long total = (long long)count[0] * n_ld;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long k = i / n_ld;
+        const int e = list[k];
+        if (e < 0 || e >= n_elem) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const int r = elem_row[(long long)e * n_ld + (i - k * n_ld)];
+        if (r < 0) continue;
+        if (r < n_rows) mark[r] = 1;
+        else flag(SSP_DEV_BAD_INDEX);
+    }
+}
+
+// The marked CSR rows of src stored to dst (device-mapped host memory), a warp per row: each store
+// instruction writes 256 contiguous bytes of one row over the host link; unmarked rows cost one
+// byte read.
+__global__ void copy_rows_out_kernel(const double *__restrict__ src, const int32_t *__restrict__ indptr,
+                                     const uint8_t *__restrict__ mark, int n_rows, long long nnz,
+                                     double *__restrict__ dst) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < n_rows; row += warps) {
+        if (!mark[row]) continue;
+        const long long b = indptr[row], e = indptr[row + 1];
+        if (b < 0 || e < b || e > nnz) {
+            if (lane == 0) flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        for (long long k = b + lane; k < e; k += 32) dst[k] = src[k];
+    }
+}
+
 __global__ void gather_rows_kernel(const double *__restrict__ src, const int32_t *__restrict__ idx, int n,
                                    double *__restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1004,25 +1043,60 @@ int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *
     return launch_status();
 }
 
-int ssp_host_writable(const void *host_ptr) {
-    if (!host_ptr) return 0;
+}  // extern "C"
+
+// The device address of pinned, device-mapped host memory (nullptr if the pointer is not such memory).
+static void *mapped_device_pointer(const void *host_ptr) {
+    if (!host_ptr) return nullptr;
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, host_ptr) != cudaSuccess) {
         cudaGetLastError();
-        return 0;
+        return nullptr;
     }
-    return at.type == cudaMemoryTypeHost && at.devicePointer == host_ptr ? 1 : 0;
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+extern "C" {
+
+int ssp_host_writable(const void *host_ptr) { return mapped_device_pointer(host_ptr) != nullptr ? 1 : 0; }
+
+int ssp_mark_element_rows(const int32_t *elem_row, int n_elem, int n_ld, const int32_t *elem_list,
+                          const int32_t *elem_count, int n_rows, uint8_t *row_mark, void *stream) {
+    if (n_elem < 0 || n_ld <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0 || n_rows == 0) return SSP_OK;
+    if (!elem_row || !elem_list || !elem_count || !row_mark) return SSP_ERR_INVALID;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    mark_rows_kernel<<<static_cast<unsigned>(sms * 4), 256, 0, as_stream(stream)>>>(elem_row, n_elem, n_ld, elem_list,
+                                                                                   elem_count, n_rows, row_mark);
+    return launch_status();
+}
+
+int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                      double *dst_host, void *stream) {
+    if (n_rows < 0 || nnz < 0) return SSP_ERR_INVALID;
+    if (n_rows == 0 || nnz == 0) return SSP_OK;
+    double *dst = static_cast<double *>(mapped_device_pointer(dst_host));
+    if (!src || !indptr || !row_mark || !dst) return SSP_ERR_INVALID;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
+                                                                                       nnz, dst);
+    return launch_status();
 }
 
 int ssp_copy_out(const double *src, long long n, double *dst_host, void *stream) {
     if (n < 0) return SSP_ERR_INVALID;
     if (n == 0) return SSP_OK;
-    if (!src || !dst_host || !ssp_host_writable(dst_host)) return SSP_ERR_INVALID;
+    double *dst = static_cast<double *>(mapped_device_pointer(dst_host));
+    if (!src || !dst) return SSP_ERR_INVALID;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst_host)) & 15u) == 0;
-    copy_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, n, dst_host, vec ? 1 : 0);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0;
+    copy_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, n, dst, vec ? 1 : 0);
     return launch_status();
 }
 

@@ -72,19 +72,41 @@ class OwnedCSRMatrix:
         self.data = self._host.numpy()
         self._copy_stream = t.cuda.Stream()
         self._copied = None  # event recorded after the last host copy
+        self._indptr_dev = t.as_tensor(self.indptr, device=values.device)  # for the row-wise refresh
+        # which build the host mirror holds: (start key, build number) or None (unknown)
+        self.mirror = None
         self.handle = OwnedCSRMatrix._next_handle
         OwnedCSRMatrix._next_handle += 1
 
-    def sync_host(self, stream=None):
+    def sync_host(self, stream=None, *, rows=None, mirror=None):
+        """Refresh the pinned host mirror from the device values on a side stream.  rows: a device
+        uint8 mark per CSR row; only the marked rows are stored (ssp_copy_rows_out), the caller
+        having established that the other rows equal the mirror already.  mirror: the state the
+        mirror holds afterwards."""
         t = _lib.torch()
         cur = t.cuda.current_stream()
         self._copy_stream.wait_stream(cur)
         with t.cuda.stream(self._copy_stream):
-            self._host.copy_(self.values, non_blocking=True)
+            if rows is not None:
+                _lib.call("ssp_copy_rows_out", _lib.ptr(self.values), _lib.ptr(self._indptr_dev), _lib.ptr(rows),
+                          int(self.shape[0]), int(self.values.numel()), self._host.data_ptr(),
+                          self._copy_stream.cuda_stream)
+            else:
+                self._host.copy_(self.values, non_blocking=True)
             self._copied = t.cuda.Event()
             self._copied.record(self._copy_stream)
         self.values.record_stream(self._copy_stream)
+        self.mirror = mirror
+        self._last_rows = rows
         return self
+
+    def host_copy_bytes(self) -> int:
+        """Bytes of CSR values the last sync_host moved to the host (synchronises)."""
+        rows = getattr(self, "_last_rows", None)
+        if rows is None:
+            return 8 * int(self.values.numel())
+        lengths = self._indptr_dev[1:] - self._indptr_dev[:-1]
+        return 8 * int((lengths * rows[: lengths.numel()].to(lengths.dtype)).sum().item())
 
     def fence(self):
         """Make the current stream wait until the last host copy has read the values."""
@@ -107,6 +129,34 @@ class OwnedCSRMatrix:
 
     def destroy(self):
         self.values = None
+
+
+class CapturedBuild:
+    """A composite Newton build recorded as a CUDA graph (ConstitutiveOperator.capture_regularized_build)."""
+
+    def __init__(self, graph, F, K, op):
+        self.graph, self.F, self.K, self._op = graph, F, K, op
+        # the graph addresses the operator's device buffers as they were at capture: hold them, so
+        # a later change of the operator's configuration cannot free memory the graph still writes
+        # (such a change needs a new capture to take effect)
+        t = _lib.torch()
+        keep, todo = [], [op.__dict__, getattr(op.owned_tangent_pattern, "device", {})]
+        while todo:
+            x = todo.pop()
+            if isinstance(x, t.Tensor):
+                keep.append(x)
+            elif isinstance(x, dict):
+                todo.extend(x.values())
+            elif isinstance(x, (list, tuple)):
+                todo.extend(x)
+            elif isinstance(x, OwnedCSRMatrix):
+                keep.append(x.values)
+        self._buffers = keep
+
+    def replay(self):
+        """Re-run the recorded kernels on the current contents of U; returns (F, K)."""
+        self.graph.replay()
+        return self.F, self.K
 
 
 @dataclass
@@ -166,6 +216,11 @@ class ConstitutiveOperator:
         # the strain and return mapping run (_stage_values); (key, values, event) of that copy
         self.stage_values = True
         self._staged_values = None
+        # host outputs: the pinned mirror of the values is refreshed row by row where the values
+        # can have changed since the previous build (_changed_rows), else copied in full
+        self.incremental_host_copy = True
+        self._last_build = {}
+        self._build_no = 0
         # How 3D tangents are evaluated (all give the same results): "binned" -- two passes with
         # exact branch binning; "unsorted" -- one pass in point order; "learned" -- points binned
         # by the branch_model's proposal, then the exact return mapping bin by bin.
@@ -225,6 +280,7 @@ class ConstitutiveOperator:
         self._K_el = None
         self._blend_base = None
         self._staged_values = None
+        self._last_build = {}
         self._red_key = None
         self._clear_owned_local_cache()
         if pattern is not None:
@@ -540,24 +596,36 @@ class ConstitutiveOperator:
                 entry = "ssp_tangent_plastic_correction_mixed"
             n_el = int(pat.overlap_elements.size)
             dv = self._dev
-            if "plastic_elems" not in dv:
+            kind = key[0]
+            lists = dv.setdefault("plastic_lists", {})
+            if kind not in lists:
                 t = _lib.torch()
-                dv["plastic_elems"] = t.empty(max(n_el, 1), dtype=t.int32, device="cuda")
-                dv["plastic_count"] = t.empty(1, dtype=t.int32, device="cuda")
+                lists[kind] = [(t.empty(max(n_el, 1), dtype=t.int32, device="cuda"),
+                                t.empty(1, dtype=t.int32, device="cuda")) for _ in range(2)]
+            # two plastic-element lists per kind, alternating: the previous build's list stays
+            # valid for the incremental host refresh (_changed_rows)
+            last = self._last_build.get(kind)
+            same = last is not None and last["key"] == key and last["values"] is values
+            cur = 1 - last["list"] if last is not None else 0
+            elist, ecount = lists[kind][cur]
             # the correction visits the plastic elements only (an even share per warp)
-            _lib.call("ssp_plastic_elements", _lib.ptr(self._branch), n_el, pat.n_q, _lib.ptr(dv["plastic_elems"]),
-                      _lib.ptr(dv["plastic_count"]), st)
+            _lib.call("ssp_plastic_elements", _lib.ptr(self._branch), n_el, pat.n_q, _lib.ptr(elist), _lib.ptr(ecount),
+                      st)
             _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
                       _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
                       _lib.ptr(self._branch), _lib.ptr(dv["shear"]), _lib.ptr(dv["lame"]), _lib.ptr(d["scatter_map"]),
-                      n_el, pat.n_p, pat.n_q, pat.nnz, scale, _lib.ptr(values), _lib.ptr(dv["plastic_elems"]),
-                      _lib.ptr(dv["plastic_count"]), st)
+                      n_el, pat.n_p, pat.n_q, pat.nnz, scale, _lib.ptr(values), _lib.ptr(elist), _lib.ptr(ecount), st)
+            self._build_no += 1
+            self._last_build[kind] = {"kind": kind, "key": key, "values": values, "list": cur,
+                                      "prev": last["list"] if same else None, "no": self._build_no,
+                                      "prev_no": last["no"] if same else None}
             if ev is not None:
                 e1.record()
                 ev.append((e0, e1))
         else:
             if ev is not None:
                 e0.record()
+            self._last_build.clear()
             tangent_values_device(pat, self._DS_aos, kernel=self.owned_tangent_kernel, symmetric=self._ds_symmetric,
                                   out=values)
             if ev is not None:
@@ -588,9 +656,36 @@ class ConstitutiveOperator:
             if mat is None:
                 mat = OwnedCSRMatrix(pat, values)
             if self.host_outputs:
-                mat.sync_host()
+                kind = "tangent" if which == "tangent" else "regularized"
+                info = self._last_build.get(kind)
+                rows = self._changed_rows(info, mat) if info is not None else None
+                mat.sync_host(rows=rows, mirror=(info["key"], info["no"]) if info is not None else None)
         setattr(self, attr, mat)
         return mat
+
+    def _changed_rows(self, info, mat):
+        """Row marks of the CSR rows that can differ between the host mirror and the device values:
+        when the mirror holds the previous build of the same kind and start (the same r), only the
+        rows of that build's and this build's plastic elements (every other entry equals the start
+        values in both).  None: refresh everything."""
+        if not self.incremental_host_copy or info["prev"] is None or mat.mirror != (info["key"], info["prev_no"]):
+            return None
+        if not _lib.host_writable(mat._host.data_ptr()):
+            return None
+        t = _lib.torch()
+        pat = self._require_pattern()
+        n_rows, n_el = int(pat.local_matrix_pattern.shape[0]), int(pat.overlap_elements.size)
+        dv = self._dev
+        if "row_mark" not in dv:
+            dv["row_mark"] = t.empty(max(n_rows, 1), dtype=t.uint8, device="cuda")
+        mark = dv["row_mark"]
+        mark.zero_()
+        lists = dv["plastic_lists"][info["kind"]]
+        for idx in (info["prev"], info["list"]):
+            elist, ecount = lists[idx]
+            _lib.call("ssp_mark_element_rows", _lib.ptr(pat.device["elem_row"]), n_el, pat.dim * pat.n_p, _lib.ptr(elist),
+                      _lib.ptr(ecount), n_rows, _lib.ptr(mark), _lib.stream_handle())
+        return mark
 
     def _build_owned_tangent_matrix(self):
         t = _lib.require_cuda()
@@ -723,6 +818,37 @@ class ConstitutiveOperator:
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F_free, r)
 
+    def capture_regularized_build(self, lam, U, r, *, free: bool = True):
+        """One Newton iteration's composite build as a CUDA graph, for a fixed strength-reduction
+        factor lam and regularisation r (both fixed while Newton iterates on one continuation step).
+
+        U must be a CUDA float64 array [dim, n_nodes] (or its flat form) that the caller updates in
+        place between replays.  Returns a CapturedBuild whose replay() re-runs, on the current
+        stream, every kernel build_F_K_regularized_all[_free](lam, U, r) launches (the staged
+        values copy, strain, return mapping, tangent corrections and internal force) and whose F and
+        K are the device outputs that each replay overwrites.  Replays skip the host work of the
+        Python entry point (argument checks, ctypes calls, allocations): the launches are recorded
+        once.  Requires device outputs (host_outputs = False).  The graph keeps the configuration
+        it was captured with (tangent_form, return_mapping, branch model): capture again after
+        changing one."""
+        t = _lib.require_cuda()
+        if self.host_outputs:
+            raise ValueError("capture_regularized_build needs host_outputs = False (device outputs)")
+        if not (isinstance(U, t.Tensor) and U.is_cuda and U.dtype == t.float64):
+            raise ValueError("U must be a CUDA float64 tensor updated in place between replays")
+        build = self.build_F_K_regularized_all_free if free else self.build_F_K_regularized_all
+        # first use: buffers, caches, the reduction for lam and the blend for r, outside the graph
+        side = t.cuda.Stream()
+        side.wait_stream(t.cuda.current_stream())
+        with t.cuda.stream(side):
+            build(lam, U, r)
+        t.cuda.current_stream().wait_stream(side)
+        t.cuda.synchronize()
+        graph = t.cuda.CUDAGraph()
+        with t.cuda.graph(graph):
+            F, K = build(lam, U, r)
+        return CapturedBuild(graph, F, K, self)
+
     def build_F_K_regularized_reduced(self, U, r):
         self._stage_values(r)
         self.constitutive_problem_stress_tangent(U)
@@ -762,3 +888,4 @@ class ConstitutiveOperator:
         self._tangent_values = None
         self._regularized_values = None
         self._staged_values = None
+        self._last_build = {}

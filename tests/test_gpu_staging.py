@@ -52,3 +52,98 @@ def test_staged_values_copy_gives_the_same_matrices(cuda_device, form):
         assert err <= 1e-14
         assert rel_err(forces[0], forces[1]) <= 1e-14
     _lib.raise_on_device_status()
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_captured_build_replays_match_direct_builds(cuda_device, form):
+    """capture_regularized_build: replays on U updated in place give the direct builds' F and K."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib, synthetic
+
+    mats = synthetic.MaterialSet.layered(4, seed=3)
+    mesh = synthetic.slope_mesh_3d(12, 5, 6, elem_type="P2", n_layers=4)
+    cap, ref = _op(mesh, mats, True), _op(mesh, mats, True)
+    for op in (cap, ref):
+        op.tangent_form, op.host_outputs = form, False
+    U0 = synthetic.displacement_field(mesh, mats, amplitude=0.01, seed=1)
+    U = torch.as_tensor(U0, device="cuda").clone()
+    run = cap.capture_regularized_build(1.2, U, 0.3)
+    for amp, seed in ((0.02, 2), (0.005, 3), (0.03, 4)):
+        Un = synthetic.displacement_field(mesh, mats, amplitude=amp, seed=seed)
+        U.copy_(torch.as_tensor(Un, device="cuda"))
+        F, K = run.replay()
+        F_ref, K_ref = ref.build_F_K_regularized_all_free(1.2, torch.as_tensor(Un, device="cuda"), 0.3)
+        torch.cuda.synchronize()
+        err_k = rel_err(K.values.cpu().numpy(), K_ref.values.cpu().numpy())
+        err_f = rel_err(F.cpu().numpy(), F_ref.cpu().numpy())
+        print(f"amp {amp}: replay vs direct K {err_k:.2e}, F {err_f:.2e}")
+        assert err_k <= 1e-14 and err_f <= 1e-14
+        assert torch.equal(cap._branch, ref._branch)
+    _lib.raise_on_device_status()
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_incremental_host_refresh_gives_full_copies(cuda_device, form):
+    """Host outputs: the pinned mirror refreshed row by row (rows of the previous and current
+    plastic elements) equals a full device -> host copy, over states whose plastic sets grow,
+    shrink and move, with r changes, tangent builds and device-output builds in between."""
+    from slope_stability_petsc4py_gb300 import _lib, synthetic
+
+    mats = synthetic.MaterialSet.layered(4, seed=3)
+    mesh = synthetic.slope_mesh_3d(12, 5, 6, elem_type="P2", n_layers=4)
+    inc, full = _op(mesh, mats, True), _op(mesh, mats, True)
+    full.incremental_host_copy = False
+    for op in (inc, full):
+        op.tangent_form = form
+    seq = [(0.010, 1, 0.3, "host"), (0.025, 2, 0.3, "host"), (0.006, 3, 0.3, "host"), (0.030, 4, 0.3, "tangent"),
+           (0.015, 5, 0.3, "host"), (0.020, 6, 0.3, "device"), (0.020, 7, 0.3, "host"), (0.004, 8, 0.3, "host"),
+           (0.012, 9, 0.5, "host"), (0.018, 10, 0.5, "host")]
+    _lib.TRACE = []
+    try:
+        for amp, seed, r, kind in seq:
+            U = synthetic.displacement_field(mesh, mats, amplitude=amp, seed=seed)
+            vals = []
+            for op in (inc, full):
+                op.host_outputs = kind != "device"
+                if kind == "tangent":
+                    _F, K = op.build_F_K_tangent_all(1.2, U)
+                else:
+                    _F, K = op.build_F_K_regularized_all_free(1.2, U, r)
+                vals.append(np.array(K.getValuesCSR()[2] if op.host_outputs else K.values.cpu().numpy(), copy=True))
+            err = rel_err(vals[0], vals[1])
+            print(f"{kind} amp {amp} r {r}: incremental vs full host copy {err:.2e}")
+            assert err <= 1e-14
+        refreshes = sum(1 for name, _a, _b in _lib.TRACE if name == "ssp_copy_rows_out")
+    finally:
+        _lib.TRACE = None
+    _lib.raise_on_device_status()
+    print(f"{refreshes} row-wise refreshes")
+    # host builds right after a synced host build with the same r: 2nd, 3rd, 8th and 10th
+    assert refreshes >= 4
+
+
+def test_copy_out_into_pinned_memory(cuda_device):
+    """ssp_copy_out / ssp_copy_rows_out into a pinned torch tensor (device-mapped host memory)."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    n_rows, per = 1000, 7
+    src = torch.randn(n_rows * per, dtype=torch.float64, device="cuda")
+    host = torch.zeros(n_rows * per, dtype=torch.float64, pin_memory=True)
+    assert _lib.host_writable(host.data_ptr())
+    assert not _lib.host_writable(torch.zeros(4, dtype=torch.float64).data_ptr())  # pageable
+    _lib.call("ssp_copy_out", _lib.ptr(src), src.numel(), host.data_ptr(), _lib.stream_handle())
+    torch.cuda.synchronize()
+    assert torch.equal(host, src.cpu())
+    host.zero_()
+    indptr = torch.arange(0, n_rows * per + 1, per, dtype=torch.int32, device="cuda")
+    mark = (torch.arange(n_rows, device="cuda") % 3 == 0).to(torch.uint8)
+    _lib.call("ssp_copy_rows_out", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), n_rows, src.numel(),
+              host.data_ptr(), _lib.stream_handle())
+    torch.cuda.synchronize()
+    rows = mark.cpu().numpy().astype(bool).repeat(per)
+    expect = np.where(rows, src.cpu().numpy(), 0.0)
+    assert np.array_equal(host.numpy(), expect)
+    _lib.raise_on_device_status()

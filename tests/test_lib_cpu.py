@@ -109,3 +109,24 @@ def test_quadrature_and_basis_match_reference_dphi(oracle):
         (d1, d2), w = oracle.geometry(g["coord"], g["elem"][:, g["overlap_elements"]], 2, fem.reference_gradients(2, "P2"), wf)
         assert np.max(np.abs(d1 - g["dphi1"])) <= 1e-12 * np.max(np.abs(g["dphi1"]))
         assert np.max(np.abs(w - g["weight"])) <= 1e-12 * np.max(np.abs(g["weight"]))
+
+
+def test_operator_api_surface_without_a_gpu():
+    """The drop-in operator keeps the reference's constructor fields and entry points (checked on
+    the class: constructing one needs a GPU)."""
+    import dataclasses
+    import inspect
+
+    from slope_stability_petsc4py_gb300 import CapturedBuild, ConstitutiveOperator
+
+    assert dataclasses.is_dataclass(ConstitutiveOperator) and not dataclasses.is_dataclass(CapturedBuild)
+    fields = {f.name for f in dataclasses.fields(ConstitutiveOperator)}
+    assert {"B", "c0", "phi", "psi", "Davis_type", "shear", "bulk", "lame", "WEIGHT", "n_strain", "n_int", "dim",
+            "q_mask"} <= fields
+    for name in ("reduction", "constitutive_problem_stress", "constitutive_problem_stress_tangent", "build_F",
+                 "build_F_free", "build_K_regularized", "build_F_K_tangent", "build_F_K_regularized_all",
+                 "build_F_K_regularized_all_free", "build_F_K_regularized_reduced",
+                 "build_F_K_regularized_reduced_free", "set_owned_tangent_pattern", "capture_regularized_build"):
+        assert callable(getattr(ConstitutiveOperator, name)), name
+    assert list(inspect.signature(ConstitutiveOperator.build_F_K_regularized_all_free).parameters) == \
+        ["self", "lam", "U", "r"]
