@@ -6,6 +6,11 @@ Drop-in replacements for the reference's constitutive builder and owned-row asse
 The arithmetic runs in hand-written CUDA kernels behind the C ABI of ``include/ssp_gb300.h``.
 """
 
+from .bddc import (  # noqa: F401
+    BDDCSubdomainPattern,
+    assemble_bddc_subdomain_tangent_values,
+    prepare_bddc_subdomain_pattern,
+)
 from .distributed_tangent import (  # noqa: F401
     DEFAULT_TANGENT_KERNEL,
     OwnedTangentPattern,
@@ -17,7 +22,7 @@ from .distributed_tangent import (  # noqa: F401
     prepare_owned_tangent_pattern,
 )
 from .materials import MaterialSpec, heterogenous_materials  # noqa: F401
-from .problem import CapturedBuild, ConstitutiveOperator, OwnedCSRMatrix  # noqa: F401
+from .problem import CapturedBuild, ConstitutiveOperator, OwnedCSRMatrix, SubdomainCSRMatrix  # noqa: F401
 from .reduction import reduction  # noqa: F401
 
 __version__ = "0.1.0"

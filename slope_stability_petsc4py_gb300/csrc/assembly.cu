@@ -824,6 +824,7 @@ int dispatch_element(int dim, int n_p, int n_q, const ElemArgs &a, cudaStream_t 
     if (dim == 3 && n_p == 4 && n_q == 1) return launch_element<3, 4, 1, 32, SYM, CORR>(a, st);
     if (dim == 2 && n_p == 6 && n_q == 7) return launch_element<2, 6, 7, 32, SYM, CORR>(a, st);
     if (dim == 2 && n_p == 3 && n_q == 1) return launch_element<2, 3, 1, 32, SYM, CORR>(a, st);
+    if (dim == 2 && n_p == 15 && n_q == 12) return launch_element_warp<2, 15, 12, SYM, CORR>(a, st);
     return SSP_ERR_UNSUPPORTED;
 }
 
@@ -973,6 +974,8 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
     if (dim == 3 && n_p == 10 && n_q == 11) return launch_element_warp<3, 10, 11, true, true, true>(a, st);
     if (dim == 3 && n_p == 4 && n_q == 1) return launch_element_warp<3, 4, 1, true, true, true>(a, st);
     if (dim == 2 && n_p == 6 && n_q == 7) return launch_element_warp<2, 6, 7, true, true, true>(a, st);
+    if (dim == 2 && n_p == 3 && n_q == 1) return launch_element_warp<2, 3, 1, true, true, true>(a, st);
+    if (dim == 2 && n_p == 15 && n_q == 12) return launch_element_warp<2, 15, 12, true, true, true>(a, st);
     if (dim == 3 && n_p == 35 && n_q == 24)
         return correction_tc_p4(dphi1, dphi2, dphi3, ds, weight, branch, shear, lame, scatter_map, n_elem, nnz_out, scale,
                                 out_values, elem_list, elem_count, st);

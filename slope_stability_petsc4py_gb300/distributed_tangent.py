@@ -574,3 +574,15 @@ def assemble_owned_regularized_matrix(pattern: OwnedTangentPattern, DS, r: float
     _lib.raise_on_device_status()
     lp = pattern.local_matrix_pattern
     return csr_matrix((values, lp.indices.copy(), lp.indptr.copy()), shape=lp.shape)
+
+
+_BDDC_NAMES = ("BDDCSubdomainPattern", "prepare_bddc_subdomain_pattern", "assemble_bddc_subdomain_tangent_values")
+
+
+def __getattr__(name):
+    # the subdomain (BDDC) half of the reference module lives in .bddc, which imports this module
+    if name in _BDDC_NAMES:
+        from . import bddc
+
+        return getattr(bddc, name)
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")

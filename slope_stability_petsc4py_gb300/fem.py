@@ -19,9 +19,9 @@ from functools import lru_cache
 
 import numpy as np
 
-from .synthetic import tet_node_tuples
+from .synthetic import tet_node_tuples, tri_node_tuples
 
-N_NODES = {(2, "P1"): 3, (2, "P2"): 6, (3, "P1"): 4, (3, "P2"): 10, (3, "P4"): 35}
+N_NODES = {(2, "P1"): 3, (2, "P2"): 6, (2, "P4"): 15, (3, "P1"): 4, (3, "P2"): 10, (3, "P4"): 35}
 
 
 def quadrature(dim: int, elem_type: str) -> tuple[np.ndarray, np.ndarray]:
@@ -34,6 +34,19 @@ def quadrature(dim: int, elem_type: str) -> tuple[np.ndarray, np.ndarray]:
             a, b, c, d = 0.1012865073235, 0.7974269853531, 0.4701420641051, 0.0597158717898
             xi = np.array([[a, b, a, c, c, d, 1 / 3], [a, a, b, d, c, c, 1 / 3]])
             wf = np.array([0.1259391805448] * 3 + [0.1323941527885] * 3 + [0.225]) / 2
+            return xi, wf
+        if et == "P4":
+            # 12-point rule: two 3-point orbits and one 6-point orbit (quadrature.py:28-51)
+            a1, b1 = 0.063089014491502, 0.873821971016996
+            a2, b2 = 0.249286745170910, 0.501426509658179
+            p, q, r = 0.310352451033785, 0.053145049844816, 0.636502499121399
+            xi = np.array(
+                [
+                    [a1, a1, b1, a2, a2, b2, p, p, q, q, r, r],
+                    [a1, b1, a1, a2, b2, a2, q, r, p, r, p, q],
+                ]
+            )
+            wf = np.array([0.050844906370207] * 3 + [0.116786275726379] * 3 + [0.082851075618374] * 6) / 2
             return xi, wf
     if dim == 3:
         if et == "P1":
@@ -106,6 +119,43 @@ def _tet_lagrange_grads(order: int, xi: np.ndarray) -> tuple[np.ndarray, np.ndar
     return out[0], out[1], out[2]
 
 
+def _tri_lagrange(order: int, xi: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Values and (xi1, xi2) derivatives of the order-p triangle basis from barycentric products."""
+    bary = (1.0 - xi[0] - xi[1], xi[0], xi[1])
+    tuples = tri_node_tuples(order)
+    n_q = xi.shape[1]
+    val = np.empty((len(tuples), n_q))
+    d = [np.empty((len(tuples), n_q)) for _ in range(2)]
+    for idx, counts in enumerate(tuples):
+        vals, ders = zip(*(_lagrange_factor(order, c, lv) for lv, c in zip(bary, counts)))
+        val[idx] = vals[0] * vals[1] * vals[2]
+        dl = [ders[0] * vals[1] * vals[2], vals[0] * ders[1] * vals[2], vals[0] * vals[1] * ders[2]]
+        for ax in range(2):
+            d[ax][idx] = dl[ax + 1] - dl[0]
+    return val, d[0], d[1]
+
+
+def _reference_p4_tri_dxi2_quarter_nodes(xi: np.ndarray) -> np.ndarray:
+    """The reference's tabulated d/dxi2 of the 2D P4 quarter-point nodes 8-11.
+
+    ``src/slope_stability/fem/basis.py:100-123`` lists, for nodes 8-11, expressions that are not
+    the xi2-derivatives of its own basis functions (lines 68-71): for example node 10's entry is the
+    xi1-derivative of node 10's function, and the four rows do not sum with the others to zero.
+    The strain, force and tangent of a 2D P4 element are sums over these tabulated values, so they
+    are reproduced here value for value; the table's other 26 rows are the exact derivatives.
+    Returns shape (4, n_q).
+    """
+    x1, x2 = xi
+    x0 = 1.0 - x1 - x2
+    k = 8.0 / 3.0
+    return np.array([
+        k * x1 * ((4 * x1 - 1) * (4 * x1 - 2) + 4 * x2 * (4 * x1 - 1)),
+        k * x1 * ((4 * x1 - 1) * (4 * x2 - 1) + 4 * x2 * (4 * x2 - 1)),
+        -k * x2 * (4 * x2 - 1) * (4 * x2 - 2),
+        k * x2 * ((4 * x2 - 1) * (4 * x2 - 2) + 4 * x0 * (4 * x2 - 2) + 4 * x0 * (4 * x2 - 1)),
+    ])
+
+
 @lru_cache(maxsize=None)
 def reference_values(dim: int, elem_type: str) -> np.ndarray:
     """Basis values at the quadrature points, shape (n_p, n_q) (basis.py:15-33, 134-157)."""
@@ -126,6 +176,8 @@ def reference_values(dim: int, elem_type: str) -> np.ndarray:
             return np.array(lam)
         verts = [lv * (2.0 * lv - 1.0) for lv in lam]
         return np.array(verts + [4.0 * lam[1] * lam[2], 4.0 * lam[0] * lam[2], 4.0 * lam[0] * lam[1]])
+    if dim == 2 and et == "P4":
+        return _tri_lagrange(4, xi)[0]
     if dim == 3 and et == "P4":
         bary = (1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2])
         out = np.empty((N_NODES[(3, "P4")], xi.shape[1]))
@@ -154,6 +206,9 @@ def reference_gradients(dim: int, elem_type: str) -> np.ndarray:
         elif et == "P2":
             g1 = np.array([1 - 4 * x0, 4 * x1 - 1, z, 4 * x2, -4 * x2, 4 * (x0 - x1)])
             g2 = np.array([1 - 4 * x0, z, 4 * x2 - 1, 4 * x1, 4 * (x0 - x2), -4 * x1])
+        elif et == "P4":
+            _, g1, g2 = _tri_lagrange(4, xi)
+            g2[8:12] = _reference_p4_tri_dxi2_quarter_nodes(xi)
         else:
             raise ValueError(et)
         return np.stack((g1, g2))

@@ -49,6 +49,9 @@ except Exception:  # pragma: no cover
     PETSc = None
 
 _OWNED_MODES = {"overlap", "unique_exchange", "unique", "unique_gather", "no_overlap", "partitioned"}
+# (dim, nodes per element) with a mixed-precision plastic-correction kernel (CUDA-core warp kernel
+# for the triangles and P1/P2 tets, tcgen05 tensor-core kernel for P4 tets)
+MIXED_TANGENT_ELEMENTS = {(2, 3), (2, 6), (2, 15), (3, 4), (3, 10), (3, 35)}
 
 
 class OwnedCSRMatrix:
@@ -131,6 +134,21 @@ class OwnedCSRMatrix:
         self.values = None
 
 
+class SubdomainCSRMatrix(OwnedCSRMatrix):
+    """Local square CSR of a BDDC subdomain, updated in place (stable ``handle``): what the
+    reference passes to ``local_csr_to_petsc_matis_matrix`` (problem.py:1738-1749) -- the local
+    values and pattern, the local-to-global dof map, the global size, block size, local vector size
+    and the BDDC metadata (problem.py:1658-1708, without the PETSc objects)."""
+
+    def __init__(self, pattern, values, *, global_size: int, block_size: int, metadata: dict):
+        super().__init__(pattern, values)
+        self.local_to_global = np.asarray(pattern.local_global_dofs, dtype=np.int64)
+        self.global_size = int(global_size)
+        self.block_size = int(block_size)
+        self.local_vector_size = int(block_size * (pattern.owned_node_range[1] - pattern.owned_node_range[0]))
+        self.metadata = metadata
+
+
 class CapturedBuild:
     """A composite Newton build recorded as a CUDA graph (ConstitutiveOperator.capture_regularized_build)."""
 
@@ -197,6 +215,7 @@ class ConstitutiveOperator:
         self.time_local_force_gather = []
         self.owned_tangent_pattern: OwnedTangentPattern | None = None
         self.bddc_subdomain_pattern = None
+        self._bddc = {}  # BDDC subdomain matrices and value buffers, per kind
         self.use_compiled_owned_tangent = True
         self.owned_tangent_kernel = DEFAULT_TANGENT_KERNEL
         self.use_compiled_owned_constitutive = True
@@ -297,7 +316,9 @@ class ConstitutiveOperator:
                 self._dev["red_index"] = _lib.to_device(inv.reshape(-1).astype(np.int32), t.int32)
 
     def set_bddc_subdomain_pattern(self, pattern) -> None:
-        raise NotImplementedError("BDDC subdomain assembly is outside the GPU hot path")
+        """Attach a BDDCSubdomainPattern (problem.py:1297-1298); its matrices are rebuilt on demand."""
+        self.bddc_subdomain_pattern = pattern
+        self._bddc = {}
 
     # -------------------------------------------------------------------- state views
 
@@ -592,7 +613,7 @@ class ConstitutiveOperator:
             if ev is not None:
                 e0.record()
             entry = "ssp_tangent_plastic_correction"
-            if self.tangent_form == "mixed" and (pat.n_p <= 10 or (pat.dim == 3 and pat.n_p == 35)):
+            if self.tangent_form == "mixed" and (pat.dim, pat.n_p) in MIXED_TANGENT_ELEMENTS:
                 entry = "ssp_tangent_plastic_correction_mixed"
             n_el = int(pat.overlap_elements.size)
             dv = self._dev
@@ -706,6 +727,112 @@ class ConstitutiveOperator:
             self._owned_regularized_mat.fence()
         self._tangent_into(self._regularized_values, r=r)
         return self._matrix("regularized", self._regularized_values)
+
+    # -------------------------------------------------------------------- BDDC subdomain matrices
+
+    def _bddc_pattern(self):
+        pattern = self.bddc_subdomain_pattern
+        if pattern is None:
+            raise ValueError("BDDC subdomain pattern not configured")
+        return pattern
+
+    def _bddc_local_DS(self):
+        """DS rows of the subdomain's points as an AoS CUDA tensor (n_local, n_strain^2): gathered
+        from the owned (overlap) evaluation, else taken from a global ``DS`` (problem.py:1646-1656)."""
+        t = _lib.require_cuda()
+        pattern = self._bddc_pattern()
+        if self._DS_aos is not None:
+            if int(pattern.overlap_local_positions.size) != int(pattern.local_int_indices.size):
+                raise RuntimeError("BDDC overlap-local integration-point map is incomplete")
+            pos = pattern.device.get("overlap_positions")
+            if pos is None:
+                pos = pattern.device["overlap_positions"] = t.as_tensor(
+                    pattern.overlap_local_positions.astype(np.int64), device="cuda")
+            return self._DS_aos.index_select(0, pos)
+        if self.DS is None:
+            raise ValueError("Tangent DS not computed")
+        ds = np.asarray(self.DS, dtype=np.float64)[:, pattern.local_int_indices]
+        return _lib.to_device(np.ascontiguousarray(ds.T), t.float64)
+
+    def _bddc_matrix_metadata(self, pattern) -> dict:
+        """The BDDC set-up data handed over with the subdomain matrix (problem.py:1658-1708):
+        Dirichlet rows, coordinates, block size, dof ordering, adjacency, per-component fields and
+        primal vertices, as integer arrays where the reference builds PETSc index sets.  The
+        near-nullspace bases the reference adds there come from its linear-solver utilities and stay
+        with the solver."""
+        owned_coord = np.asarray(pattern.owned_coord, dtype=np.float64)
+        dim = int(self.dim)
+        nodes = np.asarray(pattern.local_nodes, dtype=np.int64)
+        vertex_major = dim * np.repeat(nodes, dim) + np.tile(np.arange(dim, dtype=np.int64), nodes.size)
+        meta = {
+            "bddc_dirichlet_local": np.asarray(pattern.local_dirichlet_dofs, dtype=np.int32),
+            "bddc_local_coordinates": np.asarray(owned_coord.T, dtype=np.float64),
+            "bddc_local_block_size": dim,
+            "bddc_adjacency_source": str(pattern.adjacency_source),
+            "bddc_local_vertex_major_ordering": bool(np.array_equal(pattern.local_global_dofs, vertex_major)),
+        }
+        if pattern.local_field_dofs:
+            meta["bddc_field_is_local"] = tuple(np.asarray(v, dtype=np.int32) for v in pattern.local_field_dofs)
+        if int(pattern.local_adjacency_indptr.size) and int(pattern.local_adjacency_indices.size):
+            meta["bddc_local_adjacency"] = (np.asarray(pattern.local_adjacency_indptr, dtype=np.int32),
+                                            np.asarray(pattern.local_adjacency_indices, dtype=np.int32))
+        if int(pattern.local_primal_vertices.size):
+            meta["bddc_primal_vertices_local"] = np.asarray(pattern.local_primal_vertices, dtype=np.int32)
+        return meta
+
+    def _bddc_matrix(self, kind: str, values):
+        pattern = self._bddc_pattern()
+        mat = self._bddc.get(kind + "_mat")
+        if mat is None:
+            global_size = int(self.q_mask.size) if self.q_mask is not None else 0
+            mat = SubdomainCSRMatrix(pattern, values, global_size=global_size, block_size=self.dim,
+                                     metadata=self._bddc_matrix_metadata(pattern))
+            self._bddc[kind + "_mat"] = mat
+        if self.host_outputs:
+            mat.sync_host()
+        return mat
+
+    def _bddc_values(self, kind: str):
+        t = _lib.torch()
+        buf = self._bddc.get(kind)
+        if buf is None:
+            mat = self._bddc.get(kind + "_mat")
+            if mat is not None:
+                mat.fence()
+            nnz = self._bddc_pattern().nnz
+            buf = self._bddc[kind] = t.empty(max(nnz, 1), dtype=t.float64, device="cuda")[:nnz]
+        elif self._bddc.get(kind + "_mat") is not None:
+            self._bddc[kind + "_mat"].fence()
+        return buf
+
+    def _build_bddc_tangent_matrix(self, *, local_mat_type: str = "aij"):
+        """Subdomain tangent (problem.py:1710-1767); ``local_mat_type`` is accepted for compatibility."""
+        from .bddc import bddc_tangent_values_device
+
+        pattern = self._bddc_pattern()
+        t0 = perf_counter()
+        vals = bddc_tangent_values_device(pattern, self._bddc_local_DS(), out=self._bddc_values("tangent"))
+        self.time_build_tangent_local.append(perf_counter() - t0)
+        return self._bddc_matrix("tangent", vals)
+
+    def _build_bddc_elastic_matrix(self, *, local_mat_type: str = "aij"):
+        """Subdomain elastic matrix (problem.py:1769-1801)."""
+        pattern = self._bddc_pattern()
+        vals = self._bddc_values("elastic")
+        vals.copy_(pattern.device["elastic_values"])
+        return self._bddc_matrix("elastic", vals)
+
+    def _build_bddc_regularized_matrix(self, r: float, *, local_mat_type: str = "aij"):
+        """(1-r) K_tangent + r K_elastic on the subdomain pattern (problem.py:1803-1857)."""
+        from .bddc import bddc_tangent_values_device
+
+        pattern = self._bddc_pattern()
+        t0 = perf_counter()
+        vals = bddc_tangent_values_device(pattern, self._bddc_local_DS(), out=self._bddc_values("regularized"))
+        _lib.call("ssp_finish_values", _lib.ptr(vals), pattern.nnz, None, 0, _lib.ptr(pattern.device["elastic_values"]),
+                  float(r), _lib.stream_handle())
+        self.time_build_tangent_local.append(perf_counter() - t0)
+        return self._bddc_matrix("regularized", vals)
 
     def build_K_regularized(self, r: float):
         if self.owned_tangent_pattern is None:
@@ -889,3 +1016,7 @@ class ConstitutiveOperator:
         self._regularized_values = None
         self._staged_values = None
         self._last_build = {}
+        for key, mat in list(self._bddc.items()):
+            if key.endswith("_mat"):
+                mat.destroy()
+        self._bddc = {}

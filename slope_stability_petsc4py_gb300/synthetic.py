@@ -154,24 +154,50 @@ def tet_node_tuples(order: int) -> tuple[tuple[int, int, int, int], ...]:
     return tuple(out)
 
 
-def elevate_tets(vcoord: np.ndarray, tet4: np.ndarray, order: int) -> tuple[np.ndarray, np.ndarray]:
-    """Elevate a linear tet mesh to Lagrange order 1, 2 or 4 with shared higher-order nodes.
+@lru_cache(maxsize=None)
+def tri_node_tuples(order: int) -> tuple[tuple[int, int, int], ...]:
+    """Barycentric count tuples (v0, v1, v2) of the order-p triangle, in the reference's node order.
+
+    P1: the vertices.  P2: vertices, then the midpoints of edges (1,2), (0,2), (0,1)
+    (``src/slope_stability/fem/basis.py:22-33``).  P4: vertices, the midpoints of edges (0,1),
+    (1,2), (2,0), the quarter points of those edges in the same edge order, each edge walked from
+    its first vertex, then the three interior nodes nearest v0, v1, v2
+    (``src/slope_stability/mesh/textmesh_2d.py:116-184``, ``fem/basis.py:57-75``).
+    """
+    p = int(order)
+    verts = ((p, 0, 0), (0, p, 0), (0, 0, p))
+    if p == 1:
+        return verts
+    if p == 2:
+        return verts + ((0, 1, 1), (1, 0, 1), (1, 1, 0))
+    if p == 4:
+        mids = ((2, 2, 0), (0, 2, 2), (2, 0, 2))
+        quarters = ((3, 1, 0), (1, 3, 0), (0, 3, 1), (0, 1, 3), (1, 0, 3), (3, 0, 1))
+        interior = ((2, 1, 1), (1, 2, 1), (1, 1, 2))
+        return verts + mids + quarters + interior
+    raise ValueError(f"unsupported triangle order {order}")
+
+
+def elevate_simplices(vcoord: np.ndarray, cells: np.ndarray, tuples) -> tuple[np.ndarray, np.ndarray]:
+    """Elevate a linear simplex mesh (cells: (dim+1, n_e) vertex ids) to the Lagrange nodes
+    ``tuples`` (barycentric counts, vertices first) with shared higher-order nodes.
 
     A higher-order node is identified by the vertices it lies on and its barycentric counts,
     so nodes on shared edges and faces are created once.  New nodes are numbered after all
-    vertices, in order of first appearance.
+    vertices, in order of first appearance (element-major, then local node).
     """
-    tuples = tet_node_tuples(order)
+    n_vert = cells.shape[0]
+    order = int(sum(tuples[0]))
     n_v = vcoord.shape[1]
-    n_e = tet4.shape[1]
+    n_e = cells.shape[1]
     elem = np.empty((len(tuples), n_e), dtype=np.int64)
-    elem[:4] = tet4
-    if order == 1:
+    elem[:n_vert] = cells
+    if len(tuples) == n_vert:
         return vcoord.copy(), elem
     # key of a higher-order node: its (vertex, count) pairs sorted by vertex, padded with (-1, 0)
-    hi = np.asarray(tuples[4:], dtype=np.int64)  # (n_hi, 4) barycentric counts
+    hi = np.asarray(tuples[n_vert:], dtype=np.int64)  # (n_hi, n_vert) barycentric counts
     width = int((hi > 0).sum(axis=1).max())
-    verts = tet4.T  # (n_e, 4)
+    verts = cells.T  # (n_e, n_vert)
     key_v = np.full((n_e, hi.shape[0], width), -1, dtype=np.int64)
     key_c = np.zeros((n_e, hi.shape[0], width), dtype=np.int64)
     for li, t in enumerate(hi):
@@ -186,14 +212,24 @@ def elevate_tets(vcoord: np.ndarray, tet4: np.ndarray, order: int) -> tuple[np.n
     rank = np.empty(uniq.shape[0], dtype=np.int64)
     rank[np.argsort(first, kind="stable")] = np.arange(uniq.shape[0])
     gid = n_v + rank[inverse.reshape(-1)]
-    elem[4:] = gid.reshape(n_e, hi.shape[0]).T
+    elem[n_vert:] = gid.reshape(n_e, hi.shape[0]).T
     # coordinates of the new nodes from their first element
     occ = np.sort(first)
     e_of, li_of = occ // hi.shape[0], occ % hi.shape[0]
-    bary = hi[li_of].astype(np.float64) / order  # (n_new, 4)
-    new_pts = np.einsum("dkn,nk->dn", vcoord[:, tet4[:, e_of]], bary)
+    bary = hi[li_of].astype(np.float64) / order  # (n_new, n_vert)
+    new_pts = np.einsum("dkn,nk->dn", vcoord[:, cells[:, e_of]], bary)
     coord = np.concatenate((vcoord, new_pts), axis=1)
     return coord, elem
+
+
+def elevate_tets(vcoord: np.ndarray, tet4: np.ndarray, order: int) -> tuple[np.ndarray, np.ndarray]:
+    """Elevate a linear tet mesh to Lagrange order 1, 2 or 4 (reference node order)."""
+    return elevate_simplices(vcoord, tet4, tet_node_tuples(order))
+
+
+def elevate_triangles(vcoord: np.ndarray, tri3: np.ndarray, order: int) -> tuple[np.ndarray, np.ndarray]:
+    """Elevate a linear triangle mesh to Lagrange order 1, 2 or 4 (reference node order)."""
+    return elevate_simplices(vcoord, tri3, tri_node_tuples(order))
 
 
 def _kuhn_tets(nx: int, ny: int, nz: int) -> np.ndarray:
@@ -256,27 +292,10 @@ def slope_mesh_2d(nx: int, ny: int, *, elem_type: str = "P2", n_layers: int = 1)
     t1 = np.stack((vid(I, J), vid(I + 1, J), vid(I + 1, J + 1)))
     t2 = np.stack((vid(I, J), vid(I + 1, J + 1), vid(I, J + 1)))
     tri = np.stack((t1, t2), axis=2).reshape(3, -1)
-    if elem_type.upper() == "P1":
-        coord, elem = vcoord.copy(), tri.astype(np.int64)
-    elif elem_type.upper() == "P2":
-        n_v = vcoord.shape[1]
-        keys: dict[tuple[int, int], int] = {}
-        pts: list[np.ndarray] = []
-        elem = np.empty((6, tri.shape[1]), dtype=np.int64)
-        elem[:3] = tri
-        for e in range(tri.shape[1]):
-            for li, (a, b) in enumerate(((1, 2), (0, 2), (0, 1))):
-                va, vb = int(tri[a, e]), int(tri[b, e])
-                key = (min(va, vb), max(va, vb))
-                gid = keys.get(key)
-                if gid is None:
-                    gid = n_v + len(pts)
-                    keys[key] = gid
-                    pts.append(0.5 * (vcoord[:, va] + vcoord[:, vb]))
-                elem[3 + li, e] = gid
-        coord = np.concatenate((vcoord, np.stack(pts, axis=1)), axis=1)
-    else:
+    order = {"P1": 1, "P2": 2, "P4": 4}.get(elem_type.upper())
+    if order is None:
         raise ValueError(f"unsupported 2D element type {elem_type!r}")
+    coord, elem = elevate_triangles(vcoord, tri.astype(np.int64), order)
     x_max = float(np.max(coord[0])) - 1.0e-9
     q = np.zeros((2, coord.shape[1]), dtype=bool)
     q[0] = (coord[0] > 0.0) & (coord[1] > 0.0) & (coord[0] < x_max)

@@ -381,18 +381,128 @@ def gen_pattern_2d(ref):
         print("pattern2d", tag, pat.local_matrix_pattern.nnz, "nnz")
 
 
-def main():
+def gen_pattern_2d_p4(ref):
+    """2D P4 (15-node triangles) on the reference's own slope generator (``mesh/slope_2d.py:351-376``,
+    node order of ``mesh/textmesh_2d.py:116-184``); dphi come from the reference's basis table."""
+    dt = ref["dt"]
+    slope_2d = importlib.import_module("slope_stability.mesh.slope_2d")
+    m = slope_2d.generate_homogeneous_slope_mesh_2d(elem_type="P4", h=5.0)
+    coord, elem = np.asarray(m.coord, dtype=np.float64), np.asarray(m.elem, dtype=np.int64)
+    q_mask = np.asarray(m.q_mask, dtype=bool)
+    n_nodes = coord.shape[1]
+    mat = {"c0": 6.0, "phi": 45.0, "psi": 0.0, "young": 2.0e4, "poisson": 0.49, "gamma_sat": 20.0,
+           "gamma_unsat": 20.0}
+    for tag, owned in (("P4_full", (0, n_nodes)), ("P4_partial", (n_nodes // 3, 2 * n_nodes // 3))):
+        pat = dt.prepare_owned_tangent_pattern(coord, elem, q_mask, np.zeros(elem.shape[1], np.int64), [mat], owned,
+                                               elem_type="P4", include_unique=(tag == "P4_full"))
+        rng = np.random.default_rng(13)
+        n_loc = pat.local_int_indices.size
+        ds = rng.standard_normal((9, n_loc))
+        U = rng.standard_normal((2, n_nodes))
+        stress = rng.standard_normal((3, n_loc))
+        legacy_py = dt.assemble_owned_tangent_values(pat, ds, use_compiled=False, kernel="legacy")
+        strain_py = dt.assemble_overlap_strain(pat, U, use_compiled=False)
+        force_py = dt.assemble_owned_force_from_local_stress(pat, stress, use_compiled=False)
+        np.savez_compressed(HERE / f"pattern2d_{tag}.npz", elem_type=np.array("P4"), coord=coord, elem=elem,
+                            q_mask=q_mask, owned_node_range=np.asarray(owned), ds=ds, U=U, stress=stress,
+                            legacy_py=legacy_py, strain_py=strain_py, force_py=force_py, **pattern_arrays(pat))
+        print("pattern2d", tag, pat.local_matrix_pattern.nnz, "nnz")
+
+
+BDDC_KEYS = ("local_nodes", "local_elements", "local_coord", "local_q_mask", "local_global_dofs", "elastic_values",
+             "local_assembly_weight", "dphi1", "dphi2", "dphi3", "local_int_indices", "overlap_local_positions",
+             "scatter_map", "local_dirichlet_dofs", "constrained_diag_positions", "local_adjacency_indptr",
+             "local_adjacency_indices", "local_primal_vertices", "owned_coord")
+
+
+def bddc_cases():
+    """(name, elem_type, coord, elem, q_mask, owned range, adjacency_source, corner_only_primals)."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    slope_2d = importlib.import_module("slope_stability.mesh.slope_2d")
+    def owner_range(elem, lo, hi):
+        # elements belong to the subdomain owning their smallest node: cut at owner quantiles
+        owners = np.sort(np.min(elem, axis=0))
+        return int(owners[int(lo * (owners.size - 1))]), int(owners[int(hi * (owners.size - 1))])
+
+    out = []
+    m = synthetic.slope_mesh_3d(3, 2, 2, depth=6.0, elem_type="P2")
+    n = m.coord.shape[1]
+    out.append(("3d_P2_mid", "P2", m.coord, m.elem, m.q_mask, owner_range(m.elem, 0.3, 0.7), "csr", True))
+    out.append(("3d_P2_all", "P2", m.coord, m.elem, m.q_mask, (0, n), "topology", False))
+    out.append(("3d_P2_empty", "P2", m.coord, m.elem, m.q_mask, (n - 5, n), "csr", True))
+    m4 = synthetic.slope_mesh_3d(2, 1, 1, depth=6.0, elem_type="P4")
+    out.append(("3d_P4_head", "P4", m4.coord, m4.elem, m4.q_mask, owner_range(m4.elem, 0.0, 0.6), "topology", True))
+    m2 = synthetic.slope_mesh_2d(4, 3, elem_type="P2")
+    out.append(("2d_P2_tail", "P2", m2.coord, m2.elem, m2.q_mask, owner_range(m2.elem, 0.5, 1.0), "none", True))
+    r4 = slope_2d.generate_homogeneous_slope_mesh_2d(elem_type="P4", h=5.0)
+    e4 = np.asarray(r4.elem, dtype=np.int64)
+    out.append(("2d_P4_mid", "P4", np.asarray(r4.coord, dtype=np.float64), e4, np.asarray(r4.q_mask, dtype=bool),
+                owner_range(e4, 0.25, 0.75), "csr", False))
+    return out
+
+
+def gen_bddc(ref, kern):
+    """BDDC subdomain patterns and tangent values (``fem/distributed_tangent.py:1178-1434``)."""
+    dt = ref["dt"]
+    for name, et, coord, elem, q_mask, owned, adj, corners in bddc_cases():
+        dim = coord.shape[0]
+        mat_id = (np.arange(elem.shape[1]) % 2).astype(np.int64)
+        mats = [MATERIAL, dict(MATERIAL, young=2.0 * MATERIAL["young"], poisson=0.3)]
+        owned_pat = dt.prepare_owned_tangent_pattern(coord, elem, q_mask, mat_id, mats, owned, elem_type=et,
+                                                     include_unique=False)
+        dt._kernels = kern  # the production path: elastic values through the compiled 3D kernel
+        pat = dt.prepare_bddc_subdomain_pattern(coord, elem, q_mask, mat_id, mats, owned, elem_type=et,
+                                                overlap_local_int_indices=owned_pat.local_int_indices,
+                                                adjacency_source=adj, corner_only_primals=corners)
+        ns = 6 if dim == 3 else 3
+        rng = np.random.default_rng(17)
+        ds = rng.standard_normal((ns * ns, pat.local_int_indices.size))
+        dt._kernels = None
+        values_py = dt.assemble_bddc_subdomain_tangent_values(pat, ds, use_compiled=False)
+        extra = {}
+        if dim == 3:
+            dt._kernels = kern
+            extra["values_c"] = dt.assemble_bddc_subdomain_tangent_values(pat, ds, use_compiled=True)
+            dt._kernels = None
+        np.savez_compressed(
+            HERE / f"bddc_{name}.npz", elem_type=np.array(et), coord=coord, elem=elem, q_mask=q_mask,
+            owned_node_range=np.asarray(owned), material_identifier=mat_id, adjacency_source=np.array(adj),
+            corner_only_primals=np.array(corners), overlap_local_int_indices=owned_pat.local_int_indices, ds=ds,
+            values_py=values_py, indptr=np.asarray(pat.local_matrix_pattern.indptr, dtype=np.int32),
+            indices=np.asarray(pat.local_matrix_pattern.indices, dtype=np.int32),
+            local_field_dofs=np.stack(pat.local_field_dofs) if pat.local_field_dofs[0].size else np.zeros((dim, 0), np.int32),
+            n_p=np.int64(pat.n_p), n_q=np.int64(pat.n_q),
+            **{k: np.asarray(getattr(pat, k)) for k in BDDC_KEYS}, **extra,
+        )
+        print("bddc", name, pat.local_matrix_pattern.nnz, "nnz", pat.local_elements.size, "elements")
+
+
+GENERATORS = ("constitutive_3d", "constitutive_2d", "reduction", "patterns", "pattern_2d", "pattern_2d_p4", "bddc")
+
+
+def main(which=GENERATORS):
+    """``python tests/golden/make_golden.py [generator ...]`` (default: all of GENERATORS)."""
     oracle_py.build(ref=True)
     libref = oracle_py.ref_lib()
     assert libref is not None, "reference kernels did not build"
     ref = import_reference()
     kern = compiled_kernels_module(libref)
-    gen_constitutive(kern, ref["problem"], libref)
-    gen_constitutive_2d(ref["problem"], ref["reduction"])
-    gen_reduction(ref["reduction"])
-    gen_patterns(ref, kern)
-    gen_pattern_2d(ref)
+    if "constitutive_3d" in which:
+        gen_constitutive(kern, ref["problem"], libref)
+    if "constitutive_2d" in which:
+        gen_constitutive_2d(ref["problem"], ref["reduction"])
+    if "reduction" in which:
+        gen_reduction(ref["reduction"])
+    if "patterns" in which:
+        gen_patterns(ref, kern)
+    if "pattern_2d" in which:
+        gen_pattern_2d(ref)
+    if "pattern_2d_p4" in which:
+        gen_pattern_2d_p4(ref)
+    if "bddc" in which:
+        gen_bddc(ref, kern)
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or GENERATORS)

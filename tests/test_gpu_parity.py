@@ -317,6 +317,57 @@ def test_2d_assembly_matches_reference(name, oracle):
     assert rel_err(assemble_owned_force_from_local_stress(pat, g["stress"]), g["force_py"]) <= PLAIN_RTOL
 
 
+@pytest.mark.parametrize("et,dims", [("P1", (24, 12)), ("P2", (14, 8)), ("P4", (7, 4))])
+def test_2d_operator_against_oracle_on_slope(oracle, et, dims):
+    """Plane strain on a layered synthetic slope: strain -> S/DS -> F -> regularised K through the
+    operator, against the oracle chain (P4: the reference's 15-node triangles and basis table);
+    then the mixed form's tangent against the FP64 one."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
+    from slope_stability_petsc4py_gb300.distributed_tangent import _PatternBuild
+
+    mats = synthetic.MaterialSet.layered(4, seed=2)
+    mesh = synthetic.slope_mesh_2d(*dims, elem_type=et, n_layers=4)
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type=et)
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.05, seed=3)
+    pat = op.owned_tangent_pattern
+    lam, r = 1.1, 0.25
+    op.reduction(lam)
+    op.constitutive_problem_stress_tangent(U)
+    idx = pat.local_int_indices
+    cb, sp = oracle.reduction(op.c0[idx], op.phi[idx], op.psi[idx], lam, "B")
+    u_ov = U.reshape(-1, order="F")[pat.overlap_global_dofs]
+    E = oracle.strain_2d(pat.dphi1, pat.dphi2, u_ov, pat.overlap_element_dof_lids, pat.n_q)
+    S, DS = oracle.constitutive_2d(E.T, cb, sp, op.shear[idx], op.bulk[idx], op.lame[idx])
+    plastic = np.mean(np.abs(DS[1] - op.lame[idx]) > 1e-9 * op.lame[idx])
+    assert 0.02 < plastic < 0.8
+    assert rel_err(np.asarray(op._owned_local_S), S) <= PLAIN_RTOL
+    assert rel_err(np.asarray(op._owned_local_DS), DS) <= PLAIN_RTOL
+    F = op.build_F_local()
+    f_ov = oracle.overlap_force_2d(pat.dphi1, pat.dphi2, np.ascontiguousarray(S[:3].T), pat.overlap_assembly_weight,
+                                   pat.overlap_element_dof_lids, pat.n_q, pat.overlap_global_dofs.size)
+    F_o = f_ov[pat.owned_local_overlap_dofs]
+    F_o[~pat.owned_free_mask] = 0.0
+    assert rel_err(F, F_o) <= PLAIN_RTOL
+    _, _, kv = op.build_K_regularized(r).getValuesCSR()
+    kv = kv.copy()
+    pb = _PatternBuild(mesh.elem, mesh.q_mask, (0, mesh.n_nodes))
+    scatter = pb.get("scatter_map")
+    pb.close()
+    K_o = oracle.tangent_scatter(2, pat.dphi1, pat.dphi2, None, np.ascontiguousarray(DS.T), pat.overlap_assembly_weight,
+                                 scatter, pat.n_q, pat.nnz)
+    K_o[pat.constrained_diag_positions] = 1.0
+    K_o = (1.0 - r) * K_o + r * pat.elastic_values
+    assert rel_err(kv, K_o) <= PLAIN_RTOL
+    op.tangent_form = "mixed"
+    op.constitutive_problem_stress_tangent(U)
+    _, _, km = op.build_K_regularized(r).getValuesCSR()
+    err = rel_err(km, kv)
+    print(f"2D {et}: plastic fraction {plastic:.3f}, mixed tangent error {err:.3e}")
+    assert err <= 1.0e-6
+
+
 def _slope_operator(et, nx, ny, nz, materials=None, lam=1.1):
     from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
 

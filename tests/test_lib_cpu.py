@@ -105,8 +105,10 @@ def test_quadrature_and_basis_match_reference_dphi(oracle):
 
     for name in golden_files("pattern2d_"):
         g = golden(name)
-        xi, wf = fem.quadrature(2, "P2")
-        (d1, d2), w = oracle.geometry(g["coord"], g["elem"][:, g["overlap_elements"]], 2, fem.reference_gradients(2, "P2"), wf)
+        et = str(g["elem_type"])
+        xi, wf = fem.quadrature(2, et)
+        (d1, d2), w = oracle.geometry(g["coord"], g["elem"][:, g["overlap_elements"]], 2, fem.reference_gradients(2, et), wf)
+        assert np.max(np.abs(d2 - g["dphi2"])) <= 1e-12 * np.max(np.abs(g["dphi2"]))
         assert np.max(np.abs(d1 - g["dphi1"])) <= 1e-12 * np.max(np.abs(g["dphi1"]))
         assert np.max(np.abs(w - g["weight"])) <= 1e-12 * np.max(np.abs(g["weight"]))
 
@@ -130,3 +132,16 @@ def test_operator_api_surface_without_a_gpu():
         assert callable(getattr(ConstitutiveOperator, name)), name
     assert list(inspect.signature(ConstitutiveOperator.build_F_K_regularized_all_free).parameters) == \
         ["self", "lam", "U", "r"]
+
+
+@pytest.mark.parametrize("name", [n for n in golden_files("pattern2d_") if "P4" in n])
+def test_triangle_p4_node_order_matches_reference_generator(name):
+    """The reference's P4 triangle mesh places local node k at the barycentric point
+    tri_node_tuples(4)[k] / 4 of its vertices, as the synthetic generator here does."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    tup = np.asarray(synthetic.tri_node_tuples(4), dtype=np.float64) / 4.0
+    for coord, elem in ((golden(name)["coord"], golden(name)["elem"]),
+                        (lambda m: (m.coord, m.elem))(synthetic.slope_mesh_2d(4, 3, elem_type="P4"))):
+        X = coord[:, elem]
+        assert np.max(np.abs(np.einsum("dve,kv->dke", X[:, :3], tup) - X)) <= 1e-12 * np.max(np.abs(coord))
