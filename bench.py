@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="3d_p2_homo")
+    ap.add_argument("--mesh", default=None, help="a gmsh .msh tet4 file as the workload (overrides --config)")
+    ap.add_argument("--mesh-elem", default="P2", choices=["P1", "P2", "P4"], help="element order for --mesh")
     ap.add_argument("--form", default="plain", choices=["plain", "mixed"],
                     help="plain: FP64 tangent (the drop-in); mixed: FP32 plastic-point products")
     ap.add_argument("--return-mapping", default="binned", choices=["binned", "unsorted", "learned"],
@@ -548,6 +550,10 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.mesh:
+        from slope_stability_petsc4py_gb300 import synthetic
+
+        args.config = synthetic.register_mesh_file(args.mesh, elem_type=args.mesh_elem)
     if args.impl == "reference":
         run_reference(args)
     else:

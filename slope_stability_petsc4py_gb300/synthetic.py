@@ -6,11 +6,15 @@ package, so the workloads here are structured stand-ins with the same geometry:
 
 * 2D: a structured quad grid mapped onto the slope profile, each quad split into two
   triangles, elevated to 6-node P2 triangles (node order of
-  ``src/slope_stability/fem/basis.py:21-56``: vertices, then edges (1,2), (0,2), (0,1)).
+  ``src/slope_stability/fem/basis.py:21-56``: vertices, then edges (1,2), (0,2), (0,1)) or
+  15-node P4 triangles (node order of ``src/slope_stability/mesh/textmesh_2d.py:116-184``).
 * 3D: the same profile extruded ``depth`` metres in z, each hexahedral cell split into six
   tetrahedra along its main diagonal (a conforming Freudenthal split), elevated to P2
   (edge order of ``src/slope_stability/core/simplex_lagrange.py:11``) or P4 (node tuples of
   ``simplex_lagrange.py:50-83``).
+
+A gmsh tet4 file (the reference's own slope meshes, for instance) becomes a workload through
+``register_mesh_file`` (read and elevated by ``mesh_io``).
 
 Displacements are a gravity-loaded, elastic-like settlement field plus a ``tanh`` shear
 band of width ``band_width`` along a 30 degree plane through the toe, with an amplitude
@@ -22,6 +26,7 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 from functools import lru_cache
 from itertools import permutations
+from pathlib import Path
 
 import numpy as np
 
@@ -367,9 +372,28 @@ CONFIGS = {
 }
 
 
+def register_mesh_file(path, *, elem_type: str = "P2", amplitude: float = 0.003, name: str | None = None) -> str:
+    """Make a gmsh tet4 file (e.g. one of the reference's slope meshes) a named workload: its
+    tetrahedra elevated to ``elem_type``, its material ids as the layers of the seeded layered
+    material set, and the same synthetic gravity + shear-band displacement as the other workloads."""
+    from .mesh_io import load_mesh_file
+
+    et = str(elem_type).upper()
+    data = load_mesh_file(path, elem_type=et)
+    key = name or f"file:{Path(path).stem}:{et.lower()}"
+    n_mat = int(data.material.max()) + 1 if data.material.size else 1
+    CONFIGS[key] = dict(dim=3, elem_type=et, amplitude=float(amplitude), n_layers=max(n_mat, 1), mesh=data)
+    return key
+
+
 def build_config_mesh(name: str) -> SlopeMesh:
     cfg = dict(CONFIGS[name])
     cfg.pop("amplitude", None)
+    if "mesh" in cfg:
+        d = cfg["mesh"]
+        depth = float(d.coord[2].max() - d.coord[2].min()) if d.coord.size else 0.0
+        return SlopeMesh(3, cfg["elem_type"], d.coord, d.elem, d.q_mask, np.asarray(d.material, dtype=np.int64),
+                         {"depth": depth})
     if cfg.pop("dim") == 2:
         return slope_mesh_2d(cfg["nx"], cfg["ny"], elem_type=cfg["elem_type"], n_layers=cfg["n_layers"])
     return slope_mesh_3d(cfg["nx"], cfg["ny"], cfg["nz"], elem_type=cfg["elem_type"], n_layers=cfg["n_layers"])

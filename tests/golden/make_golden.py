@@ -478,7 +478,79 @@ def gen_bddc(ref, kern):
         print("bddc", name, pat.local_matrix_pattern.nnz, "nnz", pat.local_elements.size, "elements")
 
 
-GENERATORS = ("constitutive_3d", "constitutive_2d", "reduction", "patterns", "pattern_2d", "pattern_2d_p4", "bddc")
+def gmsh_like_tet4_mesh(seed=23):
+    """A tet4 box mesh numbered the way a mesh file may be: shuffled vertex ids, shuffled element
+    order, rotated vertex order per tet; boundary triangles labelled by box face (1: x=0, 2: x=max,
+    3: z=0, 4: z=max, 5: y=0, 6: top) and two material ids."""
+    from itertools import combinations
+
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    rng = np.random.default_rng(seed)
+    m = synthetic.slope_mesh_3d(3, 2, 2, depth=6.0, elem_type="P1")
+    n_v = m.coord.shape[1]
+    perm = rng.permutation(n_v)
+    coord = np.empty_like(m.coord)
+    coord[:, perm] = m.coord
+    tet = perm[m.elem][:, rng.permutation(m.elem.shape[1])]
+    rot = rng.integers(0, 4, tet.shape[1])
+    tet = np.stack([np.roll(tet[:, e], rot[e]) for e in range(tet.shape[1])], axis=1)
+    faces = {}
+    for e in range(tet.shape[1]):
+        for f in combinations(range(4), 3):
+            key = tuple(sorted(tet[list(f), e]))
+            faces[key] = (faces.get(key, (0, None))[0] + 1, tet[list(f), e])
+    tris, labels = [], []
+    x_max, z_max = coord[0].max(), coord[2].max()
+    for key, (count, local) in faces.items():
+        if count != 1:
+            continue
+        c = coord[:, list(key)]
+        if np.all(c[0] < 1e-9):
+            lab = 1
+        elif np.all(c[0] > x_max - 1e-9):
+            lab = 2
+        elif np.all(c[2] < 1e-9):
+            lab = 3
+        elif np.all(c[2] > z_max - 1e-9):
+            lab = 4
+        elif np.all(c[1] < 1e-9):
+            lab = 5
+        else:
+            lab = 6
+        tris.append(local)
+        labels.append(lab)
+    order = rng.permutation(len(tris))
+    tri = np.stack(tris, axis=1)[:, order]
+    boundary = np.asarray(labels, dtype=np.int64)[order]
+    material = (np.arange(tet.shape[1]) % 3).astype(np.int64)
+    return coord, tet.astype(np.int64), tri.astype(np.int64), boundary, material
+
+
+def gen_mesh_io(ref):
+    """Tet4 -> tet10 / tet35 elevation and Dirichlet masks of the reference's gmsh loader
+    (``io.py:61-93, 216-398``) on a file-like numbered tet4 mesh."""
+    io = importlib.import_module("slope_stability.io")
+    coord, tet, tri, boundary, material = gmsh_like_tet4_mesh()
+    out = {"coord": coord, "tet4": tet, "tri3": tri, "boundary": boundary, "material": material}
+    where = Path("/tmp/not_a_mesh_family/mesh.msh")  # outside the reference's meshes: default labels
+    for order, fn in ((2, io._elevate_tet4_mesh_to_tet10), (4, io._elevate_tet4_mesh_to_tet35)):
+        c, e, s = fn(coord, tet, tri)
+        out[f"coord_p{order}"], out[f"elem_p{order}"], out[f"surf_p{order}"] = c, e, s
+        for bt in (0, 1):
+            out[f"q_mask_p{order}_bt{bt}"] = io._build_dirichlet_mask(3, c.shape[1], s, boundary, path=where,
+                                                                     boundary_type=bt)
+    out["q_mask_p1_bt0"] = io._build_dirichlet_mask(3, coord.shape[1], tri, boundary, path=where, boundary_type=0)
+    field = {"boundary_0": np.array([11, 2]), "boundary_1": np.array([12, 2]), "material_0": np.array([7, 3]),
+             "material_1": np.array([8, 3]), "other": np.array([9, 3])}
+    out["physical_tags"] = np.array([12, 11, 11, 12], dtype=np.int64)
+    out["physical_mapped"] = io._map_physical_ids(out["physical_tags"], field, 2, "boundary")
+    np.savez_compressed(HERE / "mesh_io.npz", **out)
+    print("mesh_io", tet.shape[1], "tets", tri.shape[1], "boundary triangles")
+
+
+GENERATORS = ("constitutive_3d", "constitutive_2d", "reduction", "patterns", "pattern_2d", "pattern_2d_p4", "bddc",
+              "mesh_io")
 
 
 def main(which=GENERATORS):
@@ -502,6 +574,8 @@ def main(which=GENERATORS):
         gen_pattern_2d_p4(ref)
     if "bddc" in which:
         gen_bddc(ref, kern)
+    if "mesh_io" in which:
+        gen_mesh_io(ref)
 
 
 if __name__ == "__main__":
