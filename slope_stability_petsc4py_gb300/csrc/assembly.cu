@@ -453,16 +453,18 @@ template <int DIM, int NP, int NQ, bool MIXED>
 struct WarpSlice {
     static constexpr int NS = DIM == 3 ? 6 : 3;
     static constexpr int NLD = DIM * NP;
-    struct Work {
-        double sg[MIXED ? 1 : NQ][DIM][NP];  // gradients of the contributing points (FP64 form)
-        double sD[MIXED ? 1 : NQ][NS * NS];  // w * D of the contributing points (FP64 form)
-        double sH[MIXED ? 1 : NLD * NS];     // B^T (w D) of one point (FP64 form)
-        df32 sgm[MIXED ? NQ : 1][DIM][NP];   // gradients as hi + lo (mixed form)
-        df32 sDm[MIXED ? NQ : 1][NS * NS];   // w * D as hi + lo (mixed form)
-        float2 sHhl[MIXED ? NLD * NS : 1];   // B^T (w D) of one point as hi + lo (mixed form)
+    struct WorkF64 {
+        double sg[NQ][DIM][NP];  // gradients of the contributing points
+        double sD[NQ][NS * NS];  // w * D of the contributing points
+        double sH[NLD * NS];     // B^T (w D) of one point
+    };
+    struct WorkMixed {
+        df32 sgm[NQ][DIM][NP];  // gradients as hi + lo
+        df32 sDm[NQ][NS * NS];  // w * D as hi + lo
+        float2 sHhl[NLD * NS];  // B^T (w D) of one point as hi + lo
     };
     union {
-        Work w;                            // while the products are formed
+        typename std::conditional<MIXED, WorkMixed, WorkF64>::type w;  // while the products are formed
         double sK[NLD * NLD];              // then the element's sums, staged for the row-wise scatter
     } u;
     alignas(16) int32_t smap[NLD * NLD];   // the element's row of the element->CSR map
@@ -471,53 +473,92 @@ struct WarpSlice {
 };
 
 template <int DIM, int NP, int NQ, int WARPS, bool SYM, bool CORR, bool MIXED>
-__global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(ElemArgs A) {
+__global__ void __launch_bounds__(32 * WARPS, MIXED ? 5 : 4) tangent_element_warp_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
+    // FP64 form (bound by the FP64 pipe): each lane owns PER scattered entries of K_e, which keeps
+    // 97 % of the lanes' FP64 slots busy.  Mixed form (bound by issue): each lane owns whole
+    // node-pair blocks (a, b) of DIM x DIM entries (a <= b when SYM), so it reads one row of H per
+    // block row and one gradient per direction and reuses them across the block's entries.
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
-    constexpr int PER = (NENT + 31) / 32;
+    constexpr int PER = (NENT + 31) / 32;  // entries per lane (FP64 form)
+    constexpr int NBLK = SYM ? NP * (NP + 1) / 2 : NP * NP;
+    constexpr int BPL = MIXED ? (NBLK + 31) / 32 : 1;  // blocks per lane (mixed form)
     constexpr int MAPV = NLD * NLD / 4;  // 16-byte chunks of one element's map row
     static_assert(NQ <= 32, "one branch code per lane");
     static_assert((NLD * NLD) % 4 == 0, "map rows are whole 16-byte chunks");
-    using acc_t = typename std::conditional<MIXED, float, double>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Slice = WarpSlice<DIM, NP, NQ, MIXED>;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Slice &S = reinterpret_cast<Slice *>(smem_raw)[wid];
-    double(*sg)[DIM][NP] = S.u.w.sg;
-    double(*sD)[NS * NS] = S.u.w.sD;
-    double *sH = S.u.w.sH;
-    df32(*sgm)[DIM][NP] = S.u.w.sgm;
-    df32(*sDm)[NS * NS] = S.u.w.sDm;
-    float2 *sHhl = S.u.w.sHhl;
+    double(*sg)[DIM][NP] = nullptr;  // FP64 form
+    double(*sD)[NS * NS] = nullptr;
+    double *sH = nullptr;
+    df32(*sgm)[DIM][NP] = nullptr;  // mixed form
+    df32(*sDm)[NS * NS] = nullptr;
+    float2 *sHhl = nullptr;
+    if constexpr (MIXED) {
+        sgm = S.u.w.sgm;
+        sDm = S.u.w.sDm;
+        sHhl = S.u.w.sHhl;
+    } else {
+        sg = S.u.w.sg;
+        sD = S.u.w.sD;
+        sH = S.u.w.sH;
+    }
     double *sK = S.u.sK;
     int32_t *smap = S.smap;
     double(*spt)[NQ] = S.spt;
     int *sq = S.sq;
     const bool map_aligned = (reinterpret_cast<uintptr_t>(A.emap) & 15u) == 0;
 
-    int code[PER];
+    int code[MIXED ? 1 : PER];  // FP64 form: entry alpha | beta << 8 of each of the lane's entries, or -1
+    if constexpr (!MIXED) {
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        const int id = lane + i * 32;
+        for (int i = 0; i < PER; ++i) {
+            const int id = lane + i * 32;
+            int c = -1;
+            if (id < NENT) {
+                int a, b;
+                if (SYM) {  // row-major upper triangle: row a holds NLD - a entries
+                    int rem = id;
+                    a = 0;
+                    while (rem >= NLD - a) {
+                        rem -= NLD - a;
+                        ++a;
+                    }
+                    b = a + rem;
+                } else {
+                    a = id / NLD;
+                    b = id % NLD;
+                }
+                c = a | (b << 8);
+            }
+            code[i] = c;
+        }
+    }
+    int blk[BPL];  // mixed form: node pair a | b << 8 of each of the lane's blocks, or -1
+#pragma unroll
+    for (int j = 0; j < BPL; ++j) {
+        const int id = lane + j * 32;
         int c = -1;
-        if (id < NENT) {
+        if (MIXED && id < NBLK) {
             int a, b;
-            if (SYM) {
+            if (SYM) {  // row-major upper triangle of node pairs: row a holds NP - a pairs
                 int rem = id;
                 a = 0;
-                while (rem >= NLD - a) {
-                    rem -= NLD - a;
+                while (rem >= NP - a) {
+                    rem -= NP - a;
                     ++a;
                 }
                 b = a + rem;
             } else {
-                a = id / NLD;
-                b = id % NLD;
+                a = id / NP;
+                b = id % NP;
             }
             c = a | (b << 8);
         }
-        code[i] = c;
+        blk[j] = c;
     }
 
     const long long warp_global = (long long)blockIdx.x * WARPS + wid;
@@ -579,9 +620,16 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
                 sD[k][kk] = spt[0][k] * v;
             }
         }
-        acc_t acc[PER];
+        float acc[MIXED ? BPL : 1][DIM][DIM];  // mixed form
+        double dacc[MIXED ? 1 : PER];           // FP64 form
 #pragma unroll
-        for (int i = 0; i < PER; ++i) acc[i] = acc_t(0);
+        for (int j = 0; j < (MIXED ? BPL : 1); ++j)
+#pragma unroll
+            for (int c = 0; c < DIM; ++c)
+#pragma unroll
+                for (int c2 = 0; c2 < DIM; ++c2) acc[j][c][c2] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < (MIXED ? 1 : PER); ++i) dacc[i] = 0.0;
         __syncwarp();
         for (int q = 0; q < nq; ++q) {
             for (int it = lane; it < NLD * NS; it += 32) {
@@ -606,27 +654,49 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
                 }
             }
             __syncwarp();
+            if constexpr (MIXED) {
+                // K[(a,c)][(b,c2)] += sum_r H[(a,c)][m(c2,r)] g[r][b]: per block the DIM gradients of
+                // node b and, per block row, the NS entries of H's row are read once;
+                // (Hh + Hl)(gh + gl) without the Hl gl term, FP32 accumulation
 #pragma unroll
-            for (int i = 0; i < PER; ++i) {
-                const int c = code[i];
-                if (c >= 0) {
-                    const int alpha = c & 0xff, beta = c >> 8;
-                    const int b = beta / DIM, cp = beta % DIM;
-                    acc_t v = acc[i];
+                for (int j = 0; j < BPL; ++j) {
+                    const int bc = blk[j];
+                    if (bc < 0) continue;
+                    const int a = bc & 0xff, b = bc >> 8;
+                    df32 gb[DIM];
 #pragma unroll
-                    for (int r = 0; r < DIM; ++r) {
-                        const int m = DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r);
-                        if (MIXED) {  // (Hh + Hl)(gh + gl) without the Hl gl term, FP32 accumulation
-                            const df32 gb = sgm[q][r][b];
-                            const float2 hl = sHhl[alpha * NS + m];
-                            v = fmaf(hl.x, gb.hi, v);
-                            v = fmaf(hl.y, gb.hi, v);
-                            v = fmaf(hl.x, gb.lo, v);
-                        } else {
-                            v += sH[alpha * NS + m] * sg[q][r][b];
+                    for (int r = 0; r < DIM; ++r) gb[r] = sgm[q][r][b];
+#pragma unroll
+                    for (int c = 0; c < DIM; ++c) {
+                        float2 h[NS];
+#pragma unroll
+                        for (int m = 0; m < NS; ++m) h[m] = sHhl[(a * DIM + c) * NS + m];
+#pragma unroll
+                        for (int c2 = 0; c2 < DIM; ++c2) {
+                            float v = acc[j][c][c2];
+#pragma unroll
+                            for (int r = 0; r < DIM; ++r) {
+                                const float2 hl = h[DIM == 3 ? bt_row3(c2, r) : bt_row2(c2, r)];
+                                v = fmaf(hl.x, gb[r].hi, v);
+                                v = fmaf(hl.y, gb[r].hi, v);
+                                v = fmaf(hl.x, gb[r].lo, v);
+                            }
+                            acc[j][c][c2] = v;
                         }
                     }
-                    acc[i] = v;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < PER; ++i) {
+                    const int c = code[i];
+                    if (c >= 0) {
+                        const int alpha = c & 0xff, beta = c >> 8;
+                        const int b = beta / DIM, cp = beta % DIM;
+                        double v = dacc[i];
+#pragma unroll
+                        for (int r = 0; r < DIM; ++r) v += sH[alpha * NS + (DIM == 3 ? bt_row3(cp, r) : bt_row2(cp, r))] * sg[q][r][b];
+                        dacc[i] = v;
+                    }
                 }
             }
             __syncwarp();
@@ -635,14 +705,25 @@ __global__ void __launch_bounds__(32 * WARPS, 4) tangent_element_warp_kernel(Ele
         // stage the sums (the products are done with the work buffers), then scatter every entry
         // row by row: consecutive lanes take consecutive columns of one CSR row, so a warp's
         // reductions share cache lines; SYM reads alpha > beta from the mirrored entry
+        if constexpr (MIXED) {
 #pragma unroll
-        for (int i = 0; i < PER; ++i) {
-            const int c = code[i];
-            if (c >= 0) {
-                double v;
-                if constexpr (MIXED) v = f32_widen(acc[i]);  // exact, on the integer pipe
-                else v = acc[i];
-                sK[(c & 0xff) * NLD + (c >> 8)] = v;
+            for (int j = 0; j < BPL; ++j) {
+                const int bc = blk[j];
+                if (bc < 0) continue;
+                const int a = bc & 0xff, b = bc >> 8;
+#pragma unroll
+                for (int c = 0; c < DIM; ++c)
+#pragma unroll
+                    for (int c2 = 0; c2 < DIM; ++c2) {
+                        if (SYM && a == b && c2 < c) continue;  // below the diagonal: mirrored in the scatter
+                        sK[(a * DIM + c) * NLD + b * DIM + c2] = f32_widen(acc[j][c][c2]);  // exact, integer pipe
+                    }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const int c = code[i];
+                if (c >= 0) sK[(c & 0xff) * NLD + (c >> 8)] = dacc[i];
             }
         }
         __syncwarp();
@@ -803,6 +884,10 @@ int launch_element_warp(const ElemArgs &a, cudaStream_t st) {
     auto kernel = tangent_element_warp_kernel<DIM, NP, NQ, WARPS, SYM, CORR, MIXED>;
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
         cudaSuccess)
+        return SSP_ERR_CUDA;
+    // the mixed form fits five CTAs per SM when the unified L1 / shared memory is mostly shared
+    if (MIXED && cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxShared) != cudaSuccess)
         return SSP_ERR_CUDA;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
