@@ -83,6 +83,8 @@ __global__ void __launch_bounds__(128) strain3_mixed_kernel(const float2 *__rest
 
 // Force from hi + lo pairs of w * dphi (split once per pattern) and of the stresses, which the block
 // splits itself into shared memory for the elements its threads cover (each stress value once).
+// One thread per (element, node) accumulates the node's three displacement components, so each
+// w * dphi value is loaded once.
 constexpr int kForceThreads = 128, kForceMaxStress = 6 * 24 * 8;  // up to 8 elements of 24 points
 __global__ void __launch_bounds__(kForceThreads) force3_mixed_kernel(const float2 *__restrict__ wg1,
                                                                      const float2 *__restrict__ wg2,
@@ -92,10 +94,9 @@ __global__ void __launch_bounds__(kForceThreads) force3_mixed_kernel(const float
                                                                      int n_elem, int n_p, int n_q,
                                                                      double *__restrict__ F) {
     __shared__ float2 s_hl[kForceMaxStress];
-    const int nld = 3 * n_p;
     const long long t0 = (long long)blockIdx.x * kForceThreads;
-    const long long e_first = t0 / nld;
-    long long e_last = (t0 + kForceThreads - 1) / nld;
+    const long long e_first = t0 / n_p;
+    long long e_last = (t0 + kForceThreads - 1) / n_p;
     if (e_last >= n_elem) e_last = n_elem - 1;
     const int n_vals = static_cast<int>(e_last - e_first + 1) * n_q * 6;  // <= kForceMaxStress (host check)
     const double *Sb = S + e_first * n_q * 6;
@@ -105,28 +106,36 @@ __global__ void __launch_bounds__(kForceThreads) force3_mixed_kernel(const float
     }
     __syncthreads();
     const long long t = t0 + threadIdx.x;
-    if (t >= (long long)n_elem * nld) return;
-    const long long e = t / nld;
-    const int alpha = static_cast<int>(t % nld);
-    const int row = elem_row[t];
-    if (row < 0) return;
-    if (row >= n_rows) {
+    if (t >= (long long)n_elem * n_p) return;
+    const long long e = t / n_p;
+    const int node = static_cast<int>(t % n_p);
+    const int32_t *er = elem_row + (e * n_p + node) * 3;
+    const int r0 = er[0], r1 = er[1], r2 = er[2];
+    if (r0 < 0 && r1 < 0 && r2 < 0) return;
+    if (r0 >= n_rows || r1 >= n_rows || r2 >= n_rows) {
         flag(SSP_DEV_BAD_INDEX);
         return;
     }
-    const int node = alpha / 3, comp = alpha % 3;
-    // the stress components multiplying d/dx, d/dy, d/dz for this displacement component
-    const int k0 = bt_row3(comp, 0), k1 = bt_row3(comp, 1), k2 = bt_row3(comp, 2);
     const float2 *sl = s_hl + (e - e_first) * n_q * 6;
-    CSum acc;
+    // component c sums d/dx, d/dy, d/dz times the stresses bt_row3(c, 0..2): {0,3,5}, {3,1,4}, {5,4,2}
+    CSum a0, a1, a2;
     for (int q = 0; q < n_q; ++q) {
-        const long long g = e * n_q + q;
+        const long long g = (e * n_q + q) * n_p + node;
+        const df32 x = ld(wg1 + g), y = ld(wg2 + g), z = ld(wg3 + g);
         const float2 *sq = sl + 6 * q;
-        acc.add_prod(ld(wg1 + g * n_p + node), ld(sq + k0));
-        acc.add_prod(ld(wg2 + g * n_p + node), ld(sq + k1));
-        acc.add_prod(ld(wg3 + g * n_p + node), ld(sq + k2));
+        a0.add_prod(x, ld(sq + 0));
+        a0.add_prod(y, ld(sq + 3));
+        a0.add_prod(z, ld(sq + 5));
+        a1.add_prod(x, ld(sq + 3));
+        a1.add_prod(y, ld(sq + 1));
+        a1.add_prod(z, ld(sq + 4));
+        a2.add_prod(x, ld(sq + 5));
+        a2.add_prod(y, ld(sq + 4));
+        a2.add_prod(z, ld(sq + 2));
     }
-    red_add(F + row, acc.value());
+    if (r0 >= 0) red_add(F + r0, a0.value());
+    if (r1 >= 0) red_add(F + r1, a1.value());
+    if (r2 >= 0) red_add(F + r2, a2.value());
 }
 
 }  // namespace
@@ -162,14 +171,14 @@ int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2
                                      const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                      int n_rows, double *out_values, void *stream) {
     if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
-    // a block's threads cover at most 128 / (3 n_p) + 2 elements, whose stresses it stages
-    if ((kForceThreads / (3 * n_p) + 2) * n_q * 6 > kForceMaxStress) return SSP_ERR_UNSUPPORTED;
+    // a block's threads cover at most 128 / n_p + 2 elements, whose stresses it stages
+    if ((kForceThreads / n_p + 2) * n_q * 6 > kForceMaxStress) return SSP_ERR_UNSUPPORTED;
     if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
     cudaStream_t st = as_stream(stream);
     if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
     if (n_elem == 0) return SSP_OK;
     if (!wdphi1_hl || !wdphi2_hl || !wdphi3_hl || !stress || !elem_row) return SSP_ERR_INVALID;
-    const long long n = (long long)n_elem * 3 * n_p;
+    const long long n = (long long)n_elem * n_p;
     force3_mixed_kernel<<<grid_for(n, kForceThreads), kForceThreads, 0, st>>>(
         reinterpret_cast<const float2 *>(wdphi1_hl), reinterpret_cast<const float2 *>(wdphi2_hl),
         reinterpret_cast<const float2 *>(wdphi3_hl), stress, elem_row, n_rows, n_elem, n_p, n_q, out_values);
