@@ -69,6 +69,7 @@ def parse():
                     help="binned: two-pass exact binning; unsorted: one divergent pass; learned: bins proposed "
                          "by the branch network (trained on the GPU before the timed region)")
     ap.add_argument("--no-forms", action="store_true", help="skip timing the mixed / learned / unsorted forms")
+    ap.add_argument("--bddc", action="store_true", help="also time the BDDC subdomain tangent of half the mesh")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
@@ -340,6 +341,42 @@ def compare_forms(torch, lib, op, mesh, mats, args, step, ms_plain):
     return out
 
 
+def measure_bddc(torch, lib, op, mesh, specs, args, step):
+    """BDDC subdomain tangent of the workload's state: the subdomain owning the elements of the
+    lower half of the node range (prepare_bddc_subdomain_pattern), one regularised subdomain build
+    per Newton iteration after the owned evaluation; timed with the elastic predictor + plastic
+    corrections (FP64 and mixed), and with the full contraction of every subdomain point."""
+    from slope_stability_petsc4py_gb300 import prepare_bddc_subdomain_pattern
+
+    owners = np.sort(mesh.elem.min(axis=0))
+    owned = (0, int(owners[owners.size // 2]))
+    t0 = time.perf_counter()
+    pat = prepare_bddc_subdomain_pattern(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, owned,
+                                         elem_type=mesh.elem_type,
+                                         overlap_local_int_indices=op.owned_tangent_pattern.local_int_indices)
+    prep_s = time.perf_counter() - t0
+    op.set_bddc_subdomain_pattern(pat)
+    w = max(args.warmup, 3)
+    out = {"subdomain_elements": int(pat.local_elements.size), "subdomain_points": pat.n_local_int,
+           "nnz": pat.nnz, "owned_node_range": list(owned), "prepare_s": prep_s}
+    for name, form in (("plain", "plain"), ("mixed", "mixed")):
+        op.tangent_form = form
+        step()
+        ms = time_steps(torch, lambda: op._build_bddc_regularized_matrix(R_REG), w, args.steps)
+        out[name] = {"ms_per_build": ms, "subdomain_quad_pts_per_s": pat.n_local_int / (ms * 1e-3),
+                     "assembled_nnz_per_s": pat.nnz / (ms * 1e-3)}
+    op.tangent_form = "plain"
+    step()
+    kp = op._build_bddc_regularized_matrix(R_REG).values.clone()
+    op._bddc["predictor_ok"] = False  # time the full contraction of every subdomain point
+    ms = time_steps(torch, lambda: op._build_bddc_regularized_matrix(R_REG), w, args.steps)
+    kf = op._build_bddc_regularized_matrix(R_REG).values
+    out["full_contraction"] = {"ms_per_build": ms, "max_rel_diff_vs_predictor": float((kf - kp).abs().max() / kp.abs().max())}
+    op.set_bddc_subdomain_pattern(None)
+    lib.raise_on_device_status()
+    return out
+
+
 def train_branch_model(torch, op, mesh, mats, name):
     """Train the branch-proposal network on continuation states other than the timed one
     (strength-reduction factors 1.0..1.4, shear-band amplitudes 0.4..1.6 x the workload's)."""
@@ -489,6 +526,8 @@ def run_gpu(args):
 
     if args.form == "plain" and args.return_mapping == "binned" and pat.dim == 3 and not args.no_forms:
         line["forms"] = compare_forms(torch, _lib, op, mesh, mats, args, step, ms)
+    if args.bddc:
+        line["bddc"] = measure_bddc(torch, _lib, op, mesh, specs, args, step)
 
     if rank == 0 and not args.no_e2e:
         op.host_outputs = True

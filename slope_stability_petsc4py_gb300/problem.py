@@ -805,13 +805,62 @@ class ConstitutiveOperator:
             self._bddc[kind + "_mat"].fence()
         return buf
 
-    def _build_bddc_tangent_matrix(self, *, local_mat_type: str = "aij"):
-        """Subdomain tangent (problem.py:1710-1767); ``local_mat_type`` is accepted for compatibility."""
+    def _bddc_predictor_ok(self, pattern) -> bool:
+        """Whether the subdomain tangent may start from the pattern's elastic values: the subdomain's
+        DS rows come from this operator's own evaluation (symmetric, branch codes known) and the
+        pattern's elastic moduli are the operator's at the same points (checked once per pattern)."""
+        if self._branch is None or not self._ds_symmetric or self._DS_aos is None:
+            return False
+        if "predictor_ok" not in self._bddc:
+            t = _lib.torch()
+            d, pos = pattern.device, pattern.device.get("overlap_positions")
+            ok = pos is not None and "shear" in d and "lame" in d
+            if ok:
+                ok = bool(t.equal(self._dev["shear"].index_select(0, pos), d["shear"])) and bool(
+                    t.equal(self._dev["lame"].index_select(0, pos), d["lame"]))
+            self._bddc["predictor_ok"] = ok
+        return self._bddc["predictor_ok"]
+
+    def _bddc_tangent_into(self, values, r=None):
+        """Subdomain tangent values into ``values``; with r, the regularised (1-r) K + r K_el.
+
+        When the elastic predictor applies (_bddc_predictor_ok), the elastic subdomain values plus
+        the plastic elements' corrections B^T w (DS - D_el) B scaled by (1-r) -- the owned path's
+        assembly, FP64 or mixed-precision by ``tangent_form``; otherwise the full element contraction
+        of every subdomain point (problem.py:1710-1857)."""
         from .bddc import bddc_tangent_values_device
 
         pattern = self._bddc_pattern()
+        ds = self._bddc_local_DS()
+        d, st = pattern.device, _lib.stream_handle()
+        n_el = int(pattern.local_elements.size)
+        if n_el and self._bddc_predictor_ok(pattern):
+            t = _lib.torch()
+            branch = self._branch.index_select(0, d["overlap_positions"])
+            if "plastic_list" not in self._bddc:
+                self._bddc["plastic_list"] = (t.empty(n_el, dtype=t.int32, device="cuda"),
+                                              t.empty(1, dtype=t.int32, device="cuda"))
+            elist, ecount = self._bddc["plastic_list"]
+            values.copy_(d["elastic_values"])
+            _lib.call("ssp_plastic_elements", _lib.ptr(branch), n_el, pattern.n_q, _lib.ptr(elist), _lib.ptr(ecount), st)
+            mixed = self.tangent_form == "mixed" and (pattern.dim, pattern.n_p) in MIXED_TANGENT_ELEMENTS
+            entry = "ssp_tangent_plastic_correction_mixed" if mixed else "ssp_tangent_plastic_correction"
+            _lib.call(entry, pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
+                      _lib.ptr(d["dphi3"]) if pattern.dim == 3 else None, _lib.ptr(ds), _lib.ptr(d["weight"]),
+                      _lib.ptr(branch), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), _lib.ptr(d["scatter_map"]), n_el,
+                      pattern.n_p, pattern.n_q, pattern.nnz, 1.0 if r is None else 1.0 - float(r), _lib.ptr(values),
+                      _lib.ptr(elist), _lib.ptr(ecount), st)
+            return values
+        bddc_tangent_values_device(pattern, ds, out=values)
+        if r is not None and pattern.nnz:
+            _lib.call("ssp_finish_values", _lib.ptr(values), pattern.nnz, None, 0, _lib.ptr(d["elastic_values"]),
+                      float(r), st)
+        return values
+
+    def _build_bddc_tangent_matrix(self, *, local_mat_type: str = "aij"):
+        """Subdomain tangent (problem.py:1710-1767); ``local_mat_type`` is accepted for compatibility."""
         t0 = perf_counter()
-        vals = bddc_tangent_values_device(pattern, self._bddc_local_DS(), out=self._bddc_values("tangent"))
+        vals = self._bddc_tangent_into(self._bddc_values("tangent"))
         self.time_build_tangent_local.append(perf_counter() - t0)
         return self._bddc_matrix("tangent", vals)
 
@@ -824,13 +873,8 @@ class ConstitutiveOperator:
 
     def _build_bddc_regularized_matrix(self, r: float, *, local_mat_type: str = "aij"):
         """(1-r) K_tangent + r K_elastic on the subdomain pattern (problem.py:1803-1857)."""
-        from .bddc import bddc_tangent_values_device
-
-        pattern = self._bddc_pattern()
         t0 = perf_counter()
-        vals = bddc_tangent_values_device(pattern, self._bddc_local_DS(), out=self._bddc_values("regularized"))
-        _lib.call("ssp_finish_values", _lib.ptr(vals), pattern.nnz, None, 0, _lib.ptr(pattern.device["elastic_values"]),
-                  float(r), _lib.stream_handle())
+        vals = self._bddc_tangent_into(self._bddc_values("regularized"), r=r)
         self.time_build_tangent_local.append(perf_counter() - t0)
         return self._bddc_matrix("regularized", vals)
 

@@ -112,4 +112,38 @@ def test_operator_bddc_matrices_against_oracle(oracle, dim, et):
     op.reduction(1.0)
     op.constitutive_problem_stress_tangent(U)
     assert op._build_bddc_tangent_matrix().handle == handle  # updated in place
+    # the mixed form (plastic corrections in compensated FP32) against the FP64 tangent
+    op.reduction(1.2)
+    op.tangent_form = "mixed"
+    op.constitutive_problem_stress_tangent(U)
+    _, _, km = op._build_bddc_regularized_matrix(r).getValuesCSR()
+    err = rel_err(km, (1.0 - r) * K_o + r * pat.elastic_values)
+    print(f"BDDC {dim}D {et}: mixed regularised subdomain tangent error {err:.2e}")
+    assert err <= 1.0e-6
     op.release_petsc_caches()
+
+
+def test_bddc_predictor_needs_matching_moduli(oracle):
+    """A subdomain pattern prepared with other elastic moduli than the operator's: the subdomain
+    tangent falls back to the full contraction of the operator's DS (still the reference's result)."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, prepare_bddc_subdomain_pattern, synthetic
+
+    mats = synthetic.MaterialSet.layered(4, seed=5)
+    mesh = synthetic.slope_mesh_3d(6, 3, 3, elem_type="P2", n_layers=4)
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
+    other = [dict(sp, young=1.5 * sp["young"]) for sp in specs]
+    pat = prepare_bddc_subdomain_pattern(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, other,
+                                         (0, mesh.n_nodes), elem_type="P2",
+                                         overlap_local_int_indices=op.owned_tangent_pattern.local_int_indices)
+    op.set_bddc_subdomain_pattern(pat)
+    op.reduction(1.2)
+    op.constitutive_problem_stress_tangent(synthetic.displacement_field(mesh, mats, amplitude=0.05, seed=7))
+    DS = np.asarray(op._owned_local_DS)[:, pat.overlap_local_positions]
+    K_o = oracle.tangent_scatter(3, pat.dphi1, pat.dphi2, pat.dphi3, np.ascontiguousarray(DS.T),
+                                 pat.local_assembly_weight, pat.scatter_map, pat.n_q, pat.nnz)
+    K_o[pat.constrained_diag_positions] = 1.0
+    _, _, vals = op._build_bddc_tangent_matrix().getValuesCSR()
+    assert not op._bddc["predictor_ok"]
+    assert rel_err(vals, K_o) <= PLAIN_RTOL
