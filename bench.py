@@ -283,6 +283,10 @@ def algorithmic(name, st):
     if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d", "ssp_assemble_overlap_strain_3d_mixed"):
         fp64 = 0 if name.endswith("_mixed") else n * 2 * 9 * n_p  # the mixed kernel's products are FP32
         return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": fp64}
+    if name == "ssp_assemble_overlap_strain_3d_affine_mixed":  # J^{-1} per element instead of per-point gradients
+        return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": 0}
+    if name == "ssp_assemble_force_element_affine_mixed":
+        return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": 0}
     if name in ("ssp_assemble_force_element", "ssp_assemble_force_element_mixed"):
         fp64 = 0 if name.endswith("_mixed") else n * nld * 8
         return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": fp64}

@@ -167,6 +167,18 @@ int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2
                                      const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                      int n_rows, double *out_values, void *stream);
 
+/* The same strain and force for affine (straight-sided) tetrahedra, whose gradients are
+ * J^{-T} ghat(q): jinv_hl [n_elem][3][3] hi + lo pairs of each element's J^{-1} (row-major),
+ * ghat_hl [n_q][n_p][3] hi + lo pairs of the reference-element gradient table, w_hl [n_int] of the
+ * point weights.  Reads 9 pairs per element instead of 3 n_p pairs per point; the caller checks
+ * that its elements are affine.  No reference counterpart. */
+int ssp_assemble_overlap_strain_3d_affine_mixed(const float *jinv_hl, const float *ghat_hl, const float *u_hl, int n_u,
+                                                const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                                double *out_values, void *stream);
+int ssp_assemble_force_element_affine_mixed(const float *jinv_hl, const float *ghat_hl, const float *w_hl,
+                                            const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                            int n_rows, double *out_values, void *stream);
+
 /* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
  * Deterministic row gather; rows without slots come out 0. */
 int ssp_assemble_force_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *stress,

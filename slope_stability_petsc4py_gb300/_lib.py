@@ -50,6 +50,8 @@ _SIGS = {
     "ssp_assemble_force_element": [_c_int] + [_vp] * 6 + [_c_int] * 4 + [_vp, _vp],
     "ssp_assemble_overlap_strain_3d_mixed": [_vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_force_element_mixed": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
+    "ssp_assemble_overlap_strain_3d_affine_mixed": [_vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_force_element_affine_mixed": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
     "ssp_split_f64": [_vp, _vp, _c_ll, _c_int, _vp, _vp],
     "ssp_assemble_tangent_values_3d_rows": [_vp] * 9 + [_c_int] * 6 + [_vp, _vp],
     "ssp_assemble_tangent_values_3d_p2": [_vp] * 6 + [_c_int] * 5 + [_vp, _vp],
@@ -118,6 +120,7 @@ _KERNELS_PER_CALL = {
     "ssp_copy_out": 1, "ssp_host_writable": 0, "ssp_plastic_elements": 1, "ssp_mark_element_rows": 1,
     "ssp_copy_rows_out": 1,
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
+    "ssp_assemble_overlap_strain_3d_affine_mixed": 1, "ssp_assemble_force_element_affine_mixed": 1,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_constitutive_3d_sds_binned_mixed": 3, "ssp_constitutive_3d_sds_learned_mixed": 4,

@@ -138,6 +138,167 @@ __global__ void __launch_bounds__(kForceThreads) force3_mixed_kernel(const float
     if (r2 >= 0) red_add(F + r2, a2.value());
 }
 
+// Affine elements (straight-sided tetrahedra, every point with the same Jacobian J): the gradients
+// are dphi_a(q) = J^{-T} ghat_a(q) with ghat the reference-element table, the same for every
+// element.  The kernels below read J^{-1} once per element (9 hi + lo pairs) and the table from
+// shared memory instead of the per-point gradients (3 n_p hi + lo pairs per point), at the cost
+// of the product with J^{-1}.  ghat: [n_q][n_p][3] hi + lo pairs; jinv: [n_elem][3][3] row-major.
+
+// Strain: grad u = G J^{-1} with G_ik = sum_{a>=1} (u_a - u_0)_i ghat_a,k(q) (rigid translation
+// removed as in strain3_mixed_kernel); E = the engineering strains of grad u, each a compensated
+// sum of its 3 or 6 products G_ik J^{-1}_kj.
+__global__ void __launch_bounds__(128) strain3_affine_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                   const float2 *__restrict__ ghat,
+                                                                   const float2 *__restrict__ u,
+                                                                   const int32_t *__restrict__ dof, long long n_u,
+                                                                   int n_elem, int n_p, int n_q,
+                                                                   double *__restrict__ E) {
+    // shared: the reference table, then the displacements of the elements the block's points
+    // belong to (gathered once per element instead of once per point)
+    extern __shared__ float2 s_dyn[];
+    float2 *s_ghat = s_dyn;                // n_q * n_p * 3
+    float2 *s_u = s_dyn + n_q * n_p * 3;   // (elements of the block) * 3 n_p
+    for (int i = threadIdx.x; i < n_q * n_p * 3; i += blockDim.x) s_ghat[i] = ghat[i];
+    const int nld = 3 * n_p;
+    const long long g0 = (long long)blockIdx.x * blockDim.x;
+    const long long e_first = g0 / n_q;
+    long long e_last = (g0 + blockDim.x - 1) / n_q;
+    if (e_last >= n_elem) e_last = n_elem - 1;
+    const int n_vals = static_cast<int>(e_last - e_first + 1) * nld;
+    bool bad = false;
+    for (int i = threadIdx.x; i < n_vals; i += blockDim.x) {
+        const int32_t lid = dof[e_first * nld + i];
+        if (lid < 0 || lid >= n_u) {
+            bad = true;
+            s_u[i] = make_float2(0.0f, 0.0f);
+        } else {
+            s_u[i] = u[lid];
+        }
+    }
+    if (bad) flag(SSP_DEV_BAD_INDEX);
+    __syncthreads();
+    const long long g = g0 + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const long long e = g / n_q;
+    const int q = static_cast<int>(g - e * n_q);
+    const float2 *ue = s_u + (e - e_first) * nld;
+    const df32 u0x = df_neg(ld(ue)), u0y = df_neg(ld(ue + 1)), u0z = df_neg(ld(ue + 2));
+    CSum G[3][3];
+    const float2 *gq = s_ghat + q * n_p * 3;
+    for (int a = 1; a < n_p; ++a) {
+        const df32 du[3] = {df_add(ld(ue + 3 * a), u0x), df_add(ld(ue + 3 * a + 1), u0y),
+                            df_add(ld(ue + 3 * a + 2), u0z)};
+        const df32 gh[3] = {ld(gq + 3 * a), ld(gq + 3 * a + 1), ld(gq + 3 * a + 2)};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) G[i][k].add_prod(du[i], gh[k]);
+    }
+    df32 Gd[3][3], J[3][3];
+    const float2 *je = jinv + e * 9;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            Gd[i][k] = G[i][k].df();
+            J[i][k] = ld(je + 3 * i + k);
+        }
+    // E_11, E_22, E_33: (G J^{-1})_ii; E_12, E_23, E_13: (G J^{-1})_ij + (G J^{-1})_ji
+    CSum s[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        s[0].add_prod(Gd[0][k], J[k][0]);
+        s[1].add_prod(Gd[1][k], J[k][1]);
+        s[2].add_prod(Gd[2][k], J[k][2]);
+        s[3].add_prod(Gd[0][k], J[k][1]);
+        s[3].add_prod(Gd[1][k], J[k][0]);
+        s[4].add_prod(Gd[1][k], J[k][2]);
+        s[4].add_prod(Gd[2][k], J[k][1]);
+        s[5].add_prod(Gd[0][k], J[k][2]);
+        s[5].add_prod(Gd[2][k], J[k][0]);
+    }
+    double2 *o = reinterpret_cast<double2 *>(E + 6 * g);
+    o[0] = make_double2(s[0].value(), s[1].value());
+    o[1] = make_double2(s[2].value(), s[3].value());
+    o[2] = make_double2(s[4].value(), s[5].value());
+}
+
+// Force: F_(a,i) = sum_q sum_k T_ik(q) ghat_a,k(q) with T(q) = w_q sigma_q J^{-T}, i.e.
+// T_ik = w sum_j sigma_ij J^{-1}_kj.  The block forms T of every point of the elements its
+// threads cover in shared memory (each once); one thread per (element, node) then sums its
+// three components over the points.
+__global__ void __launch_bounds__(kForceThreads) force3_affine_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                            const float2 *__restrict__ ghat,
+                                                                            const float2 *__restrict__ w,
+                                                                            const double *__restrict__ S,
+                                                                            const int32_t *__restrict__ elem_row,
+                                                                            int n_rows, int n_elem, int n_p, int n_q,
+                                                                            double *__restrict__ F) {
+    extern __shared__ float2 s_dyn[];
+    float2 *s_ghat = s_dyn;                   // n_q * n_p * 3
+    float2 *s_T = s_dyn + n_q * n_p * 3;      // (elements of the block) * n_q * 9
+    for (int i = threadIdx.x; i < n_q * n_p * 3; i += kForceThreads) s_ghat[i] = ghat[i];
+    const long long t0 = (long long)blockIdx.x * kForceThreads;
+    const long long e_first = t0 / n_p;
+    long long e_last = (t0 + kForceThreads - 1) / n_p;
+    if (e_last >= n_elem) e_last = n_elem - 1;
+    const int n_pts = static_cast<int>(e_last - e_first + 1) * n_q;
+    for (int i = threadIdx.x; i < n_pts; i += kForceThreads) {
+        const long long g = e_first * n_q + i;
+        const long long e = g / n_q;
+        const df32 wq = ld(w + g);
+        const double *sg = S + 6 * g;
+        // w sigma, symmetric: sigma_00..22 = s0, s1, s2; sigma_01 = s3, sigma_12 = s4, sigma_02 = s5
+        const df32 s0 = df_mul(wq, df_from_f64(sg[0])), s1 = df_mul(wq, df_from_f64(sg[1])),
+                   s2 = df_mul(wq, df_from_f64(sg[2])), s3 = df_mul(wq, df_from_f64(sg[3])),
+                   s4 = df_mul(wq, df_from_f64(sg[4])), s5 = df_mul(wq, df_from_f64(sg[5]));
+        const df32 ws[3][3] = {{s0, s3, s5}, {s3, s1, s4}, {s5, s4, s2}};
+        const float2 *je = jinv + e * 9;
+        float2 *T = s_T + i * 9;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                CSum acc;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) acc.add_prod(ws[a][j], ld(je + 3 * k + j));
+                const df32 v = acc.df();
+                T[3 * a + k] = make_float2(v.hi, v.lo);
+            }
+    }
+    __syncthreads();
+    const long long t = t0 + threadIdx.x;
+    if (t >= (long long)n_elem * n_p) return;
+    const long long e = t / n_p;
+    const int node = static_cast<int>(t - e * n_p);
+    const int32_t *er = elem_row + (e * n_p + node) * 3;
+    const int r0 = er[0], r1 = er[1], r2 = er[2];
+    if (r0 < 0 && r1 < 0 && r2 < 0) return;
+    if (r0 >= n_rows || r1 >= n_rows || r2 >= n_rows) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    const float2 *Te = s_T + (e - e_first) * n_q * 9;
+    CSum a0, a1, a2;
+    for (int q = 0; q < n_q; ++q) {
+        const float2 *gh = s_ghat + (q * n_p + node) * 3;
+        const df32 g0 = ld(gh), g1 = ld(gh + 1), g2 = ld(gh + 2);
+        const float2 *T = Te + q * 9;
+        a0.add_prod(ld(T + 0), g0);
+        a0.add_prod(ld(T + 1), g1);
+        a0.add_prod(ld(T + 2), g2);
+        a1.add_prod(ld(T + 3), g0);
+        a1.add_prod(ld(T + 4), g1);
+        a1.add_prod(ld(T + 5), g2);
+        a2.add_prod(ld(T + 6), g0);
+        a2.add_prod(ld(T + 7), g1);
+        a2.add_prod(ld(T + 8), g2);
+    }
+    if (r0 >= 0) red_add(F + r0, a0.value());
+    if (r1 >= 0) red_add(F + r1, a1.value());
+    if (r2 >= 0) red_add(F + r2, a2.value());
+}
+
 }  // namespace
 }  // namespace ssp
 
@@ -182,6 +343,41 @@ int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2
     force3_mixed_kernel<<<grid_for(n, kForceThreads), kForceThreads, 0, st>>>(
         reinterpret_cast<const float2 *>(wdphi1_hl), reinterpret_cast<const float2 *>(wdphi2_hl),
         reinterpret_cast<const float2 *>(wdphi3_hl), stress, elem_row, n_rows, n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_3d_affine_mixed(const float *jinv_hl, const float *ghat_hl, const float *u_hl, int n_u,
+                                                const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                                double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv_hl || !ghat_hl || !u_hl || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    // the table plus the displacements of the at most 128 / n_q + 2 elements a block's points cover
+    const size_t smem = sizeof(float2) * (3 * (size_t)n_p * n_q + 3 * (size_t)n_p * (128 / n_q + 2));
+    if (smem > 48 * 1024) return SSP_ERR_UNSUPPORTED;
+    strain3_affine_mixed_kernel<<<grid_for(n_int, 128), 128, smem, as_stream(stream)>>>(
+        reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(ghat_hl),
+        reinterpret_cast<const float2 *>(u_hl), elem_dof_lids, n_u, n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_element_affine_mixed(const float *jinv_hl, const float *ghat_hl, const float *w_hl,
+                                            const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                            int n_rows, double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    // a block's threads cover at most 128 / n_p + 2 elements, whose points' T it stages
+    const size_t smem = sizeof(float2) * (3 * (size_t)n_p * n_q + 9 * (size_t)(kForceThreads / n_p + 2) * n_q);
+    if (smem > 48 * 1024) return SSP_ERR_UNSUPPORTED;
+    if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv_hl || !ghat_hl || !w_hl || !stress || !elem_row) return SSP_ERR_INVALID;
+    const long long n = (long long)n_elem * n_p;
+    force3_affine_mixed_kernel<<<grid_for(n, kForceThreads), kForceThreads, smem, st>>>(
+        reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(ghat_hl),
+        reinterpret_cast<const float2 *>(w_hl), stress, elem_row, n_rows, n_elem, n_p, n_q, out_values);
     return launch_status();
 }
 

@@ -186,6 +186,7 @@ struct CSum {
         c = __fadd_rn(c, __fadd_rn(t.lo, x.lo));
     }
     __device__ __forceinline__ double value() const { return df_to_f64(df_fast_two_sum(s, c)); }
+    __device__ __forceinline__ df32 df() const { return df_fast_two_sum(s, c); }
 };
 
 }  // namespace ssp

@@ -142,6 +142,8 @@ class OwnedTangentPattern:
     device: dict = field(repr=False)
     stats: dict = field(default_factory=dict)
     timings: dict = field(default_factory=dict)
+    # whether every overlap element is affine (the mixed form's J^{-1} strain and force); None: not checked
+    affine: bool | None = field(default=None, repr=False)
 
     # host views of device-resident per-point data (copied on first access)
     def _host(self, key):
@@ -266,6 +268,12 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
               int(ov_nodes.size), n_ov, n_p, n_q, _lib.ptr(dev["dphi1"]), _lib.ptr(dev["dphi2"]),
               _lib.ptr(dev["dphi3"]) if dim == 3 else None, _lib.ptr(dev["weight"]), _lib.stream_handle())
     del coord_ov, elem_d
+    if dim == 3 and n_ov:
+        # J^{-1} of every overlap element from its vertices, J = [x1 - x0, x2 - x0, x3 - x0] (the
+        # mixed form's affine strain and force use it where the elements are straight-sided)
+        xv = coord[:, elem[:4, ov_el]]  # (3, 4, n_ov)
+        J = np.transpose(xv[:, 1:4, :] - xv[:, :1, :], (2, 0, 1))  # (n_ov, 3, 3): J[e, i, j] = x_{j+1,i} - x_{0,i}
+        dev["jinv"] = _lib.to_device(np.ascontiguousarray(np.linalg.inv(J).reshape(n_ov, 9)), f64)
     timings["overlap_geometry_s"] = perf_counter() - t1
 
     t2 = perf_counter()
@@ -391,14 +399,45 @@ def _split_pairs(x, scale=None, group: int = 1):
     return out
 
 
-def _mixed_inputs(pattern):
-    """Per-pattern hi + lo pairs of the gradients and of w * gradient (the mixed form's constant
-    inputs), split once and kept with the pattern's device arrays."""
+def _affine_elements(pattern, rtol: float = 1e-10, chunk: int = 1 << 16) -> bool:
+    """Whether every overlap element's gradients are J^{-T} ghat(q) (straight-sided tetrahedra):
+    the stored dphi against the reconstruction from J^{-1} and the reference table, per element,
+    relative to the element's largest gradient."""
+    t = _lib.torch()
     d = pattern.device
-    if "dphi1_hl" not in d:
-        for k in ("dphi1", "dphi2", "dphi3"):
-            d[k + "_hl"] = _split_pairs(d[k])
-            d["w" + k + "_hl"] = _split_pairs(d[k], d["weight"], pattern.n_p)
+    if pattern.dim != 3 or "jinv" not in d:
+        return False
+    n_el, n_q, n_p = int(pattern.overlap_elements.size), pattern.n_q, pattern.n_p
+    ghat = t.as_tensor(np.ascontiguousarray(np.transpose(reference_gradients(3, pattern.elem_type), (2, 1, 0))),
+                       device="cuda")  # (n_q, n_p, 3): [q][a][k]
+    for e0 in range(0, n_el, chunk):
+        e1 = min(n_el, e0 + chunk)
+        jinv = d["jinv"][e0:e1].reshape(-1, 3, 3)  # [e][k][j]
+        rec = t.einsum("ekj,qak->eqaj", jinv, ghat)  # dphi_j of node a at point q
+        stored = t.stack([d[k][e0 * n_q:e1 * n_q].reshape(e1 - e0, n_q, n_p) for k in ("dphi1", "dphi2", "dphi3")], -1)
+        scale = stored.abs().amax(dim=(1, 2, 3))
+        if bool(((rec - stored).abs().amax(dim=(1, 2, 3)) > rtol * scale).any()):
+            return False
+    return True
+
+
+def _mixed_inputs(pattern):
+    """Per-pattern hi + lo pairs of the mixed form's constant inputs, split once and kept with the
+    pattern's device arrays: of the gradients and w * gradient, or, when every element is affine,
+    of J^{-1} per element, the reference gradient table and the weights."""
+    d = pattern.device
+    if pattern.affine is None:
+        pattern.affine = _affine_elements(pattern)
+        if pattern.affine:
+            t = _lib.torch()
+            table = np.ascontiguousarray(np.transpose(reference_gradients(3, pattern.elem_type), (2, 1, 0)))
+            d["ghat_hl"] = _split_pairs(t.as_tensor(table, device="cuda"))
+            d["jinv_hl"] = _split_pairs(d["jinv"])
+            d["w_hl"] = _split_pairs(d["weight"])
+        else:
+            for k in ("dphi1", "dphi2", "dphi3"):
+                d[k + "_hl"] = _split_pairs(d[k])
+                d["w" + k + "_hl"] = _split_pairs(d[k], d["weight"], pattern.n_p)
     return d
 
 
@@ -415,9 +454,14 @@ def overlap_strain_device(pattern, U, *, mixed: bool = False):
     if pattern.dim == 3 and mixed:
         d = _mixed_inputs(pattern)
         u_hl = _split_pairs(u_ov)
-        _lib.call("ssp_assemble_overlap_strain_3d_mixed", _lib.ptr(d["dphi1_hl"]), _lib.ptr(d["dphi2_hl"]),
-                  _lib.ptr(d["dphi3_hl"]), _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el,
-                  pattern.n_p, pattern.n_q, _lib.ptr(E), st)
+        if pattern.affine:
+            _lib.call("ssp_assemble_overlap_strain_3d_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["ghat_hl"]),
+                      _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p,
+                      pattern.n_q, _lib.ptr(E), st)
+        else:
+            _lib.call("ssp_assemble_overlap_strain_3d_mixed", _lib.ptr(d["dphi1_hl"]), _lib.ptr(d["dphi2_hl"]),
+                      _lib.ptr(d["dphi3_hl"]), _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el,
+                      pattern.n_p, pattern.n_q, _lib.ptr(E), st)
     elif pattern.dim == 3:
         _lib.call("ssp_assemble_overlap_strain_3d", _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
                   _lib.ptr(u_ov), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p, pattern.n_q,
@@ -465,9 +509,15 @@ def owned_force_device(pattern, S_aos, *, mixed: bool = False):
     F = t.empty(n_rows, dtype=t.float64, device="cuda")
     if mixed and pattern.dim == 3:
         d = _mixed_inputs(pattern)
-        _lib.call("ssp_assemble_force_element_mixed", _lib.ptr(d["wdphi1_hl"]), _lib.ptr(d["wdphi2_hl"]),
-                  _lib.ptr(d["wdphi3_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
-                  pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
+        if pattern.affine:
+            _lib.call("ssp_assemble_force_element_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["ghat_hl"]),
+                      _lib.ptr(d["w_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
+                      pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
+        else:
+            _lib.call("ssp_assemble_force_element_mixed", _lib.ptr(d["wdphi1_hl"]), _lib.ptr(d["wdphi2_hl"]),
+                      _lib.ptr(d["wdphi3_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]),
+                      int(pattern.overlap_elements.size), pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F),
+                      _lib.stream_handle())
         return F
     _lib.call("ssp_assemble_force_element", pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
               _lib.ptr(d["dphi3"]) if pattern.dim == 3 else None, _lib.ptr(S_aos), _lib.ptr(d["weight"]),

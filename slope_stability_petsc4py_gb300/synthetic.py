@@ -361,6 +361,7 @@ def point_materials(mesh: SlopeMesh, materials: MaterialSet, n_q: int) -> dict[s
 # about 7.5 % under gravity alone).
 CONFIGS = {
     "2d_p2_homo": dict(dim=2, elem_type="P2", nx=100, ny=100, n_layers=1, amplitude=0.0072),  # 20,000 triangles
+    "2d_p4_homo": dict(dim=2, elem_type="P4", nx=80, ny=72, n_layers=1, amplitude=0.0072),  # 11,520 triangles
     "3d_p2_homo": dict(dim=3, elem_type="P2", nx=40, ny=14, nz=30, n_layers=1, amplitude=0.0157),  # 100,800 tets
     "3d_p2_hetero": dict(dim=3, elem_type="P2", nx=64, ny=26, nz=40, n_layers=4, amplitude=0.003),  # 399,360 tets
     "3d_p4_hetero": dict(dim=3, elem_type="P4", nx=30, ny=12, nz=23, n_layers=4, amplitude=0.003),  # 49,680 tets

@@ -99,9 +99,40 @@ def test_compensated_strain_and_force_match_fp64(cuda_device, elem_type, dims, a
     F64 = owned_force_device(pat, S).cpu().numpy()
     Fmx = owned_force_device(pat, S, mixed=True).cpu().numpy()
     err_f = rel_err(Fmx, F64)
-    print(f"{elem_type}: strain error {err_e:.2e}, force error {err_f:.2e}")
+    print(f"{elem_type}: strain error {err_e:.2e}, force error {err_f:.2e} (affine kernels {pat.affine})")
+    assert pat.affine  # straight-sided tetrahedra: J^{-1} per element and the reference table
     assert err_e <= 1e-11 and err_f <= 1e-11
     torch.cuda.synchronize()
+
+
+def test_mixed_strain_and_force_on_curved_elements(cuda_device):
+    """Mid-edge nodes moved off their edges (curved P2 tetrahedra, gradients no longer J^{-T} ghat):
+    the affine check fails and the mixed form reads the per-point gradients instead; errors as above."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
+    from slope_stability_petsc4py_gb300.distributed_tangent import overlap_strain_device, owned_force_device
+
+    mats = synthetic.MaterialSet.layered(4, seed=1)
+    mesh = synthetic.slope_mesh_3d(8, 4, 4, elem_type="P2", n_layers=4)
+    coord = mesh.coord.copy()
+    n_v = int(mesh.elem[:4].max()) + 1  # vertices first, then the edge nodes
+    rng = np.random.default_rng(3)
+    interior = np.all(mesh.q_mask[:, n_v:], axis=0)
+    coord[:, n_v:][:, interior] += 0.02 * rng.standard_normal((3, int(interior.sum())))
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=0.0, young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    op = ConstitutiveOperator.from_mesh(coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
+    pat = op.owned_tangent_pattern
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.02, seed=8)
+    E64 = overlap_strain_device(pat, U).cpu().numpy()
+    Emx = overlap_strain_device(pat, U, mixed=True).cpu().numpy()
+    assert pat.affine is False
+    op.reduction(1.1)
+    op.constitutive_problem_stress_tangent(U)
+    F64 = owned_force_device(pat, op._S_aos).cpu().numpy()
+    Fmx = owned_force_device(pat, op._S_aos, mixed=True).cpu().numpy()
+    err_e, err_f = rel_err(Emx, E64), rel_err(Fmx, F64)
+    print(f"curved P2: strain error {err_e:.2e}, force error {err_f:.2e}")
+    assert err_e <= 1e-11 and err_f <= 1e-11
 
 
 def test_compensated_plastic_ds_matches_fp64(cuda_device):
