@@ -63,6 +63,15 @@ int ssp_constitutive_3d_sds(const double *E, const double *c_bar, const double *
 int ssp_constitutive_3d_branch(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                                const double *lame, int n_int, double *S_out, int8_t *branch_out, void *stream);
 
+/* Binned plane-strain return mapping: the same branch codes as ssp_constitutive_sds_branch(2, ...)
+ * and S, DS within a few ulps of it, with the elastic points finished in a first pass
+ * and the plastic branches run only on the listed points.  scratch: 1 + n_int int32 (caller
+ * allocated; a count then the listed points).  Replaces the reference's NumPy
+ * constitutive_problem_2D (src/slope_stability/constitutive/problem.py:143-475) in the operator. */
+int ssp_constitutive_2d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                                   int32_t *scratch, void *stream);
+
 /* S, DS and the branch code of every point (2D or 3D); the branch codes drive the plastic-only
  * tangent correction (ssp_tangent_plastic_correction).  Same arithmetic as ssp_constitutive_3d_sds /
  * ssp_constitutive_2d. */

@@ -50,6 +50,7 @@ _SIGS = {
     "ssp_assemble_force_element": [_c_int] + [_vp] * 6 + [_c_int] * 4 + [_vp, _vp],
     "ssp_assemble_overlap_strain_3d_mixed": [_vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_force_element_mixed": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
+    "ssp_constitutive_2d_sds_binned": [_vp] * 5 + [_c_int] + [_vp] * 5,
     "ssp_assemble_overlap_strain_3d_affine_mixed": [_vp, _vp, _vp, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_force_element_affine_mixed": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
     "ssp_split_f64": [_vp, _vp, _c_ll, _c_int, _vp, _vp],
@@ -121,6 +122,7 @@ _KERNELS_PER_CALL = {
     "ssp_copy_rows_out": 1,
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
     "ssp_assemble_overlap_strain_3d_affine_mixed": 1, "ssp_assemble_force_element_affine_mixed": 1,
+    "ssp_constitutive_2d_sds_binned": 2,
     "ssp_tangent_plastic_correction": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_constitutive_3d_sds_binned_mixed": 3, "ssp_constitutive_3d_sds_learned_mixed": 4,

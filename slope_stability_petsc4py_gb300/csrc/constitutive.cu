@@ -801,17 +801,73 @@ int launch_binned(const double *E, const double *c_bar, const double *sin_phi, c
 // ---------------------------------------------------------------------------- 2D
 
 // Plane strain, E = [e11, e22, g12] -> S = [s11, s22, s12, s33], DS 3x3 column-major.
-__device__ int mc2d_point(const double *E, double c, double s, double G, double lam, double *S, double *DS) {
+
+// The trial state of a point: in-plane principal values ev0 (with the out-of-plane 0), their
+// order (0,2,1) when ev0[0] >= 0 > ev0[1] and (2,0,1) when 0 > ev0[0], the ordered principal
+// values e1 >= e2 >= e3 and the trial yield function.
+struct Trial2 {
+    double ev0[3], rad, e1, e2, e3, tr, f_tr;
+    int ord[3];
+};
+
+__device__ __forceinline__ Trial2 mc2d_trial(const double *E, double c, double s, double G, double lam) {
+    Trial2 t;
     const double e11 = E[0], e22 = E[1], g12 = E[2];
     const double tr2 = e11 + e22;
-    const double rad = sqrt((e11 - e22) * (e11 - e22) + g12 * g12);
-    const double ev0[3] = {0.5 * (tr2 + rad), 0.5 * (tr2 - rad), 0.0};
-    // projections in [11, 22, 12, 33] representation and their derivatives (3x3 in-plane)
+    t.rad = sqrt((e11 - e22) * (e11 - e22) + g12 * g12);
+    t.ev0[0] = 0.5 * (tr2 + t.rad);
+    t.ev0[1] = 0.5 * (tr2 - t.rad);
+    t.ev0[2] = 0.0;
+    t.ord[0] = 0;
+    t.ord[1] = 1;
+    t.ord[2] = 2;
+    if (t.ev0[0] >= t.ev0[2] && t.ev0[2] > t.ev0[1]) {
+        t.ord[1] = 2;
+        t.ord[2] = 1;
+    } else if (t.ev0[2] > t.ev0[0]) {
+        t.ord[0] = 2;
+        t.ord[1] = 0;
+        t.ord[2] = 1;
+    }
+    t.e1 = t.ev0[t.ord[0]];
+    t.e2 = t.ev0[t.ord[1]];
+    t.e3 = t.ev0[t.ord[2]];
+    t.tr = t.e1 + t.e2 + t.e3;
+    t.f_tr = 2.0 * G * ((1.0 + s) * t.e1 - (1.0 - s) * t.e3) + 2.0 * lam * s * t.tr - c;
+    return t;
+}
+
+__device__ __forceinline__ void mc2d_elastic(const double *E, double G, double lam, double *S, double *DS) {
+    const double e11 = E[0], e22 = E[1], g12 = E[2];
+    const double vt = e11 + e22;  // iota4 . [e11, e22, g12, 0]
+    S[0] = lam * vt + 2.0 * G * e11;
+    S[1] = lam * vt + 2.0 * G * e22;
+    S[2] = 2.0 * G * (0.5 * g12);
+    S[3] = lam * vt;
+    if (DS) {
+        const double io[3] = {1.0, 1.0, 0.0}, hI[3] = {1.0, 1.0, 0.5};
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) DS[i + 3 * j] = io[i] * io[j] * lam + 2.0 * ((i == j) ? hI[i] : 0.0) * G;
+    }
+}
+
+__device__ int mc2d_point(const double *E, double c, double s, double G, double lam, double *S, double *DS) {
+    const Trial2 t = mc2d_trial(E, c, s, G, lam);
+    if (t.f_tr <= 0.0) {
+        mc2d_elastic(E, G, lam, S, DS);
+        return kElastic;
+    }
+    // projections in [11, 22, 12, 33] representation and their derivatives (3x3 in-plane): the
+    // plastic branches only
+    const double e11 = E[0], e22 = E[1], g12 = E[2];
+    const double rad = t.rad;
     double P0[4], P1[4];
     double dP0[9];
     if (rad != 0.0) {
-        P0[0] = (e11 - ev0[1]) / rad;
-        P0[1] = (e22 - ev0[1]) / rad;
+        P0[0] = (e11 - t.ev0[1]) / rad;
+        P0[1] = (e22 - t.ev0[1]) / rad;
         P0[2] = (g12 / 2.0) / rad;
     } else {
         P0[0] = 1.0;
@@ -829,44 +885,19 @@ __device__ int mc2d_point(const double *E, double c, double s, double G, double 
 #pragma unroll
         for (int i = 0; i < 3; ++i)
             dP0[i + 3 * j] = rad != 0.0 ? (((i == j) ? hI[i] : 0.0) - P0[i] * P0[j] - P1[i] * P1[j]) / rad : 0.0;
-    // sort: (0,2,1) when ev0[0] >= 0 > ev0[1]; (2,0,1) when 0 > ev0[0]
-    int ord[3] = {0, 1, 2};
-    if (ev0[0] >= ev0[2] && ev0[2] > ev0[1]) {
-        ord[1] = 2;
-        ord[2] = 1;
-    } else if (ev0[2] > ev0[0]) {
-        ord[0] = 2;
-        ord[1] = 0;
-        ord[2] = 1;
-    }
-    double ev[3], P[3][4], dP[3][9];
+    double P[3][4], dP[3][9];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const int o = ord[k];
-        ev[k] = ev0[o];
+        const int o = t.ord[k];
 #pragma unroll
         for (int i = 0; i < 4; ++i) P[k][i] = o == 0 ? P0[i] : (o == 1 ? P1[i] : (i == 3 ? 1.0 : 0.0));
 #pragma unroll
         for (int i = 0; i < 9; ++i) dP[k][i] = o == 0 ? dP0[i] : (o == 1 ? -dP0[i] : 0.0);
     }
-    const double e1 = ev[0], e2 = ev[1], e3 = ev[2];
-    const double tr = e1 + e2 + e3;
-    const double f_tr = 2.0 * G * ((1.0 + s) * e1 - (1.0 - s) * e3) + 2.0 * lam * s * tr - c;
+    const double e1 = t.e1, e2 = t.e2, e3 = t.e3;
+    const double tr = t.tr;
+    const double f_tr = t.f_tr;
     const double io[3] = {1.0, 1.0, 0.0};
-    if (f_tr <= 0.0) {
-        const double vt = e11 + e22;  // iota4 . [e11, e22, g12, 0]
-        S[0] = lam * vt + 2.0 * G * e11;
-        S[1] = lam * vt + 2.0 * G * e22;
-        S[2] = 2.0 * G * (0.5 * g12);
-        S[3] = lam * vt;
-        if (DS) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-#pragma unroll
-                for (int i = 0; i < 3; ++i) DS[i + 3 * j] = io[i] * io[j] * lam + 2.0 * ((i == j) ? hI[i] : 0.0) * G;
-        }
-        return kElastic;
-    }
     const double g_sl = (e1 - e2) / (1.0 + s);
     const double g_sr = (e2 - e3) / (1.0 - s);
     const double g_la = (e1 + e2 - 2.0 * e3) / (3.0 - s);
@@ -966,6 +997,64 @@ __global__ void __launch_bounds__(128) mc2d_kernel(const double *__restrict__ E,
 #pragma unroll
     for (int k = 0; k < 4; ++k) S[4ll * p + k] = s[k];
     if (TANGENT) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) DS[9ll * p + k] = ds[k];
+    }
+}
+
+// Binned 2D return mapping.  Pass A decides every point's trial state (the closed-form in-plane
+// eigenvalues, exactly mc2d_point's arithmetic), finishes the elastic points and lists the others
+// (scratch[0] = count, scratch[1..] = points); pass B runs mc2d_point on the listed points only, so
+// no warp pays for the projections and the plastic branches of another point.  Same arithmetic as
+// mc2d_kernel (same branch codes; values within a few ulps, where the compiler contracts a
+// multiply-add into an FMA differently in the two kernels).
+__global__ void __launch_bounds__(128) mc2d_screen_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
+                                                          const double *__restrict__ sin_phi,
+                                                          const double *__restrict__ shear,
+                                                          const double *__restrict__ lame, int n,
+                                                          double *__restrict__ S, double *__restrict__ DS,
+                                                          int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool listed = false;
+    if (p < n) {
+        const double e[3] = {E[3ll * p], E[3ll * p + 1], E[3ll * p + 2]};
+        const double G = shear[p], lam = lame[p];
+        const Trial2 t = mc2d_trial(e, c_bar[p], sin_phi[p], G, lam);
+        if (t.f_tr <= 0.0) {
+            double s[4], ds[9];
+            mc2d_elastic(e, G, lam, s, ds);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) S[4ll * p + k] = s[k];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) DS[9ll * p + k] = ds[k];
+            branch[p] = static_cast<int8_t>(kElastic);
+        } else {
+            listed = true;
+        }
+    }
+    const int slot = warp_append(listed, scratch);
+    if (listed) scratch[1 + slot] = p;
+}
+
+__global__ void __launch_bounds__(128) mc2d_list_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
+                                                        const double *__restrict__ sin_phi,
+                                                        const double *__restrict__ shear,
+                                                        const double *__restrict__ lame, int n,
+                                                        double *__restrict__ S, double *__restrict__ DS,
+                                                        int8_t *__restrict__ branch,
+                                                        const int32_t *__restrict__ scratch) {
+    const int cnt = scratch[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        const int p = scratch[1 + i];
+        if (p < 0 || p >= n) {
+            flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const double e[3] = {E[3ll * p], E[3ll * p + 1], E[3ll * p + 2]};
+        double s[4], ds[9];
+        branch[p] = static_cast<int8_t>(mc2d_point(e, c_bar[p], sin_phi[p], shear[p], lame[p], s, ds));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) S[4ll * p + k] = s[k];
 #pragma unroll
         for (int k = 0; k < 9; ++k) DS[9ll * p + k] = ds[k];
     }
@@ -1144,6 +1233,28 @@ int ssp_constitutive_sds_branch(int dim, const double *E, const double *c_bar, c
     else
         mc2d_kernel<true><<<grid_for(n_int, 128), 128, 0, as_stream(stream)>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
                                                                                 DS_out, branch_out);
+    return launch_status();
+}
+
+int ssp_constitutive_2d_sds_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out,
+                                   int32_t *scratch, void *stream) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+        return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(scratch, 0, sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    mc2d_screen_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                             branch_out, scratch);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long gx = (long long)sms * 8;  // grid-stride over the listed points (count on the device)
+    const long long need = ((long long)n_int + 127) / 128;
+    if (gx > need) gx = need;
+    mc2d_list_kernel<<<static_cast<unsigned>(gx), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
+                                                                branch_out, scratch);
     return launch_status();
 }
 

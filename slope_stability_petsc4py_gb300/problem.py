@@ -429,8 +429,15 @@ class ConstitutiveOperator:
         args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                 _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
         branch = None
-        mode = self.return_mapping if pat.dim == 3 else "unsorted"
-        if tangent and mode in ("binned", "learned"):
+        mode = self.return_mapping if pat.dim == 3 else ("unsorted" if self.return_mapping == "unsorted" else "binned2d")
+        if tangent and mode == "binned2d":  # elastic points finished first, the return mapping on the rest
+            branch = t.empty(n, dtype=t.int8, device="cuda")
+            if self._scratch is None or self._scratch.numel() < n + 1:
+                self._scratch = t.empty(3 * n + 12, dtype=t.int32, device="cuda")
+            _lib.call("ssp_constitutive_2d_sds_binned", _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
+                      _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
+                      _lib.ptr(DS), _lib.ptr(branch), _lib.ptr(self._scratch), st)
+        elif tangent and mode in ("binned", "learned"):
             branch = t.empty(n, dtype=t.int8, device="cuda")
             need = (8 if mode == "learned" else 3) * n + 12
             if self._scratch is None or self._scratch.numel() < need:

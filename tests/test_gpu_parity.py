@@ -169,6 +169,59 @@ def test_constitutive_2d_matches_reference_numpy():
         assert rel_err(DS.cpu().numpy().T, g[f"{tag}_DS"]) <= PLAIN_RTOL
 
 
+def test_binned_2d_return_mapping_matches_single_pass_and_reference():
+    """ssp_constitutive_2d_sds_binned (elastic points first, plastic branches on the listed points):
+    the reference's fixture at 1e-12, and against the single-pass kernel the same branch codes and
+    S, DS within a few ulps (the same source in two kernels may contract multiply-adds differently),
+    on the fixture's points and on 200k random points over four strain magnitudes."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib
+
+    def run(entry, E, args):
+        n = E.shape[0]
+        Ed = _dev(E)
+        A = [_dev(a) for a in args]
+        S = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+        DS = torch.empty((n, 9), dtype=torch.float64, device="cuda")
+        br = torch.empty(n, dtype=torch.int8, device="cuda")
+        if entry == "ssp_constitutive_2d_sds_binned":
+            scratch = torch.empty(n + 1, dtype=torch.int32, device="cuda")
+            _lib.call(entry, _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br),
+                      _lib.ptr(scratch), _lib.stream_handle())
+        else:
+            _lib.call(entry, 2, _lib.ptr(Ed), *[_lib.ptr(a) for a in A], n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(br),
+                      _lib.stream_handle())
+        return S, DS, br
+
+    g = golden("constitutive_2d.npz")
+    for tag in ("l1.0", "l1.2"):
+        args = [g[f"{tag}_{k}"] for k in ("c_bar", "sin_phi", "shear", "lame")]
+        S, DS, br = run("ssp_constitutive_2d_sds_binned", np.ascontiguousarray(g["E"].T), args)
+        assert rel_err(S.cpu().numpy().T, g[f"{tag}_S"]) <= PLAIN_RTOL
+        assert rel_err(DS.cpu().numpy().T, g[f"{tag}_DS"]) <= PLAIN_RTOL
+        S1, DS1, br1 = run("ssp_constitutive_sds_branch", np.ascontiguousarray(g["E"].T), args)
+        assert torch.equal(br, br1)
+        assert rel_err(S.cpu().numpy(), S1.cpu().numpy()) <= 1e-14 and rel_err(DS.cpu().numpy(), DS1.cpu().numpy()) <= 1e-14
+    rng = np.random.default_rng(21)
+    n = 200_000
+    E = rng.standard_normal((n, 3)) * np.repeat(np.array([1e-4, 1e-3, 3e-3, 1e-2]), n // 4)[:, None]
+    young, nu = rng.uniform(1e4, 5e4, n), rng.uniform(0.2, 0.45, n)
+    shear = young / (2 * (1 + nu))
+    lame = young / (3 * (1 - 2 * nu)) - 2 * shear / 3
+    phi = np.deg2rad(rng.uniform(20.0, 45.0, n))
+    args = [2 * rng.uniform(5.0, 30.0, n) * np.cos(phi), np.sin(phi), shear, lame]
+    a = run("ssp_constitutive_2d_sds_binned", E, args)
+    b = run("ssp_constitutive_sds_branch", E, args)
+    counts = torch.bincount(a[2].long(), minlength=5).cpu().numpy()
+    assert (counts > 100).all(), counts  # every branch occurs
+    assert torch.equal(a[2], b[2])
+    for x, y in zip(a[:2], b[:2]):
+        assert rel_err(x.cpu().numpy(), y.cpu().numpy()) <= 1e-14  # max-norm over all points, as in 3D
+        rows = (x - y).abs().amax(dim=1) / y.abs().amax(dim=1).clamp_min(1e-300)
+        assert float(rows.max()) <= PLAIN_RTOL  # and every point within the parity tolerance
+
+
 def test_reduction_matches_reference():
     from slope_stability_petsc4py_gb300 import reduction
 
