@@ -381,6 +381,23 @@ def measure_bddc(torch, lib, op, mesh, specs, args, step):
     return out
 
 
+def measure_graph_replay(torch, lib, op, U_dev, args):
+    """The same step as a CUDA graph (ConstitutiveOperator.capture_regularized_build), replayed on
+    the displacement tensor: the kernels of build_F_K_regularized_all_free without the host work of
+    the Python entry point, for the plain and the mixed form."""
+    n_int = op.owned_tangent_pattern.n_local_int
+    w = max(args.warmup, 3)
+    out = {}
+    for form in ("plain", "mixed"):
+        op.tangent_form = form
+        run = op.capture_regularized_build(LAMBDA, U_dev, R_REG)
+        ms = time_steps(torch, run.replay, w, args.steps)
+        out[form] = {"value": n_int / (ms * 1e-3), "ms_per_step": ms}
+    op.tangent_form = "plain"
+    lib.raise_on_device_status()
+    return out
+
+
 def train_branch_model(torch, op, mesh, mats, name):
     """Train the branch-proposal network on continuation states other than the timed one
     (strength-reduction factors 1.0..1.4, shear-band amplitudes 0.4..1.6 x the workload's)."""
@@ -532,6 +549,8 @@ def run_gpu(args):
         line["forms"] = compare_forms(torch, _lib, op, mesh, mats, args, step, ms)
     if args.bddc:
         line["bddc"] = measure_bddc(torch, _lib, op, mesh, specs, args, step)
+    if args.form == "plain" and args.return_mapping == "binned" and not args.no_forms:
+        line["graph_replay"] = measure_graph_replay(torch, _lib, op, U_dev, args)
 
     if rank == 0 and not args.no_e2e:
         op.host_outputs = True

@@ -18,7 +18,8 @@ def _op(mesh, mats, staged):
 
     specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=0.0, young=float(mats.young[i]),
                   poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
-    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs,
+                                        elem_type=mesh.elem_type)
     op.stage_values = staged
     return op
 
@@ -54,15 +55,17 @@ def test_staged_values_copy_gives_the_same_matrices(cuda_device, form):
     _lib.raise_on_device_status()
 
 
-@pytest.mark.parametrize("form", ["plain", "mixed"])
-def test_captured_build_replays_match_direct_builds(cuda_device, form):
-    """capture_regularized_build: replays on U updated in place give the direct builds' F and K."""
+@pytest.mark.parametrize("form,dim", [("plain", 3), ("mixed", 3), ("plain", 2), ("mixed", 2)])
+def test_captured_build_replays_match_direct_builds(cuda_device, form, dim):
+    """capture_regularized_build: replays on U updated in place give the direct builds' F and K
+    (3D P2, and 2D P4 with the binned plane-strain return mapping)."""
     import torch
 
     from slope_stability_petsc4py_gb300 import _lib, synthetic
 
     mats = synthetic.MaterialSet.layered(4, seed=3)
-    mesh = synthetic.slope_mesh_3d(12, 5, 6, elem_type="P2", n_layers=4)
+    mesh = (synthetic.slope_mesh_3d(12, 5, 6, elem_type="P2", n_layers=4) if dim == 3
+            else synthetic.slope_mesh_2d(12, 8, elem_type="P4", n_layers=4))
     cap, ref = _op(mesh, mats, True), _op(mesh, mats, True)
     for op in (cap, ref):
         op.tangent_form, op.host_outputs = form, False
