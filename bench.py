@@ -39,7 +39,9 @@ LAMBDA, R_REG = 1.1, 0.1
 NCU_TRAFFIC = {
     "3d_p2_homo": {
         "ssp_tangent_plastic_correction": 286.20e6 + 63.73e6,
-        "ssp_tangent_plastic_correction_mixed": 297.67e6 + 70.18e6,
+        "ssp_tangent_plastic_correction_mixed": 298.00e6 + 72.01e6,
+        "ssp_assemble_overlap_strain_3d_affine_mixed": 22.82e6 + 0.04e6,
+        "ssp_assemble_force_element_affine_mixed": 84.88e6 + 1.49e6,
         "ssp_assemble_overlap_strain_3d_mixed": 281.74e6 + 35.76e6,
         "ssp_assemble_overlap_strain_3d": 284.63e6 + 36.25e6,
         "ssp_assemble_force_element": 343.75e6 + 2.57e6,
