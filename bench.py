@@ -244,6 +244,7 @@ def peaks():
 def kernel_profile(torch, lib, step, op, reps=3):
     """Per-entry-point CUDA-event times, the launches serialised on one stream (the concurrent force
     and the staged values copy would otherwise share the GPU with the kernels inside the brackets)."""
+    saved = (op.concurrent_force, op.stage_values)
     op.concurrent_force = False
     op.stage_values = False
     lib.TRACE = []
@@ -254,8 +255,7 @@ def kernel_profile(torch, lib, step, op, reps=3):
     for name, a, b in lib.TRACE:
         per.setdefault(name, []).append(a.elapsed_time(b))
     lib.TRACE = None
-    op.concurrent_force = True
-    op.stage_values = True
+    op.concurrent_force, op.stage_values = saved
     total = sum(sum(v) for v in per.values()) / reps
     return {k: {"ms_per_launch": float(np.mean(v)), "launches_per_step": len(v) / reps,
                 "ms_per_step": float(np.sum(v)) / reps, "share": float(np.sum(v)) / reps / total}

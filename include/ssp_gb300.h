@@ -288,6 +288,11 @@ int ssp_gather(const double *src, const int32_t *idx, int n, double *dst, void *
  * points below address it through its device mapping (cudaPointerGetAttributes). */
 int ssp_host_writable(const void *host_ptr);
 
+/* dst[0..n) := src[0..n), both device memory, by a grid-stride kernel on the SMs (16-byte vectors
+ * where both are aligned) rather than a memcpy: the operator's copy of a tangent's starting values,
+ * which is then a kernel node when the build is captured in a CUDA graph.  No reference counterpart. */
+int ssp_copy_device(const double *src, long long n, double *dst, void *stream);
+
 /* dst_host[0..n) = src[0..n) written by the SMs into pinned, device-mapped host memory
  * (ssp_host_writable(dst_host) must hold, else SSP_ERR_INVALID); asynchronous on the stream.
  * The operator's host hand-off of the CSR values; no reference counterpart. */

@@ -1175,6 +1175,18 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
     return launch_status();
 }
 
+int ssp_copy_device(const double *src, long long n, double *dst, void *stream) {
+    if (n < 0) return SSP_ERR_INVALID;
+    if (n == 0) return SSP_OK;
+    if (!src || !dst) return SSP_ERR_INVALID;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0;
+    copy_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, n, dst, vec ? 1 : 0);
+    return launch_status();
+}
+
 int ssp_copy_out(const double *src, long long n, double *dst_host, void *stream) {
     if (n < 0) return SSP_ERR_INVALID;
     if (n == 0) return SSP_OK;

@@ -235,6 +235,10 @@ class ConstitutiveOperator:
         # the strain and return mapping run (_stage_values); (key, values, event) of that copy
         self.stage_values = True
         self._staged_values = None
+        # how the tangent's starting values are copied: "kernel" (the library's SM copy; measured as
+        # fast as a stream memcpy in direct calls and, unlike a memcpy node, no slower in a
+        # captured graph) or "memcpy"
+        self.values_copy = "kernel"
         # host outputs: the pinned mirror of the values is refreshed row by row where the values
         # can have changed since the previous build (_changed_rows), else copied in full
         self.incremental_host_copy = True
@@ -252,8 +256,10 @@ class ConstitutiveOperator:
         # force in compensated double-float arithmetic (~1e-13); the return mapping and every CSR /
         # force accumulation stay FP64 (about 1e-7 relative tangent error)
         self.tangent_form = "plain"
-        # composite builds with device outputs run the force concurrently with the tangent
-        self.concurrent_force = True
+        # composite builds with device outputs: True runs the force on the second stream at the same
+        # time as the tangent; measured 2-5 % slower than one stream on the GB300 (the two compete
+        # for the SMs), so off by default
+        self.concurrent_force = False
         self._force_stream = None
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
@@ -567,6 +573,14 @@ class ConstitutiveOperator:
             _lib.torch().cuda.current_stream().wait_event(staged[2])
         return staged
 
+    def _copy_values(self, dst, src):
+        """dst := src (CSR values, device): a stream memcpy, or with values_copy = "kernel" the
+        library's SM copy kernel (a kernel node when the build is captured in a CUDA graph)."""
+        if self.values_copy == "kernel":
+            _lib.call("ssp_copy_device", _lib.ptr(src), int(src.numel()), _lib.ptr(dst), _lib.stream_handle())
+        else:
+            dst.copy_(src)
+
     def _stage_values(self, r):
         """Issue the copy of the regularised tangent's starting values into its values array on the
         second stream, ahead of the strain and return-mapping kernels that the build runs first:
@@ -587,7 +601,7 @@ class ConstitutiveOperator:
         main, side = t.cuda.current_stream(), self._aux_stream()
         side.wait_stream(main)
         with t.cuda.stream(side):
-            values.copy_(start)
+            self._copy_values(values, start)
         values.record_stream(side)
         start.record_stream(side)
         done = t.cuda.Event()
@@ -614,7 +628,7 @@ class ConstitutiveOperator:
                 start, key, scale = self._regularized_start(r), ("regularized", float(r)), 1.0 - float(r)
             staged = self._drain_staged()
             if staged is None or staged[0] != key or staged[1] is not values:
-                values.copy_(start)
+                self._copy_values(values, start)
             # else the copy of start, issued on the second stream ahead of the strain and return
             # mapping (_stage_values), has overlapped them
             if ev is not None:
