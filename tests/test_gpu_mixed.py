@@ -3,7 +3,7 @@
 The mixed form keeps the return mapping's eigendecomposition, branch tests, plastic multipliers
 and stresses and the CSR accumulation in FP64; it forms the plastic points' consistent tangent DS,
 the strain, the force and the plastic-point products B^T (w D B) in compensated FP32
-(double-float) arithmetic.  Tolerance of the spec mixed form: 1e-6 relative tangent error.
+(double-float) arithmetic.  Tolerance of the mixed form: 1e-6 relative tangent error.
 """
 
 from __future__ import annotations

@@ -4,6 +4,7 @@ and the elevated meshes through the host pattern builder."""
 
 from __future__ import annotations
 
+import os
 import struct
 from pathlib import Path
 
@@ -12,7 +13,8 @@ import pytest
 
 from conftest import golden
 
-REF_MESH = Path("/root/reference/meshes/3d_hetero_ssr/SSR_hetero_ada_L1.msh")
+# the reference checkout, where this container has it (the GPU machines do not)
+REF_MESH = Path(os.environ.get("SSP_REFERENCE_ROOT", "/root/reference")) / "meshes/3d_hetero_ssr/SSR_hetero_ada_L1.msh"
 
 
 def _write_msh(path, coord, tet, tri, tet_tags, tri_tags, names, *, binary, big_endian=False, id_offset=0):
