@@ -24,8 +24,11 @@ def _op(mesh, mats, staged):
     return op
 
 
-@pytest.mark.parametrize("form", ["plain", "mixed"])
-def test_staged_values_copy_gives_the_same_matrices(cuda_device, form):
+@pytest.mark.parametrize("form,copy,concurrent", [("plain", "kernel", False), ("mixed", "kernel", False),
+                                                  ("plain", "memcpy", True), ("mixed", "memcpy", True)])
+def test_staged_values_copy_gives_the_same_matrices(cuda_device, form, copy, concurrent):
+    """The staged copy of the starting values (by the SM copy kernel or a memcpy) and the force on
+    a second stream give the matrices and forces of the one-stream, unstaged builds."""
     from slope_stability_petsc4py_gb300 import _lib, synthetic
 
     mats = synthetic.MaterialSet.layered(4, seed=3)
@@ -33,6 +36,8 @@ def test_staged_values_copy_gives_the_same_matrices(cuda_device, form):
     ops = (_op(mesh, mats, True), _op(mesh, mats, False))
     for op in ops:
         op.tangent_form = form
+    ops[0].values_copy, ops[0].concurrent_force = copy, concurrent
+    ops[1].values_copy, ops[1].concurrent_force = "memcpy", False
     seq = [(0.010, 1, 0.3, "device"), (0.025, 2, 0.3, "device"), (0.006, 3, 0.3, "tangent"),
            (0.030, 4, 0.5, "device"), (0.015, 5, 0.5, "host"), (0.020, 6, 0.5, "device"), (0.004, 8, 0.3, "device")]
     for amp, seed, r, kind in seq:
