@@ -47,6 +47,7 @@ using namespace tc;
 constexpr int kNP = 35, kNQ = 24, kNLD = 105, kNS = 6;
 constexpr int kM = 128, kN = 112, kPts = 4, kK = kPts * kNS;  // 24 = three K steps of 8
 constexpr int kThreads = 512;
+constexpr int kScatterBatch = 8;                               // map entries a thread loads before its reductions
 constexpr int kTmemCols = 512;                                 // two (hi*hi, cross) accumulator pairs
 constexpr int kColsPerWarp = kN / 4;                           // 28 accumulator columns per drain warp
 constexpr uint32_t kLboA = (kM / 8) * 128, kLboB = (kN / 8) * 128, kSbo = 128;
@@ -69,9 +70,14 @@ struct PointData {  // inputs of the group being built, as double-float (hi + lo
     df32 g[kPts][3][kNP];
     df32 dD[kPts][kNS * kNS];
 };
+struct RawInputs {  // FP64 inputs of the next group, copied ahead by cp.async
+    double g[kPts * 3 * kNP];
+    double ds[kPts * kNS * kNS], w[kPts * kNS * kNS], sh[kPts * kNS * kNS], la[kPts * kNS * kNS];
+};
 struct Smem {
     Stage stage[2];
     PointData pts;
+    RawInputs raw;
     double ke[kNLD * kNLD];  // the element's FP64 sums (upper triangle used), staged for a row-wise scatter
     unsigned long long mbar[2];
     uint32_t tmem_slot;
@@ -127,6 +133,12 @@ __device__ __forceinline__ void drain_add(uint32_t taddr_hh, uint32_t taddr_x, f
         sum[j] = t;
     }
 }
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam) {
     if (i < 3 && j < 3) return i == j ? 2.0 * G + lam : lam;
@@ -207,34 +219,57 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
         float sum[kColsPerWarp], comp[kColsPerWarp];
 #pragma unroll
         for (int j = 0; j < kColsPerWarp; ++j) sum[j] = comp[j] = 0.0f;
+        // the raw FP64 inputs of a group are copied into shared memory one group ahead (cp.async, in
+        // flight while the current group's H is formed and multiplied): thread t < 420 one gradient
+        // value, thread t < 144 one DS entry with its point's w, shear and lame; each thread later
+        // converts only the entries it copied itself
+        // (indices recomputed from tid where used: cheaper than keeping them live across the loop)
+        auto load_group = [&](int grp) {
+            if (tid < kPts * 3 * kNP) {
+                const int gi_pi = tid / (3 * kNP), gi_r = (tid % (3 * kNP)) / kNP, gi_a = tid % kNP;
+                const int k = grp * kPts + gi_pi;
+                if (k < nq) {
+                    const long long src = (g0 + S.sq[k]) * kNP + gi_a;
+                    cp_async8(&S.raw.g[tid], (gi_r == 0 ? d1 : (gi_r == 1 ? d2 : d3)) + src);
+                }
+            }
+            if (tid < kPts * kNS * kNS) {
+                const int k = grp * kPts + tid / (kNS * kNS);
+                if (k < nq) {
+                    const long long gq = g0 + S.sq[k];
+                    cp_async8(&S.raw.ds[tid], DS + gq * (kNS * kNS) + tid % (kNS * kNS));
+                    cp_async8(&S.raw.w[tid], w + gq);
+                    cp_async8(&S.raw.sh[tid], shear + gq);
+                    cp_async8(&S.raw.la[tid], lame + gq);
+                }
+            }
+            cp_async_commit();
+        };
+        load_group(0);
         for (int grp = 0; grp < groups; ++grp) {
             const int b = grp & 1;  // stage buffer and accumulator pair; both were released by drain(grp - 2)
             // inputs of the group's points as hi + lo pairs (absent slots are zero): the gradients,
             // and w s (DS - D_el) with the FP64 subtraction only where D_el is nonzero
-            for (int i = tid; i < kPts * 3 * kNP; i += kThreads) {
-                const int pi = i / (3 * kNP), rem = i % (3 * kNP), r = rem / kNP, a = rem % kNP;
-                const int k = grp * kPts + pi;
-                df32 v{0.0f, 0.0f};
-                if (k < nq) {
-                    const long long src = (g0 + S.sq[k]) * kNP + a;
-                    v = df_from_f64(r == 0 ? d1[src] : (r == 1 ? d2[src] : d3[src]));
-                }
-                S.pts.g[pi][r][a] = v;
+            cp_async_wait_all();
+            if (tid < kPts * 3 * kNP) {
+                const int gi_pi = tid / (3 * kNP), gi_r = (tid % (3 * kNP)) / kNP, gi_a = tid % kNP;
+                const int k = grp * kPts + gi_pi;
+                S.pts.g[gi_pi][gi_r][gi_a] = k < nq ? df_from_f64(S.raw.g[tid]) : df32{0.0f, 0.0f};
             }
-            for (int i = tid; i < kPts * kNS * kNS; i += kThreads) {
-                const int pi = i / (kNS * kNS), kk = i % (kNS * kNS);
-                const int k = grp * kPts + pi;
+            if (tid < kPts * kNS * kNS) {
+                const int di_pi = tid / (kNS * kNS), di_kk = tid % (kNS * kNS);
+                const int k = grp * kPts + di_pi;
                 df32 v{0.0f, 0.0f};
                 if (k < nq) {
-                    const long long gq = g0 + S.sq[k];
-                    double d = DS[gq * (kNS * kNS) + kk];
-                    const double de = elastic_d3(kk % kNS, kk / kNS, shear[gq], lame[gq]);
+                    double d = S.raw.ds[tid];
+                    const double de = elastic_d3(di_kk % kNS, di_kk / kNS, S.raw.sh[tid], S.raw.la[tid]);
                     if (de != 0.0) d -= de;
-                    v = df_mul(df_from_f64(d), df_from_f64(scale * w[gq]));
+                    v = df_mul(df_from_f64(d), df_from_f64(scale * S.raw.w[tid]));
                 }
-                S.pts.dD[pi][kk] = v;
+                S.pts.dD[di_pi][di_kk] = v;
             }
             __syncthreads();
+            if (grp + 1 < groups) load_group(grp + 1);
             Stage &st = S.stage[b];
             unsigned char *a_hi = reinterpret_cast<unsigned char *>(st.a_hi);
             unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
@@ -302,13 +337,23 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
             }
         }
         __syncthreads();
+        // the element's map row (44 KB, not staged) is read kScatterBatch entries per thread at a
+        // time, so a thread's loads are in flight together before its reductions
         const int32_t *em = emap + (long long)e * kNLD * kNLD;
-        for (int idx = tid; idx < kNLD * kNLD; idx += kThreads) {
-            const int a = idx / kNLD, bcol = idx - a * kNLD;
-            const double val = bcol >= a ? S.ke[idx] : S.ke[bcol * kNLD + a];
-            const int32_t p = em[idx];
-            if (p >= 0) {
-                if (p < nnz) red_add(values + p, val);
+        for (int base = tid; base < kNLD * kNLD; base += kThreads * kScatterBatch) {
+            int32_t p[kScatterBatch];
+#pragma unroll
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kThreads;
+                p[u] = idx < kNLD * kNLD ? em[idx] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kThreads;
+                if (p[u] < 0) continue;
+                const int a = idx / kNLD, bcol = idx - a * kNLD;
+                const double val = bcol >= a ? S.ke[idx] : S.ke[bcol * kNLD + a];
+                if (p[u] < nnz) red_add(values + p[u], val);
                 else flag(SSP_DEV_BAD_INDEX);
             }
         }
