@@ -292,6 +292,11 @@ int ssp_host_writable(const void *host_ptr);
  * where both are aligned) rather than a memcpy: the operator's copy of a tangent's starting values,
  * which is then a kernel node when the build is captured in a CUDA graph.  No reference counterpart. */
 int ssp_copy_device(const double *src, long long n, double *dst, void *stream);
+/* The CSR rows r with row_mark[r] != 0 of src copied into dst (both device memory, the same
+ * pattern indptr): restores a values array to its starting values where the previous build's
+ * plastic-element corrections changed it.  No reference counterpart. */
+int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                         double *dst, void *stream);
 
 /* dst_host[0..n) = src[0..n) written by the SMs into pinned, device-mapped host memory
  * (ssp_host_writable(dst_host) must hold, else SSP_ERR_INVALID); asynchronous on the stream.

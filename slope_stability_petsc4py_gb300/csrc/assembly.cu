@@ -1175,6 +1175,19 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
     return launch_status();
 }
 
+int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                         double *dst, void *stream) {
+    if (n_rows < 0 || nnz < 0) return SSP_ERR_INVALID;
+    if (n_rows == 0 || nnz == 0) return SSP_OK;
+    if (!src || !indptr || !row_mark || !dst) return SSP_ERR_INVALID;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
+                                                                                       nnz, dst);
+    return launch_status();
+}
+
 int ssp_copy_device(const double *src, long long n, double *dst, void *stream) {
     if (n < 0) return SSP_ERR_INVALID;
     if (n == 0) return SSP_OK;

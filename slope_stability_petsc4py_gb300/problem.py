@@ -239,6 +239,8 @@ class ConstitutiveOperator:
         # fast as a stream memcpy in direct calls and, unlike a memcpy node, no slower in a
         # captured graph) or "memcpy"
         self.values_copy = "kernel"
+        # restore only the rows the previous build's plastic elements changed (same start values)
+        self.incremental_values = True
         # host outputs: the pinned mirror of the values is refreshed row by row where the values
         # can have changed since the previous build (_changed_rows), else copied in full
         self.incremental_host_copy = True
@@ -581,6 +583,33 @@ class ConstitutiveOperator:
         else:
             dst.copy_(src)
 
+    def _restore_start(self, values, start, kind, key):
+        """values := start.  When values holds start plus the corrections of the last build of this
+        kind with the same start (key), only the rows of that build's plastic elements differ from
+        start, and only those rows are copied (row marks through the element -> row map, then a row
+        copy); otherwise every value is copied.  Not while a CUDA graph is being captured: replays
+        do not alternate the plastic-element lists the restore reads."""
+        t = _lib.torch()
+        last = self._last_build.get(kind)
+        if not (self.incremental_values and last is not None and last["key"] == key and last["values"] is values
+                and not t.cuda.is_current_stream_capturing()):
+            self._copy_values(values, start)
+            return
+        pat = self._require_pattern()
+        dv, d = self._dev, pat.device
+        n_rows, n_el = int(pat.local_matrix_pattern.shape[0]), int(pat.overlap_elements.size)
+        if "restore_mark" not in dv:
+            dv["restore_mark"] = t.empty(max(n_rows, 1), dtype=t.uint8, device="cuda")
+        if "indptr" not in d:
+            d["indptr"] = t.as_tensor(np.asarray(pat.local_matrix_pattern.indptr, dtype=np.int32), device="cuda")
+        mark, st = dv["restore_mark"], _lib.stream_handle()
+        mark.zero_()
+        elist, ecount = dv["plastic_lists"][kind][last["list"]]
+        _lib.call("ssp_mark_element_rows", _lib.ptr(d["elem_row"]), n_el, pat.dim * pat.n_p, _lib.ptr(elist),
+                  _lib.ptr(ecount), n_rows, _lib.ptr(mark), st)
+        _lib.call("ssp_copy_rows_device", _lib.ptr(start), _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows,
+                  int(values.numel()), _lib.ptr(values), st)
+
     def _stage_values(self, r):
         """Issue the copy of the regularised tangent's starting values into its values array on the
         second stream, ahead of the strain and return-mapping kernels that the build runs first:
@@ -601,7 +630,7 @@ class ConstitutiveOperator:
         main, side = t.cuda.current_stream(), self._aux_stream()
         side.wait_stream(main)
         with t.cuda.stream(side):
-            self._copy_values(values, start)
+            self._restore_start(values, start, "regularized", ("regularized", float(r)))
         values.record_stream(side)
         start.record_stream(side)
         done = t.cuda.Event()
@@ -628,7 +657,7 @@ class ConstitutiveOperator:
                 start, key, scale = self._regularized_start(r), ("regularized", float(r)), 1.0 - float(r)
             staged = self._drain_staged()
             if staged is None or staged[0] != key or staged[1] is not values:
-                self._copy_values(values, start)
+                self._restore_start(values, start, key[0], key)
             # else the copy of start, issued on the second stream ahead of the strain and return
             # mapping (_stage_values), has overlapped them
             if ev is not None:

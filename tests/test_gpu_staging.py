@@ -27,8 +27,10 @@ def _op(mesh, mats, staged):
 @pytest.mark.parametrize("form,copy,concurrent", [("plain", "kernel", False), ("mixed", "kernel", False),
                                                   ("plain", "memcpy", True), ("mixed", "memcpy", True)])
 def test_staged_values_copy_gives_the_same_matrices(cuda_device, form, copy, concurrent):
-    """The staged copy of the starting values (by the SM copy kernel or a memcpy) and the force on
-    a second stream give the matrices and forces of the one-stream, unstaged builds."""
+    """The staged copy of the starting values (by the SM copy kernel or a memcpy; restoring only
+    the rows the previous build changed where it can) and the force on a second stream give the
+    matrices and forces of one-stream, unstaged builds that copy every starting value, over states
+    whose plastic sets grow, shrink and move, with r changes, tangent builds and host outputs."""
     from slope_stability_petsc4py_gb300 import _lib, synthetic
 
     mats = synthetic.MaterialSet.layered(4, seed=3)
@@ -37,7 +39,7 @@ def test_staged_values_copy_gives_the_same_matrices(cuda_device, form, copy, con
     for op in ops:
         op.tangent_form = form
     ops[0].values_copy, ops[0].concurrent_force = copy, concurrent
-    ops[1].values_copy, ops[1].concurrent_force = "memcpy", False
+    ops[1].values_copy, ops[1].concurrent_force, ops[1].incremental_values = "memcpy", False, False
     seq = [(0.010, 1, 0.3, "device"), (0.025, 2, 0.3, "device"), (0.006, 3, 0.3, "tangent"),
            (0.030, 4, 0.5, "device"), (0.015, 5, 0.5, "host"), (0.020, 6, 0.5, "device"), (0.004, 8, 0.3, "device")]
     for amp, seed, r, kind in seq:
@@ -53,7 +55,7 @@ def test_staged_values_copy_gives_the_same_matrices(cuda_device, form, copy, con
             vals.append(np.array(v, copy=True))
             forces.append(np.asarray(F.cpu().numpy() if hasattr(F, "cpu") else F, dtype=np.float64).copy())
         err = rel_err(vals[0], vals[1])
-        print(f"{kind} amp {amp} r {r}: staged vs unstaged values {err:.2e}")
+        print(f"{kind} amp {amp} r {r}: staged / incremental vs unstaged full-copy values {err:.2e}")
         # the corrections' CSR reductions run in an unspecified order: equal up to rounding
         assert err <= 1e-14
         assert rel_err(forces[0], forces[1]) <= 1e-14
