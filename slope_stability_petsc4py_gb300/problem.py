@@ -587,22 +587,18 @@ class ConstitutiveOperator:
         """values := start.  When values holds start plus the corrections of the last build of this
         kind with the same start (key), only the rows of that build's plastic elements differ from
         start, and only those rows are copied (row marks through the element -> row map, then a row
-        copy); otherwise every value is copied.  Not while a CUDA graph is being captured: replays
-        do not alternate the plastic-element lists the restore reads."""
+        copy); otherwise every value is copied.  In a captured CUDA graph the build reads and rewrites
+        the same plastic-element list (_tangent_into), so every replay restores the rows of the
+        previous replay's list."""
         t = _lib.torch()
         last = self._last_build.get(kind)
-        if not (self.incremental_values and last is not None and last["key"] == key and last["values"] is values
-                and not t.cuda.is_current_stream_capturing()):
+        if not (self.incremental_values and last is not None and last["key"] == key and last["values"] is values):
             self._copy_values(values, start)
             return
         pat = self._require_pattern()
         dv, d = self._dev, pat.device
         n_rows, n_el = int(pat.local_matrix_pattern.shape[0]), int(pat.overlap_elements.size)
-        if "restore_mark" not in dv:
-            dv["restore_mark"] = t.empty(max(n_rows, 1), dtype=t.uint8, device="cuda")
-        if "indptr" not in d:
-            d["indptr"] = t.as_tensor(np.asarray(pat.local_matrix_pattern.indptr, dtype=np.int32), device="cuda")
-        mark, st = dv["restore_mark"], _lib.stream_handle()
+        mark, st = dv["restore_mark"], _lib.stream_handle()  # allocated with the plastic lists
         mark.zero_()
         elist, ecount = dv["plastic_lists"][kind][last["list"]]
         _lib.call("ssp_mark_element_rows", _lib.ptr(d["elem_row"]), n_el, pat.dim * pat.n_p, _lib.ptr(elist),
@@ -673,11 +669,22 @@ class ConstitutiveOperator:
                 t = _lib.torch()
                 lists[kind] = [(t.empty(max(n_el, 1), dtype=t.int32, device="cuda"),
                                 t.empty(1, dtype=t.int32, device="cuda")) for _ in range(2)]
+                # buffers of the incremental restore (_restore_start), allocated before any capture
+                n_rows = int(pat.local_matrix_pattern.shape[0])
+                if "restore_mark" not in dv:
+                    dv["restore_mark"] = t.empty(max(n_rows, 1), dtype=t.uint8, device="cuda")
+                if "indptr" not in d:
+                    d["indptr"] = t.as_tensor(np.asarray(pat.local_matrix_pattern.indptr, dtype=np.int32),
+                                              device="cuda")
             # two plastic-element lists per kind, alternating: the previous build's list stays
             # valid for the incremental host refresh (_changed_rows)
             last = self._last_build.get(kind)
             same = last is not None and last["key"] == key and last["values"] is values
             cur = 1 - last["list"] if last is not None else 0
+            if same and _lib.torch().cuda.is_current_stream_capturing():
+                # a graph's replays do not alternate: the build restores (_restore_start) and then
+                # rewrites the one list, so each replay restores the previous replay's rows
+                cur = last["list"]
             elist, ecount = lists[kind][cur]
             # the correction visits the plastic elements only (an even share per warp)
             _lib.call("ssp_plastic_elements", _lib.ptr(self._branch), n_el, pat.n_q, _lib.ptr(elist), _lib.ptr(ecount),
