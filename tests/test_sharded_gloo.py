@@ -7,6 +7,10 @@ owned-row pattern of half the nodes with the host pattern builder and evaluate t
 oracle (CPU); rank 0 gathers the rows and they must equal the single-rank rows bit for bit.  This
 is the host-side logic of a sharded multi-GPU run (one rank per GPU, no data-path collective); it
 needs no GPU.
+
+The BDDC case (``src/slope_stability/fem/distributed_tangent.py`` ``prepare_bddc_subdomain_pattern``)
+gives each rank the elements it owns and a local square matrix over their nodes; the subdomain
+matrices, summed through their local-to-global dof maps, must give the whole-mesh tangent.
 """
 
 from __future__ import annotations
@@ -110,3 +114,91 @@ def test_two_gloo_ranks_build_the_single_rank_rows():
             a1, b1 = ip1[j], ip1[j + 1]
             assert np.array_equal(ix_r[a:b], ix1[a1:b1])  # same global columns, same order
             assert np.array_equal(K_r[a:b], K1[a1:b1])
+
+
+# ---------------------------------------------------------------------------- BDDC subdomains
+
+
+def _bddc_local(n_range):
+    """A rank's non-overlapping subdomain (host structure) and its local square tangent values,
+    evaluated by the oracle: DS from the return mapping of the points' strains."""
+    from oracle import oracle_py as oracle
+    from slope_stability_petsc4py_gb300.bddc import bddc_local_structure
+
+    mats, mesh, U = _problem()
+    xi, wf = fem.quadrature(3, "P2")
+    n_q = xi.shape[1]
+    s = bddc_local_structure(mesh.coord, mesh.elem, mesh.q_mask, n_range, n_q=n_q)
+    nodes, elem_local = s["local_nodes"], s["elem_local"]
+    dphi, w = oracle.geometry(mesh.coord[:, nodes], elem_local, 3, fem.reference_gradients(3, "P2"), wf)
+    dof = (3 * elem_local.T[:, :, None] + np.arange(3)[None, None, :]).reshape(elem_local.shape[1], -1).astype(np.int32)
+    u_loc = np.ascontiguousarray(U.reshape(-1, order="F")[s["local_global_dofs"]])
+    E = oracle.strain_3d(dphi[0], dphi[1], dphi[2], u_loc, dof, n_q)
+    n = E.shape[0]
+    shear, lame = np.full(n, float(mats.shear[0])), np.full(n, float(mats.lame[0]))
+    c_bar, sin_phi = oracle.reduction(np.full(n, float(mats.c0[0])), np.full(n, np.deg2rad(float(mats.phi[0]))),
+                                      np.zeros(n), 1.1, "B")
+    _, DS = oracle.constitutive_3d(E, c_bar, sin_phi, shear, shear, lame)
+    lp = s["local_matrix_pattern"]
+    K = oracle.tangent_scatter(3, dphi[0], dphi[1], dphi[2], DS, w, s["scatter_map"], n_q, lp.nnz)
+    K[s["constrained_diag_positions"]] = 1.0
+    return {"elements": s["local_elements"], "gdofs": s["local_global_dofs"], "free": s["free_local"],
+            "indptr": lp.indptr, "indices": lp.indices, "values": K}
+
+
+def _bddc_rank_main(rank, world, port, queue, split):
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    _, mesh, _ = _problem()
+    bounds = [0, split, mesh.n_nodes]
+    mine = _bddc_local((bounds[rank], bounds[rank + 1]))
+    gathered = [None] * world
+    dist.all_gather_object(gathered, mine)
+    if rank == 0:
+        queue.put(gathered)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_bddc_subdomains_sum_to_the_global_tangent():
+    """Each rank owns the elements whose smallest node lies in its node range: the subdomains
+    partition the elements, and their local square tangents, summed through the local-to-global
+    dof maps, give the single-subdomain (whole-mesh) tangent on the free dofs."""
+    import torch.multiprocessing as mp
+    from scipy.sparse import coo_matrix, csr_matrix
+
+    from oracle import oracle_py as oracle
+
+    oracle.build()
+    _, mesh, _ = _problem()
+    owners = np.sort(mesh.elem.min(axis=0))
+    split = int(owners[owners.size // 2])
+    ctx = mp.get_context("spawn")
+    queue = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_bddc_rank_main, args=(r, 2, port, queue, split)) for r in range(2)]
+    for p in procs:
+        p.start()
+    parts = queue.get(timeout=300)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    elems = np.concatenate([p["elements"] for p in parts])
+    assert np.array_equal(np.sort(elems), np.arange(mesh.n_elem))  # a partition of the elements
+    assert all(p["elements"].size > 0 for p in parts)
+    n_dof = 3 * mesh.n_nodes
+    free = mesh.q_mask.reshape(-1, order="F")
+
+    def assemble(p):
+        A = csr_matrix((p["values"], p["indices"], p["indptr"]), shape=(p["gdofs"].size,) * 2).tocoo()
+        keep = p["free"][A.row] & p["free"][A.col]  # the free-free block (Dirichlet rows are local identities)
+        return coo_matrix((A.data[keep], (p["gdofs"][A.row[keep]], p["gdofs"][A.col[keep]])), shape=(n_dof, n_dof))
+
+    K_sum = (assemble(parts[0]) + assemble(parts[1])).tocsr()
+    K_one = assemble(_bddc_local((0, mesh.n_nodes))).tocsr()
+    diff = abs(K_sum - K_one).max()
+    assert diff <= 1e-12 * abs(K_one).max()
+    assert K_one[free][:, free].nnz > 0 and K_sum[~free].nnz == 0
