@@ -128,6 +128,20 @@ int ssp_constitutive_3d_sds_binned_noalloc(const double *E, const double *c_bar,
 int ssp_constitutive_2d(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                         const double *bulk, const double *lame, int n_int, double *S_out, double *DS_out, void *stream);
 
+/* Replaces potential_3D / potential_2D (src/slope_stability/constitutive/problem.py:1111-1190,
+ * 1029-1108) and the weighted sum of ConstitutiveOperator.potential_energy (problem.py:2148-2157):
+ *   psi_out[p]   = the Mohr-Coulomb potential energy density at point p (NULL: not written);
+ *   branch_out[p] = its branch, 0 elastic, 1 smooth, 2 left edge, 3 right edge, 4 apex (NULL: not written);
+ *   *total_out   = sum_p weight[p] * psi[p], one double on the device (NULL: not computed; weight
+ *                  and partial are then unused and may be NULL).
+ * E is [n_int][6] (3D) or [n_int][3] (2D); bulk enters the apex branch.  partial is caller scratch
+ * of SSP_POTENTIAL_PARTIALS doubles; the sum is deterministic (fixed grid, fixed trees) for a
+ * given n_int.  Two launches when total_out is given, one otherwise. */
+#define SSP_POTENTIAL_PARTIALS 1024
+int ssp_potential_energy(int dim, const double *E, const double *c_bar, const double *sin_phi, const double *shear,
+                         const double *bulk, const double *lame, const double *weight, int n_int, double *psi_out,
+                         int8_t *branch_out, double *partial, double *total_out, void *stream);
+
 /* Replaces reduction(c0, phi, psi, lam, Davis_type) (src/slope_stability/constitutive/reduction.py:14-78).
  * davis_type is 'A', 'B' or 'C'; lam must be > 0. */
 int ssp_reduction(const double *c0, const double *phi, const double *psi, int n_int, double lam, char davis_type,

@@ -7,6 +7,7 @@ checker used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
 Restated reference routines (paths relative to the reference project root):
 
 * ``constitutive_2d``      -- src/slope_stability/constitutive/problem.py:143-475
+* ``potential_2d``, ``potential_3d`` -- src/slope_stability/constitutive/problem.py:1029-1190
 * ``reduction``            -- src/slope_stability/constitutive/reduction.py:14-78
 * ``geometry``             -- src/slope_stability/fem/assembly.py:50-136 (2D), :139-245 (3D)
 * ``owned_pattern``        -- src/slope_stability/fem/distributed_tangent.py:297-478, 937-1175
@@ -295,6 +296,99 @@ def constitutive_2d(E, c_bar, sin_phi, shear, bulk, lame, tangent=True):
     S[:, ap] = iota4[:, None] * (c[ap] / (2.0 * s[ap]))[None, :]
     DS[:, ap] = 0.0
     return (S, DS) if tangent else S
+
+
+def _np_safe_denominator(d):
+    """The reference's guard: a denominator below 1e-15 in magnitude becomes +-1e-15."""
+    return np.where(np.abs(d) < 1.0e-15, np.sign(d + 1.0e-15) * 1.0e-15, d)
+
+
+def _mc_potential(e1, e2, e3, tr, c, s, G, K, lam, d_s, d_l, d_r):
+    """Branch selection and energy shared by the 2D and 3D potentials (the reference's
+    src/slope_stability/constitutive/problem.py:1075-1108 and :1158-1190)."""
+    f_tr = 2.0 * G * ((1.0 + s) * e1 - (1.0 - s) * e3) + 2.0 * (lam * s) * tr - c
+    g_sl = (e1 - e2) / np.maximum(1.0e-15, 1.0 + s)
+    g_sr = (e2 - e3) / np.maximum(1.0e-15, 1.0 - s)
+    g_la = (e1 + e2 - 2.0 * e3) / np.maximum(1.0e-15, 3.0 - s)
+    g_ra = (2.0 * e1 - e2 - e3) / np.maximum(1.0e-15, 3.0 + s)
+    d_a = 4.0 * K * s ** 2
+    l_s = f_tr / _np_safe_denominator(d_s)
+    l_l = (G * ((1.0 + s) * (e1 + e2) - 2.0 * (1.0 - s) * e3) + 2.0 * lam * s * tr - c) / _np_safe_denominator(d_l)
+    l_r = (G * (2.0 * (1.0 + s) * e1 - (1.0 - s) * (e2 + e3)) + 2.0 * lam * s * tr - c) / _np_safe_denominator(d_r)
+    l_a = (2.0 * K * s * tr - c) / _np_safe_denominator(d_a)
+    vol = 0.5 * lam * tr ** 2
+    el = f_tr <= 0.0
+    sm = (l_s <= np.minimum(g_sl, g_sr)) & ~el
+    lm = (g_sl < g_sr) & (l_l >= g_sl) & (l_l <= g_la) & ~(el | sm)
+    rm = (g_sl > g_sr) & (l_r >= g_sr) & (l_r <= g_ra) & ~(el | sm)
+    elastic = vol + G * (e1 ** 2 + e2 ** 2 + e3 ** 2)
+    psi = 0.5 * K * tr ** 2 - 0.5 * d_a * l_a ** 2
+    psi = np.where(rm, vol + G * (e1 ** 2 + 0.5 * (e2 + e3) ** 2) - 0.5 * d_r * l_r ** 2, psi)
+    psi = np.where(lm, vol + G * (e3 ** 2 + 0.5 * (e1 + e2) ** 2) - 0.5 * d_l * l_l ** 2, psi)
+    psi = np.where(sm, elastic - 0.5 * d_s * l_s ** 2, psi)
+    psi = np.where(el, elastic, psi)
+    branch = np.select([el, sm, lm, rm], [0, 1, 2, 3], 4).astype(np.int8)
+    return psi, branch
+
+
+def potential_3d(E, c_bar, sin_phi, shear, bulk, lame, *, with_branch=False):
+    """Mohr-Coulomb potential energy density, E (6, n) -> Psi (n,)  (the reference's
+    ``potential_3D``, src/slope_stability/constitutive/problem.py:1111-1190).
+
+    As the reference does: the invariants take E's rows 3, 4, 5 as the tensor entries
+    (12), (13), (23) without halving the engineering shears, while E is ordered
+    [11, 22, 33, 12, 23, 13] -- so I3 pairs e22 with gamma_23 and e11 with gamma_13 -- and the
+    eigenvalues come from the trigonometric formula with the 1e-15 guard on sqrt(Q^3)."""
+    E = np.asarray(E, dtype=np.float64)
+    c, s, G, K, lam = (np.asarray(a, dtype=np.float64).ravel() for a in (c_bar, sin_phi, shear, bulk, lame))
+    e11, e22, e33, r3, r4, r5 = E
+    I1 = e11 + e22 + e33
+    I2 = e11 * e22 + e11 * e33 + e22 * e33 - r3 * r3 - r4 * r4 - r5 * r5
+    I3 = e11 * e22 * e33 - e33 * r3 * r3 - e22 * r4 * r4 - e11 * r5 * r5 + 2.0 * r3 * r4 * r5
+    Q = np.maximum(0.0, (I1 * I1 - 3.0 * I2) / 9.0)
+    R = (-2.0 * I1 ** 3 + 9.0 * I1 * I2 - 27.0 * I3) / 54.0
+    theta = np.zeros_like(Q)
+    on = Q > 0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        theta[on] = np.arccos(np.clip(R[on] / np.maximum(1.0e-15, np.sqrt(Q[on] ** 3)), -1.0, 1.0)) / 3.0
+    rq = np.sqrt(Q)
+    e1 = -2.0 * rq * np.cos(theta + 2.0 * np.pi / 3.0) + I1 / 3.0
+    e2 = -2.0 * rq * np.cos(theta - 2.0 * np.pi / 3.0) + I1 / 3.0
+    e3 = -2.0 * rq * np.cos(theta) + I1 / 3.0
+    d_s = 4.0 * lam * s ** 2 + 4.0 * G * (1.0 + s ** 2)
+    d_l = 4.0 * lam * s ** 2 + G * (1.0 + s) * (1.0 + s) + 2.0 * G * (1.0 - s) * (1.0 - s)
+    d_r = 4.0 * lam * s ** 2 + 2.0 * G * (1.0 + s) * (1.0 + s) + G * (1.0 - s) * (1.0 - s)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        psi, br = _mc_potential(e1, e2, e3, I1, c, s, G, K, lam, d_s, d_l, d_r)
+    return (psi, br) if with_branch else psi
+
+
+def potential_2d(E, c_bar, sin_phi, shear, bulk, lame, *, with_branch=False):
+    """Plane-strain potential energy density, E (3, n) -> Psi (n,)  (the reference's
+    ``potential_2D``, src/slope_stability/constitutive/problem.py:1029-1108).
+
+    As the reference's arrays do (its sorted eigenvalues alias the unsorted ones, so the
+    reordering overwrites before it reads): where the in-plane eigenvalues straddle the
+    out-of-plane zero (e_a >= 0 > e_b) the sorted triple is (e_a, 0, 0), and where both are
+    negative it is (0, 0, 0); otherwise (e_a, e_b, 0)."""
+    E = np.asarray(E, dtype=np.float64)
+    c, s, G, K, lam = (np.asarray(a, dtype=np.float64).ravel() for a in (c_bar, sin_phi, shear, bulk, lame))
+    e11, e22, g12 = E
+    tr2 = e11 + e22
+    rad = np.sqrt((e11 - e22) ** 2 + g12 * g12)
+    ea, eb = (tr2 + rad) / 2.0, (tr2 - rad) / 2.0
+    straddle = (ea >= 0.0) & (0.0 > eb)
+    negative = 0.0 > ea
+    e1 = np.where(negative, 0.0, ea)
+    e2 = np.where(straddle | negative, 0.0, eb)
+    e3 = np.zeros_like(ea)
+    tr = e1 + e2 + e3
+    d_s = 4.0 * lam * s ** 2 + 2.0 * G * (1.0 + s) ** 2 + 2.0 * G * (1.0 - s) ** 2
+    d_l = 4.0 * lam * s ** 2 + G * (1.0 + s) ** 2 + 2.0 * G * (1.0 - s) ** 2
+    d_r = 4.0 * lam * s ** 2 + 2.0 * G * (1.0 + s) ** 2 + G * (1.0 - s) ** 2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        psi, br = _mc_potential(e1, e2, e3, tr, c, s, G, K, lam, d_s, d_l, d_r)
+    return (psi, br) if with_branch else psi
 
 
 def geometry(coord, elem, dim, dhat, wf):

@@ -16,6 +16,8 @@ import numpy as np
 from . import build as _build
 
 _LIB = None
+# SSP_POTENTIAL_PARTIALS of the header: the block partials ssp_potential_energy needs as scratch
+POTENTIAL_PARTIALS = 1024
 _c_int, _c_ll, _c_dbl, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported element", 4: "int32 overflow",
@@ -26,6 +28,7 @@ _SIGS = {
     "ssp_constitutive_3d_sds": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_3d_branch": [_vp] * 5 + [_c_int, _vp, _vp, _vp],
     "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
+    "ssp_potential_energy": [_c_int] + [_vp] * 7 + [_c_int] + [_vp] * 5,
     "ssp_host_writable": [_vp],
     "ssp_copy_out": [_vp, _c_ll, _vp, _vp],
     "ssp_copy_device": [_vp, _c_ll, _vp, _vp],
@@ -132,6 +135,7 @@ _KERNELS_PER_CALL = {
     "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 4,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
+    "ssp_potential_energy": lambda a: int(a[8] > 0) + int(a[12] is not None),
 }
 LAUNCHES = {"count": 0}
 # When set to a list, every kernel-launching call appends (name, start_event, end_event), recorded

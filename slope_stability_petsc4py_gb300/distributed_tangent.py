@@ -268,6 +268,12 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
               int(ov_nodes.size), n_ov, n_p, n_q, _lib.ptr(dev["dphi1"]), _lib.ptr(dev["dphi2"]),
               _lib.ptr(dev["dphi3"]) if dim == 3 else None, _lib.ptr(dev["weight"]), _lib.stream_handle())
     del coord_ov, elem_d
+    owner = elem[:, ov_el].min(axis=0) if n_ov else np.empty(0, dtype=np.int64)
+    owned_el = (owner >= n0) & (owner < n1)
+    if not owned_el.all():
+        # the overlap elements whose smallest node the range owns: over the ranks they partition
+        # the mesh, so the ranks' integrated potential energies add up to the whole mesh's
+        dev["energy_weight"] = dev["weight"] * _lib.to_device(np.repeat(owned_el.astype(np.float64), n_q), f64)
     if dim == 3 and n_ov:
         # J^{-1} of every overlap element from its vertices, J = [x1 - x0, x2 - x0, x3 - x0] (the
         # mixed form's affine strain and force use it where the elements are straight-sided)

@@ -252,6 +252,7 @@ class ConstitutiveOperator:
         self.return_mapping = "binned"
         self.branch_model = None
         self._scratch = None
+        self._energy_scratch = None  # block partials + total of potential_energy
         # "plain": FP64 throughout (the drop-in, parity 1e-12 with the reference);
         # "mixed": the plastic-point tangent products in FP32 (CUDA cores for P1/P2, tensor cores
         # for P4) with H = w D B formed in compensated double-float arithmetic, and the 3D strain and
@@ -1087,8 +1088,42 @@ class ConstitutiveOperator:
         self.constitutive_problem_stress_tangent(U)
         return self._regularized_pair(self.build_F_free, r)
 
-    def potential_energy(self, U):  # pragma: no cover - not on the Newton hot path
-        raise NotImplementedError("potential_energy is not part of the GPU hot path (the line search does not call it)")
+    def potential_energy(self, U):
+        """Integrated Mohr-Coulomb potential energy sum_p w_p Psi(E_p(U)) at the current reduction,
+        a float (the reference's ConstitutiveOperator.potential_energy, problem.py:2148-2157,
+        which the direct SSR continuation calls twice per step, continuation/omega.py:61,83).
+
+        FP64 strain and energy at every overlap point in one kernel with a deterministic block
+        sum.  With an owned node range that is part of the mesh, each rank sums the elements whose
+        smallest node it owns, and the ranks' sums are all-reduced when a process group is up, so
+        every rank returns the whole mesh's energy as the reference's global evaluation does."""
+        t0 = perf_counter()
+        pat = self._require_pattern()
+        if self._owned_overlap_c_bar is None:
+            raise ValueError("Material reduction not set. Call reduction(lambda) first.")
+        t = _lib.require_cuda()
+        E = overlap_strain_device(pat, U)
+        d = self._dev
+        w = pat.device.get("energy_weight", pat.device["weight"])
+        if self._energy_scratch is None:
+            self._energy_scratch = t.empty(_lib.POTENTIAL_PARTIALS + 1, dtype=t.float64, device="cuda")
+        part, total = self._energy_scratch[:-1], self._energy_scratch[-1:]
+        _lib.call("ssp_potential_energy", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
+                  _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]),
+                  _lib.ptr(w), int(pat.n_local_int), None, None, _lib.ptr(part), _lib.ptr(total),
+                  _lib.stream_handle())
+        value = float(total.item())
+        _lib.raise_on_device_status()
+        if "energy_weight" in pat.device:
+            import torch.distributed as dist
+
+            if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+                on_gpu = dist.get_backend() == "nccl"
+                buf = t.tensor([value], dtype=t.float64, device="cuda" if on_gpu else "cpu")
+                dist.all_reduce(buf)
+                value = float(buf.item())
+        self.time_potential.append(perf_counter() - t0)
+        return value
 
     def get_total_time(self):
         return {

@@ -340,6 +340,32 @@ def gen_constitutive_2d(problem, red):
     print("constitutive_2d", n, "points")
 
 
+def gen_potential(problem, red):
+    """The reference's potential_3D / potential_2D (the energy the direct SSR continuation
+    differences in lambda) on the constitutive test points, two material sets."""
+    rng = np.random.default_rng(19)
+    E3 = constitutive_points(rng).T.copy()  # (6, n)
+    E2 = np.hstack([rng.standard_normal((3, 250)) * s for s in (1e-4, 1e-3, 3e-3, 1e-2)]
+                   + [np.array([[0, 0, 0], [1e-3, 1e-3, 0], [-1e-3, -1e-3, 0], [2e-3, -1e-3, 0], [0, 0, 4e-3],
+                                [5e-3, 5e-3, 0], [-1e-3, -2e-3, 0]], dtype=np.float64).T])
+    out = {"E3": E3, "E2": E2}
+    for key, (c0, phi, young, nu, lam) in {"bench": (6.0, 45.0, 2.0e4, 0.49, 1.1),
+                                           "test": (15.0, 30.0, 1.0e4, 0.33, 1.3)}.items():
+        shear = young / (2.0 * (1.0 + nu))
+        bulk = young / (3.0 * (1.0 - 2.0 * nu))
+        lame = bulk - 2.0 * shear / 3.0
+        for dim, E in ((3, E3), (2, E2)):
+            n = E.shape[1]
+            c_bar, sin_phi = red.reduction(np.full(n, c0), np.full(n, np.deg2rad(phi)), np.zeros(n), lam, "B")
+            mats = (c_bar, sin_phi, np.full(n, shear), np.full(n, bulk), np.full(n, lame))
+            psi = (problem.potential_3D if dim == 3 else problem.potential_2D)(E, *mats)
+            tag = f"{key}_{dim}d"
+            out.update({f"{tag}_c_bar": c_bar, f"{tag}_sin_phi": sin_phi, f"{tag}_shear": mats[2],
+                        f"{tag}_bulk": mats[3], f"{tag}_lame": mats[4], f"{tag}_psi": psi})
+    np.savez_compressed(HERE / "potential.npz", **out)
+    print("potential", E3.shape[1], "3D points,", E2.shape[1], "2D points")
+
+
 def gen_reduction(red):
     rng = np.random.default_rng(3)
     n = 64
@@ -550,7 +576,7 @@ def gen_mesh_io(ref):
 
 
 GENERATORS = ("constitutive_3d", "constitutive_2d", "reduction", "patterns", "pattern_2d", "pattern_2d_p4", "bddc",
-              "mesh_io")
+              "mesh_io", "potential")
 
 
 def main(which=GENERATORS):
@@ -576,6 +602,8 @@ def main(which=GENERATORS):
         gen_bddc(ref, kern)
     if "mesh_io" in which:
         gen_mesh_io(ref)
+    if "potential" in which:
+        gen_potential(ref["problem"], ref["reduction"])
 
 
 if __name__ == "__main__":

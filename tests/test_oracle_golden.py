@@ -157,3 +157,18 @@ def test_constitutive_operator_outputs_consistent(oracle, name):
     F[~g["owned_free_mask"]] = 0.0
     assert rel_err(F, g["op_F"]) <= PLAIN_RTOL
     assert rel_err(F[g["owned_free_mask"]], g["op_F_free"]) <= PLAIN_RTOL
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_potential_restatement_matches_reference(oracle, dim):
+    """The oracle's potential energy densities equal the reference's potential_3D / potential_2D
+    (src/slope_stability/constitutive/problem.py:1029-1190) bit for bit, including what the
+    reference computes for compressive plane-strain states and unhalved 3D shears."""
+    g = golden("potential.npz")
+    E = g["E3"] if dim == 3 else g["E2"]
+    fn = oracle.potential_3d if dim == 3 else oracle.potential_2d
+    for key in ("bench", "test"):
+        tag = f"{key}_{dim}d"
+        psi, br = fn(E, *(g[f"{tag}_{k}"] for k in ("c_bar", "sin_phi", "shear", "bulk", "lame")), with_branch=True)
+        assert np.array_equal(psi, g[f"{tag}_psi"])
+        assert np.bincount(br, minlength=5).min() > 0 or dim == 2  # every 3D branch is exercised
