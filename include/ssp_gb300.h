@@ -202,6 +202,20 @@ int ssp_assemble_force_element_affine_mixed(const float *jinv_hl, const float *g
                                             const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                             int n_rows, double *out_values, void *stream);
 
+/* Straight-sided P2 tetrahedra (no reference counterpart; same results as
+ * ssp_assemble_overlap_strain_3d / ssp_assemble_force_element within rounding): the strain and
+ * the owned force through the barycentric form of the quadratic basis, from J^{-1} per element
+ * (jinv [n_elem][3][3], row k = the gradient of barycentric coordinate k+1) and the quadrature
+ * points' barycentric coordinates (bary [n_q][4]) instead of per-point gradients.  Local node order
+ * of the reference's P2 tetrahedron: vertices 0-3, edges 01, 12, 02, 13, 23, 03.  The force
+ * entry zeroes out_values first; elem_row as in ssp_assemble_force_element. */
+int ssp_assemble_overlap_strain_3d_p2_affine(const double *jinv, const double *bary, const double *u_overlap, int n_u,
+                                             const int32_t *elem_dof_lids, int n_int, int n_elem, int n_q,
+                                             double *out_values, void *stream);
+int ssp_assemble_force_element_p2_affine(const double *jinv, const double *bary, const double *stress,
+                                         const double *weight, const int32_t *elem_row, int n_elem, int n_q,
+                                         int n_rows, double *out_values, void *stream);
+
 /* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
  * Deterministic row gather; rows without slots come out 0. */
 int ssp_assemble_force_3d_rows(const double *dphi1, const double *dphi2, const double *dphi3, const double *stress,

@@ -144,6 +144,9 @@ class OwnedTangentPattern:
     timings: dict = field(default_factory=dict)
     # whether every overlap element is affine (the mixed form's J^{-1} strain and force); None: not checked
     affine: bool | None = field(default=None, repr=False)
+    # whether the plain form's regrouped P2 strain and force apply (3D P2, every element affine to
+    # rounding); None: not checked
+    affine_p2: bool | None = field(default=None, repr=False)
 
     # host views of device-resident per-point data (copied on first access)
     def _host(self, key):
@@ -427,6 +430,22 @@ def _affine_elements(pattern, rtol: float = 1e-10, chunk: int = 1 << 16) -> bool
     return True
 
 
+def _p2_affine_inputs(pattern):
+    """The device arrays with J^{-1} per element and the quadrature points' barycentric
+    coordinates when the pattern is 3D P2 and every element is affine to rounding (stored and
+    reconstructed gradients within 1e-13 of each other, so the regrouped kernels stay at the plain
+    form's 1e-12); None otherwise.  Checked once per pattern."""
+    d = pattern.device
+    if pattern.affine_p2 is None:
+        ok = pattern.dim == 3 and pattern.n_p == 10 and "jinv" in d and _affine_elements(pattern, rtol=1e-13)
+        if ok:
+            xi, _ = quadrature(3, pattern.elem_type)
+            bary = np.ascontiguousarray(np.vstack([1.0 - xi[0] - xi[1] - xi[2], xi]).T)  # (n_q, 4)
+            d["bary"] = _lib.to_device(bary, _lib.torch().float64)
+        pattern.affine_p2 = bool(ok)
+    return d if pattern.affine_p2 else None
+
+
 def _mixed_inputs(pattern):
     """Per-pattern hi + lo pairs of the mixed form's constant inputs, split once and kept with the
     pattern's device arrays: of the gradients and w * gradient, or, when every element is affine,
@@ -468,6 +487,9 @@ def overlap_strain_device(pattern, U, *, mixed: bool = False):
             _lib.call("ssp_assemble_overlap_strain_3d_mixed", _lib.ptr(d["dphi1_hl"]), _lib.ptr(d["dphi2_hl"]),
                       _lib.ptr(d["dphi3_hl"]), _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el,
                       pattern.n_p, pattern.n_q, _lib.ptr(E), st)
+    elif pattern.dim == 3 and _p2_affine_inputs(pattern) is not None:
+        _lib.call("ssp_assemble_overlap_strain_3d_p2_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]), _lib.ptr(u_ov),
+                  int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_q, _lib.ptr(E), st)
     elif pattern.dim == 3:
         _lib.call("ssp_assemble_overlap_strain_3d", _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
                   _lib.ptr(u_ov), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p, pattern.n_q,
@@ -524,6 +546,11 @@ def owned_force_device(pattern, S_aos, *, mixed: bool = False):
                       _lib.ptr(d["wdphi3_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]),
                       int(pattern.overlap_elements.size), pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F),
                       _lib.stream_handle())
+        return F
+    if pattern.dim == 3 and _p2_affine_inputs(pattern) is not None:
+        _lib.call("ssp_assemble_force_element_p2_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]), _lib.ptr(S_aos),
+                  _lib.ptr(d["weight"]), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size), pattern.n_q,
+                  n_rows, _lib.ptr(F), _lib.stream_handle())
         return F
     _lib.call("ssp_assemble_force_element", pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
               _lib.ptr(d["dphi3"]) if pattern.dim == 3 else None, _lib.ptr(S_aos), _lib.ptr(d["weight"]),

@@ -126,6 +126,7 @@ def test_mixed_strain_and_force_on_curved_elements(cuda_device):
     E64 = overlap_strain_device(pat, U).cpu().numpy()
     Emx = overlap_strain_device(pat, U, mixed=True).cpu().numpy()
     assert pat.affine is False
+    assert pat.affine_p2 is False  # the plain form reads the per-point gradients too
     op.reduction(1.1)
     op.constitutive_problem_stress_tangent(U)
     F64 = owned_force_device(pat, op._S_aos).cpu().numpy()
