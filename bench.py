@@ -293,6 +293,10 @@ def algorithmic(name, st):
         return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": n_el * 2 * (204 + 24 * n_q)}
     if name == "ssp_assemble_force_element_p2_affine":  # moments of w σ, FP64: ≈530 per 11-point element
         return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": n_el * 2 * (200 + 30 * n_q)}
+    if name == "ssp_assemble_overlap_strain_3d_p2_affine_mixed":  # double-float, barycentric form
+        return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": 0}
+    if name == "ssp_assemble_force_element_p2_affine_mixed":
+        return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": 0}
     if name in ("ssp_assemble_force_element", "ssp_assemble_force_element_mixed"):
         fp64 = 0 if name.endswith("_mixed") else n * nld * 8
         return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": fp64}

@@ -215,6 +215,15 @@ int ssp_assemble_overlap_strain_3d_p2_affine(const double *jinv, const double *b
 int ssp_assemble_force_element_p2_affine(const double *jinv, const double *bary, const double *stress,
                                          const double *weight, const int32_t *elem_row, int n_elem, int n_q,
                                          int n_rows, double *out_values, void *stream);
+/* The same two in the mixed form's double-float arithmetic (hi + lo float pairs of J^{-1}, of the
+ * barycentric coordinates, of the displacements and of the weights, as the _affine_mixed entries
+ * take them); FP64 outputs, about 1e-13 relative. */
+int ssp_assemble_overlap_strain_3d_p2_affine_mixed(const float *jinv_hl, const float *bary_hl, const float *u_hl,
+                                                   int n_u, const int32_t *elem_dof_lids, int n_int, int n_elem, int n_q,
+                                                   double *out_values, void *stream);
+int ssp_assemble_force_element_p2_affine_mixed(const float *jinv_hl, const float *bary_hl, const float *w_hl,
+                                               const double *stress, const int32_t *elem_row, int n_elem, int n_q,
+                                               int n_rows, double *out_values, void *stream);
 
 /* Replaces assemble_force_3d_rows_c (src/slope_stability/cython/assemble_tangent_values_3d.h:53-68).
  * Deterministic row gather; rows without slots come out 0. */

@@ -299,6 +299,170 @@ __global__ void __launch_bounds__(kForceThreads) force3_affine_mixed_kernel(cons
     if (r2 >= 0) red_add(F + r2, a2.value());
 }
 
+// ---------------------------------------------------------------------------- P2, barycentric form
+
+// Straight-sided P2 tetrahedra in double-float arithmetic: the barycentric regrouping of the FP64
+// strain3_p2_affine_kernel / force3_p2_affine_kernel.  ∇φ_i = (4λ_i − 1)∇λ_i at vertex i,
+// ∇φ_ij = 4(λ_i∇λ_j + λ_j∇λ_i) at the node of edge ij, ∇λ_1..3 the rows of J⁻¹, ∇λ_0 = −Σ; the
+// strain is Σ_m λ_m S_m with four strain vectors per element, the force needs the four moments
+// M_m = Σ_q λ_qm w_q σ_q.  One thread per element; local nodes: vertices 0-3, then the edges
+// 01, 12, 02, 13, 23, 03 (simplex_lagrange.py:15-83).
+__device__ __forceinline__ constexpr int p2_edge(int i, int j) {
+    return (i < j ? i : j) == 0 ? ((i > j ? i : j) == 1 ? 4 : ((i > j ? i : j) == 2 ? 6 : 9))
+                                : ((i < j ? i : j) == 1 ? ((i > j ? i : j) == 2 ? 5 : 7) : 8);
+}
+__device__ __forceinline__ df32 df_times4(df32 a) { return {4.0f * a.hi, 4.0f * a.lo}; }  // exact
+__device__ __forceinline__ df32 df_times3(df32 a) { return df_mul(a, df32{3.0f, 0.0f}); }
+
+__global__ void __launch_bounds__(64) strain3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                   const float2 *__restrict__ bary,
+                                                                   const float2 *__restrict__ u,
+                                                                   const int32_t *__restrict__ dof, long long n_u,
+                                                                   int n_elem, int n_q, double *__restrict__ E) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    df32 un[10][3];
+    const int32_t *dl = dof + e * 30;
+#pragma unroll
+    for (int a = 0; a < 10; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int32_t i = dl[3 * a + c];
+            if (i < 0 || i >= n_u) {
+                flag(SSP_DEV_BAD_INDEX);
+                un[a][c] = df32{0.0f, 0.0f};
+            } else {
+                un[a][c] = ld(u + i);
+            }
+        }
+    df32 gl[3][3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) gl[k / 3][k % 3] = ld(jinv + e * 9 + k);
+    df32 S[4][6];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        df32 A0[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            A0[c] = m == 0 ? df_times3(un[0][c]) : df_add(df_times4(un[p2_edge(0, m)][c]), df_neg(un[0][c]));
+        CSum G[3][3];
+#pragma unroll
+        for (int i = 1; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const df32 Ai = i == m ? df_times3(un[i][c]) : df_add(df_times4(un[p2_edge(i, m)][c]), df_neg(un[i][c]));
+                const df32 b = df_add(Ai, df_neg(A0[c]));
+#pragma unroll
+                for (int k = 0; k < 3; ++k) G[c][k].add_prod(b, gl[i - 1][k]);
+            }
+        S[m][0] = G[0][0].df();
+        S[m][1] = G[1][1].df();
+        S[m][2] = G[2][2].df();
+        S[m][3] = df_add(G[0][1].df(), G[1][0].df());
+        S[m][4] = df_add(G[1][2].df(), G[2][1].df());
+        S[m][5] = df_add(G[0][2].df(), G[2][0].df());
+    }
+    for (int q = 0; q < n_q; ++q) {
+        const df32 l[4] = {ld(bary + 4 * q), ld(bary + 4 * q + 1), ld(bary + 4 * q + 2), ld(bary + 4 * q + 3)};
+        double v[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            CSum acc;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) acc.add_prod(l[m], S[m][c]);
+            v[c] = acc.value();
+        }
+        double2 *o = reinterpret_cast<double2 *>(E + 6 * (e * n_q + q));
+        o[0] = make_double2(v[0], v[1]);
+        o[1] = make_double2(v[2], v[3]);
+        o[2] = make_double2(v[4], v[5]);
+    }
+}
+
+// (M v) for M symmetric as [11,22,33,12,23,13], accumulated into three compensated sums
+__device__ __forceinline__ void df_sym_matvec_add(const df32 *M, const df32 *v, CSum *out) {
+    out[0].add_prod(M[0], v[0]);
+    out[0].add_prod(M[3], v[1]);
+    out[0].add_prod(M[5], v[2]);
+    out[1].add_prod(M[3], v[0]);
+    out[1].add_prod(M[1], v[1]);
+    out[1].add_prod(M[4], v[2]);
+    out[2].add_prod(M[5], v[0]);
+    out[2].add_prod(M[4], v[1]);
+    out[2].add_prod(M[2], v[2]);
+}
+
+__global__ void __launch_bounds__(64) force3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                  const float2 *__restrict__ bary,
+                                                                  const float2 *__restrict__ w,
+                                                                  const double *__restrict__ S,
+                                                                  const int32_t *__restrict__ elem_row, int n_rows,
+                                                                  int n_elem, int n_q, double *__restrict__ F) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    CSum Ms[4][6];
+    for (int q = 0; q < n_q; ++q) {
+        const long long g = e * n_q + q;
+        const double2 *s2 = reinterpret_cast<const double2 *>(S + 6 * g);
+        const double2 a = s2[0], b = s2[1], c2 = s2[2];
+        const double sv[6] = {a.x, a.y, b.x, b.y, c2.x, c2.y};
+        const df32 wq = ld(w + g);
+        const df32 l[4] = {ld(bary + 4 * q), ld(bary + 4 * q + 1), ld(bary + 4 * q + 2), ld(bary + 4 * q + 3)};
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const df32 T = df_mul(wq, df_from_f64(sv[c]));
+#pragma unroll
+            for (int m = 0; m < 4; ++m) Ms[m][c].add_prod(l[m], T);
+        }
+    }
+    df32 M[4][6], Mt[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        CSum t;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            M[m][c] = Ms[m][c].df();
+            t.add(M[m][c]);
+        }
+        Mt[c] = t.df();
+    }
+    df32 gl[4][3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) gl[1 + k / 3][k % 3] = ld(jinv + e * 9 + k);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gl[0][k] = df_neg(df_add(df_add(gl[1][k], gl[2][k]), gl[3][k]));
+    const int32_t *er = elem_row + e * 30;
+    auto emit = [&](int a, int c, double v) {
+        const int row = er[3 * a + c];
+        if (row < 0) return;
+        if (row >= n_rows) {
+            flag(SSP_DEV_BAD_INDEX);
+            return;
+        }
+        red_add(F + row, v);
+    };
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {  // vertices: (4 M_i − Σ_m M_m) ∇λ_i
+        df32 V[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) V[c] = df_add(df_times4(M[i][c]), df_neg(Mt[c]));
+        CSum o[3];
+        df_sym_matvec_add(V, gl[i], o);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) emit(i, c, o[c].value());
+    }
+    constexpr int kEi[6] = {0, 1, 0, 1, 2, 0}, kEj[6] = {1, 2, 2, 3, 3, 3};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {  // edges: 4 (M_i ∇λ_j + M_j ∇λ_i)
+        const int i = kEi[k], j = kEj[k];
+        CSum o[3];
+        df_sym_matvec_add(M[i], gl[j], o);
+        df_sym_matvec_add(M[j], gl[i], o);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) emit(p2_edge(i, j), c, 4.0 * o[c].value());
+    }
+}
+
 }  // namespace
 }  // namespace ssp
 
@@ -343,6 +507,34 @@ int ssp_assemble_force_element_mixed(const float *wdphi1_hl, const float *wdphi2
     force3_mixed_kernel<<<grid_for(n, kForceThreads), kForceThreads, 0, st>>>(
         reinterpret_cast<const float2 *>(wdphi1_hl), reinterpret_cast<const float2 *>(wdphi2_hl),
         reinterpret_cast<const float2 *>(wdphi3_hl), stress, elem_row, n_rows, n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_3d_p2_affine_mixed(const float *jinv_hl, const float *bary_hl, const float *u_hl,
+                                                   int n_u, const int32_t *elem_dof_lids, int n_int, int n_elem, int n_q,
+                                                   double *out_values, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv_hl || !bary_hl || !u_hl || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    strain3_p2_bary_mixed_kernel<<<grid_for(n_elem, 64), 64, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(bary_hl),
+        reinterpret_cast<const float2 *>(u_hl), elem_dof_lids, n_u, n_elem, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_element_p2_affine_mixed(const float *jinv_hl, const float *bary_hl, const float *w_hl,
+                                               const double *stress, const int32_t *elem_row, int n_elem, int n_q,
+                                               int n_rows, double *out_values, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv_hl || !bary_hl || !w_hl || !stress || !elem_row) return SSP_ERR_INVALID;
+    force3_p2_bary_mixed_kernel<<<grid_for(n_elem, 64), 64, 0, st>>>(
+        reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(bary_hl),
+        reinterpret_cast<const float2 *>(w_hl), stress, elem_row, n_rows, n_elem, n_q, out_values);
     return launch_status();
 }
 

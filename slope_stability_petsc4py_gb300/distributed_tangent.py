@@ -459,6 +459,10 @@ def _mixed_inputs(pattern):
             d["ghat_hl"] = _split_pairs(t.as_tensor(table, device="cuda"))
             d["jinv_hl"] = _split_pairs(d["jinv"])
             d["w_hl"] = _split_pairs(d["weight"])
+            if pattern.n_p == 10:  # P2: the barycentric form reads the points' barycentric coordinates
+                xi, _ = quadrature(3, pattern.elem_type)
+                bary = np.ascontiguousarray(np.vstack([1.0 - xi[0] - xi[1] - xi[2], xi]).T)
+                d["bary_hl"] = _split_pairs(t.as_tensor(bary, device="cuda"))
         else:
             for k in ("dphi1", "dphi2", "dphi3"):
                 d[k + "_hl"] = _split_pairs(d[k])
@@ -479,7 +483,11 @@ def overlap_strain_device(pattern, U, *, mixed: bool = False):
     if pattern.dim == 3 and mixed:
         d = _mixed_inputs(pattern)
         u_hl = _split_pairs(u_ov)
-        if pattern.affine:
+        if pattern.affine and pattern.n_p == 10:
+            _lib.call("ssp_assemble_overlap_strain_3d_p2_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["bary_hl"]),
+                      _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_q,
+                      _lib.ptr(E), st)
+        elif pattern.affine:
             _lib.call("ssp_assemble_overlap_strain_3d_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["ghat_hl"]),
                       _lib.ptr(u_hl), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p,
                       pattern.n_q, _lib.ptr(E), st)
@@ -537,7 +545,11 @@ def owned_force_device(pattern, S_aos, *, mixed: bool = False):
     F = t.empty(n_rows, dtype=t.float64, device="cuda")
     if mixed and pattern.dim == 3:
         d = _mixed_inputs(pattern)
-        if pattern.affine:
+        if pattern.affine and pattern.n_p == 10:
+            _lib.call("ssp_assemble_force_element_p2_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["bary_hl"]),
+                      _lib.ptr(d["w_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
+                      pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
+        elif pattern.affine:
             _lib.call("ssp_assemble_force_element_affine_mixed", _lib.ptr(d["jinv_hl"]), _lib.ptr(d["ghat_hl"]),
                       _lib.ptr(d["w_hl"]), _lib.ptr(S_aos), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size),
                       pattern.n_p, pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
