@@ -45,6 +45,10 @@ NCU_TRAFFIC = {
         "ssp_assemble_overlap_strain_3d_mixed": 281.74e6 + 35.76e6,
         "ssp_assemble_overlap_strain_3d": 284.63e6 + 36.25e6,
         "ssp_assemble_force_element": 343.75e6 + 2.57e6,
+        "ssp_assemble_overlap_strain_3d_p2_affine": 22.85e6 + 1.40e6,
+        "ssp_assemble_force_element_p2_affine": 84.94e6 + 0.30e6,
+        "ssp_assemble_overlap_strain_3d_p2_affine_mixed": 23.48e6 + 2.04e6,
+        "ssp_assemble_force_element_p2_affine_mixed": 84.95e6 + 0.02e6,
         "ssp_constitutive_3d_sds_binned": (90.67 + 304.28 + 22.35 + 1.76 + 34.33 + 1.12) * 1e6,
     },
     "3d_p4_hetero": {
