@@ -271,8 +271,7 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
               int(ov_nodes.size), n_ov, n_p, n_q, _lib.ptr(dev["dphi1"]), _lib.ptr(dev["dphi2"]),
               _lib.ptr(dev["dphi3"]) if dim == 3 else None, _lib.ptr(dev["weight"]), _lib.stream_handle())
     del coord_ov, elem_d
-    owner = elem[:, ov_el].min(axis=0) if n_ov else np.empty(0, dtype=np.int64)
-    owned_el = (owner >= n0) & (owner < n1)
+    owned_el = owned_element_mask(elem, ov_el, (n0, n1))
     if not owned_el.all():
         # the overlap elements whose smallest node the range owns: over the ranks they partition
         # the mesh, so the ranks' integrated potential energies add up to the whole mesh's
@@ -428,6 +427,19 @@ def _affine_elements(pattern, rtol: float = 1e-10, chunk: int = 1 << 16) -> bool
         if bool(((rec - stored).abs().amax(dim=(1, 2, 3)) > rtol * scale).any()):
             return False
     return True
+
+
+def owned_element_mask(elem, overlap_elements, owned_node_range) -> np.ndarray:
+    """Which overlap elements the owned node range owns: those whose smallest node lies in it
+    (the BDDC subdomains' rule, distributed_tangent.py:481-623).  Over ranks whose node ranges
+    partition the nodes, the owned elements partition the mesh; the potential energy sums over
+    them."""
+    n0, n1 = (int(v) for v in owned_node_range)
+    ov = np.asarray(overlap_elements, dtype=np.int64)
+    if ov.size == 0:
+        return np.zeros(0, dtype=bool)
+    owner = np.asarray(elem)[:, ov].min(axis=0)
+    return (owner >= n0) & (owner < n1)
 
 
 def _p2_affine_inputs(pattern):

@@ -10,7 +10,9 @@ needs no GPU.
 
 The BDDC case (``src/slope_stability/fem/distributed_tangent.py`` ``prepare_bddc_subdomain_pattern``)
 gives each rank the elements it owns and a local square matrix over their nodes; the subdomain
-matrices, summed through their local-to-global dof maps, must give the whole-mesh tangent.
+matrices, summed through their local-to-global dof maps, must give the whole-mesh tangent.  The
+potential energy (``ConstitutiveOperator.potential_energy`` across ranks) sums each rank's owned
+elements and all-reduces the scalar.
 """
 
 from __future__ import annotations
@@ -202,3 +204,81 @@ def test_two_gloo_ranks_bddc_subdomains_sum_to_the_global_tangent():
     diff = abs(K_sum - K_one).max()
     assert diff <= 1e-12 * abs(K_one).max()
     assert K_one[free][:, free].nnz > 0 and K_sum[~free].nnz == 0
+
+
+# ---------------------------------------------------------------------------- potential energy
+
+
+def _potential_part(n_range):
+    """The rank's share of the integrated potential energy: the oracle's energy densities at the
+    points of the overlap elements the range owns (owned_element_mask), weighted and summed."""
+    from oracle import oracle_py as oracle
+    from slope_stability_petsc4py_gb300.distributed_tangent import _PatternBuild, owned_element_mask
+
+    mats, mesh, U = _problem()
+    pb = _PatternBuild(mesh.elem, mesh.q_mask, n_range)
+    g = {k: pb.get(k) for k in ("overlap_elements", "overlap_nodes", "overlap_element_dof_lids")}
+    pb.close()
+    xi, wf = fem.quadrature(3, "P2")
+    n_q = xi.shape[1]
+    dphi, w = oracle.geometry(mesh.coord, mesh.elem[:, g["overlap_elements"]], 3, fem.reference_gradients(3, "P2"), wf)
+    nodes = g["overlap_nodes"]
+    gdofs = 3 * np.repeat(nodes, 3) + np.tile(np.arange(3), nodes.size)
+    u_ov = np.ascontiguousarray(U.reshape(-1, order="F")[gdofs])
+    E = oracle.strain_3d(dphi[0], dphi[1], dphi[2], u_ov, g["overlap_element_dof_lids"], n_q)
+    n = E.shape[0]
+    c_bar, sin_phi = oracle.reduction(np.full(n, float(mats.c0[0])), np.full(n, np.deg2rad(float(mats.phi[0]))),
+                                      np.zeros(n), 1.1, "B")
+    full = lambda v: np.full(n, float(v[0]))  # noqa: E731
+    psi = oracle.potential_3d(E.T, c_bar, sin_phi, full(mats.shear), full(mats.bulk), full(mats.lame))
+    own = np.repeat(owned_element_mask(mesh.elem, g["overlap_elements"], n_range), n_q)
+    return float(np.dot(w[own], psi[own])), g["overlap_elements"][owned_element_mask(mesh.elem, g["overlap_elements"],
+                                                                                       n_range)]
+
+
+def _potential_rank_main(rank, world, port, queue, split):
+    import torch
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    _, mesh, _ = _problem()
+    bounds = [0, split, mesh.n_nodes]
+    part, owned = _potential_part((bounds[rank], bounds[rank + 1]))
+    buf = torch.tensor([part], dtype=torch.float64)
+    dist.all_reduce(buf)  # the exchange the operator's potential_energy does across ranks
+    gathered = [None] * world
+    dist.all_gather_object(gathered, owned)
+    if rank == 0:
+        queue.put((float(buf.item()), gathered))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_potential_energy_sums_to_the_whole_mesh():
+    """Two ranks splitting the node range at the median element owner (vertices are numbered
+    before edge nodes, so half the node range would own no element): the elements they own
+    partition the mesh, and their all-reduced energies equal the single-rank energy of the whole
+    mesh."""
+    import torch.multiprocessing as mp
+
+    from oracle import oracle_py as oracle
+
+    oracle.build()
+    _, mesh, _ = _problem()
+    split = int(np.sort(mesh.elem.min(axis=0))[mesh.n_elem // 2])
+    ctx = mp.get_context("spawn")
+    queue = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_potential_rank_main, args=(r, 2, port, queue, split)) for r in range(2)]
+    for p in procs:
+        p.start()
+    total, owned = queue.get(timeout=300)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    elems = np.concatenate(owned)
+    assert np.array_equal(np.sort(elems), np.arange(mesh.n_elem)) and all(o.size for o in owned)
+    whole, _ = _potential_part((0, mesh.n_nodes))
+    assert abs(total - whole) <= 1e-12 * abs(whole)
