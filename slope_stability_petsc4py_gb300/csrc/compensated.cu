@@ -314,62 +314,81 @@ __device__ __forceinline__ constexpr int p2_edge(int i, int j) {
 __device__ __forceinline__ df32 df_times4(df32 a) { return {4.0f * a.hi, 4.0f * a.lo}; }  // exact
 __device__ __forceinline__ df32 df_times3(df32 a) { return df_mul(a, df32{3.0f, 0.0f}); }
 
-__global__ void __launch_bounds__(64) strain3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
-                                                                   const float2 *__restrict__ bary,
-                                                                   const float2 *__restrict__ u,
-                                                                   const int32_t *__restrict__ dof, long long n_u,
-                                                                   int n_elem, int n_q, double *__restrict__ E) {
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= n_elem) return;
-    df32 un[10][3];
+// Four lanes per element (lane m = 0..3 of an aligned group of 4): the double-float chains are
+// latency-bound, so the element's work is spread over the group.  Lane m forms S_m, the group
+// swaps the four S through shuffles, and lane m evaluates the points q = m, m + 4, m + 8.
+constexpr int kBaryThreads = 128;
+
+__device__ __forceinline__ df32 shfl_df(df32 v, int src) {
+    return {__shfl_sync(0xffffffffu, v.hi, src, 4), __shfl_sync(0xffffffffu, v.lo, src, 4)};
+}
+
+__global__ void __launch_bounds__(kBaryThreads) strain3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                             const float2 *__restrict__ bary,
+                                                                             const float2 *__restrict__ u,
+                                                                             const int32_t *__restrict__ dof,
+                                                                             long long n_u, int n_elem, int n_q,
+                                                                             double *__restrict__ E) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int m = static_cast<int>(t & 3);
+    const bool valid = (t >> 2) < n_elem;
+    const long long e = valid ? (t >> 2) : (long long)n_elem - 1;  // every lane of a group shuffles
     const int32_t *dl = dof + e * 30;
-#pragma unroll
-    for (int a = 0; a < 10; ++a)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const int32_t i = dl[3 * a + c];
-            if (i < 0 || i >= n_u) {
-                flag(SSP_DEV_BAD_INDEX);
-                un[a][c] = df32{0.0f, 0.0f};
-            } else {
-                un[a][c] = ld(u + i);
-            }
+    auto load_u = [&](int node, int c) -> df32 {
+        const int32_t i = dl[3 * node + c];
+        if (i < 0 || i >= n_u) {
+            flag(SSP_DEV_BAD_INDEX);
+            return df32{0.0f, 0.0f};
         }
+        return ld(u + i);
+    };
+    // A_im = 3 u_i when i == m, else 4 u_(edge im) - u_i; as a u_i + 4 u_x with (a, x) selected per lane
+    df32 A[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool own = i == m;
+        const int x = own ? i : p2_edge(i, m);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {  // both forms computed, one selected: no divergence in the group
+            const df32 ui = load_u(i, c);
+            const df32 ux = load_u(x, c);
+            const df32 vertex = df_times3(ui), edge = df_add(df_times4(ux), df_neg(ui));
+            A[i][c] = own ? vertex : edge;
+        }
+    }
     df32 gl[3][3];
 #pragma unroll
     for (int k = 0; k < 9; ++k) gl[k / 3][k % 3] = ld(jinv + e * 9 + k);
+    CSum G[3][3];
+#pragma unroll
+    for (int i = 1; i < 4; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const df32 b = df_add(A[i][c], df_neg(A[0][c]));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) G[c][k].add_prod(b, gl[i - 1][k]);
+        }
+    df32 Sm[6];
+    Sm[0] = G[0][0].df();
+    Sm[1] = G[1][1].df();
+    Sm[2] = G[2][2].df();
+    Sm[3] = df_add(G[0][1].df(), G[1][0].df());
+    Sm[4] = df_add(G[1][2].df(), G[2][1].df());
+    Sm[5] = df_add(G[0][2].df(), G[2][0].df());
     df32 S[4][6];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        df32 A0[3];
+    for (int src = 0; src < 4; ++src)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            A0[c] = m == 0 ? df_times3(un[0][c]) : df_add(df_times4(un[p2_edge(0, m)][c]), df_neg(un[0][c]));
-        CSum G[3][3];
-#pragma unroll
-        for (int i = 1; i < 4; ++i)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const df32 Ai = i == m ? df_times3(un[i][c]) : df_add(df_times4(un[p2_edge(i, m)][c]), df_neg(un[i][c]));
-                const df32 b = df_add(Ai, df_neg(A0[c]));
-#pragma unroll
-                for (int k = 0; k < 3; ++k) G[c][k].add_prod(b, gl[i - 1][k]);
-            }
-        S[m][0] = G[0][0].df();
-        S[m][1] = G[1][1].df();
-        S[m][2] = G[2][2].df();
-        S[m][3] = df_add(G[0][1].df(), G[1][0].df());
-        S[m][4] = df_add(G[1][2].df(), G[2][1].df());
-        S[m][5] = df_add(G[0][2].df(), G[2][0].df());
-    }
-    for (int q = 0; q < n_q; ++q) {
+        for (int c = 0; c < 6; ++c) S[src][c] = shfl_df(Sm[c], src);
+    if (!valid) return;
+    for (int q = m; q < n_q; q += 4) {
         const df32 l[4] = {ld(bary + 4 * q), ld(bary + 4 * q + 1), ld(bary + 4 * q + 2), ld(bary + 4 * q + 3)};
         double v[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
             CSum acc;
 #pragma unroll
-            for (int m = 0; m < 4; ++m) acc.add_prod(l[m], S[m][c]);
+            for (int k = 0; k < 4; ++k) acc.add_prod(l[k], S[k][c]);
             v[c] = acc.value();
         }
         double2 *o = reinterpret_cast<double2 *>(E + 6 * (e * n_q + q));
@@ -392,48 +411,52 @@ __device__ __forceinline__ void df_sym_matvec_add(const df32 *M, const df32 *v, 
     out[2].add_prod(M[2], v[2]);
 }
 
-__global__ void __launch_bounds__(64) force3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
-                                                                  const float2 *__restrict__ bary,
-                                                                  const float2 *__restrict__ w,
-                                                                  const double *__restrict__ S,
-                                                                  const int32_t *__restrict__ elem_row, int n_rows,
-                                                                  int n_elem, int n_q, double *__restrict__ F) {
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= n_elem) return;
-    CSum Ms[4][6];
+// Four lanes per element: lane m accumulates the moment M_m over the element's points, the group
+// swaps the four moments, and lane m assembles vertex m and the edges m and m + 4 (edge order 01,
+// 12, 02, 13, 23, 03).
+__global__ void __launch_bounds__(kBaryThreads) force3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                            const float2 *__restrict__ bary,
+                                                                            const float2 *__restrict__ w,
+                                                                            const double *__restrict__ S,
+                                                                            const int32_t *__restrict__ elem_row,
+                                                                            int n_rows, int n_elem, int n_q,
+                                                                            double *__restrict__ F) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int m = static_cast<int>(t & 3);
+    const bool valid = (t >> 2) < n_elem;
+    const long long e = valid ? (t >> 2) : (long long)n_elem - 1;  // every lane of a group shuffles
+    CSum Ms[6];
     for (int q = 0; q < n_q; ++q) {
         const long long g = e * n_q + q;
         const double2 *s2 = reinterpret_cast<const double2 *>(S + 6 * g);
         const double2 a = s2[0], b = s2[1], c2 = s2[2];
         const double sv[6] = {a.x, a.y, b.x, b.y, c2.x, c2.y};
         const df32 wq = ld(w + g);
-        const df32 l[4] = {ld(bary + 4 * q), ld(bary + 4 * q + 1), ld(bary + 4 * q + 2), ld(bary + 4 * q + 3)};
+        const df32 lm = ld(bary + 4 * q + m);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const df32 T = df_mul(wq, df_from_f64(sv[c]));
-#pragma unroll
-            for (int m = 0; m < 4; ++m) Ms[m][c].add_prod(l[m], T);
-        }
+        for (int c = 0; c < 6; ++c) Ms[c].add_prod(lm, df_mul(wq, df_from_f64(sv[c])));
     }
     df32 M[4][6], Mt[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-        CSum t;
+        const df32 mine = Ms[c].df();
+        CSum tot;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            M[m][c] = Ms[m][c].df();
-            t.add(M[m][c]);
+        for (int src = 0; src < 4; ++src) {
+            M[src][c] = shfl_df(mine, src);
+            tot.add(M[src][c]);
         }
-        Mt[c] = t.df();
+        Mt[c] = tot.df();
     }
+    if (!valid) return;
     df32 gl[4][3];
 #pragma unroll
     for (int k = 0; k < 9; ++k) gl[1 + k / 3][k % 3] = ld(jinv + e * 9 + k);
 #pragma unroll
     for (int k = 0; k < 3; ++k) gl[0][k] = df_neg(df_add(df_add(gl[1][k], gl[2][k]), gl[3][k]));
     const int32_t *er = elem_row + e * 30;
-    auto emit = [&](int a, int c, double v) {
-        const int row = er[3 * a + c];
+    auto emit = [&](int node, int c, double v) {
+        const int row = er[3 * node + c];
         if (row < 0) return;
         if (row >= n_rows) {
             flag(SSP_DEV_BAD_INDEX);
@@ -441,25 +464,44 @@ __global__ void __launch_bounds__(64) force3_p2_bary_mixed_kernel(const float2 *
         }
         red_add(F + row, v);
     };
+    // the lane's moment and gradient, and those of the edges' end vertices, by selects (no local memory)
+    auto pick = [&](int idx, df32 *Mo, df32 *go) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {  // vertices: (4 M_i − Σ_m M_m) ∇λ_i
-        df32 V[6];
+        for (int c = 0; c < 6; ++c) Mo[c] = M[0][c];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) V[c] = df_add(df_times4(M[i][c]), df_neg(Mt[c]));
+        for (int k = 0; k < 3; ++k) go[k] = gl[0][k];
+#pragma unroll
+        for (int s = 1; s < 4; ++s) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) Mo[c] = idx == s ? M[s][c] : Mo[c];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) go[k] = idx == s ? gl[s][k] : go[k];
+        }
+    };
+    {  // vertex m: (4 M_m − Σ M) ∇λ_m
+        df32 Mm[6], gm[3], V[6];
+        pick(m, Mm, gm);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) V[c] = df_add(df_times4(Mm[c]), df_neg(Mt[c]));
         CSum o[3];
-        df_sym_matvec_add(V, gl[i], o);
+        df_sym_matvec_add(V, gm, o);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) emit(i, c, o[c].value());
+        for (int c = 0; c < 3; ++c) emit(m, c, o[c].value());
     }
-    constexpr int kEi[6] = {0, 1, 0, 1, 2, 0}, kEj[6] = {1, 2, 2, 3, 3, 3};
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {  // edges: 4 (M_i ∇λ_j + M_j ∇λ_i)
-        const int i = kEi[k], j = kEj[k];
+    for (int r = 0; r < 2; ++r) {  // edges k = m, m + 4: 4 (M_i ∇λ_j + M_j ∇λ_i)
+        const int k = m + 4 * r;
+        if (k >= 6) break;
+        const int i = (0x021010 >> (4 * k)) & 0xF, j = (0x333221 >> (4 * k)) & 0xF;
+        df32 Mi[6], gi[3], Mj[6], gj[3];
+        pick(i, Mi, gi);
+        pick(j, Mj, gj);
         CSum o[3];
-        df_sym_matvec_add(M[i], gl[j], o);
-        df_sym_matvec_add(M[j], gl[i], o);
+        df_sym_matvec_add(Mi, gj, o);
+        df_sym_matvec_add(Mj, gi, o);
+        const int node = p2_edge(i, j);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) emit(p2_edge(i, j), c, 4.0 * o[c].value());
+        for (int c = 0; c < 3; ++c) emit(node, c, 4.0 * o[c].value());
     }
 }
 
@@ -517,7 +559,7 @@ int ssp_assemble_overlap_strain_3d_p2_affine_mixed(const float *jinv_hl, const f
     if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
     if (n_elem == 0) return SSP_OK;
     if (!jinv_hl || !bary_hl || !u_hl || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
-    strain3_p2_bary_mixed_kernel<<<grid_for(n_elem, 64), 64, 0, as_stream(stream)>>>(
+    strain3_p2_bary_mixed_kernel<<<grid_for(4LL * n_elem, kBaryThreads), kBaryThreads, 0, as_stream(stream)>>>(
         reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(bary_hl),
         reinterpret_cast<const float2 *>(u_hl), elem_dof_lids, n_u, n_elem, n_q, out_values);
     return launch_status();
@@ -532,7 +574,7 @@ int ssp_assemble_force_element_p2_affine_mixed(const float *jinv_hl, const float
     if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
     if (n_elem == 0) return SSP_OK;
     if (!jinv_hl || !bary_hl || !w_hl || !stress || !elem_row) return SSP_ERR_INVALID;
-    force3_p2_bary_mixed_kernel<<<grid_for(n_elem, 64), 64, 0, st>>>(
+    force3_p2_bary_mixed_kernel<<<grid_for(4LL * n_elem, kBaryThreads), kBaryThreads, 0, st>>>(
         reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(bary_hl),
         reinterpret_cast<const float2 *>(w_hl), stress, elem_row, n_rows, n_elem, n_q, out_values);
     return launch_status();
