@@ -411,52 +411,51 @@ __device__ __forceinline__ void df_sym_matvec_add(const df32 *M, const df32 *v, 
     out[2].add_prod(M[2], v[2]);
 }
 
-// Four lanes per element: lane m accumulates the moment M_m over the element's points, the group
-// swaps the four moments, and lane m assembles vertex m and the edges m and m + 4 (edge order 01,
-// 12, 02, 13, 23, 03).
-__global__ void __launch_bounds__(kBaryThreads) force3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
-                                                                            const float2 *__restrict__ bary,
-                                                                            const float2 *__restrict__ w,
-                                                                            const double *__restrict__ S,
-                                                                            const int32_t *__restrict__ elem_row,
-                                                                            int n_rows, int n_elem, int n_q,
-                                                                            double *__restrict__ F) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const int m = static_cast<int>(t & 3);
-    const bool valid = (t >> 2) < n_elem;
-    const long long e = valid ? (t >> 2) : (long long)n_elem - 1;  // every lane of a group shuffles
-    CSum Ms[6];
+// One thread per element (spreading the points over four lanes measured slower: 81 µs against
+// 70 µs on 3d_p2_homo; the FP64 -> double-float conversions of the stresses dominate and are
+// not shared).
+__global__ void __launch_bounds__(64) force3_p2_bary_mixed_kernel(const float2 *__restrict__ jinv,
+                                                                  const float2 *__restrict__ bary,
+                                                                  const float2 *__restrict__ w,
+                                                                  const double *__restrict__ S,
+                                                                  const int32_t *__restrict__ elem_row, int n_rows,
+                                                                  int n_elem, int n_q, double *__restrict__ F) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    CSum Ms[4][6];
     for (int q = 0; q < n_q; ++q) {
         const long long g = e * n_q + q;
         const double2 *s2 = reinterpret_cast<const double2 *>(S + 6 * g);
         const double2 a = s2[0], b = s2[1], c2 = s2[2];
         const double sv[6] = {a.x, a.y, b.x, b.y, c2.x, c2.y};
         const df32 wq = ld(w + g);
-        const df32 lm = ld(bary + 4 * q + m);
+        const df32 l[4] = {ld(bary + 4 * q), ld(bary + 4 * q + 1), ld(bary + 4 * q + 2), ld(bary + 4 * q + 3)};
 #pragma unroll
-        for (int c = 0; c < 6; ++c) Ms[c].add_prod(lm, df_mul(wq, df_from_f64(sv[c])));
+        for (int c = 0; c < 6; ++c) {
+            const df32 T = df_mul(wq, df_from_f64(sv[c]));
+#pragma unroll
+            for (int m = 0; m < 4; ++m) Ms[m][c].add_prod(l[m], T);
+        }
     }
     df32 M[4][6], Mt[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-        const df32 mine = Ms[c].df();
-        CSum tot;
+        CSum t;
 #pragma unroll
-        for (int src = 0; src < 4; ++src) {
-            M[src][c] = shfl_df(mine, src);
-            tot.add(M[src][c]);
+        for (int m = 0; m < 4; ++m) {
+            M[m][c] = Ms[m][c].df();
+            t.add(M[m][c]);
         }
-        Mt[c] = tot.df();
+        Mt[c] = t.df();
     }
-    if (!valid) return;
     df32 gl[4][3];
 #pragma unroll
     for (int k = 0; k < 9; ++k) gl[1 + k / 3][k % 3] = ld(jinv + e * 9 + k);
 #pragma unroll
     for (int k = 0; k < 3; ++k) gl[0][k] = df_neg(df_add(df_add(gl[1][k], gl[2][k]), gl[3][k]));
     const int32_t *er = elem_row + e * 30;
-    auto emit = [&](int node, int c, double v) {
-        const int row = er[3 * node + c];
+    auto emit = [&](int a, int c, double v) {
+        const int row = er[3 * a + c];
         if (row < 0) return;
         if (row >= n_rows) {
             flag(SSP_DEV_BAD_INDEX);
@@ -464,44 +463,25 @@ __global__ void __launch_bounds__(kBaryThreads) force3_p2_bary_mixed_kernel(cons
         }
         red_add(F + row, v);
     };
-    // the lane's moment and gradient, and those of the edges' end vertices, by selects (no local memory)
-    auto pick = [&](int idx, df32 *Mo, df32 *go) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) Mo[c] = M[0][c];
+    for (int i = 0; i < 4; ++i) {  // vertices: (4 M_i − Σ_m M_m) ∇λ_i
+        df32 V[6];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) go[k] = gl[0][k];
-#pragma unroll
-        for (int s = 1; s < 4; ++s) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) Mo[c] = idx == s ? M[s][c] : Mo[c];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) go[k] = idx == s ? gl[s][k] : go[k];
-        }
-    };
-    {  // vertex m: (4 M_m − Σ M) ∇λ_m
-        df32 Mm[6], gm[3], V[6];
-        pick(m, Mm, gm);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) V[c] = df_add(df_times4(Mm[c]), df_neg(Mt[c]));
+        for (int c = 0; c < 6; ++c) V[c] = df_add(df_times4(M[i][c]), df_neg(Mt[c]));
         CSum o[3];
-        df_sym_matvec_add(V, gm, o);
+        df_sym_matvec_add(V, gl[i], o);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) emit(m, c, o[c].value());
+        for (int c = 0; c < 3; ++c) emit(i, c, o[c].value());
     }
+    constexpr int kEi[6] = {0, 1, 0, 1, 2, 0}, kEj[6] = {1, 2, 2, 3, 3, 3};
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {  // edges k = m, m + 4: 4 (M_i ∇λ_j + M_j ∇λ_i)
-        const int k = m + 4 * r;
-        if (k >= 6) break;
-        const int i = (0x021010 >> (4 * k)) & 0xF, j = (0x333221 >> (4 * k)) & 0xF;
-        df32 Mi[6], gi[3], Mj[6], gj[3];
-        pick(i, Mi, gi);
-        pick(j, Mj, gj);
+    for (int k = 0; k < 6; ++k) {  // edges: 4 (M_i ∇λ_j + M_j ∇λ_i)
+        const int i = kEi[k], j = kEj[k];
         CSum o[3];
-        df_sym_matvec_add(Mi, gj, o);
-        df_sym_matvec_add(Mj, gi, o);
-        const int node = p2_edge(i, j);
+        df_sym_matvec_add(M[i], gl[j], o);
+        df_sym_matvec_add(M[j], gl[i], o);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) emit(node, c, 4.0 * o[c].value());
+        for (int c = 0; c < 3; ++c) emit(p2_edge(i, j), c, 4.0 * o[c].value());
     }
 }
 
@@ -574,7 +554,7 @@ int ssp_assemble_force_element_p2_affine_mixed(const float *jinv_hl, const float
     if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
     if (n_elem == 0) return SSP_OK;
     if (!jinv_hl || !bary_hl || !w_hl || !stress || !elem_row) return SSP_ERR_INVALID;
-    force3_p2_bary_mixed_kernel<<<grid_for(4LL * n_elem, kBaryThreads), kBaryThreads, 0, st>>>(
+    force3_p2_bary_mixed_kernel<<<grid_for(n_elem, 64), 64, 0, st>>>(
         reinterpret_cast<const float2 *>(jinv_hl), reinterpret_cast<const float2 *>(bary_hl),
         reinterpret_cast<const float2 *>(w_hl), stress, elem_row, n_rows, n_elem, n_q, out_values);
     return launch_status();
