@@ -17,12 +17,17 @@
  *                           and src/slope_stability/fem/distributed_tangent.py:1437-1484 (2D)
  *   orc_strain_2d           src/slope_stability/fem/assembly.py:96-123 (B rows of the 2D operator)
  *   orc_overlap_force_2d    src/slope_stability/fem/distributed_tangent.py:845-852
+ *   orc_geometry_3d         src/slope_stability/fem/assembly.py:139-245 (dphi, weights)
+ *   orc_pattern_build       src/slope_stability/fem/distributed_tangent.py:297-478 (owned-row
+ *                           CSR, constrained diagonals, row-slot metadata) and
+ *                           src/slope_stability/fem/distributed_elastic.py:36-52 (overlap)
  *
  * Parity of this restatement is pinned against the reference's own outputs
  * (golden fixtures generated by tests/golden/make_golden.py).
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #ifdef _OPENMP
@@ -485,4 +490,352 @@ int orc_num_threads(void)
 #else
     return 1;
 #endif
+}
+
+void orc_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0)
+        omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3D geometry: per-point gradients dphi = J^{-T} dhat and weights          */
+/* w = wf |det J| (assembly.py:167-197, 232), J[r][c] = sum_a x_c(a) dhat_r. */
+/* coord [3][n_nodes]; elem [n_el][n_p] (node ids); dhat [3][n_p][n_q];     */
+/* outputs dphi_k [n_el*n_q][n_p], w [n_el*n_q].                            */
+/* ------------------------------------------------------------------------ */
+
+void orc_geometry_3d(const double *coord, int64_t n_nodes, const int64_t *elem, int64_t n_el, int n_p,
+                     int n_q, const double *dhat, const double *wf, double *dphi1, double *dphi2,
+                     double *dphi3, double *w)
+{
+    const double *X = coord, *Y = coord + n_nodes, *Z = coord + 2 * n_nodes;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < n_el; ++e) {
+        const int64_t *nd = elem + e * n_p;
+        for (int q = 0; q < n_q; ++q) {
+            double j11 = 0, j12 = 0, j13 = 0, j21 = 0, j22 = 0, j23 = 0, j31 = 0, j32 = 0, j33 = 0;
+            for (int a = 0; a < n_p; ++a) {
+                const double x = X[nd[a]], y = Y[nd[a]], z = Z[nd[a]];
+                const double h1 = dhat[(0 * n_p + a) * n_q + q], h2 = dhat[(1 * n_p + a) * n_q + q],
+                             h3 = dhat[(2 * n_p + a) * n_q + q];
+                j11 += x * h1; j12 += y * h1; j13 += z * h1;
+                j21 += x * h2; j22 += y * h2; j23 += z * h2;
+                j31 += x * h3; j32 += y * h3; j33 += z * h3;
+            }
+            const double det = j11 * (j22 * j33 - j23 * j32) - j12 * (j21 * j33 - j23 * j31) +
+                               j13 * (j21 * j32 - j22 * j31);
+            const double inv = 1.0 / det;
+            const int64_t g = e * n_q + q;
+            for (int a = 0; a < n_p; ++a) {
+                const double h1 = dhat[(0 * n_p + a) * n_q + q], h2 = dhat[(1 * n_p + a) * n_q + q],
+                             h3 = dhat[(2 * n_p + a) * n_q + q];
+                dphi1[g * n_p + a] = ((j22 * j33 - j23 * j32) * h1 - (j12 * j33 - j13 * j32) * h2 +
+                                      (j12 * j23 - j13 * j22) * h3) * inv;
+                dphi2[g * n_p + a] = (-(j21 * j33 - j23 * j31) * h1 + (j11 * j33 - j13 * j31) * h2 -
+                                      (j11 * j23 - j13 * j21) * h3) * inv;
+                dphi3[g * n_p + a] = ((j21 * j32 - j22 * j31) * h1 - (j11 * j32 - j12 * j31) * h2 +
+                                      (j11 * j22 - j12 * j21) * h3) * inv;
+            }
+            w[g] = wf[q] * fabs(det);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Owned-row pattern.  The reference builds it with Python sets and dicts:   */
+/*  - overlap elements: every element with a node in [n0, n1), ascending;    */
+/*  - a free owned row holds the free dofs of every overlap element that     */
+/*    has the row's dof, sorted; a constrained owned row only its diagonal;  */
+/*  - constrained_diag_positions: the diagonal's position per constrained    */
+/*    owned row, in row order;                                               */
+/*  - row slots: per free owned row, one slot per overlap element with the   */
+/*    row's dof, in element order: (element, local dof a, positions of the   */
+/*    element's free dofs in the row, -1 for constrained ones).              */
+/* A free row's dof belongs to one node, and the elements with that dof are  */
+/* the elements of that node, so the columns are the free dofs of the nodes  */
+/* of the node's elements: the same sets, gathered per node.                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int dim, n_p;
+    int64_t n_ov, n_ovn, n_rows, nnz, n_slots, n_cd;
+    int64_t *overlap_elements, *overlap_nodes;
+    int32_t *dof_lids, *indptr, *indices, *row_slot_ptr, *slot_elem, *slot_pos, *cdiag;
+    uint8_t *slot_lrow;
+} orc_pattern;
+
+static int orc_cmp_i64(const void *a, const void *b)
+{
+    const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* sorted distinct nodes of the elements of owned node v (adjacency adj[ap[v]..ap[v+1]]) into buf */
+static int64_t orc_node_set(const int64_t *elem, int n_p, const int64_t *ov, const int32_t *adj,
+                            const int64_t *ap, int64_t v, int64_t *buf)
+{
+    int64_t m = 0;
+    for (int64_t k = ap[v]; k < ap[v + 1]; ++k) {
+        const int64_t *nd = elem + ov[adj[k]] * n_p;
+        for (int a = 0; a < n_p; ++a)
+            buf[m++] = nd[a];
+    }
+    qsort(buf, (size_t)m, sizeof(int64_t), orc_cmp_i64);
+    int64_t u = 0;
+    for (int64_t i = 0; i < m; ++i)
+        if (u == 0 || buf[i] != buf[u - 1])
+            buf[u++] = buf[i];
+    return u;
+}
+
+static int32_t orc_find(const int32_t *a, int32_t lo, int32_t hi, int32_t key)
+{
+    while (lo < hi) {
+        const int32_t mid = lo + (hi - lo) / 2;
+        if (a[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+void orc_pattern_free(void *h)
+{
+    orc_pattern *p = (orc_pattern *)h;
+    if (!p)
+        return;
+    free(p->overlap_elements); free(p->overlap_nodes); free(p->dof_lids); free(p->indptr);
+    free(p->indices); free(p->row_slot_ptr); free(p->slot_elem); free(p->slot_pos); free(p->cdiag);
+    free(p->slot_lrow);
+    free(p);
+}
+
+/* elem: [n_elem][n_p] node ids (element-major); free_dof: [dim * n_nodes], dof = dim*node + comp.
+ * Returns a handle (NULL on allocation failure or an index beyond int32). */
+void *orc_pattern_build(int dim, int64_t n_nodes, int n_p, int64_t n_elem, const int64_t *elem,
+                        const uint8_t *free_dof, int64_t n0, int64_t n1)
+{
+    orc_pattern *p = (orc_pattern *)calloc(1, sizeof(orc_pattern));
+    if (!p)
+        return NULL;
+    p->dim = dim;
+    p->n_p = n_p;
+    const int nld = dim * n_p;
+    const int64_t n_own = n1 - n0;
+    /* overlap elements and nodes */
+    int64_t n_ov = 0;
+    for (int64_t e = 0; e < n_elem; ++e)
+        for (int a = 0; a < n_p; ++a)
+            if (elem[e * n_p + a] >= n0 && elem[e * n_p + a] < n1) { ++n_ov; break; }
+    p->n_ov = n_ov;
+    p->overlap_elements = (int64_t *)malloc((size_t)(n_ov ? n_ov : 1) * sizeof(int64_t));
+    int64_t *lid = (int64_t *)malloc((size_t)(n_nodes ? n_nodes : 1) * sizeof(int64_t));
+    if (!p->overlap_elements || !lid) { free(lid); orc_pattern_free(p); return NULL; }
+    n_ov = 0;
+    for (int64_t e = 0; e < n_elem; ++e)
+        for (int a = 0; a < n_p; ++a)
+            if (elem[e * n_p + a] >= n0 && elem[e * n_p + a] < n1) { p->overlap_elements[n_ov++] = e; break; }
+    for (int64_t v = 0; v < n_nodes; ++v)
+        lid[v] = -1;
+    for (int64_t k = 0; k < n_ov; ++k)
+        for (int a = 0; a < n_p; ++a)
+            lid[elem[p->overlap_elements[k] * n_p + a]] = 0;
+    int64_t n_ovn = 0;
+    for (int64_t v = 0; v < n_nodes; ++v)
+        if (lid[v] == 0)
+            lid[v] = n_ovn++;
+    p->n_ovn = n_ovn;
+    p->overlap_nodes = (int64_t *)malloc((size_t)(n_ovn ? n_ovn : 1) * sizeof(int64_t));
+    p->dof_lids = (int32_t *)malloc((size_t)(n_ov ? n_ov : 1) * nld * sizeof(int32_t));
+    if (!p->overlap_nodes || !p->dof_lids) { free(lid); orc_pattern_free(p); return NULL; }
+    for (int64_t v = 0; v < n_nodes; ++v)
+        if (lid[v] >= 0)
+            p->overlap_nodes[lid[v]] = v;
+    for (int64_t k = 0; k < n_ov; ++k)
+        for (int a = 0; a < n_p; ++a)
+            for (int c = 0; c < dim; ++c)
+                p->dof_lids[k * nld + dim * a + c] = (int32_t)(dim * lid[elem[p->overlap_elements[k] * n_p + a]] + c);
+    free(lid);
+
+    /* owned node -> overlap elements (ascending) */
+    int64_t *ap = (int64_t *)calloc((size_t)n_own + 1, sizeof(int64_t));
+    if (!ap) { orc_pattern_free(p); return NULL; }
+    for (int64_t k = 0; k < n_ov; ++k)
+        for (int a = 0; a < n_p; ++a) {
+            const int64_t v = elem[p->overlap_elements[k] * n_p + a];
+            if (v >= n0 && v < n1)
+                ap[v - n0 + 1]++;
+        }
+    for (int64_t v = 0; v < n_own; ++v)
+        ap[v + 1] += ap[v];
+    int32_t *adj = (int32_t *)malloc((size_t)(ap[n_own] ? ap[n_own] : 1) * sizeof(int32_t));
+    int64_t *fill = (int64_t *)malloc((size_t)(n_own ? n_own : 1) * sizeof(int64_t));
+    if (!adj || !fill) { free(ap); free(adj); free(fill); orc_pattern_free(p); return NULL; }
+    memcpy(fill, ap, (size_t)n_own * sizeof(int64_t));
+    for (int64_t k = 0; k < n_ov; ++k)
+        for (int a = 0; a < n_p; ++a) {
+            const int64_t v = elem[p->overlap_elements[k] * n_p + a];
+            if (v >= n0 && v < n1)
+                adj[fill[v - n0]++] = (int32_t)k;
+        }
+    free(fill);
+    int64_t max_deg = 0;
+    for (int64_t v = 0; v < n_own; ++v)
+        if (ap[v + 1] - ap[v] > max_deg)
+            max_deg = ap[v + 1] - ap[v];
+
+    /* row lengths */
+    const int64_t n_rows = dim * n_own;
+    p->n_rows = n_rows;
+    int64_t *rlen = (int64_t *)calloc((size_t)n_rows + 1, sizeof(int64_t));
+    if (!rlen) { free(ap); free(adj); orc_pattern_free(p); return NULL; }
+    int failed = 0;
+#pragma omp parallel
+    {
+        int64_t *buf = (int64_t *)malloc((size_t)(max_deg * n_p + 1) * sizeof(int64_t));
+        if (!buf) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t v = 0; v < n_own; ++v) {
+            if (!buf)
+                continue;
+            const int64_t m = orc_node_set(elem, n_p, p->overlap_elements, adj, ap, v, buf);
+            int64_t nfree = 0;
+            for (int64_t i = 0; i < m; ++i)
+                for (int c = 0; c < dim; ++c)
+                    nfree += free_dof[dim * buf[i] + c] != 0;
+            for (int c = 0; c < dim; ++c)
+                rlen[dim * v + c + 1] = free_dof[dim * (n0 + v) + c] ? nfree : 1;
+        }
+        free(buf);
+    }
+    for (int64_t r = 0; r < n_rows; ++r)
+        rlen[r + 1] += rlen[r];
+    p->nnz = rlen[n_rows];
+    if (failed || p->nnz > INT32_MAX) { free(rlen); free(ap); free(adj); orc_pattern_free(p); return NULL; }
+    p->indptr = (int32_t *)malloc((size_t)(n_rows + 1) * sizeof(int32_t));
+    p->indices = (int32_t *)malloc((size_t)(p->nnz ? p->nnz : 1) * sizeof(int32_t));
+    if (!p->indptr || !p->indices) { free(rlen); free(ap); free(adj); orc_pattern_free(p); return NULL; }
+    for (int64_t r = 0; r <= n_rows; ++r)
+        p->indptr[r] = (int32_t)rlen[r];
+    free(rlen);
+#pragma omp parallel
+    {
+        int64_t *buf = (int64_t *)malloc((size_t)(max_deg * n_p + 1) * sizeof(int64_t));
+        if (!buf) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 1024)
+        for (int64_t v = 0; v < n_own; ++v) {
+            if (!buf)
+                continue;
+            const int64_t m = orc_node_set(elem, n_p, p->overlap_elements, adj, ap, v, buf);
+            for (int c = 0; c < dim; ++c) {
+                const int64_t r = dim * v + c, gr = dim * (n0 + v) + c;
+                int32_t *out = p->indices + p->indptr[r];
+                if (!free_dof[gr]) {
+                    out[0] = (int32_t)gr;
+                    continue;
+                }
+                int64_t o = 0;
+                for (int64_t i = 0; i < m; ++i)
+                    for (int c2 = 0; c2 < dim; ++c2)
+                        if (free_dof[dim * buf[i] + c2])
+                            out[o++] = (int32_t)(dim * buf[i] + c2);
+            }
+        }
+        free(buf);
+    }
+    if (failed) { free(ap); free(adj); orc_pattern_free(p); return NULL; }
+
+    /* constrained diagonals, in row order */
+    int64_t n_cd = 0;
+    for (int64_t r = 0; r < n_rows; ++r)
+        n_cd += !free_dof[dim * n0 + r];
+    p->n_cd = n_cd;
+    p->cdiag = (int32_t *)malloc((size_t)(n_cd ? n_cd : 1) * sizeof(int32_t));
+    p->row_slot_ptr = (int32_t *)malloc((size_t)(n_rows + 1) * sizeof(int32_t));
+    if (!p->cdiag || !p->row_slot_ptr) { free(ap); free(adj); orc_pattern_free(p); return NULL; }
+    n_cd = 0;
+    for (int64_t r = 0; r < n_rows; ++r)
+        if (!free_dof[dim * n0 + r])
+            p->cdiag[n_cd++] = p->indptr[r];
+
+    /* row slots: a free row gets one slot per element of its node, in element order */
+    int64_t ns = 0;
+    p->row_slot_ptr[0] = 0;
+    for (int64_t r = 0; r < n_rows; ++r) {
+        if (free_dof[dim * n0 + r])
+            ns += ap[r / dim + 1] - ap[r / dim];
+        if (ns > INT32_MAX) { free(ap); free(adj); orc_pattern_free(p); return NULL; }
+        p->row_slot_ptr[r + 1] = (int32_t)ns;
+    }
+    p->n_slots = ns;
+    p->slot_elem = (int32_t *)malloc((size_t)(ns ? ns : 1) * sizeof(int32_t));
+    p->slot_lrow = (uint8_t *)malloc((size_t)(ns ? ns : 1));
+    p->slot_pos = (int32_t *)malloc((size_t)(ns ? ns : 1) * nld * sizeof(int32_t));
+    if (!p->slot_elem || !p->slot_lrow || !p->slot_pos) { free(ap); free(adj); orc_pattern_free(p); return NULL; }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < n_rows; ++r) {
+        const int64_t v = r / dim, c = r % dim, gv = n0 + v;
+        if (!free_dof[dim * gv + c])
+            continue;
+        int64_t s = p->row_slot_ptr[r];
+        for (int64_t k = ap[v]; k < ap[v + 1]; ++k, ++s) {
+            const int64_t *nd = elem + p->overlap_elements[adj[k]] * n_p;
+            int a_loc = 0;
+            while (nd[a_loc] != gv)
+                ++a_loc;
+            p->slot_elem[s] = adj[k];
+            p->slot_lrow[s] = (uint8_t)(dim * a_loc + c);
+            int32_t *pos = p->slot_pos + s * nld;
+            for (int b = 0; b < n_p; ++b)
+                for (int c2 = 0; c2 < dim; ++c2) {
+                    const int64_t col = dim * nd[b] + c2;
+                    pos[dim * b + c2] = free_dof[col]
+                        ? orc_find(p->indices, p->indptr[r], p->indptr[r + 1], (int32_t)col) : -1;
+                }
+        }
+    }
+    free(ap);
+    free(adj);
+    return p;
+}
+
+/* sizes: n_ov, n_ovn, n_rows, nnz, n_slots, n_cd */
+void orc_pattern_sizes(const void *h, int64_t *out)
+{
+    const orc_pattern *p = (const orc_pattern *)h;
+    out[0] = p->n_ov; out[1] = p->n_ovn; out[2] = p->n_rows; out[3] = p->nnz; out[4] = p->n_slots;
+    out[5] = p->n_cd;
+}
+
+/* copy one array out: 0 overlap_elements, 1 overlap_nodes, 2 dof_lids, 3 indptr, 4 indices,
+ * 5 constrained_diag_positions, 6 row_slot_ptr, 7 slot_elem, 8 slot_lrow, 9 slot_pos */
+void orc_pattern_copy(const void *h, int which, void *dst)
+{
+    const orc_pattern *p = (const orc_pattern *)h;
+    const int nld = p->dim * p->n_p;
+    switch (which) {
+    case 0: memcpy(dst, p->overlap_elements, (size_t)p->n_ov * sizeof(int64_t)); break;
+    case 1: memcpy(dst, p->overlap_nodes, (size_t)p->n_ovn * sizeof(int64_t)); break;
+    case 2: memcpy(dst, p->dof_lids, (size_t)p->n_ov * nld * sizeof(int32_t)); break;
+    case 3: memcpy(dst, p->indptr, (size_t)(p->n_rows + 1) * sizeof(int32_t)); break;
+    case 4: memcpy(dst, p->indices, (size_t)p->nnz * sizeof(int32_t)); break;
+    case 5: memcpy(dst, p->cdiag, (size_t)p->n_cd * sizeof(int32_t)); break;
+    case 6: memcpy(dst, p->row_slot_ptr, (size_t)(p->n_rows + 1) * sizeof(int32_t)); break;
+    case 7: memcpy(dst, p->slot_elem, (size_t)p->n_slots * sizeof(int32_t)); break;
+    case 8: memcpy(dst, p->slot_lrow, (size_t)p->n_slots); break;
+    case 9: memcpy(dst, p->slot_pos, (size_t)p->n_slots * nld * sizeof(int32_t)); break;
+    default: break;
+    }
 }

@@ -11,7 +11,11 @@ Restated reference routines (paths relative to the reference project root):
 * ``reduction``            -- src/slope_stability/constitutive/reduction.py:14-78
 * ``geometry``             -- src/slope_stability/fem/assembly.py:50-136 (2D), :139-245 (3D)
 * ``owned_pattern``        -- src/slope_stability/fem/distributed_tangent.py:297-478, 937-1175
-  (structural CSR, row maps, element->CSR scatter map, row-slot metadata, overlap dofs)
+  (structural CSR, row maps, element->CSR scatter map, row-slot metadata, overlap dofs); pure
+  Python, for small meshes
+* ``owned_pattern_c``      -- the same pattern (without the legacy scatter map) through the C
+  restatement ``orc_pattern_build`` in ``oracle.c``, for meshes of millions of elements
+* ``geometry_3d_c``        -- src/slope_stability/fem/assembly.py:139-245 through ``orc_geometry_3d``
 * the C functions in ``oracle.c`` (see its header) for the 3D kernels.
 """
 
@@ -73,6 +77,78 @@ def _c(a, dt):
 def num_threads() -> int:
     lib().orc_num_threads.restype = ctypes.c_int
     return int(lib().orc_num_threads())
+
+
+def set_num_threads(n: int) -> None:
+    """OpenMP threads of the C restatement's kernels (omp_set_num_threads)."""
+    lib().orc_set_num_threads(ctypes.c_int(int(n)))
+
+
+_PATTERN_ARRAYS = (("overlap_elements", np.int64), ("overlap_nodes", np.int64), ("overlap_element_dof_lids", np.int32),
+                   ("indptr", np.int32), ("indices", np.int32), ("constrained_diag_positions", np.int32),
+                   ("row_slot_ptr", np.int32), ("slot_elem", np.int32), ("slot_lrow", np.uint8),
+                   ("slot_pos", np.int32))
+
+
+def owned_pattern_c(elem, q_mask, owned_node_range):
+    """``owned_pattern`` through the C restatement (no legacy scatter map), as a dict of arrays."""
+    L = lib()
+    L.orc_pattern_build.restype = ctypes.c_void_p
+    elem = np.asarray(elem, dtype=np.int64)
+    q_mask = np.asarray(q_mask, dtype=bool)
+    dim, n_nodes = q_mask.shape
+    n_p, n_elem = elem.shape
+    nld = dim * n_p
+    elem_em = np.ascontiguousarray(elem.T)
+    free = np.ascontiguousarray(q_mask.reshape(-1, order="F").astype(np.uint8))
+    n0, n1 = (int(v) for v in owned_node_range)
+    h = L.orc_pattern_build(ctypes.c_int(dim), ctypes.c_int64(n_nodes), ctypes.c_int(n_p), ctypes.c_int64(n_elem),
+                            elem_em.ctypes.data_as(ctypes.c_void_p), free.ctypes.data_as(ctypes.c_void_p),
+                            ctypes.c_int64(n0), ctypes.c_int64(n1))
+    if not h:
+        raise MemoryError("orc_pattern_build failed (allocation, or an index beyond int32)")
+    try:
+        sz = np.zeros(6, dtype=np.int64)
+        L.orc_pattern_sizes(ctypes.c_void_p(h), sz.ctypes.data_as(ctypes.c_void_p))
+        n_ov, n_ovn, n_rows, nnz, n_slots, n_cd = (int(v) for v in sz)
+        shapes = {"overlap_elements": (n_ov,), "overlap_nodes": (n_ovn,), "overlap_element_dof_lids": (n_ov, nld),
+                  "indptr": (n_rows + 1,), "indices": (nnz,), "constrained_diag_positions": (n_cd,),
+                  "row_slot_ptr": (n_rows + 1,), "slot_elem": (n_slots,), "slot_lrow": (n_slots,),
+                  "slot_pos": (n_slots, nld)}
+        out = {}
+        for k, (name, dt) in enumerate(_PATTERN_ARRAYS):
+            a = np.empty(shapes[name], dtype=dt)
+            if a.size:
+                L.orc_pattern_copy(ctypes.c_void_p(h), ctypes.c_int(k), a.ctypes.data_as(ctypes.c_void_p))
+            out[name] = a
+    finally:
+        L.orc_pattern_free(ctypes.c_void_p(h))
+    nodes = out["overlap_nodes"]
+    lid = np.full(n_nodes, -1, dtype=np.int64)
+    lid[nodes] = np.arange(nodes.size)
+    gdofs = lambda v: (dim * np.repeat(v, dim) + np.tile(np.arange(dim), v.size)).astype(np.int64)  # noqa: E731
+    out["overlap_global_dofs"] = gdofs(nodes)
+    out["owned_local_overlap_dofs"] = gdofs(lid[np.arange(n0, n1)])
+    out["owned_free_mask"] = free[dim * n0:dim * n1].astype(bool)
+    return out
+
+
+def geometry_3d_c(coord, elem, dhat, wf):
+    """3D ``geometry`` through the C restatement: dphi1..3 (n_int, n_p) and weights (n_int,).
+    ``elem`` is (n_p, n_el) node ids, ``dhat`` (3, n_p, n_q)."""
+    coord = _c(coord, np.float64)
+    elem_em = np.ascontiguousarray(np.asarray(elem, dtype=np.int64).T)
+    dhat = _c(dhat, np.float64)
+    wf = _c(wf, np.float64)
+    n_el, n_p = elem_em.shape
+    n_q = dhat.shape[2]
+    d = [np.empty((n_el * n_q, n_p)) for _ in range(3)]
+    w = np.empty(n_el * n_q)
+    vp = ctypes.c_void_p
+    lib().orc_geometry_3d(coord.ctypes.data_as(vp), ctypes.c_int64(coord.shape[1]), elem_em.ctypes.data_as(vp),
+                          ctypes.c_int64(n_el), ctypes.c_int(n_p), ctypes.c_int(n_q), dhat.ctypes.data_as(vp),
+                          wf.ctypes.data_as(vp), *[x.ctypes.data_as(vp) for x in d], w.ctypes.data_as(vp))
+    return d, w
 
 
 # --------------------------------------------------------------------------- 3D kernels
@@ -576,4 +652,7 @@ def branch_features(E, c_bar, sin_phi, shear, lame):
 
 
 def have_reference_checkout() -> bool:
-    return os.path.isdir("/root/reference/src/slope_stability")
+    """Whether the reference's kernel sources are where ``oracle/Makefile`` looks for them
+    (``SSP_REFERENCE_ROOT``, or the recipe's default)."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "have-ref"], capture_output=True)
+    return r.returncode == 0

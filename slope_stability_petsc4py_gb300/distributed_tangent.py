@@ -205,17 +205,70 @@ def _elastic_ds_device(t, dim, shear, bulk, lame):
     return (vol_f[None, :] * lame[:, None] + 2.0 * id_f[None, :] * shear[:, None]).contiguous().reshape(n, 9)
 
 
+def _project_values_onto_pattern(source, indptr, indices, n_cols: int) -> np.ndarray:
+    """Values of a CSR matrix ``source`` (rows = the pattern's rows) at the pattern's positions;
+    entries outside the pattern are dropped, positions without an entry are 0, and of repeated
+    entries the last one counts -- what the reference's per-row dictionary lookup gives
+    (distributed_tangent.py:628-640)."""
+    src = source.tocsr() if hasattr(source, "tocsr") else source
+    indptr = np.asarray(indptr, dtype=np.int64)
+    n_rows = indptr.size - 1
+    if src.shape[0] != n_rows:
+        raise ValueError(f"elastic rows have {src.shape[0]} rows, the pattern {n_rows}")
+    keys = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(indptr)) * n_cols + np.asarray(indices, np.int64)
+    s_ptr = np.asarray(src.indptr, dtype=np.int64)
+    s_keys = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(s_ptr)) * n_cols + np.asarray(src.indices, np.int64)
+    out = np.zeros(keys.size, dtype=np.float64)
+    if keys.size == 0 or s_keys.size == 0:
+        return out
+    pos = np.minimum(np.searchsorted(keys, s_keys), keys.size - 1)
+    hit = keys[pos] == s_keys
+    out[pos[hit]] = np.asarray(src.data, dtype=np.float64)[hit]  # repeated positions: the last entry is kept
+    return out
+
+
+def _strain_operator(dim: int, dphi, elem_ov, n_q: int, n_nodes: int) -> csr_matrix:
+    """Sparse strain operator of a (sub)mesh from its per-point gradients dphi[k] (n_int, n_p):
+    E[s + n_strain * p] = sum_j B[s + n_strain * p, j] u[j], engineering shears, the reference's
+    row/column layout and canonical CSR form (fem/assembly.py:205-230 for 3D, :96-122 for 2D)."""
+    from scipy.sparse import coo_matrix
+
+    elem_ov = np.asarray(elem_ov, dtype=np.int64)
+    n_p, n_el = elem_ov.shape
+    n_int = n_el * n_q
+    pts = np.arange(n_int, dtype=np.int64)
+    node = np.repeat(elem_ov.T, n_q, axis=0)  # (n_int, n_p): node of local node a at point p
+    if dim == 3:
+        # (strain row, component, gradient) of the nine nonzeros of a node's 6x3 block
+        terms = ((0, 0, 0), (3, 0, 1), (5, 0, 2), (1, 1, 1), (3, 1, 0), (4, 1, 2), (2, 2, 2), (4, 2, 1), (5, 2, 0))
+    else:
+        terms = ((0, 0, 0), (2, 0, 1), (1, 1, 1), (2, 1, 0))
+    ns = 6 if dim == 3 else 3
+    rows = [np.broadcast_to((ns * pts + s)[:, None], (n_int, n_p)) for s, _c, _k in terms]
+    cols = [dim * node + c for _s, c, _k in terms]
+    vals = [np.asarray(dphi[k], dtype=np.float64) for _s, _c, k in terms]
+    B = coo_matrix((np.concatenate([v.ravel() for v in vals]),
+                    (np.concatenate([r.ravel() for r in rows]), np.concatenate([c.ravel() for c in cols]))),
+                   shape=(ns * n_int, dim * n_nodes)).tocsr()
+    B.eliminate_zeros()
+    return B
+
+
 def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, materials, owned_node_range, *,
                                   elem_type: str = "P2", include_unique: bool = True,
                                   include_legacy_scatter: bool = True, include_overlap_B: bool = True,
                                   elastic_rows=None, keep_slot_metadata: bool = True) -> OwnedTangentPattern:
     """Prepare the fixed owned-row pattern for repeated tangent assembly (on the current CUDA device).
 
-    ``include_overlap_B`` is accepted for compatibility; the sparse strain operator is never
-    needed by the CUDA kernels and is not built (``overlap_B`` is None).  ``elastic_rows`` may be
-    a previously prepared pattern for the same mesh and owned range, whose elastic values are
-    reused.  ``keep_slot_metadata=False`` skips the host copies of the row-slot arrays (the
-    device path does not read them).
+    ``include_overlap_B``: build the overlap submesh's sparse strain operator ``overlap_B``
+    (scipy CSR, rows ``s + n_strain * point``, columns the overlap dofs), as the reference does
+    (fem/assembly.py:205-230, 2D :96-122).  The CUDA kernels never read it; it costs host memory
+    and a device -> host copy of the gradients, so ``ConstitutiveOperator.from_mesh`` passes False.
+    ``elastic_rows``: the reference's ``OwnedElasticRows`` for the same owned range (its
+    ``local_matrix`` values are projected onto the pattern, as distributed_tangent.py:1040 does),
+    or a previously prepared pattern of this package for the same mesh and range (its device
+    elastic values are reused).  ``keep_slot_metadata=False`` skips the host copies of the
+    row-slot arrays (the device path does not read them).
     """
     t = _lib.require_cuda()
     timings = {}
@@ -304,10 +357,14 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
         dev["slot_pos"] = _lib.to_device(g["slot_pos"], t.int32)
 
     # elastic values: owned rows of K_elast on the pattern, constrained diagonals = 1
+    if elastic_rows is not None and tuple(int(v) for v in elastic_rows.owned_node_range) != (n0, n1):
+        raise ValueError("Prebuilt elastic_rows owned_node_range does not match prepare_owned_tangent_pattern request")
     if elastic_rows is not None and isinstance(elastic_rows, OwnedTangentPattern):
-        if tuple(elastic_rows.owned_node_range) != (n0, n1):
-            raise ValueError("Prebuilt elastic_rows owned_node_range does not match prepare_owned_tangent_pattern request")
         dev["elastic_values"] = elastic_rows.device["elastic_values"]
+        reused = True
+    elif elastic_rows is not None:  # the reference's OwnedElasticRows: its assembled rows, projected
+        vals = _project_values_onto_pattern(elastic_rows.local_matrix, g["indptr"], g["indices"], dim * n_nodes)
+        dev["elastic_values"] = _lib.to_device(vals, f64)
         reused = True
     else:
         _c0, _phi, _psi, shear, bulk, lame, _gamma = heterogenous_materials(
@@ -335,12 +392,16 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
         unique_elements = unique_nodes = unique_local_int_indices = np.empty(0, dtype=np.int64)
 
     pattern_matrix = csr_matrix((np.ones(nnz), g["indices"], g["indptr"]), shape=(n_rows, dim * n_nodes))
+    overlap_B = None
+    if include_overlap_B:
+        overlap_B = _strain_operator(dim, [dev[k].cpu().numpy() for k in ("dphi1", "dphi2", "dphi3")[:dim]], elem_ov,
+                                     n_q, int(ov_nodes.size))
     n_ld = dim * n_p
     scatter_host = g["scatter_map"] if include_legacy_scatter else np.empty((n_ov, 0), dtype=np.int32)
     empty_i32 = np.empty(0, dtype=np.int32)
     pat = OwnedTangentPattern(
         dim=dim, n_strain=6 if dim == 3 else 3, owned_node_range=(n0, n1), owned_row_range=(dim * n0, dim * n1),
-        overlap_nodes=ov_nodes, overlap_elements=ov_el, overlap_global_dofs=overlap_global_dofs, overlap_B=None,
+        overlap_nodes=ov_nodes, overlap_elements=ov_el, overlap_global_dofs=overlap_global_dofs, overlap_B=overlap_B,
         overlap_element_dof_lids=g["overlap_element_dof_lids"], owned_local_overlap_dofs=g["owned_local_overlap_dofs"],
         owned_free_mask=owned_free, owned_free_local_rows=owned_free_rows,
         global_free_size=int(np.count_nonzero(q_mask)), local_matrix_pattern=pattern_matrix,
@@ -354,7 +415,8 @@ def prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, mate
         "scatter_bytes": float(scatter_host.nbytes),
         "row_slot_bytes": float(sum(np.asarray(g[k]).nbytes for k in ("row_slot_ptr", "slot_elem", "slot_lrow", "slot_pos")
                                     if k in g)),
-        "overlap_B_bytes": 0.0,
+        "overlap_B_bytes": float(0 if overlap_B is None else
+                                 overlap_B.data.nbytes + overlap_B.indices.nbytes + overlap_B.indptr.nbytes),
         "unique_B_bytes": 0.0,
         "dphi_bytes": float(sum(dev[k].numel() * 8 for k in ("dphi1", "dphi2", "dphi3"))),
         "device_bytes": float(sum(v.numel() * v.element_size() for v in dev.values())),

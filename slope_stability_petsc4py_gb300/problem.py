@@ -287,7 +287,8 @@ class ConstitutiveOperator:
         coord = np.asarray(coord, dtype=np.float64)
         elem = np.asarray(elem, dtype=np.int64)
         pat = prepare_owned_tangent_pattern(coord, elem, q_mask, material_identifier, materials, (0, coord.shape[1]),
-                                            elem_type=elem_type, include_legacy_scatter=False, keep_slot_metadata=False)
+                                            elem_type=elem_type, include_legacy_scatter=False, include_overlap_B=False,
+                                            keep_slot_metadata=False)
         n_int = elem.shape[1] * pat.n_q
         c0, phi, psi, shear, bulk, lame, _g = heterogenous_materials(material_identifier, np.ones(n_int, bool), pat.n_q,
                                                                      materials)
@@ -935,6 +936,23 @@ class ConstitutiveOperator:
         vals = self._bddc_tangent_into(self._bddc_values("regularized"), r=r)
         self.time_build_tangent_local.append(perf_counter() - t0)
         return self._bddc_matrix("regularized", vals)
+
+    # public BDDC builders (problem.py:2099-2112): the reference's Newton loop finds them with
+    # getattr (nonlinear/newton.py:188-206) and asks for the subdomain matrix it preconditions with
+    def build_bddc_tangent_matrix(self, *, local_mat_type: str = "aij"):
+        if self.bddc_subdomain_pattern is None:
+            raise RuntimeError("BDDC subdomain pattern not configured")
+        return self._build_bddc_tangent_matrix(local_mat_type=local_mat_type)
+
+    def build_bddc_regularized_matrix(self, r: float, *, local_mat_type: str = "aij"):
+        if self.bddc_subdomain_pattern is None:
+            raise RuntimeError("BDDC subdomain pattern not configured")
+        return self._build_bddc_regularized_matrix(r, local_mat_type=local_mat_type)
+
+    def build_bddc_elastic_matrix(self, *, local_mat_type: str = "aij"):
+        if self.bddc_subdomain_pattern is None:
+            raise RuntimeError("BDDC subdomain pattern not configured")
+        return self._build_bddc_elastic_matrix(local_mat_type=local_mat_type)
 
     def build_K_regularized(self, r: float):
         if self.owned_tangent_pattern is None:

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this folder from the reference implementation itself.
 
-Run where the reference checkout is mounted (it is read, never modified):
+Run where a reference checkout is available (it is read, never modified), naming it by the
+environment variable ``SSP_REFERENCE_ROOT``:
 
-    python tests/golden/make_golden.py
+    SSP_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py [generator ...]
 
 What it does:
 
@@ -29,7 +30,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF_ROOT = Path(os.environ.get("SSP_REFERENCE_ROOT", "/root/reference"))
+REF_ROOT = Path(os.environ.get("SSP_REFERENCE_ROOT", ""))
 sys.path.insert(0, str(REPO))
 
 from oracle import oracle_py  # noqa: E402
@@ -575,12 +576,41 @@ def gen_mesh_io(ref):
     print("mesh_io", tet.shape[1], "tets", tri.shape[1], "boundary triangles")
 
 
+def gen_overlap_operator(ref):
+    """The reference's overlap strain operator (``overlap_B``, include_overlap_B=True) and its
+    ``OwnedElasticRows`` with the elastic values it projects onto the owned pattern, on a partially
+    owned 3D P2 slope and a partially owned 2D P2 slope."""
+    dt = ref["dt"]
+    from slope_stability.fem.distributed_elastic import assemble_owned_elastic_rows
+
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    mat = {"c0": 6.0, "phi": 45.0, "psi": 0.0, "young": 2.0e4, "poisson": 0.49, "gamma_sat": 20.0,
+           "gamma_unsat": 20.0}
+    for tag, m in (("3d", synthetic.slope_mesh_3d(3, 2, 2, depth=6.0, elem_type="P2")),
+                   ("2d", synthetic.slope_mesh_2d(4, 3, elem_type="P2"))):
+        n_nodes = m.coord.shape[1]
+        owned = (n_nodes // 3, 2 * n_nodes // 3)
+        mat_id = np.zeros(m.elem.shape[1], np.int64)
+        rows = assemble_owned_elastic_rows(m.coord, m.elem, m.q_mask, mat_id, [mat], owned, elem_type="P2")
+        pat = dt.prepare_owned_tangent_pattern(m.coord, m.elem, m.q_mask, mat_id, [mat], owned, elem_type="P2",
+                                               include_unique=False, include_overlap_B=True, elastic_rows=rows)
+        B, L = pat.overlap_B, rows.local_matrix.tocsr()
+        np.savez_compressed(HERE / f"overlap_operator_{tag}.npz", coord=m.coord, elem=m.elem, q_mask=m.q_mask,
+                            owned_node_range=np.asarray(owned), B_data=B.data, B_indices=B.indices,
+                            B_indptr=B.indptr, B_shape=np.asarray(B.shape), L_data=L.data, L_indices=L.indices,
+                            L_indptr=L.indptr, L_shape=np.asarray(L.shape), **pattern_arrays(pat))
+        print("overlap_operator", tag, B.nnz, "B nnz", L.nnz, "elastic-row nnz")
+
+
 GENERATORS = ("constitutive_3d", "constitutive_2d", "reduction", "patterns", "pattern_2d", "pattern_2d_p4", "bddc",
-              "mesh_io", "potential")
+              "mesh_io", "potential", "overlap_operator")
 
 
 def main(which=GENERATORS):
     """``python tests/golden/make_golden.py [generator ...]`` (default: all of GENERATORS)."""
+    if not (REF_ROOT / "src" / "slope_stability").is_dir():
+        raise SystemExit("set SSP_REFERENCE_ROOT to a reference checkout")
     oracle_py.build(ref=True)
     libref = oracle_py.ref_lib()
     assert libref is not None, "reference kernels did not build"
@@ -604,6 +634,8 @@ def main(which=GENERATORS):
         gen_mesh_io(ref)
     if "potential" in which:
         gen_potential(ref["problem"], ref["reduction"])
+    if "overlap_operator" in which:
+        gen_overlap_operator(ref)
 
 
 if __name__ == "__main__":

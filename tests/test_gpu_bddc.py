@@ -95,7 +95,9 @@ def test_operator_bddc_matrices_against_oracle(oracle, dim, et):
     K_o = oracle.tangent_scatter(dim, pat.dphi1, pat.dphi2, pat.dphi3 if dim == 3 else None, np.ascontiguousarray(DS.T),
                                  pat.local_assembly_weight, pat.scatter_map, pat.n_q, pat.nnz)
     K_o[pat.constrained_diag_positions] = 1.0
-    mat = op._build_bddc_tangent_matrix()
+    # through the public names, found by getattr as the reference's Newton loop finds them
+    # (nonlinear/newton.py:188-206)
+    mat = getattr(op, "build_bddc_tangent_matrix")()
     rows, cols, vals = mat.getValuesCSR()
     assert np.array_equal(rows, pat.local_matrix_pattern.indptr) and np.array_equal(cols, pat.local_matrix_pattern.indices)
     assert rel_err(vals, K_o) <= PLAIN_RTOL
@@ -104,14 +106,14 @@ def test_operator_bddc_matrices_against_oracle(oracle, dim, et):
     assert pat.local_primal_vertices.size > 0
     assert np.array_equal(mat.metadata.get("bddc_primal_vertices_local"), pat.local_primal_vertices)
     r = 0.3
-    _, _, kr = op._build_bddc_regularized_matrix(r).getValuesCSR()
+    _, _, kr = getattr(op, "build_bddc_regularized_matrix")(r).getValuesCSR()
     assert rel_err(kr, (1.0 - r) * K_o + r * pat.elastic_values) <= PLAIN_RTOL
-    _, _, ke = op._build_bddc_elastic_matrix().getValuesCSR()
+    _, _, ke = getattr(op, "build_bddc_elastic_matrix")().getValuesCSR()
     assert np.array_equal(ke, pat.elastic_values)
     handle = mat.handle
     op.reduction(1.0)
     op.constitutive_problem_stress_tangent(U)
-    assert op._build_bddc_tangent_matrix().handle == handle  # updated in place
+    assert op.build_bddc_tangent_matrix().handle == handle  # updated in place
     # the mixed form (plastic corrections in compensated FP32) against the FP64 tangent
     op.reduction(1.2)
     op.tangent_form = "mixed"

@@ -145,3 +145,42 @@ def test_triangle_p4_node_order_matches_reference_generator(name):
                         (lambda m: (m.coord, m.elem))(synthetic.slope_mesh_2d(4, 3, elem_type="P4"))):
         X = coord[:, elem]
         assert np.max(np.abs(np.einsum("dve,kv->dke", X[:, :3], tup) - X)) <= 1e-12 * np.max(np.abs(coord))
+
+
+@pytest.mark.parametrize("name", golden_files("overlap_operator_"))
+def test_overlap_strain_operator_equals_reference(name):
+    """overlap_B (include_overlap_B=True) from the pattern's gradients: the reference's sparse strain
+    operator, same rows, columns and canonical CSR structure, values to rounding of the gradients."""
+    from scipy.sparse import csr_matrix
+
+    from slope_stability_petsc4py_gb300.distributed_tangent import _strain_operator
+
+    g = golden(name)
+    dim = g["q_mask"].shape[0]
+    nodes = g["overlap_nodes"]
+    lid = np.full(g["coord"].shape[1], -1, dtype=np.int64)
+    lid[nodes] = np.arange(nodes.size)
+    elem_ov = lid[g["elem"][:, g["overlap_elements"]]]
+    dphi = [g["dphi1"], g["dphi2"]] + ([g["dphi3"]] if dim == 3 else [])
+    B = _strain_operator(dim, dphi, elem_ov, int(g["n_q"]), nodes.size)
+    ref = csr_matrix((g["B_data"], g["B_indices"], g["B_indptr"]), shape=tuple(g["B_shape"]))
+    assert B.shape == ref.shape
+    assert np.array_equal(B.indptr, ref.indptr) and np.array_equal(B.indices, ref.indices)
+    assert np.max(np.abs(B.data - ref.data)) <= 1e-12 * np.max(np.abs(ref.data))
+
+
+@pytest.mark.parametrize("name", golden_files("overlap_operator_"))
+def test_reference_elastic_rows_project_onto_the_pattern(name):
+    """A reference OwnedElasticRows passed as elastic_rows: its assembled rows projected onto the
+    owned pattern give the reference's elastic_values bit for bit (entries outside the pattern,
+    such as constrained columns, are dropped)."""
+    from scipy.sparse import csr_matrix
+
+    from slope_stability_petsc4py_gb300.distributed_tangent import _project_values_onto_pattern
+
+    g = golden(name)
+    L = csr_matrix((g["L_data"], g["L_indices"], g["L_indptr"]), shape=tuple(g["L_shape"]))
+    vals = _project_values_onto_pattern(L, g["indptr"], g["indices"], int(g["L_shape"][1]))
+    assert np.array_equal(vals, g["elastic_values"])
+    with pytest.raises(ValueError):
+        _project_values_onto_pattern(L[:-1], g["indptr"], g["indices"], int(g["L_shape"][1]))

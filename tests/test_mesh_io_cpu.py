@@ -13,8 +13,9 @@ import pytest
 
 from conftest import golden
 
-# the reference checkout, where this container has it (the GPU machines do not)
-REF_MESH = Path(os.environ.get("SSP_REFERENCE_ROOT", "/root/reference")) / "meshes/3d_hetero_ssr/SSR_hetero_ada_L1.msh"
+# a reference checkout named by SSP_REFERENCE_ROOT (the tests that read its mesh skip without one)
+_REF = os.environ.get("SSP_REFERENCE_ROOT")
+REF_MESH = Path(_REF) / "meshes/3d_hetero_ssr/SSR_hetero_ada_L1.msh" if _REF else Path("/nonexistent")
 
 
 def _write_msh(path, coord, tet, tri, tet_tags, tri_tags, names, *, binary, big_endian=False, id_offset=0):

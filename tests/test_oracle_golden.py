@@ -76,6 +76,30 @@ def test_pattern_restatement_bit_exact(oracle, name):
         assert p[key].dtype == g[key].dtype or key in ("owned_free_mask",), (key, p[key].dtype, g[key].dtype)
 
 
+@pytest.mark.parametrize("name", golden_files("pattern_") + golden_files("pattern2d_") + golden_files("overlap_operator_"))
+def test_pattern_c_restatement_bit_exact(oracle, name):
+    """The C restatement of the pattern builder (the one large meshes use) against the reference."""
+    g = golden(name)
+    p = oracle.owned_pattern_c(g["elem"], g["q_mask"], tuple(g["owned_node_range"]))
+    for key in ("indptr", "indices", "row_slot_ptr", "slot_elem", "slot_lrow", "slot_pos", "constrained_diag_positions",
+                "overlap_elements", "overlap_nodes", "overlap_global_dofs", "overlap_element_dof_lids",
+                "owned_local_overlap_dofs", "owned_free_mask"):
+        assert np.array_equal(p[key], g[key]), key
+        assert p[key].dtype == g[key].dtype or key in ("owned_free_mask",), (key, p[key].dtype, g[key].dtype)
+
+
+def test_pattern_c_restatement_equals_python_restatement_on_a_slope(oracle):
+    """C and Python restatements on a larger partially owned P2 slope with a Dirichlet base."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    m = synthetic.slope_mesh_3d(5, 3, 3, elem_type="P2")
+    rng = (m.n_nodes // 5, 3 * m.n_nodes // 5)
+    a = oracle.owned_pattern(m.elem, m.q_mask, rng)
+    b = oracle.owned_pattern_c(m.elem, m.q_mask, rng)
+    for key, val in b.items():
+        assert np.array_equal(a[key], val), key
+
+
 @pytest.mark.parametrize("name", golden_files("pattern_"))
 def test_assembly_restatement_matches_reference(oracle, name):
     g = golden(name)
@@ -134,6 +158,21 @@ def test_geometry_restatement_matches_reference(oracle, name):
     dhat = fem.reference_gradients(3, et)
     elem_ov = g["elem"][:, g["overlap_elements"]]
     (d1, d2, d3), w = oracle.geometry(g["coord"], elem_ov, 3, dhat, wf)
+    assert rel_err(d1, g["dphi1"]) <= PLAIN_RTOL
+    assert rel_err(d2, g["dphi2"]) <= PLAIN_RTOL
+    assert rel_err(d3, g["dphi3"]) <= PLAIN_RTOL
+    assert rel_err(w, g["weight"]) <= PLAIN_RTOL
+
+
+@pytest.mark.parametrize("name", golden_files("pattern_"))
+def test_geometry_c_restatement_matches_reference(oracle, name):
+    from slope_stability_petsc4py_gb300 import fem
+
+    g = golden(name)
+    et = str(g["elem_type"])
+    _xi, wf = fem.quadrature(3, et)
+    (d1, d2, d3), w = oracle.geometry_3d_c(g["coord"], g["elem"][:, g["overlap_elements"]],
+                                           fem.reference_gradients(3, et), wf)
     assert rel_err(d1, g["dphi1"]) <= PLAIN_RTOL
     assert rel_err(d2, g["dphi2"]) <= PLAIN_RTOL
     assert rel_err(d3, g["dphi3"]) <= PLAIN_RTOL
