@@ -1,29 +1,36 @@
 """Benchmark of the Newton hot path: quadrature points per second of one builder pass.
 
-One step = one Newton iteration of the reference's owned-row builder on a fixed synthetic slope:
+One step = one Newton iteration of the reference's owned-row builder on a synthetic slope:
 strength reduction -> strain B u -> Mohr-Coulomb return mapping (S and DS) -> owned internal
 force B^T (w S) -> tangent CSR values sum B^T (w DS) B -> constrained diagonals and the
-regularised blend (1-r) K + r K_elast.  ``value`` is measured with inputs resident in HBM;
-``e2e`` goes through the public ``ConstitutiveOperator`` API with pinned host inputs and host
-outputs (U uploaded, F_free and every CSR value copied back each step, as the PETSc hand-off
-needs).
+regularised blend (1-r) K + r K_elast.  The timed steps cycle through four displacement states of
+one continuation (a shear band growing at fixed lambda and r), pre-uploaded to HBM, so the plastic
+set moves from step to step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3d_p2_homo] [--impl reference]
+* ``value``: inputs resident in HBM, CUDA events over the timed steps.
+* ``e2e``: the same steps through ``ConstitutiveOperator.build_F_K_regularized_all_free`` with
+  pinned host U and host outputs (F_free and the CSR values the PETSc hand-off reads).
+* ``parity``: the GPU outputs (plain and mixed forms) of one state against the oracle -- the CPU
+  restatement of the reference's kernels -- on the whole workload, pattern included.
+* ``cpu_baseline`` / ``--impl reference``: the oracle's restatement of the reference's kernels on
+  the host cores, on a bounded sample of the workload (the owned node block of one rank).
 
-``--impl reference`` times the reference algorithm on the host cores instead (the oracle's C
-restatement of the reference kernels, all threads), on the same workload.
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3d_p2_large] [--impl reference]
 """
 
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
+import platform
 import subprocess
 import sys
 import tempfile
 import time
 from pathlib import Path
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -31,33 +38,19 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 
 METRIC = "quad-pts/s constitutive+tangent; FP64 plain vs mixed+learned at ≤1e-6 err"
-LAMBDA, R_REG = 1.1, 0.1
-
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the step kernels, from one
-# ncu capture of the full-size workload on a GB300 (one pass per launch, the second Newton step of
-# `bench.py --steps 3 --warmup 3`); keyed by workload and C-ABI entry point.
-NCU_TRAFFIC = {
-    "3d_p2_homo": {
-        "ssp_tangent_plastic_correction": 286.20e6 + 63.73e6,
-        "ssp_tangent_plastic_correction_mixed": 298.00e6 + 72.01e6,
-        "ssp_assemble_overlap_strain_3d_affine_mixed": 22.82e6 + 0.04e6,
-        "ssp_assemble_force_element_affine_mixed": 84.88e6 + 1.49e6,
-        "ssp_assemble_overlap_strain_3d_mixed": 281.74e6 + 35.76e6,
-        "ssp_assemble_overlap_strain_3d": 284.63e6 + 36.25e6,
-        "ssp_assemble_force_element": 343.75e6 + 2.57e6,
-        "ssp_assemble_overlap_strain_3d_p2_affine": 22.85e6 + 1.40e6,
-        "ssp_assemble_force_element_p2_affine": 84.94e6 + 0.30e6,
-        "ssp_assemble_overlap_strain_3d_p2_affine_mixed": 23.48e6 + 2.04e6,
-        "ssp_assemble_force_element_p2_affine_mixed": 84.95e6 + 0.02e6,
-        "ssp_constitutive_3d_sds_binned": (90.67 + 304.28 + 22.35 + 1.76 + 34.33 + 1.12) * 1e6,
-    },
-    "3d_p4_hetero": {
-        "ssp_tangent_plastic_correction_mixed": 1121.05e6 + 524.74e6,
-        "ssp_assemble_overlap_strain_3d": 1784.86e6 + 50.96e6,
-        "ssp_assemble_force_element": 1102.46e6 + 11.75e6,
-        "ssp_constitutive_3d_sds_binned": (121.29 + 245.19 + 39.91 + 39.69 + 41.21 + 1.96) * 1e6,
-    },
-}
+LAMBDA, R_REG, DAVIS = 1.1, 0.1, "B"
+DEFAULT_CONFIG = "3d_p2_large"
+# the other benchmarked configurations, measured (and checked against the oracle) after the headline
+OTHER_WORKLOADS = ("2d_p2_homo", "3d_p2_homo", "3d_p2_hetero", "3d_p4_hetero")
+# shear-band amplitude of the four timed states, times the workload's amplitude (fixed lambda and r)
+STATE_FACTORS = (0.9, 1.0, 1.1, 1.2)
+# a strength-reduction sequence: 10 lambda steps of 6 Newton iterations; the load and the band grow
+# over the steps so the plastic fraction rises from about 2 % to 35 % (3D heterogeneous slopes)
+SSR_STEPS, SSR_ITERS = 10, 6
+# points per step of the bounded CPU samples (all host threads, and one thread)
+SAMPLE_POINTS, SAMPLE_POINTS_1T = 4_000_000, 250_000
+STEP_TEXT = ("reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + constrained diagonals "
+             "+ regularised blend")
 
 
 def parse():
@@ -66,15 +59,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="3d_p2_homo")
+    ap.add_argument("--config", default=DEFAULT_CONFIG)
     ap.add_argument("--mesh", default=None, help="a gmsh .msh tet4 file as the workload (overrides --config)")
     ap.add_argument("--mesh-elem", default="P2", choices=["P1", "P2", "P4"], help="element order for --mesh")
     ap.add_argument("--form", default="plain", choices=["plain", "mixed"],
                     help="plain: FP64 tangent (the drop-in); mixed: FP32 plastic-point products")
-    ap.add_argument("--return-mapping", default="binned", choices=["binned", "unsorted", "learned"],
-                    help="binned: two-pass exact binning; unsorted: one divergent pass; learned: bins proposed "
-                         "by the branch network (trained on the GPU before the timed region)")
+    ap.add_argument("--return-mapping", default="binned", choices=["binned", "unsorted", "learned", "previous"],
+                    help="binned: exact screen/decide/finish binning; unsorted: one divergent pass; learned: bins "
+                         "proposed by the branch network; previous: bins of the previous iteration's branches")
     ap.add_argument("--no-forms", action="store_true", help="skip timing the mixed / learned / unsorted forms")
+    ap.add_argument("--no-ssr", action="store_true", help="skip the strength-reduction sequence")
+    ap.add_argument("--no-others", action="store_true", help="skip the other benchmarked configurations")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison")
     ap.add_argument("--bddc", action="store_true", help="also time the BDDC subdomain tangent of half the mesh")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -86,21 +82,52 @@ def parse():
 
 
 def workload(name: str):
+    """Mesh, materials and the displacement basis (G, V) of a named configuration: every state of
+    the benchmark is g G + a V (load factor g, shear-band amplitude a)."""
     from slope_stability_petsc4py_gb300 import synthetic
 
-    cfg = synthetic.CONFIGS[name]
-    mesh = synthetic.build_config_mesh(name)
-    mats = synthetic.MaterialSet.layered(4, seed=0) if cfg["n_layers"] > 1 else synthetic.MaterialSet.homogeneous()
-    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
-                  poisson=float(mats.poisson[i]), gamma_sat=float(mats.gamma[i]), gamma_unsat=float(mats.gamma[i]))
-             for i in range(mats.c0.size)]
-    U = synthetic.displacement_field(mesh, mats, amplitude=cfg["amplitude"], seed=3)
-    return mesh, mats, specs, U
+    return synthetic.config_workload(name)
+
+
+def timed_states(w):
+    return [w.G + (f * w.amp) * w.V for f in STATE_FACTORS]
+
+
+def ssr_target(w, k):
+    """lambda and displacement at the end of strength-reduction step k (k = -1: the undeformed start)."""
+    if k < 0:
+        return 1.0, np.zeros_like(w.G)
+    x = k / (SSR_STEPS - 1)
+    g = 0.13 * (1.0 / 0.13) ** x
+    a = 0.15 * (12.0 / 0.15) ** x
+    return 1.0 + 0.05 * k, g * w.G + (a * w.amp) * w.V
+
+
+def ssr_states(w):
+    """(lambda, U) of every Newton iteration of the sequence: within step k the iterates move from
+    the previous step's solution towards this step's by 1/2, 3/4, 7/8, ... of the increment."""
+    prev = ssr_target(w, -1)[1]
+    for k in range(SSR_STEPS):
+        lam, tgt = ssr_target(w, k)
+        for it in range(SSR_ITERS):
+            s = 1.0 - 0.5 ** (it + 1)
+            yield k, it, lam, prev + s * (tgt - prev)
+        prev = tgt
 
 
 def describe(name, mesh, n_int, nnz):
     return (f"{name}: {mesh.n_elem:,} {mesh.dim}D {mesh.elem_type} elements, {n_int:,} quadrature points, "
             f"{mesh.n_nodes * mesh.dim:,} dofs, {nnz:,} CSR nnz")
+
+
+def bench_config(w, n_int, nnz):
+    """The workload's description; both arms print this same dict."""
+    return {"workload": describe(w.name, w.mesh, n_int, nnz), "step": STEP_TEXT,
+            "states": f"{len(STATE_FACTORS)} displacement states cycled (gravity + tanh shear band, amplitude "
+                      f"{', '.join(f'{f:g}' for f in STATE_FACTORS)} x {w.amp:g} m), lambda {LAMBDA}, r {R_REG}, "
+                      f"Davis {DAVIS}",
+            "l2": f"inputs larger than L2: >= 424 B per point of constitutive data alone "
+                  f"({424 * n_int / 1e9:.2f} GB) against the 129 MB L2"}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -152,172 +179,196 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# ----------------------------------------------------------------------------- CPU reference path
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return f"{line.split(':', 1)[1].strip()} ({platform.machine()})"
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
 
 
-class OracleRunner:
-    """The reference algorithm (oracle restatement of its C kernels) on the host cores."""
-
-    def __init__(self, mesh, specs, U, dphi=None, weight=None):
-        from oracle import oracle_py as oracle
-        from slope_stability_petsc4py_gb300 import fem
-        from slope_stability_petsc4py_gb300.distributed_tangent import _PatternBuild
-        from slope_stability_petsc4py_gb300.materials import heterogenous_materials
-
-        self.o = oracle
-        oracle.build()
-        pb = _PatternBuild(mesh.elem, mesh.q_mask, (0, mesh.n_nodes))
-        keys = ("overlap_nodes", "overlap_element_dof_lids", "row_slot_ptr", "slot_elem", "slot_lrow", "slot_pos",
-                "constrained_diag_positions", "owned_free_mask", "overlap_elements")
-        self.p = {k: pb.get(k) for k in keys}
-        self.nnz = pb.sizes["nnz"]
-        pb.close()
-        xi, wf = fem.quadrature(mesh.dim, mesh.elem_type)
-        self.n_q = xi.shape[1]
-        if dphi is None:
-            dphi, weight = oracle.geometry(mesh.coord, mesh.elem[:, self.p["overlap_elements"]], mesh.dim,
-                                           fem.reference_gradients(mesh.dim, mesh.elem_type), wf)
-        self.d, self.w = dphi, weight
-        nodes = self.p["overlap_nodes"]
-        dim = mesh.dim
-        gd = dim * np.repeat(nodes, dim) + np.tile(np.arange(dim), nodes.size)
-        self.u_ov = np.ascontiguousarray(U.reshape(-1, order="F")[gd])
-        n_int = mesh.n_elem * self.n_q
-        self.mat = dict(zip(("c0", "phi", "psi", "shear", "bulk", "lame"),
-                            heterogenous_materials(mesh.material_id, np.ones(n_int, bool), self.n_q, specs)[:6]))
-        self.n_int = n_int
-        self.dim = dim
-        self.elastic = None
-
-    def step(self):
-        o, p, d = self.o, self.p, self.d
-        cb, sp = o.reduction(self.mat["c0"], self.mat["phi"], self.mat["psi"], LAMBDA, "B")
-        E = o.strain_3d(d[0], d[1], d[2], self.u_ov, p["overlap_element_dof_lids"], self.n_q)
-        S, DS = o.constitutive_3d(E, cb, sp, self.mat["shear"], self.mat["bulk"], self.mat["lame"])
-        F = o.force_rows_3d(d[0], d[1], d[2], S, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"], self.n_q)
-        F[~p["owned_free_mask"].astype(bool)] = 0.0
-        K = o.tangent_rows_3d(d[0], d[1], d[2], DS, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"],
-                              p["slot_pos"], self.n_q, self.nnz)
-        K[p["constrained_diag_positions"]] = 1.0
-        if self.elastic is not None:
-            K *= 1.0 - R_REG
-            K += R_REG * self.elastic
-        return F, K
-
-    def time_steps(self, steps, warmup, budget_s=60.0):
-        for _ in range(warmup):
-            self.step()
-        times = []
-        t_start = time.perf_counter()
-        for _ in range(steps):
-            t0 = time.perf_counter()
-            self.step()
-            times.append(time.perf_counter() - t0)
-            if time.perf_counter() - t_start > budget_s:
-                break
-        return times
+# ----------------------------------------------------------------------------- the reference on the CPU
 
 
-# ----------------------------------------------------------------------------- GPU arm
+def oracle_runner(w, owned=None):
+    from oracle.newton_step import OracleNewtonStep
+
+    return OracleNewtonStep(w.mesh, w.specs, owned)
 
 
-def fp64_peak(torch, lib):
-    """Measured FP64 FMA rate of this device (TFLOP/s), from the ssp_probe_dfma kernel."""
+def sample_block(mesh, n_points_goal, n_q):
+    """Owned node block [0, n1) of one rank of the reference's contiguous partition whose share of
+    the mesh has about n_points_goal quadrature points (the whole mesh when it is smaller)."""
+    n_int = mesh.n_elem * n_q
+    parts = max(1, int(math.ceil(n_int / n_points_goal)))
+    return (0, int(math.ceil(mesh.n_nodes / parts))), parts
+
+
+def cpu_reference_figures(w, states, *, steps, warmup, budget_s):
+    """The oracle timed on bounded samples: one rank's block with every host thread, and a smaller
+    block on one thread.  Returns (all-thread runner, result dict)."""
+    from oracle import oracle_py as o
+    from slope_stability_petsc4py_gb300 import fem
+
+    n_q = len(fem.quadrature(w.mesh.dim, w.mesh.elem_type)[1])
+    block, parts = sample_block(w.mesh, SAMPLE_POINTS, n_q)
+    runner = oracle_runner(w, block)
+    times = runner.time_steps(states, steps, warmup, LAMBDA, R_REG, budget_s=budget_s)
+    t = float(np.median(times))
+    threads = o.num_threads()
+    block1, parts1 = sample_block(w.mesh, SAMPLE_POINTS_1T, n_q)
+    one = oracle_runner(w, block1)
+    o.set_num_threads(1)
+    try:
+        t1 = float(np.median(one.time_steps(states, 2, 1, LAMBDA, R_REG)))
+    finally:
+        o.set_num_threads(threads)
+    res = {"value": runner.n_int / t, "unit": "quad-pts/s", "cores": threads, "kind": "port",
+           "cpu_model": cpu_model(), "ms_per_step": t * 1e3, "steps": len(times),
+           "sample": f"owned node block {list(block)} of {w.mesh.n_nodes:,} nodes (rank 0 of a {parts}-way "
+                     f"partition: {runner.n_int:,} points of its {runner.p['overlap_elements'].size:,} overlap "
+                     f"elements, {runner.nnz:,} nnz), median of {len(times)} steps after {warmup} warm-up; "
+                     f"the reference's C kernels restated (oracle), OpenMP",
+           "one_thread": {"value": one.n_int / t1, "unit": "quad-pts/s", "cores": 1, "ms_per_step": t1 * 1e3,
+                          "sample": f"owned node block {list(block1)} (rank 0 of {parts1}): {one.n_int:,} points, "
+                                    f"median of 2 steps"}}
+    return runner, res
+
+
+# ----------------------------------------------------------------------------- GPU arm helpers
+
+
+def fp64_peak(torch):
+    """Measured FP64 FMA rate of this device (TFLOP/s): the bench-only probe library's kernel, eight
+    independent FMA chains per thread over 8 CTAs per SM."""
+    import ctypes
+
+    from slope_stability_petsc4py_gb300 import build
+
+    lib = ctypes.CDLL(str(build.PROBE_LIB))
+    lib.ssp_probe_dfma.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 2
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     blocks, threads, iters = sms * 8, 256, 8192
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
     for _ in range(2):
-        lib.call("ssp_probe_dfma", iters, blocks, threads, lib.ptr(out), lib.stream_handle())
+        assert lib.ssp_probe_dfma(iters, blocks, threads, out.data_ptr(), st) == 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    lib.call("ssp_probe_dfma", iters, blocks, threads, lib.ptr(out), lib.stream_handle())
+    assert lib.ssp_probe_dfma(iters, blocks, threads, out.data_ptr(), st) == 0
     e1.record()
     torch.cuda.synchronize()
-    flops = 16.0 * iters * threads * blocks
-    return flops / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    return 16.0 * iters * threads * blocks / (e0.elapsed_time(e1) * 1e-3) / 1e12
 
 
 def peaks():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback (6.8 TB/s)"
 
 
-def kernel_profile(torch, lib, step, op, reps=3):
-    """Per-entry-point CUDA-event times, the launches serialised on one stream (the concurrent force
-    and the staged values copy would otherwise share the GPU with the kernels inside the brackets)."""
+def make_step(op, states_dev, lam=LAMBDA, r=R_REG):
+    """One Newton iteration per call through the operator's composite entry point, cycling the
+    pre-uploaded states."""
+    k = [0]
+
+    def step():
+        op.build_F_K_regularized_all_free(lam, states_dev[k[0] % len(states_dev)], r)
+        k[0] += 1
+
+    return step
+
+
+def kernel_profile(torch, lib, op, states_dev):
+    """Per-entry-point CUDA-event times over one pass through the states, the launches serialised on
+    one stream (the concurrent force and the staged values copy would otherwise share the GPU with
+    the kernels inside the brackets); plastic counts per state."""
     saved = (op.concurrent_force, op.stage_values)
     op.concurrent_force = False
     op.stage_values = False
-    lib.TRACE = []
-    for _ in range(reps):
+    step = make_step(op, states_dev)
+    for _ in range(len(states_dev)):  # settle the incremental restore on this state order
         step()
+    torch.cuda.synchronize()
+    lib.TRACE = []
+    plastic = []
+    for _ in range(len(states_dev)):
+        step()
+        plastic.append(workload_plastic(op))
     torch.cuda.synchronize()
     per = {}
     for name, a, b in lib.TRACE:
         per.setdefault(name, []).append(a.elapsed_time(b))
     lib.TRACE = None
     op.concurrent_force, op.stage_values = saved
+    reps = len(states_dev)
     total = sum(sum(v) for v in per.values()) / reps
-    return {k: {"ms_per_launch": float(np.mean(v)), "launches_per_step": len(v) / reps,
-                "ms_per_step": float(np.sum(v)) / reps, "share": float(np.sum(v)) / reps / total}
-            for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]))}
+    kernels = {k: {"ms_per_launch": float(np.mean(v)), "launches_per_step": len(v) / reps,
+                   "ms_per_step": float(np.sum(v)) / reps, "share": float(np.sum(v)) / reps / total}
+               for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]))}
+    return kernels, plastic
 
 
-def workload_stats(op):
+def workload_plastic(op):
+    n_q = op.owned_tangent_pattern.n_q
+    plastic = op._branch.view(-1, n_q) != 0
+    return {"n_plastic": int(plastic.sum().item()), "n_plastic_el": int(plastic.any(dim=1).sum().item())}
+
+
+def workload_stats(op, plastic):
     pat = op.owned_tangent_pattern
-    n_q = pat.n_q
-    br = op._branch.view(-1, n_q)
-    plastic = br != 0
-    return {"n": pat.n_local_int, "n_el": int(pat.overlap_elements.size), "n_p": pat.n_p, "n_q": n_q, "dim": pat.dim,
-            "ns": pat.n_strain, "nnz": pat.nnz, "n_rows": int(pat.local_matrix_pattern.shape[0]),
-            "n_u": int(pat.overlap_global_dofs.size), "n_plastic": int(plastic.sum().item()),
-            "n_plastic_el": int(plastic.any(dim=1).sum().item()),
-            "working_set": sum(v.numel() * v.element_size() for v in pat.device.values())}
+    return {"n": pat.n_local_int, "n_el": int(pat.overlap_elements.size), "n_p": pat.n_p, "n_q": pat.n_q,
+            "dim": pat.dim, "ns": pat.n_strain, "nnz": pat.nnz, "n_rows": int(pat.local_matrix_pattern.shape[0]),
+            "n_u": int(pat.overlap_global_dofs.size),
+            "n_plastic": float(np.mean([p["n_plastic"] for p in plastic])),
+            "n_plastic_el": float(np.mean([p["n_plastic_el"] for p in plastic])),
+            "device_bytes": sum(v.numel() * v.element_size() for v in pat.device.values())}
 
 
 def algorithmic(name, st):
-    """Algorithmic HBM bytes and FP64 flops of one launch (each datum read or written once)."""
+    """Algorithmic bytes and FP64 flops of one launch, from the per-unit costs of the hot-path cost
+    table (reference layouts, every datum moved once):
+      return mapping S+DS  424 B/point (3D: E 48, five material arrays 40, S 48, DS 288; 2D: 168)
+      S only               136 B/point
+      strain               24 n_p + 48 B/point + 3 n_p (8 + 4) B/element (2D: 16 n_p + 24, 2 n_p * 12)
+      force                48 + 24 n_p B/point + 8 B/row (2D: 32 + 16 n_p)
+      tangent values       per element: 288 n_q + 24 n_p n_q + 8 n_q + 4 (3 n_p)^2 + 8 nnz/n_el;
+                           2 n_q 3 n_p (18 + 9 n_p) flops ('rows' formulation);
+                           the plastic correction counts the plastic elements it visits.
+    'fp64' is the FP64 work this library's kernels execute (symmetric halves, plastic points only)."""
     n, n_el, n_p, n_q, dim, ns = st["n"], st["n_el"], st["n_p"], st["n_q"], st["dim"], st["ns"]
     nld = dim * n_p
-    s_out = 6 if dim == 3 else 4
-    if name in ("ssp_constitutive_sds_branch", "ssp_constitutive_3d_sds_binned", "ssp_constitutive_3d_sds_learned",
-                "ssp_constitutive_3d_sds_binned_mixed", "ssp_constitutive_3d_sds_learned_mixed"):
-        return {"bytes": n * (8 * ns + 4 * 8 + 8 * s_out + 8 * ns * ns + 1), "flops": 0}
-    if name in ("ssp_assemble_overlap_strain_3d", "ssp_assemble_overlap_strain_2d", "ssp_assemble_overlap_strain_3d_mixed"):
-        fp64 = 0 if name.endswith("_mixed") else n * 2 * 9 * n_p  # the mixed kernel's products are FP32
-        return {"bytes": n * (8 * dim * n_p + 8 * ns) + n_el * 4 * nld + 8 * st["n_u"], "flops": fp64}
-    if name == "ssp_assemble_overlap_strain_3d_affine_mixed":  # J^{-1} per element instead of per-point gradients
-        return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": 0}
-    if name == "ssp_assemble_force_element_affine_mixed":
-        return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": 0}
-    if name == "ssp_assemble_overlap_strain_3d_p2_affine":  # barycentric regrouping, FP64: ≈470 per element
-        return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": n_el * 2 * (204 + 24 * n_q)}
-    if name == "ssp_assemble_force_element_p2_affine":  # moments of w σ, FP64: ≈530 per 11-point element
-        return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": n_el * 2 * (200 + 30 * n_q)}
-    if name == "ssp_assemble_overlap_strain_3d_p2_affine_mixed":  # double-float, barycentric form
-        return {"bytes": n * 8 * ns + n_el * (4 * nld + 72) + 8 * st["n_u"], "flops": 0}
-    if name == "ssp_assemble_force_element_p2_affine_mixed":
-        return {"bytes": n * (8 * ns + 8) + n_el * (4 * nld + 72) + 8 * st["n_rows"], "flops": 0}
-    if name in ("ssp_assemble_force_element", "ssp_assemble_force_element_mixed"):
-        fp64 = 0 if name.endswith("_mixed") else n * nld * 8
-        return {"bytes": n * (8 * dim * n_p + 8 * ns + 8) + n_el * 4 * nld + 8 * st["n_rows"], "flops": fp64}
-    if name == "ssp_blend_values":
-        return {"bytes": 3 * 8 * st["nnz"], "flops": 0}
-    if name == "ssp_reduction":
-        return {"bytes": 40 * n, "flops": 0}
-    if name == "ssp_gather":
-        return {"bytes": 20 * st["n_u"], "flops": 0}
+    if name == "ssp_constitutive_3d_s":
+        return {"bytes": 136 * n, "flops": 0, "fp64": 0}
+    if name.startswith("ssp_constitutive"):
+        per = 424 if dim == 3 else 24 + 40 + 32 + 72
+        return {"bytes": per * n, "flops": 0, "fp64": 0}
+    if name.startswith("ssp_assemble_overlap_strain"):
+        per_pt = 24 * n_p + 48 if dim == 3 else 16 * n_p + 24
+        fp64 = 0 if "mixed" in name else (n_el * 2 * (204 + 24 * n_q) if "p2_affine" in name else n * 2 * 9 * n_p)
+        return {"bytes": n * per_pt + n_el * nld * 12, "flops": n * 2 * ns * dim * n_p, "fp64": fp64}
+    if name.startswith("ssp_assemble_force"):
+        per_pt = 48 + 24 * n_p if dim == 3 else 32 + 16 * n_p
+        fp64 = 0 if "mixed" in name else (n_el * 2 * (200 + 30 * n_q) if "p2_affine" in name else n * nld * 8)
+        return {"bytes": n * per_pt + 8 * st["n_rows"], "flops": n * 2 * ns * nld, "fp64": fp64}
+    per_el = 288 * n_q + 24 * n_p * n_q + 8 * n_q + 4 * nld * nld + 8 * st["nnz"] / max(n_el, 1)
+    fl_el = 2 * n_q * nld * (18 + 9 * n_p)
     if name.startswith("ssp_tangent_plastic_correction"):
-        npl, npe = st["n_plastic"], st["n_plastic_el"]
-        fp64 = npl * 2.0 * nld * ns * dim  # H = B^T (w D): FP64 in both forms
+        units = st["n_plastic_el"]
+        fp64 = st["n_plastic"] * 2.0 * nld * ns * dim  # H = B^T (w dD): FP64 in both forms
         if not name.endswith("_mixed"):
-            fp64 += npl * 2.0 * nld * (nld + 1) // 2 * dim  # the B^T H products
-        return {"bytes": n + npl * (8 * ns * ns + 8 * dim * n_p + 24) + npe * (4 * nld * nld + 16 * nld * nld),
-                "flops": fp64}
-    return {"bytes": 0, "flops": 0}
+            fp64 += st["n_plastic"] * 2.0 * nld * (nld + 1) // 2 * dim  # the B^T H products, upper half
+        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": fp64}
+    if name in ("ssp_tangent_element", "ssp_assemble_tangent_values_3d_rows", "ssp_assemble_tangent_values_3d_p2"):
+        return {"bytes": n_el * per_el, "flops": n_el * fl_el, "fp64": n_el * fl_el}
+    if name == "ssp_blend_values":
+        return {"bytes": 24 * st["nnz"], "flops": 0, "fp64": 0}
+    return {"bytes": 0, "flops": 0, "fp64": 0}
 
 
 def time_steps(torch, step, warmup, steps):
@@ -333,110 +384,314 @@ def time_steps(torch, step, warmup, steps):
     return e0.elapsed_time(e1) / steps
 
 
-def compare_forms(torch, lib, op, mesh, mats, args, step, ms_plain):
-    """The same step in the other forms, on the same state and timed the same way: the mixed
-    tangent, the mixed tangent with the learned branch proposal, and the unsorted single-pass
-    return mapping (the method without binning).  Restores the plain form afterwards."""
+def train_branch_model(torch, op, w, *, max_per_state=500_000):
+    """Train the branch-proposal network on the exact return mapping's (features, branch) pairs of a
+    strength-reduction sequence: the last Newton iterate of each of its ten lambda steps (plastic
+    fraction about 2 % to 35 %), at most max_per_state screen-listed points per state.  The timed
+    states are not among them."""
+    from slope_stability_petsc4py_gb300 import learned
+
+    t0 = time.perf_counter()
+    states = [(lam, torch.as_tensor(U, device="cuda")) for k, it, lam, U in ssr_states(w) if it == SSR_ITERS - 1]
+    X, y = learned.collect_training_data(op, states, max_per_state=max_per_state)
+    del states
+    model = learned.BranchProposal(seed=0)
+    epochs = 4
+    hist = model.train(X, y, epochs=epochs, batch=16384, lr=3e-3)
+    torch.cuda.synchronize()
+    op.branch_model = model
+    counts = torch.bincount(y.long(), minlength=5).cpu().numpy()
+    op.reduction(LAMBDA)
+    return {"training_samples": int(X.shape[0]), "samples": "points the elastic screen lists",
+            "label_counts": {b: int(c) for b, c in zip(learned.BRANCHES, counts)}, "epochs": epochs, "batch": 16384,
+            "final_loss": hist[-1][0], "final_train_accuracy": hist[-1][1], "training_s": time.perf_counter() - t0,
+            "training_states": f"the last iterate of each of the {SSR_STEPS} lambda steps of the strength-reduction "
+                               f"sequence (lambda 1.0..1.45), at most {max_per_state:,} listed points each"}
+
+
+def compare_forms(torch, lib, op, w, states_dev, args, ms_plain):
+    """The same steps in the other forms, on the same moving states, timed the same way: the mixed
+    tangent; the exact binning replaced by the network's proposal (learned) or by the previous
+    iteration's branches (previous, the trivial predictor); the single-pass unsorted return mapping
+    (the method without binning).  Restores the plain binned form afterwards."""
     n_int = op.owned_tangent_pattern.n_local_int
     out = {"plain": {"value": n_int / (ms_plain * 1e-3), "ms_per_step": ms_plain}}
-    w = max(args.warmup, 3)
-    op.tangent_form = "plain"
-    step()
-    kp = op.build_K_regularized(R_REG).values.clone()
+    wu = max(args.warmup, 3)
+    step = make_step(op, states_dev)
+    op.tangent_form, op.return_mapping = "plain", "binned"
+    for _ in range(len(states_dev)):
+        step()
+    ref_K = []
+    for U in states_dev:
+        op.build_F_K_regularized_all_free(LAMBDA, U, R_REG)
+        ref_K.append(op.build_K_regularized(R_REG).values.clone())
     for name, form, mapping in (("mixed", "mixed", "binned"), ("mixed+learned", "mixed", "learned"),
-                                ("plain+unsorted", "plain", "unsorted"), ("plain+learned", "plain", "learned")):
+                                ("mixed+previous", "mixed", "previous"), ("plain+unsorted", "plain", "unsorted"),
+                                ("plain+learned", "plain", "learned"), ("plain+previous", "plain", "previous")):
         if mapping == "learned" and op.branch_model is None:
-            out["learned_training"] = train_branch_model(torch, op, mesh, mats, args.config)
+            out["learned_training"] = train_branch_model(torch, op, w)
         op.tangent_form, op.return_mapping = form, mapping
-        ms = time_steps(torch, step, w, args.steps)
+        ms = time_steps(torch, step, wu, args.steps)
         entry = {"value": n_int / (ms * 1e-3), "ms_per_step": ms, "speedup_vs_plain": ms_plain / ms}
         if form == "mixed":
-            km = op.build_K_regularized(R_REG).values
-            entry["tangent_error_vs_fp64"] = float((km - kp).abs().max() / kp.abs().max())
+            errs = []
+            for U, kp in zip(states_dev, ref_K):
+                op.build_F_K_regularized_all_free(LAMBDA, U, R_REG)
+                km = op.build_K_regularized(R_REG).values
+                errs.append(float((km - kp).abs().max() / kp.abs().max()))
+            entry["tangent_error_vs_fp64"] = max(errs)
         out[name] = entry
     op.tangent_form, op.return_mapping = "plain", "binned"
     lib.raise_on_device_status()
     return out
 
 
-def measure_bddc(torch, lib, op, mesh, specs, args, step):
-    """BDDC subdomain tangent of the workload's state: the subdomain owning the elements of the
-    lower half of the node range (prepare_bddc_subdomain_pattern), one regularised subdomain build
-    per Newton iteration after the owned evaluation; timed with the elastic predictor + plastic
-    corrections (FP64 and mixed), and with the full contraction of every subdomain point."""
-    from slope_stability_petsc4py_gb300 import prepare_bddc_subdomain_pattern
-
-    owners = np.sort(mesh.elem.min(axis=0))
-    owned = (0, int(owners[owners.size // 2]))
-    t0 = time.perf_counter()
-    pat = prepare_bddc_subdomain_pattern(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, owned,
-                                         elem_type=mesh.elem_type,
-                                         overlap_local_int_indices=op.owned_tangent_pattern.local_int_indices)
-    prep_s = time.perf_counter() - t0
-    op.set_bddc_subdomain_pattern(pat)
-    w = max(args.warmup, 3)
-    out = {"subdomain_elements": int(pat.local_elements.size), "subdomain_points": pat.n_local_int,
-           "nnz": pat.nnz, "owned_node_range": list(owned), "prepare_s": prep_s}
-    for name, form in (("plain", "plain"), ("mixed", "mixed")):
+def measure_new_lambda_r(torch, lib, op, states_dev, reps=6):
+    """Steps that start a new continuation step: every one at a new (lambda, r), so the reduction
+    and the regularised elastic base are recomputed inside it (CUDA events around each step)."""
+    out = {}
+    for form in ("plain", "mixed"):
         op.tangent_form = form
-        step()
-        ms = time_steps(torch, lambda: op._build_bddc_regularized_matrix(R_REG), w, args.steps)
-        out[name] = {"ms_per_build": ms, "subdomain_quad_pts_per_s": pat.n_local_int / (ms * 1e-3),
-                     "assembled_nnz_per_s": pat.nnz / (ms * 1e-3)}
+        times = []
+        for k in range(reps):
+            lam, r = LAMBDA + 0.013 * (k + 1), R_REG + 0.007 * (k + 1)
+            U = states_dev[k % len(states_dev)]
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            op.build_F_K_regularized_all_free(lam, U, r)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        out[form] = {"ms_per_step": float(np.median(times[1:])), "steps": reps - 1,
+                     "value": op.owned_tangent_pattern.n_local_int / (np.median(times[1:]) * 1e-3)}
     op.tangent_form = "plain"
-    step()
-    kp = op._build_bddc_regularized_matrix(R_REG).values.clone()
-    op._bddc["predictor_ok"] = False  # time the full contraction of every subdomain point
-    ms = time_steps(torch, lambda: op._build_bddc_regularized_matrix(R_REG), w, args.steps)
-    kf = op._build_bddc_regularized_matrix(R_REG).values
-    out["full_contraction"] = {"ms_per_build": ms, "max_rel_diff_vs_predictor": float((kf - kp).abs().max() / kp.abs().max())}
-    op.set_bddc_subdomain_pattern(None)
+    op.build_F_K_regularized_all_free(LAMBDA, states_dev[0], R_REG)  # back to the timed lambda and r
+    torch.cuda.synchronize()
     lib.raise_on_device_status()
     return out
 
 
-def measure_graph_replay(torch, lib, op, U_dev, args):
-    """The same step as a CUDA graph (ConstitutiveOperator.capture_regularized_build), replayed on
-    the displacement tensor: the kernels of build_F_K_regularized_all_free without the host work of
-    the Python entry point, for the plain and the mixed form."""
+def measure_ssr(torch, lib, op, w, forms=(("plain", "plain", "binned"), ("mixed", "mixed", "binned"),
+                                        ("mixed+learned", "mixed", "learned"))):
+    """The strength-reduction sequence (10 lambda steps x 6 Newton iterations, load and shear band
+    growing, r fixed) with every state pre-uploaded: each iteration one composite build; per-lambda-step
+    plastic fractions and the time of the whole sequence per form."""
+    seq = [(k, it, lam, torch.as_tensor(U, device="cuda")) for k, it, lam, U in ssr_states(w)]
     n_int = op.owned_tangent_pattern.n_local_int
-    w = max(args.warmup, 3)
+    out = {"lambda_steps": SSR_STEPS, "newton_iterations_per_step": SSR_ITERS, "r": R_REG}
+    fractions = []
+    for name, form, mapping in forms:
+        if mapping == "learned" and op.branch_model is None:
+            continue
+        op.tangent_form, op.return_mapping = form, mapping
+        for k, it, lam, U in seq[:3]:  # warm-up
+            op.build_F_K_regularized_all_free(lam, U, R_REG)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k, it, lam, U in seq:
+            op.build_F_K_regularized_all_free(lam, U, R_REG)
+            if name == "plain" and it == SSR_ITERS - 1:
+                fractions.append((k, lam, (op._branch != 0).float().mean()))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / len(seq)
+        out[name] = {"ms_per_iteration": ms, "value": n_int / (ms * 1e-3)}
+    out["plastic_fraction_per_step"] = [{"step": k, "lambda": round(lam, 3), "plastic_fraction": float(f.item())}
+                                        for k, lam, f in fractions]
+    op.tangent_form, op.return_mapping = "plain", "binned"
+    del seq
+    lib.raise_on_device_status()
+    return out
+
+
+def measure_graph_replay(torch, lib, op, states_dev, args):
+    """The same steps as a CUDA graph (ConstitutiveOperator.capture_regularized_build), replayed
+    after each state is copied into the captured displacement buffer (the copy is timed too)."""
+    n_int = op.owned_tangent_pattern.n_local_int
+    wu = max(args.warmup, 3)
     out = {}
+    U_buf = states_dev[0].clone()
     for form in ("plain", "mixed"):
         op.tangent_form = form
-        run = op.capture_regularized_build(LAMBDA, U_dev, R_REG)
-        ms = time_steps(torch, run.replay, w, args.steps)
+        run = op.capture_regularized_build(LAMBDA, U_buf, R_REG)
+        k = [0]
+
+        def replay():
+            U_buf.copy_(states_dev[k[0] % len(states_dev)])
+            k[0] += 1
+            run.replay()
+
+        ms = time_steps(torch, replay, wu, args.steps)
         out[form] = {"value": n_int / (ms * 1e-3), "ms_per_step": ms}
     op.tangent_form = "plain"
     lib.raise_on_device_status()
     return out
 
 
-def train_branch_model(torch, op, mesh, mats, name):
-    """Train the branch-proposal network on continuation states other than the timed one
-    (strength-reduction factors 1.0..1.4, shear-band amplitudes 0.4..1.6 x the workload's)."""
-    from slope_stability_petsc4py_gb300 import learned, synthetic
+def measure_bddc(torch, lib, op, w, states_dev, args):
+    """BDDC subdomain tangent (prepare_bddc_subdomain_pattern on the lower half of the node range),
+    one regularised subdomain build per Newton iteration after the owned evaluation: elastic
+    predictor + plastic corrections (FP64 and mixed), and the full contraction of every point."""
+    from slope_stability_petsc4py_gb300 import prepare_bddc_subdomain_pattern
 
-    amp0 = synthetic.CONFIGS[name]["amplitude"]
+    mesh = w.mesh
+    owners = np.sort(mesh.elem.min(axis=0))
+    owned = (0, int(owners[owners.size // 2]))
     t0 = time.perf_counter()
-    states = [(float(lam), torch.as_tensor(synthetic.displacement_field(mesh, mats, amplitude=amp0 * f, seed=100 + k),
-                                           device="cuda"))
-              for k, (lam, f) in enumerate(zip(np.linspace(1.0, 1.4, 6), np.linspace(0.4, 1.6, 6)))]
-    X, y = learned.collect_training_data(op, states)
-    model = learned.BranchProposal(seed=0)
-    hist = model.train(X, y, epochs=6, batch=8192, lr=3e-3)
+    pat = prepare_bddc_subdomain_pattern(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, w.specs, owned,
+                                         elem_type=mesh.elem_type,
+                                         overlap_local_int_indices=op.owned_tangent_pattern.local_int_indices)
+    prep_s = time.perf_counter() - t0
+    op.set_bddc_subdomain_pattern(pat)
+    wu = max(args.warmup, 3)
+    out = {"subdomain_elements": int(pat.local_elements.size), "subdomain_points": pat.n_local_int,
+           "nnz": pat.nnz, "owned_node_range": list(owned), "prepare_s": prep_s}
+    op.build_F_K_regularized_all_free(LAMBDA, states_dev[1], R_REG)
+    for form in ("plain", "mixed"):
+        op.tangent_form = form
+        op.build_F_K_regularized_all_free(LAMBDA, states_dev[1], R_REG)
+        ms = time_steps(torch, lambda: op.build_bddc_regularized_matrix(R_REG), wu, args.steps)
+        out[form] = {"ms_per_build": ms, "subdomain_quad_pts_per_s": pat.n_local_int / (ms * 1e-3),
+                     "assembled_nnz_per_s": pat.nnz / (ms * 1e-3)}
+    op.tangent_form = "plain"
+    op.build_F_K_regularized_all_free(LAMBDA, states_dev[1], R_REG)
+    kp = op.build_bddc_regularized_matrix(R_REG).values.clone()
+    op._bddc["predictor_ok"] = False  # time the full contraction of every subdomain point
+    ms = time_steps(torch, lambda: op.build_bddc_regularized_matrix(R_REG), wu, args.steps)
+    kf = op.build_bddc_regularized_matrix(R_REG).values
+    out["full_contraction"] = {"ms_per_build": ms, "max_rel_diff_vs_predictor": float((kf - kp).abs().max() /
+                                                                                       kp.abs().max())}
+    op.set_bddc_subdomain_pattern(None)
+    lib.raise_on_device_status()
+    return out
+
+
+def measure_e2e(torch, op, states_host, args, form):
+    """The timed steps through the public API with host buffers: pinned host U in, F_free and the
+    CSR values (K.getValuesCSR(), the PETSc hand-off's input) out, wall clock per step."""
+    op.host_outputs = True
+    op.tangent_form = form
+    pinned = [torch.as_tensor(U).pin_memory() for U in states_host]
+    nst = len(pinned)
+    for k in range(max(3, nst)):
+        op.build_F_K_regularized_all_free(LAMBDA, pinned[k % nst], R_REG)[1].getValuesCSR()
     torch.cuda.synchronize()
-    op.branch_model = model
-    return {"training_samples": int(X.shape[0]), "samples": "points the elastic screen lists", "epochs": 6,
-            "batch": 8192, "final_loss": hist[-1][0],
-            "final_train_accuracy": hist[-1][1], "training_s": time.perf_counter() - t0,
-            "training_states": "6 states, lambda 1.0..1.4, amplitude 0.4..1.6x (the timed state is held out)"}
+    times, d2h = [], []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        F_free, K = op.build_F_K_regularized_all_free(LAMBDA, pinned[k % nst], R_REG)
+        K.getValuesCSR()  # synchronises: the CSR values are on the host
+        times.append(time.perf_counter() - t0)
+        d2h.append(int(F_free.nbytes + K.host_copy_bytes()))
+    op.host_outputs = False
+    op.tangent_form = "plain"
+    t = float(np.median(times))
+    n_int = op.owned_tangent_pattern.n_local_int
+    return {"value": n_int / t, "unit": "quad-pts/s", "h2d_bytes_per_step": int(states_host[0].nbytes),
+            "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": t * 1e3, "d2h_csr_bytes_full": 8 * op.owned_tangent_pattern.nnz,
+            "api": "ConstitutiveOperator.build_F_K_regularized_all_free(lam, U_host, r) + K.getValuesCSR()"}
+
+
+def parity_check(torch, op, runner, U_host, U_dev):
+    """Plain and mixed GPU outputs of one state against the oracle's on the same inputs (max-norm
+    relative errors; comparisons on the device), the CSR pattern and the element -> CSR map bit for
+    bit.  The oracle builds its own pattern, geometry and elastic values."""
+    pat = op.owned_tangent_pattern
+    t0 = time.perf_counter()
+    ref = runner.step(U_host, LAMBDA, R_REG, DAVIS)
+    oracle_s = time.perf_counter() - t0
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda")  # noqa: E731
+
+    def rel(a, b):
+        scale = b.abs().max().clamp_min(1e-300)
+        return float(((a - b).abs().max() / scale).item())
+
+    K_o, F_o = dev(ref["K"]), dev(ref["F"][runner.free])
+    S_o, DS_o = dev(ref["S"]), dev(ref["DS"])
+    out = {"state": f"amplitude {STATE_FACTORS[1]:g} x, lambda {LAMBDA}, r {R_REG}", "oracle_step_s": oracle_s,
+           "oracle_pattern_s": runner.pattern_s, "points": runner.n_int, "nnz": runner.nnz}
+    out["indices_bit_exact"] = bool(np.array_equal(pat.local_matrix_pattern.indptr, runner.p["indptr"]) and
+                                    np.array_equal(pat.local_matrix_pattern.indices, runner.p["indices"]))
+    sm = pat.device["scatter_map"]
+    p = runner.p
+    nld = pat.dim * pat.n_p
+    se = torch.as_tensor(p["slot_elem"].astype(np.int64), device="cuda")
+    sl = torch.as_tensor(p["slot_lrow"].astype(np.int64), device="cuda")
+    cols = sl[:, None] * nld + torch.arange(nld, device="cuda")[None, :]
+    out["element_map_bit_exact"] = bool(torch.equal(sm[se[:, None], cols], dev(p["slot_pos"])))
+    out["constrained_diagonals_bit_exact"] = bool(np.array_equal(pat.constrained_diag_positions,
+                                                                 p["constrained_diag_positions"]))
+    del se, sl, cols
+    for form in ("plain", "mixed"):
+        op.tangent_form = form
+        F, K = op.build_F_K_regularized_all_free(LAMBDA, U_dev, R_REG)
+        torch.cuda.synchronize()
+        out[form] = {"S": rel(op._S_aos, S_o), "DS": rel(op._DS_aos, DS_o), "F_free": rel(F, F_o),
+                     "K": rel(K.values, K_o)}
+    op.tangent_form = "plain"
+    out["tolerance"] = {"plain": "1e-12 max-norm relative (S, DS, F_free, K)",
+                        "mixed": "1e-6 tangent (K), 1e-11 force (F_free)"}
+    out["pass"] = bool(out["indices_bit_exact"] and out["element_map_bit_exact"] and
+                       out["constrained_diagonals_bit_exact"] and
+                       all(v <= 1e-12 for v in out["plain"].values()) and out["mixed"]["K"] <= 1e-6 and
+                       out["mixed"]["F_free"] <= 1e-11)
+    del K_o, F_o, S_o, DS_o
+    return out
+
+
+def measure_workload(torch, lib, w, args, *, headline):
+    """Build the operator of workload w and measure it.  headline: the full set of figures of the
+    bench line; otherwise the summary of an other configuration (plain, mixed, the proposal forms on
+    3D P4, and parity against the oracle)."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator
+
+    mesh = w.mesh
+    t0 = time.perf_counter()
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, w.specs,
+                                        elem_type=mesh.elem_type)
+    setup_s = time.perf_counter() - t0
+    pat = op.owned_tangent_pattern
+    states_host = timed_states(w)
+    states_dev = [torch.as_tensor(U, device="cuda") for U in states_host]
+    op.host_outputs = False
+    res = SimpleNamespace(op=op, states_host=states_host, states_dev=states_dev, setup_s=setup_s)
+    if headline:
+        return res
+    wu = max(args.warmup, 3)
+    step = make_step(op, states_dev)
+    out = {"workload": describe(w.name, mesh, pat.n_local_int, pat.nnz), "setup_s": setup_s}
+    for name, form, mapping in (("plain", "plain", "binned"), ("mixed", "mixed", "binned")):
+        if mesh.dim == 2 and form == "mixed":
+            continue
+        op.tangent_form, op.return_mapping = form, mapping
+        ms = time_steps(torch, step, wu, args.steps)
+        out[name] = {"value": pat.n_local_int / (ms * 1e-3), "ms_per_step": ms}
+    if mesh.dim == 3 and mesh.elem_type == "P4":  # the learned form's configuration
+        out["learned_training"] = train_branch_model(torch, op, w)
+        for name, form, mapping in (("mixed+learned", "mixed", "learned"), ("mixed+previous", "mixed", "previous"),
+                                    ("plain+unsorted", "plain", "unsorted"), ("plain+learned", "plain", "learned"),
+                                    ("plain+previous", "plain", "previous")):
+            op.tangent_form, op.return_mapping = form, mapping
+            ms = time_steps(torch, step, wu, args.steps)
+            out[name] = {"value": pat.n_local_int / (ms * 1e-3), "ms_per_step": ms,
+                         "speedup_vs_plain": out["plain"]["ms_per_step"] / ms}
+    op.tangent_form, op.return_mapping = "plain", "binned"
+    if "mixed" in out:
+        out["mixed"]["speedup_vs_plain"] = out["plain"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    if not args.no_parity:
+        runner = oracle_runner(w)
+        out["parity"] = parity_check(torch, op, runner, states_host[1], states_dev[1])
+        del runner
+    lib.raise_on_device_status()
+    return out
 
 
 def run_gpu(args):
     import torch
 
-    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, _lib
+    from slope_stability_petsc4py_gb300 import _lib
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -447,22 +702,17 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    mesh, mats, specs, U = workload(args.config)
-    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs,
-                                        elem_type=mesh.elem_type)
+    w = workload(args.config)
+    res = measure_workload(torch, _lib, w, args, headline=True)
+    op, states_dev, states_host = res.op, res.states_dev, res.states_host
     pat = op.owned_tangent_pattern
     n_int, nnz = pat.n_local_int, pat.nnz
-    U_dev = torch.as_tensor(U, device="cuda")
-    op.host_outputs = False
     op.tangent_form = args.form
     learned_info = None
     if args.return_mapping == "learned":
-        learned_info = train_branch_model(torch, op, mesh, mats, args.config)
+        learned_info = train_branch_model(torch, op, w)
     op.return_mapping = args.return_mapping
-
-    def step():  # one Newton iteration through the operator's composite entry point
-        op.build_F_K_regularized_all_free(LAMBDA, U_dev, R_REG)
-
+    step = make_step(op, states_dev)
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -495,122 +745,81 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # per-kernel durations from a separate traced pass (CUDA events on the launch stream)
-    kernels = kernel_profile(torch, _lib, step, op, reps=3)
-    stats = workload_stats(op)
+    kernels, plastic = kernel_profile(torch, _lib, op, states_dev)
+    stats = workload_stats(op, plastic)
     hbm_peak, hbm_src = peaks()
-    fp64_tf = fp64_peak(torch, _lib)
+    fp64_tf = fp64_peak(torch)
     dominant = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
     alg = algorithmic(dominant, stats)
     k_ms = kernels[dominant]["ms_per_launch"]
     achieved_gbs = alg["bytes"] / (k_ms * 1e-3) / 1e9
-    corr = "ssp_tangent_plastic_correction" + ("_mixed" if args.form == "mixed" else "")
-    tangent_err = None
-    if args.form == "mixed":  # tangent error of this form against the FP64 form, same state
-        op.tangent_form = "plain"
-        step()
-        kp = op.build_K_regularized(R_REG).values.clone()
-        op.tangent_form = "mixed"
-        step()
-        km = op.build_K_regularized(R_REG).values
-        tangent_err = {"max_norm_rel": float((km - kp).abs().max() / kp.abs().max()),
-                       "frobenius_rel": float(torch.linalg.norm(km - kp) / torch.linalg.norm(kp))}
-    fl = algorithmic(corr, stats)["flops"]
-    corr_ms = kernels.get(corr, {}).get("ms_per_launch")
+    rooflines = {}
+    for name, kv in kernels.items():
+        a = algorithmic(name, stats)
+        if a["bytes"]:
+            t_s = kv["ms_per_launch"] * 1e-3
+            rooflines[name] = {"achieved_gbs": a["bytes"] / t_s / 1e9, "frac_hbm": a["bytes"] / t_s / 1e9 / hbm_peak,
+                               "fp64_tflops": a["fp64"] / t_s / 1e12, "frac_fp64": a["fp64"] / t_s / 1e12 / fp64_tf}
     line = {
         "metric": METRIC, "value": world * n_int / (ms * 1e-3), "unit": "quad-pts/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "tangent_error_vs_fp64": tangent_err,
-        "config": {"workload": describe(args.config, mesh, n_int, nnz), "form": args.form,
-                   "return_mapping": args.return_mapping,
-                   "plastic_elements": stats["n_plastic_el"],
-                   "step": "reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + "
-                           "constrained diagonals + regularised blend",
-                   "plastic_fraction": stats["n_plastic"] / n_int,
-                   "l2": f"inputs larger than L2 (per-step HBM working set {stats['working_set'] / 1e9:.2f} GB > 129 MB)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.form == "plain" else "f64 (FP32 tangent products)",
+        "data": "synthetic",
+        "config": bench_config(w, n_int, nnz),
+        "gpu_form": {"form": args.form, "return_mapping": args.return_mapping,
+                     "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                     "plastic_points_per_state": [p["n_plastic"] for p in plastic],
+                     "plastic_elements_per_state": [p["n_plastic_el"] for p in plastic],
+                     "plastic_fraction": stats["n_plastic"] / n_int,
+                     "device_pattern_bytes": stats["device_bytes"], "setup_s": res.setup_s},
         "assembled_nnz_per_s": world * nnz / (ms * 1e-3),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak,
-                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else hbm_src,
-                     "traffic": NCU_TRAFFIC.get(args.config, {}).get(dominant), "ms_per_launch": k_ms,
-                     "algorithmic_bytes": alg["bytes"]},
-        "roofline_fp64": ({"bound": "fp64", "kernel": corr, "achieved": fl / (corr_ms * 1e-3) / 1e12, "peak": fp64_tf,
-                           "unit": "TFLOP/s", "frac": fl / (corr_ms * 1e-3) / 1e12 / fp64_tf,
-                           "peak_source": "measured live (ssp_probe_dfma, FP64 FMA)", "algorithmic_flops": fl,
-                           "ms_per_launch": corr_ms} if corr_ms else None),
+                     "frac": achieved_gbs / hbm_peak, "peak_source": hbm_src, "traffic": None,
+                     "traffic_note": "DRAM bytes of the kernels are measured by ncu, outside this run: see profiles/",
+                     "ms_per_launch": k_ms, "algorithmic_bytes": alg["bytes"],
+                     "units": f"{stats['n_plastic_el']:.0f} plastic elements per launch"
+                     if dominant.startswith("ssp_tangent_plastic_correction") else None},
+        "roofline_fp64": {"bound": "fp64", "kernel": dominant, "achieved": alg["fp64"] / (k_ms * 1e-3) / 1e12,
+                          "peak": fp64_tf, "unit": "TFLOP/s", "frac": alg["fp64"] / (k_ms * 1e-3) / 1e12 / fp64_tf,
+                          "peak_source": "measured live (bench-only FP64 FMA probe)",
+                          "executed_fp64_flops": alg["fp64"], "algorithmic_flops": alg["flops"]},
+        "kernel_rooflines": rooflines,
         "kernels": kernels,
         "host_enqueue_ms_per_step": host_ms,
         "gpu_launches": launches,
         "clocks": clock_info,
     }
     if learned_info is not None:
-        from slope_stability_petsc4py_gb300 import learned
-
-        br = op._branch
-        listed, bins = learned.proposal_bins(op._scratch, br.numel())
-        n_listed = max(1, listed.numel())
-        learned_info["listed_points"] = int(listed.numel())
-        learned_info["bench_state_accuracy_listed"] = float(
-            sum(int((br.index_select(0, bins[k]) == k).sum().item()) for k in range(5)) / n_listed)
-        learned_info["distinct_branches_per_warp_listed"] = {
-            "screen_order": learned.warp_branch_mix(br, listed),
-            "learned_bins": learned.warp_branch_mix(br, torch.cat(bins))}
         line["learned"] = learned_info
 
-    if args.form == "plain" and args.return_mapping == "binned" and pat.dim == 3 and not args.no_forms:
-        line["forms"] = compare_forms(torch, _lib, op, mesh, mats, args, step, ms)
+    rich = args.form == "plain" and args.return_mapping == "binned"
+    if rich and pat.dim == 3 and not args.no_forms:
+        line["forms"] = compare_forms(torch, _lib, op, w, states_dev, args, ms)
+        line["new_lambda_r"] = measure_new_lambda_r(torch, _lib, op, states_dev)
+    if rich and pat.dim == 3 and not args.no_ssr:
+        line["ssr_sequence"] = measure_ssr(torch, _lib, op, w)
     if args.bddc:
-        line["bddc"] = measure_bddc(torch, _lib, op, mesh, specs, args, step)
-    if args.form == "plain" and args.return_mapping == "binned" and not args.no_forms:
-        line["graph_replay"] = measure_graph_replay(torch, _lib, op, U_dev, args)
-
+        line["bddc"] = measure_bddc(torch, _lib, op, w, states_dev, args)
+    if rich and not args.no_forms:
+        line["graph_replay"] = measure_graph_replay(torch, _lib, op, states_dev, args)
     if rank == 0 and not args.no_e2e:
-        op.host_outputs = True
-        U_pin = torch.as_tensor(U).pin_memory()
-        for _ in range(3):
-            F_free, K = op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)
-            K.getValuesCSR()
-        torch.cuda.synchronize()
-        times = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            F_free, K = op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)
-            K.getValuesCSR()  # synchronises: the CSR values are on the host
-            times.append(time.perf_counter() - t0)
-        t_e2e = float(np.median(times))
-        # the host mirror of K is refreshed where the values can have changed since the previous
-        # build (rows of both builds' plastic elements); the rest already holds this r's values
-        line["e2e"] = {"value": n_int / t_e2e, "unit": "quad-pts/s", "h2d_bytes_per_step": int(U.nbytes),
-                       "d2h_bytes_per_step": int(F_free.nbytes + K.host_copy_bytes()), "ms_per_step": t_e2e * 1e3,
-                       "d2h_csr_bytes_full": 8 * nnz,
-                       "api": "ConstitutiveOperator.build_F_K_regularized_all_free(lam, U_host, r) + K.getValuesCSR()"}
-        if args.form == "plain" and pat.dim == 3 and not args.no_forms:
-            # the same end-to-end step in the mixed form
-            op.tangent_form = "mixed"
-            for _ in range(3):
-                op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)[1].getValuesCSR()
-            times = []
-            for _ in range(args.steps):
-                t0 = time.perf_counter()
-                F_free, K = op.build_F_K_regularized_all_free(LAMBDA, U_pin, R_REG)
-                K.getValuesCSR()
-                times.append(time.perf_counter() - t0)
-            op.tangent_form = "plain"
-            t_mx = float(np.median(times))
-            line["e2e"]["mixed"] = {"value": n_int / t_mx, "ms_per_step": t_mx * 1e3,
-                                    "d2h_bytes_per_step": int(F_free.nbytes + K.host_copy_bytes())}
-
+        line["e2e"] = measure_e2e(torch, op, states_host, args, args.form)
+        if rich and pat.dim == 3 and not args.no_forms:
+            line["e2e"]["mixed"] = measure_e2e(torch, op, states_host, args, "mixed")
+    if rank == 0 and not args.no_parity:
+        runner = oracle_runner(w)
+        line["parity"] = parity_check(torch, op, runner, states_host[1], states_dev[1])
+        del runner
     if rank == 0 and not args.no_cpu_baseline:
-        runner = OracleRunner(mesh, specs, U, dphi=(pat.dphi1, pat.dphi2, pat.dphi3), weight=pat.overlap_assembly_weight)
-        runner.elastic = pat.elastic_values
-        times = runner.time_steps(steps=5, warmup=1, budget_s=30.0)
-        t_cpu = float(np.median(times))
-        line["cpu_baseline"] = {"value": n_int / t_cpu, "unit": "quad-pts/s", "cores": runner.o.num_threads(),
-                                "kind": "port",
-                                "sample": f"full workload, {len(times)} passes after 1 warm-up, median; oracle C "
-                                          f"restatement of the reference kernels (rows tangent), OpenMP"}
+        _runner, line["cpu_baseline"] = cpu_reference_figures(w, states_host, steps=5, warmup=1, budget_s=30.0)
+    del op, res, states_dev
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_others and args.config == DEFAULT_CONFIG and args.form == "plain":
+        line["other_workloads"] = {}
+        for name in OTHER_WORKLOADS:
+            ow = workload(name)
+            line["other_workloads"][name] = measure_workload(torch, _lib, ow, args, headline=False)
+            torch.cuda.empty_cache()
     if dist is not None:
         dist.destroy_process_group()
     if rank == 0:
@@ -618,24 +827,38 @@ def run_gpu(args):
 
 
 def run_reference(args):
+    """The reference arm: the oracle's restatement of the reference's kernels on the host cores,
+    one rank's owned node block per step (all host threads), same workload and states."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh, mats, specs, U = workload(args.config)
-    runner = OracleRunner(mesh, specs, U)
-    times = runner.time_steps(args.steps, args.warmup, budget_s=150.0)
+    w = workload(args.config)
+    from oracle import oracle_py as o
+    from slope_stability_petsc4py_gb300 import fem
+
+    states = timed_states(w)
+    n_q = len(fem.quadrature(w.mesh.dim, w.mesh.elem_type)[1])
+    block, parts = sample_block(w.mesh, SAMPLE_POINTS, n_q)
+    runner = oracle_runner(w, block)
+    times = runner.time_steps(states, args.steps, args.warmup, LAMBDA, R_REG)
     t = float(np.median(times))
     value = runner.n_int / t
+    n_int = w.mesh.n_elem * n_q
+    nnz_full = int(o.owned_pattern_c(w.mesh.elem, w.mesh.q_mask, (0, w.mesh.n_nodes))["indices"].size) \
+        if parts > 1 else runner.nnz
+    sample = (f"owned node block {list(block)} of {w.mesh.n_nodes:,} nodes per step (rank 0 of a {parts}-way "
+              f"partition: {runner.n_int:,} points of its overlap elements, {runner.nnz:,} nnz), median of "
+              f"{len(times)} steps after {args.warmup} warm-up; the reference's C kernels restated (oracle), "
+              f"OpenMP on {o.num_threads()} threads; pattern, geometry and elastic values built once outside the steps")
     line = {"metric": METRIC, "value": value, "unit": "quad-pts/s", "n_gpus": world, "steps": len(times),
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": describe(args.config, mesh, runner.n_int, runner.nnz), "form": "plain",
-                       "parallelism": "host cores (OpenMP)"},
-            "cpu_baseline": {"value": value, "unit": "quad-pts/s", "cores": runner.o.num_threads(), "kind": "port",
-                             "sample": f"full workload per step, median of {len(times)}; the reference's C kernels "
-                                       f"restated (oracle), constrained diagonals without the elastic blend"},
-            "e2e": {"value": value, "unit": "quad-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": bench_config(w, n_int, nnz_full),
+            "cpu_baseline": {"value": value, "unit": "quad-pts/s", "cores": o.num_threads(), "kind": "port",
+                             "cpu_model": cpu_model(), "sample": sample},
+            "e2e": {"value": value, "unit": "quad-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": {"pattern": runner.pattern_s, "geometry": runner.geometry_s, "elastic_values": runner.elastic_s}}
     print(json.dumps(line))
 
 

@@ -113,7 +113,10 @@ int ssp_constitutive_3d_sds_binned_mixed(const double *E, const double *c_bar, c
  * call.
  *   - n_int above SSP_NOALLOC_MAX_POINTS returns SSP_ERR_TOO_LARGE before any work.
  *   - The first call on each device looks up the array's device address (cudaGetSymbolAddress,
- *     with that device current) and caches it; make that first call before any stream capture.
+ *     with that device current) and caches it for the life of the process; make that first call
+ *     before any stream capture.  A reset of the device's context (cudaDeviceReset, or a release
+ *     of its primary context) invalidates the cached address: do not call this entry point on a
+ *     device after resetting it.
  *   - Every call on a device shares the one array and leaves the last call's lists in it; the
  *     counters are cleared at the start of each call.  Calls that overlap on the GPU (different
  *     streams, or host threads sharing a device) race on the array: serialise them. */
@@ -304,6 +307,13 @@ int ssp_tangent_plastic_correction_mixed(int dim, const double *dphi1, const dou
  * stride byte offsets (0 is the kernel's).  No reference counterpart. */
 int ssp_tc_tf32_probe(const float *A, const float *B, int K, int convention, float *D, void *stream);
 
+/* Test support for the bounded waits of the tensor-core kernels (no reference counterpart): one
+ * CTA takes tensor memory, waits on an mbarrier that nothing arrives on for at most limit_clocks SM
+ * clocks (1 .. 2e9), then frees the tensor memory and returns.  On expiry it sets SSP_DEV_TIMEOUT
+ * in the device status word and writes 1 to *expired (a device int), else 0.  No tensor-core
+ * operation is issued, so nothing is left in flight. */
+int ssp_tc_wait_probe(long long limit_clocks, int *expired, void *stream);
+
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
                                void *stream);
 
@@ -355,11 +365,6 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
 /* Reads the device status word (SSP_DEV_* bits); clear != 0 resets it.  Synchronous. */
 int ssp_device_status(int *status_out, int clear);
 
-/* Measurement probe (no reference counterpart): blocks*threads threads each run `iters`
- * iterations of 8 independent FP64 FMAs (16*iters flops per thread) and write one double to
- * out[blocks*threads].  Timing it gives the device's FP64 FMA rate. */
-int ssp_probe_dfma(int iters, int blocks, int threads, double *out, void *stream);
-
 /* ------------------------------------------------------------------ learned branch proposal */
 
 /* No counterpart in the reference (it has no learned component).  A 6 -> 32 -> 32 -> 5 ReLU MLP
@@ -404,6 +409,21 @@ int ssp_constitutive_3d_sds_learned_mixed(const float *params, const double *E, 
                                           const double *sin_phi, const double *shear, const double *lame, int n_int,
                                           double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
                                           void *stream);
+
+/* No counterpart in the reference: the trivial branch predictor beside the network.  The return
+ * mapping with the points the elastic screen lists binned by given branch codes proposal [n_int]
+ * (e.g. the previous Newton iteration's branch_out; codes outside 0..4 go to the elastic bin), then
+ * the exact decision and finish passes as in ssp_constitutive_3d_sds_learned.  Same outputs, same
+ * scratch layout; proposal must not alias branch_out. */
+int ssp_constitutive_3d_sds_proposed(const int8_t *proposal, const double *E, const double *c_bar,
+                                     const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                     double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                     void *stream);
+/* The same in the mixed-precision form (DS as ssp_constitutive_3d_sds_binned_mixed). */
+int ssp_constitutive_3d_sds_proposed_mixed(const int8_t *proposal, const double *E, const double *c_bar,
+                                           const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                           double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                           void *stream);
 
 /* ------------------------------------------------------------------ pattern (host) */
 

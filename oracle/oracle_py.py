@@ -133,6 +133,37 @@ def owned_pattern_c(elem, q_mask, owned_node_range):
     return out
 
 
+def elastic_ds(dim, shear, bulk, lame):
+    """Per-point elastic D blocks (n, n_s*n_s), each column-major, of build_elastic_stiffness_matrix
+    (src/slope_stability/fem/assembly.py:281-302): K vol + 2G (I_half - vol/3) in 3D,
+    lame vol + 2G diag(1, 1, 1/2) in 2D."""
+    shear, bulk, lame = (np.asarray(a, dtype=np.float64).ravel() for a in (shear, bulk, lame))
+    if dim == 3:
+        iota = np.array([1.0, 1.0, 1.0, 0.0, 0.0, 0.0])
+        vol = np.outer(iota, iota)
+        ident = np.diag([1.0, 1.0, 1.0, 0.5, 0.5, 0.5]) - vol / 3.0
+        coeff = bulk
+    else:
+        iota = np.array([1.0, 1.0, 0.0])
+        vol = np.outer(iota, iota)
+        ident = np.diag([1.0, 1.0, 0.5])
+        coeff = lame
+    return np.ascontiguousarray(coeff[:, None] * vol.reshape(-1, order="F")[None, :]
+                                + 2.0 * shear[:, None] * ident.reshape(-1, order="F")[None, :])
+
+
+def scatter_from_slots(p, n_ld):
+    """The element -> CSR scatter map (distributed_tangent.py:328-366) from row-slot metadata: row
+    slot (element e, local dof a) holds exactly scatter[e, a*n_ld : (a+1)*n_ld] (the reference's own
+    test pins slot_pos to the scatter map, tests/test_distributed_tangent_rows.py:135-153)."""
+    n_ov = p["overlap_elements"].size
+    scatter = np.full((n_ov, n_ld * n_ld), -1, dtype=np.int32)
+    rows = p["slot_elem"].astype(np.int64)
+    cols = p["slot_lrow"].astype(np.int64)[:, None] * n_ld + np.arange(n_ld)[None, :]
+    scatter[rows[:, None], cols] = p["slot_pos"]
+    return scatter
+
+
 def geometry_3d_c(coord, elem, dhat, wf):
     """3D ``geometry`` through the C restatement: dphi1..3 (n_int, n_p) and weights (n_int,).
     ``elem`` is (n_p, n_el) node ids, ``dhat`` (3, n_p, n_q)."""

@@ -40,6 +40,7 @@ _SIGS = {
     "ssp_mark_element_rows": [_vp, _c_int, _c_int, _vp, _vp, _c_int, _vp, _vp],
     "ssp_copy_rows_out": [_vp, _vp, _vp, _c_int, _c_ll, _vp, _vp],
     "ssp_tc_tf32_probe": [_vp, _vp, _c_int, _c_int, _vp, _vp],
+    "ssp_tc_wait_probe": [_c_ll, _vp, _vp],
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_binned_mixed": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _vp],
@@ -69,7 +70,6 @@ _SIGS = {
     "ssp_finish_values": [_vp, _c_ll, _vp, _c_int, _vp, _c_dbl, _vp],
     "ssp_gather": [_vp, _vp, _c_int, _vp, _vp],
     "ssp_device_status": [ctypes.POINTER(_c_int), _c_int],
-    "ssp_probe_dfma": [_c_int, _c_int, _c_int, _vp, _vp],
     "ssp_branch_features": [_vp] * 5 + [_c_int, _vp, _vp],
     "ssp_mlp_predict": [_vp, _vp, _c_int, _c_int, _vp, _vp],
     "ssp_mlp_loss_grad": [_vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
@@ -77,6 +77,8 @@ _SIGS = {
                      ctypes.c_float, _vp],
     "ssp_constitutive_3d_sds_learned": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_learned_mixed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_constitutive_3d_sds_proposed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_constitutive_3d_sds_proposed_mixed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_pattern_build": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _c_int, _c_int, ctypes.POINTER(_vp)],
     "ssp_pattern_sizes": [_vp, _vp],
     "ssp_pattern_copy": [_vp, ctypes.c_char_p, _vp],
@@ -126,7 +128,7 @@ _KERNELS_PER_CALL = {
     "ssp_constitutive_2d": 1, "ssp_reduction": 1, "ssp_geometry": 1, "ssp_assemble_overlap_strain_3d": 1,
     "ssp_assemble_overlap_strain_2d": 1, "ssp_assemble_force_3d_rows": 1, "ssp_assemble_force_element": 1,
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
-    "ssp_gather": 1, "ssp_probe_dfma": 1, "ssp_tc_tf32_probe": 1, "ssp_constitutive_sds_branch": 1,
+    "ssp_gather": 1, "ssp_tc_tf32_probe": 1, "ssp_tc_wait_probe": 1, "ssp_constitutive_sds_branch": 1,
     "ssp_copy_out": 1, "ssp_copy_device": 1, "ssp_copy_rows_device": 1, "ssp_host_writable": 0, "ssp_plastic_elements": 1, "ssp_mark_element_rows": 1,
     "ssp_copy_rows_out": 1,
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
@@ -139,6 +141,7 @@ _KERNELS_PER_CALL = {
     "ssp_constitutive_3d_sds_binned_mixed": 3, "ssp_constitutive_3d_sds_learned_mixed": 4,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
     "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 4,
+    "ssp_constitutive_3d_sds_proposed": 4, "ssp_constitutive_3d_sds_proposed_mixed": 4,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
     "ssp_potential_energy": lambda a: int(a[8] > 0) + int(a[12] is not None),

@@ -20,6 +20,9 @@ REPO = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libssp_gb300.so"
+# the benchmark's FP64 rate probe, kept out of the product library
+PROBE_SRC = CSRC / "bench" / "fp64_probe.cu"
+PROBE_LIB = BUILD / "libssp_fp64_probe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               f"-I{REPO / 'include'}"]
@@ -40,7 +43,7 @@ def _sources() -> tuple[list[Path], list[Path]]:
 def _fingerprint() -> str:
     h = hashlib.sha256()
     cu, cpp = _sources()
-    for p in [*cu, *cpp, *sorted(CSRC.glob("*.cuh")), REPO / "include" / "ssp_gb300.h", Path(__file__)]:
+    for p in [*cu, *cpp, *sorted(CSRC.glob("*.cuh")), PROBE_SRC, REPO / "include" / "ssp_gb300.h", Path(__file__)]:
         h.update(p.name.encode())
         h.update(p.read_bytes())
     h.update(" ".join(ARCH + NVCC_FLAGS).encode())
@@ -51,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     stamp = BUILD / "fingerprint"
     fp = _fingerprint()
-    if LIB.exists() and not force and stamp.exists() and stamp.read_text() == fp:
+    if LIB.exists() and PROBE_LIB.exists() and not force and stamp.exists() and stamp.read_text() == fp:
         return LIB
     nvcc = _nvcc()
     cu, cpp = _sources()
@@ -71,8 +74,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             raise RuntimeError(f"compile failed: {cmd[-3]}")
         return cmd[-1]
 
-    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+    probe_tmp = BUILD / (PROBE_LIB.name + ".tmp")
+    probe_job = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-shared", str(PROBE_SRC),
+                 "-o", str(probe_tmp)]
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs) + 1, os.cpu_count() or 4))) as ex:
+        probe_done = ex.submit(run, probe_job)
         objs = list(ex.map(run, jobs))
+        probe_done.result()
+    probe_tmp.replace(PROBE_LIB)
     tmp = BUILD / (LIB.name + ".tmp")
     link = [nvcc, *ARCH, "-shared", "-rdc=true", "-Xcompiler", "-fPIC", *objs, "-o", str(tmp), "-lcudart"]
     run(link)

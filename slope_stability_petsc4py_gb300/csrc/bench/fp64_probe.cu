@@ -1,6 +1,7 @@
-// Measurement probe: a stream of independent FP64 fused multiply-adds, used to measure the
-// FP64 issue rate of the device the hot path runs on (the denominator of the FP64 roofline).
-#include "ssp_internal.cuh"
+// Measurement probe (not part of the product library): a stream of independent FP64 fused
+// multiply-adds, used by the benchmark to measure the FP64 issue rate of the device the hot path
+// runs on (the denominator of its FP64 roofline).  Built into _build/libssp_fp64_probe.so.
+#include "../ssp_internal.cuh"
 
 namespace ssp {
 namespace {

@@ -463,6 +463,69 @@ int launch_mlp_tc(const float *params, const float *X, const double *E, const do
     return launch_status();
 }
 
+// The trivial predictor beside the network: each point listed by pass A goes to the bin of a given
+// branch code (the previous Newton iteration's, for instance); codes outside 0..4 go to bin 0.
+// Same list layout as the network's proposal (five lists of stride n after the 8 counters).
+__global__ void __launch_bounds__(256) propose_given_kernel(const int8_t *__restrict__ proposal, int n,
+                                                            int32_t *__restrict__ scratch) {
+    const int cnt = scratch[0];
+    const int32_t *listed = scratch + 4;
+    int32_t *counts = scratch + 4 + 3ll * n, *lists = scratch + 12 + 3ll * n;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    const int iters = (cnt + stride - 1) / stride;
+    for (int it = 0; it < iters; ++it) {  // whole warps iterate together (the appends are warp-collective)
+        const int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        int p = -1, b = -1;
+        if (i < cnt) {
+            p = listed[i];
+            if (p < 0 || p >= n) {
+                flag(SSP_DEV_BAD_INDEX);
+                p = -1;
+            } else {
+                b = proposal[p];
+                if (b < 0 || b >= kOut) b = 0;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) {
+            const unsigned mask = __ballot_sync(0xffffffffu, b == k);
+            if (mask == 0u) continue;
+            const int leader = __ffs(mask) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(counts + k, __popc(mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (b == k) lists[(long long)k * n + base + __popc(mask & ((1u << lane) - 1u))] = p;
+        }
+    }
+}
+
+// Pass A, the given codes' bins for its listed points, then passes B (over the five bins) and C.
+int proposed_return_mapping(const int8_t *proposal, const double *E, const double *c_bar, const double *sin_phi,
+                            const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
+                            int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st) {
+    if (n_int < 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!proposal || !E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+        return SSP_ERR_INVALID;
+    if (proposal == branch_out) return SSP_ERR_INVALID;  // pass A overwrites the codes it reads
+    int32_t *counts = scratch + 4 + 3ll * n_int, *lists = scratch + 12 + 3ll * n_int;
+    if (cudaMemsetAsync(counts, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
+    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+    if (rc != SSP_OK) return rc;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (long long)sms * 8;
+    const long long need = (n_int + 255) / 256;
+    if (grid > need) grid = need;
+    propose_given_kernel<<<static_cast<unsigned>(grid), 256, 0, st>>>(proposal, n_int, scratch);
+    rc = launch_status();
+    if (rc != SSP_OK) return rc;
+    return binned_decide_finish(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, lists,
+                                counts, kOut, n_int, compensated_ds, st);
+}
+
 // Pass A of the binned return mapping, the proposal for its listed points, then passes B (over
 // the five proposal bins) and C.
 int learned_return_mapping(const float *params, const double *E, const double *c_bar, const double *sin_phi,
@@ -541,6 +604,22 @@ int ssp_constitutive_3d_sds_learned(const float *params, const double *E, const 
                                     void *stream) {
     return learned_return_mapping(params, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
                                   false, as_stream(stream));
+}
+
+int ssp_constitutive_3d_sds_proposed(const int8_t *proposal, const double *E, const double *c_bar,
+                                     const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                     double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                     void *stream) {
+    return proposed_return_mapping(proposal, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out,
+                                   scratch, false, as_stream(stream));
+}
+
+int ssp_constitutive_3d_sds_proposed_mixed(const int8_t *proposal, const double *E, const double *c_bar,
+                                           const double *sin_phi, const double *shear, const double *lame, int n_int,
+                                           double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
+                                           void *stream) {
+    return proposed_return_mapping(proposal, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out,
+                                   scratch, true, as_stream(stream));
 }
 
 int ssp_constitutive_3d_sds_learned_mixed(const float *params, const double *E, const double *c_bar,

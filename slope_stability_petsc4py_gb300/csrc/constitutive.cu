@@ -1109,7 +1109,8 @@ int32_t *g_fixed_ptr[kMaxDevices] = {};
 
 // Device address of g_fixed_scratch on the current device.  In host code the symbol's name is a
 // host-side stand-in, not a device address, so it is looked up once per device (with that device
-// current) and cached; nullptr on failure.
+// current) and cached; nullptr on failure.  The cache assumes the device's context lives as long as
+// the process: after a device reset the address would be stale (documented in the header).
 int32_t *fixed_scratch_for_current_device() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;

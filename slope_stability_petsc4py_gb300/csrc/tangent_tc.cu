@@ -437,6 +437,36 @@ __global__ void __launch_bounds__(128, 1) tc_probe_kernel(const float *__restric
     }
 }
 
+// The expiry path of the bounded waits, exercised without a tensor-core operation: warp 0 takes
+// tensor memory as the kernels do, thread 0 waits on an mbarrier nothing ever arrives on, with a
+// limit of `limit` clocks; on expiry it sets SSP_DEV_TIMEOUT, and the CTA frees the tensor memory
+// and returns, as the kernels do when a wait expires.
+__global__ void __launch_bounds__(128) tc_wait_probe_kernel(long long limit, int *expired) {
+    __shared__ uint32_t slot;
+    __shared__ __align__(8) uint64_t mbar;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(&slot, 32);
+    if (tid == 0) {
+        mbar_init(smem_u32(&mbar));
+        mbar_init_fence();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = slot;
+    if (tid == 0) {
+        const bool done = mbar_wait(smem_u32(&mbar), 0, limit);
+        *expired = done ? 0 : 1;
+        if (!done) flag(SSP_DEV_TIMEOUT);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after_sync();
+        tmem_dealloc(tmem, 32);
+    }
+}
+
 }  // namespace
 
 int correction_tc_p4(const double *d1, const double *d2, const double *d3, const double *DS, const double *w,
@@ -461,6 +491,12 @@ int correction_tc_p4(const double *d1, const double *d2, const double *d3, const
 }  // namespace ssp
 
 using namespace ssp;
+
+extern "C" int ssp_tc_wait_probe(long long limit_clocks, int *expired, void *stream) {
+    if (limit_clocks <= 0 || limit_clocks > kWaitLimitClocks || !expired) return SSP_ERR_INVALID;
+    tc_wait_probe_kernel<<<1, 128, 0, as_stream(stream)>>>(limit_clocks, expired);
+    return launch_status();
+}
 
 extern "C" int ssp_tc_tf32_probe(const float *A, const float *B, int K, int convention, float *D, void *stream) {
     if ((K != 8 && K != 16 && K != 24) || (convention != 0 && convention != 1) || !A || !B || !D)

@@ -90,11 +90,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the completion of the phase with the given parity (about 1 s of SM clocks).
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+// Bounded wait for the completion of the phase with the given parity: false after limit SM clocks
+// (default about 1 s) without it.
+constexpr long long kWaitLimitClocks = 2000000000ll;
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, long long limit = kWaitLimitClocks) {
     const long long t0 = clock64();
     while (!mbar_try_wait(addr, parity)) {
-        if (clock64() - t0 > 2000000000ll) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
 }

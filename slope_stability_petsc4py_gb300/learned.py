@@ -73,13 +73,16 @@ def screen_listed(E, c_bar, sin_phi, shear, lame):
     return scratch[4: 4 + int(scratch[0])].long(), br
 
 
-def collect_training_data(op, states, listed_only: bool = True):
+def collect_training_data(op, states, listed_only: bool = True, max_per_state: int | None = None, seed: int = 0):
     """(features, labels) from the exact return mapping over continuation states [(lam, U), ...].
     With listed_only, only the points the elastic screen lists: the ones the learned return
-    mapping asks the network about."""
+    mapping asks the network about.  max_per_state: a seeded uniform sample of at most that many
+    of a state's points (large meshes list millions per state)."""
     t = _lib.require_cuda()
     pat = op.owned_tangent_pattern
     Xs, ys = [], []
+    gen = t.Generator(device="cuda")
+    gen.manual_seed(seed)
     for lam, U in states:
         op.reduction(lam)
         E = overlap_strain_device(pat, U)
@@ -87,12 +90,13 @@ def collect_training_data(op, states, listed_only: bool = True):
         args = (E, op._owned_overlap_c_bar, op._owned_overlap_sin_phi, d["shear"], d["lame"])
         X = features(*args)
         if listed_only:
-            listed, br = screen_listed(*args)
-            Xs.append(X.index_select(0, listed))
-            ys.append(br.index_select(0, listed))
+            pick, br = screen_listed(*args)
         else:
-            Xs.append(X)
-            ys.append(exact_branches(*args))
+            pick, br = t.arange(X.shape[0], device="cuda"), exact_branches(*args)
+        if max_per_state is not None and pick.numel() > max_per_state:
+            pick = pick.index_select(0, t.randperm(pick.numel(), device="cuda", generator=gen)[:max_per_state])
+        Xs.append(X.index_select(0, pick))
+        ys.append(br.index_select(0, pick))
     return t.cat(Xs), t.cat(ys)
 
 

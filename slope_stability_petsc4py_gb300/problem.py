@@ -228,6 +228,7 @@ class ConstitutiveOperator:
         self._DS_aos = None
         self._ds_symmetric = False
         self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
+        self._prev_branch = None  # branch codes of the last evaluation that produced them ("previous")
         self._K_el = None  # elastic tangent CSR values (device), built on first use
         self._blend_base = None  # (r, (1-r) K_el,t + r K_el) for the last regularisation factor
         self._dev = None
@@ -248,7 +249,9 @@ class ConstitutiveOperator:
         self._build_no = 0
         # How 3D tangents are evaluated (all give the same results): "binned" -- two passes with
         # exact branch binning; "unsorted" -- one pass in point order; "learned" -- points binned
-        # by the branch_model's proposal, then the exact return mapping bin by bin.
+        # by the branch_model's proposal, then the exact return mapping bin by bin; "previous" --
+        # points binned by the previous evaluation's branch codes (the trivial predictor; the first
+        # evaluation of a pattern runs "binned").
         self.return_mapping = "binned"
         self.branch_model = None
         self._scratch = None
@@ -312,6 +315,7 @@ class ConstitutiveOperator:
         self._last_build = {}
         self._red_key = None
         self._clear_owned_local_cache()
+        self._prev_branch = None
         if pattern is not None:
             t = _lib.require_cuda()
             idx = np.asarray(pattern.local_int_indices, dtype=np.int64)
@@ -447,9 +451,12 @@ class ConstitutiveOperator:
             _lib.call("ssp_constitutive_2d_sds_binned", _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
                       _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
                       _lib.ptr(DS), _lib.ptr(branch), _lib.ptr(self._scratch), st)
-        elif tangent and mode in ("binned", "learned"):
+        elif tangent and mode in ("binned", "learned", "previous"):
+            prev = self._prev_branch if mode == "previous" else None
+            if mode == "previous" and (prev is None or prev.numel() != n):
+                mode = "binned"
             branch = t.empty(n, dtype=t.int8, device="cuda")
-            need = (8 if mode == "learned" else 3) * n + 12
+            need = (3 if mode == "binned" else 8) * n + 12
             if self._scratch is None or self._scratch.numel() < need:
                 self._scratch = t.empty(need, dtype=t.int32, device="cuda")
             mat = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
@@ -461,6 +468,8 @@ class ConstitutiveOperator:
                 if self.branch_model is None:
                     raise ValueError("return_mapping='learned' needs a trained branch_model")
                 _lib.call("ssp_constitutive_3d_sds_learned" + sfx, _lib.ptr(self.branch_model.params), *mat)
+            elif mode == "previous":
+                _lib.call("ssp_constitutive_3d_sds_proposed" + sfx, _lib.ptr(prev), *mat)
             else:
                 _lib.call("ssp_constitutive_3d_sds_binned" + sfx, *mat)
         elif tangent:
@@ -476,6 +485,8 @@ class ConstitutiveOperator:
         self._S_aos = S
         self._DS_aos = DS
         self._branch = branch
+        if branch is not None:
+            self._prev_branch = branch
         self._ds_symmetric = bool(tangent)
         self.S = None
         self.DS = None

@@ -341,6 +341,15 @@ def displacement_field(mesh: SlopeMesh, materials: MaterialSet, amplitude: float
     return u
 
 
+def displacement_basis(mesh: SlopeMesh, materials: MaterialSet, *, seed: int = 0, **kw) -> tuple[np.ndarray, np.ndarray]:
+    """(G, V) with displacement_field(mesh, materials, a, seed=seed) = G + a V: the field is affine in
+    the shear-band amplitude (its noise is scaled by the amplitude too), so a continuation's states
+    g G + a V (load factor g, band amplitude a) cost one axpy each."""
+    G = displacement_field(mesh, materials, 0.0, seed=seed, **kw)
+    V = displacement_field(mesh, materials, 1.0, seed=seed, **kw) - G
+    return G, V
+
+
 def point_materials(mesh: SlopeMesh, materials: MaterialSet, n_q: int) -> dict[str, np.ndarray]:
     """Per-integration-point material arrays (``src/slope_stability/mesh/materials.py:33-101``)."""
     mid = np.repeat(mesh.material_id, n_q)
@@ -398,3 +407,19 @@ def build_config_mesh(name: str) -> SlopeMesh:
     if cfg.pop("dim") == 2:
         return slope_mesh_2d(cfg["nx"], cfg["ny"], elem_type=cfg["elem_type"], n_layers=cfg["n_layers"])
     return slope_mesh_3d(cfg["nx"], cfg["ny"], cfg["nz"], elem_type=cfg["elem_type"], n_layers=cfg["n_layers"])
+
+
+def config_workload(name: str):
+    """A named configuration as a workload: mesh, material set, the reference's material specs and
+    the displacement basis (G, V) (displacement_basis, seed 3) with the configuration's shear-band
+    amplitude, so its states are g G + a V."""
+    from types import SimpleNamespace
+
+    cfg = CONFIGS[name]
+    mesh = build_config_mesh(name)
+    mats = MaterialSet.layered(4, seed=0) if cfg["n_layers"] > 1 else MaterialSet.homogeneous()
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=float(mats.psi[i]), young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=float(mats.gamma[i]), gamma_unsat=float(mats.gamma[i]))
+             for i in range(mats.c0.size)]
+    G, V = displacement_basis(mesh, mats, seed=3)
+    return SimpleNamespace(name=name, mesh=mesh, mats=mats, specs=specs, G=G, V=V, amp=float(cfg["amplitude"]))

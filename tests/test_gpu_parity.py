@@ -263,6 +263,40 @@ def test_pattern_geometry_and_elastic_values(name):
     assert np.all(pat.elastic_values[pat.constrained_diag_positions] == 1.0)
 
 
+@pytest.mark.parametrize("name", golden_files("overlap_operator_"))
+def test_overlap_operator_and_reference_elastic_rows(name):
+    """include_overlap_B=True gives the reference's sparse strain operator; a reference
+    OwnedElasticRows passed as elastic_rows gives its projected elastic values; overlap_B applied to
+    the overlap displacements equals the strain kernel."""
+    from types import SimpleNamespace
+
+    from scipy.sparse import csr_matrix
+
+    from slope_stability_petsc4py_gb300 import assemble_overlap_strain, prepare_owned_tangent_pattern
+
+    g = golden(name)
+    dim = g["q_mask"].shape[0]
+    mat = {"c0": 6.0, "phi": 45.0, "psi": 0.0, "young": 2.0e4, "poisson": 0.49, "gamma_sat": 20.0, "gamma_unsat": 20.0}
+    owned = tuple(int(v) for v in g["owned_node_range"])
+    L = csr_matrix((g["L_data"], g["L_indices"], g["L_indptr"]), shape=tuple(g["L_shape"]))
+    rows = SimpleNamespace(owned_node_range=owned, owned_row_range=(dim * owned[0], dim * owned[1]), local_matrix=L)
+    pat = prepare_owned_tangent_pattern(g["coord"], g["elem"], g["q_mask"], np.zeros(g["elem"].shape[1], np.int64),
+                                        [mat], owned, elem_type="P2", include_overlap_B=True, elastic_rows=rows)
+    assert np.array_equal(pat.elastic_values, g["elastic_values"])
+    assert pat.timings["elastic_pattern_reused"] == 1.0
+    B = pat.overlap_B
+    ref = csr_matrix((g["B_data"], g["B_indices"], g["B_indptr"]), shape=tuple(g["B_shape"]))
+    assert np.array_equal(B.indptr, ref.indptr) and np.array_equal(B.indices, ref.indices)
+    assert rel_err(B.data, ref.data) <= PLAIN_RTOL
+    U = np.random.default_rng(3).standard_normal(g["q_mask"].shape)
+    E = assemble_overlap_strain(pat, U)
+    u_ov = U.reshape(-1, order="F")[pat.overlap_global_dofs]
+    assert rel_err(np.asarray(B @ u_ov).reshape(pat.n_strain, -1, order="F"), E) <= PLAIN_RTOL
+    with pytest.raises(ValueError):
+        prepare_owned_tangent_pattern(g["coord"], g["elem"], g["q_mask"], np.zeros(g["elem"].shape[1], np.int64),
+                                      [mat], (0, owned[1]), elem_type="P2", elastic_rows=rows)
+
+
 @pytest.mark.parametrize("name", golden_files("pattern_"))
 def test_assembly_matches_reference(name):
     from slope_stability_petsc4py_gb300 import (assemble_overlap_strain, assemble_owned_force_from_local_stress,
