@@ -628,7 +628,7 @@ def parity_check(torch, op, runner, U_host, U_dev):
         op.tangent_form = form
         F, K = op.build_F_K_regularized_all_free(LAMBDA, U_dev, R_REG)
         torch.cuda.synchronize()
-        out[form] = {"S": rel(op._S_aos, S_o), "DS": rel(op._DS_aos, DS_o), "F_free": rel(F, F_o),
+        out[form] = {"S": rel(op._S_aos, S_o), "DS": rel(op._owned_local_DS.aos, DS_o), "F_free": rel(F, F_o),
                      "K": rel(K.values, K_o)}
     op.tangent_form = "plain"
     out["tolerance"] = {"plain": "1e-12 max-norm relative (S, DS, F_free, K)",

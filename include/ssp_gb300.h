@@ -314,6 +314,12 @@ int ssp_tc_tf32_probe(const float *A, const float *B, int K, int convention, flo
  * operation is issued, so nothing is left in flight. */
 int ssp_tc_wait_probe(long long limit_clocks, int *expired, void *stream);
 
+/* DS rows [n_int][n_s*n_s] of the points whose branch code is 0 (elastic) set to the elastic matrix
+ * the return mapping emits for them (bit for bit); other rows untouched.  Completes the DS of a
+ * return mapping run with SSP_RM_PLASTIC_DS_ONLY.  No reference counterpart. */
+int ssp_fill_elastic_ds(int dim, const int8_t *branch, const double *shear, const double *lame, int n_int,
+                        double *ds_inout, void *stream);
+
 int ssp_elastic_tangent_blocks(int dim, const double *shear, const double *lame, int n_int, double *ds_out,
                                void *stream);
 
@@ -424,6 +430,27 @@ int ssp_constitutive_3d_sds_proposed_mixed(const int8_t *proposal, const double 
                                            const double *sin_phi, const double *shear, const double *lame, int n_int,
                                            double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
                                            void *stream);
+
+/* No counterpart in the reference: every screened form of the 3D return mapping behind one entry.
+ * Pass A (the FP32 elastic screen) finishes the points it proves elastic; the listed points are
+ * binned by `bins` -- SSP_BINS_EXACT: one list, exact FP64 decision then one branch per warp
+ * (ssp_constitutive_3d_sds_binned; scratch 3*n_int + 4 int32); SSP_BINS_LEARNED: the MLP's
+ * proposal, bin_source = the FP32 parameter vector (ssp_constitutive_3d_sds_learned); SSP_BINS_GIVEN:
+ * given branch codes, bin_source = int8 [n_int] not aliasing branch_out
+ * (ssp_constitutive_3d_sds_proposed); the last two need scratch of 8*n_int + 12 int32.
+ * options: SSP_RM_COMPENSATED_DS -- the plastic DS in double-float arithmetic (the mixed form);
+ * SSP_RM_PLASTIC_DS_ONLY -- the DS rows of points that return elastic are not written (they equal
+ * the elastic matrix; the tangent's plastic corrections never read them; ssp_fill_elastic_ds
+ * writes them when a caller needs every row).  S and branch_out are always complete. */
+#define SSP_BINS_EXACT 0
+#define SSP_BINS_LEARNED 1
+#define SSP_BINS_GIVEN 2
+#define SSP_RM_COMPENSATED_DS 1
+#define SSP_RM_PLASTIC_DS_ONLY 2
+int ssp_constitutive_3d_sds_screened(const double *E, const double *c_bar, const double *sin_phi,
+                                     const double *shear, const double *lame, int n_int, double *S_out,
+                                     double *DS_out, int8_t *branch_out, int32_t *scratch, int bins,
+                                     const void *bin_source, int options, void *stream);
 
 /* ------------------------------------------------------------------ pattern (host) */
 

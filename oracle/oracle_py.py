@@ -55,6 +55,14 @@ def lib():
     return _LIB
 
 
+def nofma_lib():
+    """The C restatement compiled without fused multiply-adds (-ffp-contract=off)."""
+    path = HERE / "_build" / "liboracle_nofma.so"
+    if not path.exists():
+        build()
+    return ctypes.CDLL(str(path))
+
+
 def ref_lib():
     """The reference's own C kernels compiled from its sources (only where it is mounted)."""
     if not REF_LIB_PATH.exists():
@@ -194,7 +202,7 @@ def constitutive_3d(E, c_bar, sin_phi, shear, bulk, lame, *, tangent=True, libra
     S = np.empty((n, 6))
     DS = np.empty((n, 36)) if tangent else None
     L = library or lib()
-    if library is None:
+    if hasattr(L, "orc_constitutive_3d"):  # this restatement (or its no-FMA build)
         L.orc_constitutive_3d(_d(E), *[_d(a) for a in args], ctypes.c_int(n), _d(S),
                               _d(DS) if tangent else None)
     elif tangent:
@@ -204,14 +212,14 @@ def constitutive_3d(E, c_bar, sin_phi, shear, bulk, lame, *, tangent=True, libra
     return (S, DS) if tangent else S
 
 
-def strain_3d(dphi1, dphi2, dphi3, u_overlap, dof_lids, n_q):
+def strain_3d(dphi1, dphi2, dphi3, u_overlap, dof_lids, n_q, library=None):
     d1, d2, d3 = (_c(a, np.float64) for a in (dphi1, dphi2, dphi3))
     dof = _c(dof_lids, np.int32)
     u = _c(u_overlap, np.float64)
     n_elem, nld = dof.shape
     n_p = nld // 3
     E = np.empty((n_elem * n_q, 6))
-    lib().orc_strain_3d(_d(d1), _d(d2), _d(d3), _d(u), _i(dof), n_elem, n_p, n_q, _d(E))
+    (library or lib()).orc_strain_3d(_d(d1), _d(d2), _d(d3), _d(u), _i(dof), n_elem, n_p, n_q, _d(E))
     return E
 
 

@@ -20,6 +20,10 @@ _LIB = None
 POTENTIAL_PARTIALS = 1024
 _c_int, _c_ll, _c_dbl, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
 
+# ssp_constitutive_3d_sds_screened: binning sources and option bits (include/ssp_gb300.h)
+BINS_EXACT, BINS_LEARNED, BINS_GIVEN = 0, 1, 2
+RM_COMPENSATED_DS, RM_PLASTIC_DS_ONLY = 1, 2
+
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported element", 4: "int32 overflow",
           5: "pattern is missing a structural entry", 6: "more points than the fixed scratch holds"}
 
@@ -78,6 +82,8 @@ _SIGS = {
     "ssp_constitutive_3d_sds_learned": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_learned_mixed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_constitutive_3d_sds_proposed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
+    "ssp_constitutive_3d_sds_screened": [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _c_int, _vp],
+    "ssp_fill_elastic_ds": [_c_int, _vp, _vp, _vp, _c_int, _vp, _vp],
     "ssp_constitutive_3d_sds_proposed_mixed": [_vp] * 6 + [_c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_pattern_build": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _c_int, _c_int, ctypes.POINTER(_vp)],
     "ssp_pattern_sizes": [_vp, _vp],
@@ -142,6 +148,7 @@ _KERNELS_PER_CALL = {
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,
     "ssp_mlp_loss_grad": 1, "ssp_mlp_adam": 1, "ssp_constitutive_3d_sds_learned": 4,
     "ssp_constitutive_3d_sds_proposed": 4, "ssp_constitutive_3d_sds_proposed_mixed": 4,
+    "ssp_constitutive_3d_sds_screened": lambda a: 3 if a[10] == 0 else 4, "ssp_fill_elastic_ds": 1,
     "ssp_elastic_tangent_blocks": 1, "ssp_blend_values": 1,
     "ssp_finish_values": lambda a: int(bool(a[3])) + int(a[4] is not None),
     "ssp_potential_energy": lambda a: int(a[8] > 0) + int(a[12] is not None),

@@ -924,6 +924,19 @@ __global__ void elastic_blocks_kernel(const double *__restrict__ shear, const do
     DS[t] = elastic_d<DIM>(kk % NS, kk / NS, shear[g], lame[g]);
 }
 
+// The elastic rows of a DS whose return mapping left them unwritten: rows of points with branch 0.
+template <int DIM>
+__global__ void fill_elastic_ds_kernel(const int8_t *__restrict__ branch, const double *__restrict__ shear,
+                                       const double *__restrict__ lame, int n, double *__restrict__ DS) {
+    constexpr int NS = DIM == 3 ? 6 : 3;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * NS * NS) return;
+    const long long g = t / (NS * NS);
+    if (branch[g] != 0) return;
+    const int kk = static_cast<int>(t % (NS * NS));
+    DS[t] = elastic_d<DIM>(kk % NS, kk / NS, shear[g], lame[g]);
+}
+
 // ---------------------------------------------------------------------------- epilogue
 
 __global__ void set_positions_kernel(double *__restrict__ values, const int32_t *__restrict__ pos, int n, long long nnz,
@@ -1254,6 +1267,19 @@ int ssp_plastic_elements(const int8_t *branch, int n_elem, int n_q, int32_t *lis
     if (n_elem == 0) return SSP_OK;
     if (!branch || !list_out) return SSP_ERR_INVALID;
     plastic_elements_kernel<<<grid_for(n_elem, 256), 256, 0, st>>>(branch, n_elem, n_q, list_out, count_out);
+    return launch_status();
+}
+
+int ssp_fill_elastic_ds(int dim, const int8_t *branch, const double *shear, const double *lame, int n_int,
+                        double *ds_inout, void *stream) {
+    if (n_int < 0 || (dim != 2 && dim != 3)) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    if (!branch || !shear || !lame || !ds_inout) return SSP_ERR_INVALID;
+    const long long n = (long long)n_int * (dim == 3 ? 36 : 9);
+    if (dim == 3)
+        fill_elastic_ds_kernel<3><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(branch, shear, lame, n_int, ds_inout);
+    else
+        fill_elastic_ds_kernel<2><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(branch, shear, lame, n_int, ds_inout);
     return launch_status();
 }
 

@@ -503,7 +503,8 @@ __global__ void __launch_bounds__(256) propose_given_kernel(const int8_t *__rest
 // Pass A, the given codes' bins for its listed points, then passes B (over the five bins) and C.
 int proposed_return_mapping(const int8_t *proposal, const double *E, const double *c_bar, const double *sin_phi,
                             const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
-                            int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st) {
+                            int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st,
+                            bool write_elastic_ds = true) {
     if (n_int < 0) return SSP_ERR_INVALID;
     if (n_int == 0) return SSP_OK;
     if (!proposal || !E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
@@ -511,7 +512,8 @@ int proposed_return_mapping(const int8_t *proposal, const double *E, const doubl
     if (proposal == branch_out) return SSP_ERR_INVALID;  // pass A overwrites the codes it reads
     int32_t *counts = scratch + 4 + 3ll * n_int, *lists = scratch + 12 + 3ll * n_int;
     if (cudaMemsetAsync(counts, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st,
+                           write_elastic_ds);
     if (rc != SSP_OK) return rc;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -530,14 +532,16 @@ int proposed_return_mapping(const int8_t *proposal, const double *E, const doubl
 // the five proposal bins) and C.
 int learned_return_mapping(const float *params, const double *E, const double *c_bar, const double *sin_phi,
                            const double *shear, const double *lame, int n_int, double *S_out, double *DS_out,
-                           int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st) {
+                           int8_t *branch_out, int32_t *scratch, bool compensated_ds, cudaStream_t st,
+                           bool write_elastic_ds = true) {
     if (n_int < 0) return SSP_ERR_INVALID;
     if (n_int == 0) return SSP_OK;
     if (!params || !E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
         return SSP_ERR_INVALID;
     int32_t *counts = scratch + 4 + 3ll * n_int, *lists = scratch + 12 + 3ll * n_int;
     if (cudaMemsetAsync(counts, 0, 8 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+    int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st,
+                           write_elastic_ds);
     if (rc != SSP_OK) return rc;
     rc = launch_mlp_tc<true>(params, nullptr, E, c_bar, sin_phi, shear, lame, n_int, nullptr, scratch, st);
     if (rc != SSP_OK) return rc;
@@ -620,6 +624,36 @@ int ssp_constitutive_3d_sds_proposed_mixed(const int8_t *proposal, const double 
                                            void *stream) {
     return proposed_return_mapping(proposal, E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out,
                                    scratch, true, as_stream(stream));
+}
+
+int ssp_constitutive_3d_sds_screened(const double *E, const double *c_bar, const double *sin_phi,
+                                     const double *shear, const double *lame, int n_int, double *S_out,
+                                     double *DS_out, int8_t *branch_out, int32_t *scratch, int bins,
+                                     const void *bin_source, int options, void *stream) {
+    if (n_int < 0 || (options & ~(SSP_RM_COMPENSATED_DS | SSP_RM_PLASTIC_DS_ONLY)) != 0) return SSP_ERR_INVALID;
+    if (n_int == 0) return SSP_OK;
+    const bool comp = (options & SSP_RM_COMPENSATED_DS) != 0;
+    const bool write_el = (options & SSP_RM_PLASTIC_DS_ONLY) == 0;
+    cudaStream_t st = as_stream(stream);
+    switch (bins) {
+    case SSP_BINS_EXACT: {
+        if (!E || !c_bar || !sin_phi || !shear || !lame || !S_out || !DS_out || !branch_out || !scratch)
+            return SSP_ERR_INVALID;
+        const int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st,
+                                     write_el);
+        if (rc != SSP_OK) return rc;
+        return binned_decide_finish(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
+                                    scratch + 4, scratch, 1, 0, comp, st);
+    }
+    case SSP_BINS_LEARNED:
+        return learned_return_mapping(static_cast<const float *>(bin_source), E, c_bar, sin_phi, shear, lame, n_int,
+                                      S_out, DS_out, branch_out, scratch, comp, st, write_el);
+    case SSP_BINS_GIVEN:
+        return proposed_return_mapping(static_cast<const int8_t *>(bin_source), E, c_bar, sin_phi, shear, lame, n_int,
+                                       S_out, DS_out, branch_out, scratch, comp, st, write_el);
+    default:
+        return SSP_ERR_INVALID;
+    }
 }
 
 int ssp_constitutive_3d_sds_learned_mixed(const float *params, const double *E, const double *c_bar,

@@ -632,18 +632,21 @@ __device__ __forceinline__ int warp_append(bool want, int32_t *ctr) {
 // memory (row stride 37 doubles, so the per-lane row writes are at most 2-way bank conflicts) and
 // the warp writes the block with consecutive 8-byte stores (full cache lines) instead of 32
 // strided rows.  Rows of listed points are written with whatever the stage holds; passes B and C
-// overwrite them.
+// overwrite them.  WRITE_EL = false: the rows of the points the screen finishes are not written at
+// all (they hold the elastic matrix, which the tangent's plastic corrections never read; a
+// caller that needs them fills them from the branch codes, ssp_fill_elastic_ds).
 constexpr int kDsStride = 37;
+template <bool WRITE_EL>
 __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict__ E, const double *__restrict__ c_bar,
                                                        const double *__restrict__ sin_phi,
                                                        const double *__restrict__ shear, const double *__restrict__ lame,
                                                        int n, double *__restrict__ S, double *__restrict__ DS,
                                                        int8_t *__restrict__ branch, int32_t *__restrict__ scratch) {
-    __shared__ double stage[4][32 * kDsStride];
+    __shared__ double stage[WRITE_EL ? 4 : 1][WRITE_EL ? 32 * kDsStride : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int p0 = blockIdx.x * blockDim.x + warp * 32;
-    double *w = stage[warp];
+    double *w = stage[WRITE_EL ? warp : 0];
     bool listed = false;
     if (p < n) {
         double e[6];
@@ -652,22 +655,26 @@ __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict_
         if (screen_elastic(e, m)) {
             double t[6], I1, s[6], ds[36];
             elastic_trial(e, t, I1);
-            finish_elastic(t, I1, m, s, ds);
+            finish_elastic(t, I1, m, s, WRITE_EL ? ds : nullptr);
             store6(S, p, s);
+            if (WRITE_EL) {
 #pragma unroll
-            for (int k = 0; k < 36; ++k) w[lane * kDsStride + k] = ds[k];
+                for (int k = 0; k < 36; ++k) w[lane * kDsStride + k] = ds[k];
+            }
             branch[p] = static_cast<int8_t>(kElastic);
         } else {
             listed = true;
         }
     }
-    __syncwarp();
-    if (p0 < n) {
-        const int nw = n - p0 < 32 ? n - p0 : 32;
-        double *dst = DS + 36ll * p0;
-        for (int idx = lane; idx < nw * 36; idx += 32) {
-            const int pt = idx / 36;
-            dst[idx] = w[pt * kDsStride + (idx - pt * 36)];
+    if (WRITE_EL) {
+        __syncwarp();
+        if (p0 < n) {
+            const int nw = n - p0 < 32 ? n - p0 : 32;
+            double *dst = DS + 36ll * p0;
+            for (int idx = lane; idx < nw * 36; idx += 32) {
+                const int pt = idx / 36;
+                dst[idx] = w[pt * kDsStride + (idx - pt * 36)];
+            }
         }
     }
     const int slot = warp_append(listed, scratch);
@@ -756,13 +763,18 @@ __global__ void __launch_bounds__(128, 3) mc3d_finish_kernel(const double *__res
 
 }  // namespace
 
-// Pass A on one stream (counters zeroed first).  scratch: 4 + 3 n int32.
+// Pass A on one stream (counters zeroed first).  scratch: 4 + 3 n int32.  write_elastic_ds = false
+// leaves the DS rows of the points it finishes unwritten (mc3d_bin_kernel).
 int binned_screen(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
-                  cudaStream_t st) {
+                  cudaStream_t st, bool write_elastic_ds) {
     if (cudaMemsetAsync(scratch, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return SSP_ERR_CUDA;
-    mc3d_bin_kernel<<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out,
-                                                          branch_out, scratch);
+    if (write_elastic_ds)
+        mc3d_bin_kernel<true><<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                    DS_out, branch_out, scratch);
+    else
+        mc3d_bin_kernel<false><<<grid_for(n_int, 128), 128, 0, st>>>(E, c_bar, sin_phi, shear, lame, n_int, S_out,
+                                                                     DS_out, branch_out, scratch);
     return launch_status();
 }
 
@@ -791,8 +803,9 @@ namespace {
 
 int launch_binned(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
-                  bool compensated_ds, cudaStream_t st) {
-    const int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st);
+                  bool compensated_ds, cudaStream_t st, bool write_elastic_ds = true) {
+    const int rc = binned_screen(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch, st,
+                                 write_elastic_ds);
     if (rc != SSP_OK) return rc;
     return binned_decide_finish(E, c_bar, sin_phi, shear, lame, n_int, S_out, DS_out, branch_out, scratch,
                                 scratch + 4, scratch, 1, 0, compensated_ds, st);

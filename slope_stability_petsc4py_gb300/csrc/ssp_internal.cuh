@@ -55,10 +55,11 @@ __host__ __device__ __forceinline__ int bt_row2(int comp, int grad) {
 // The binned 3D return mapping (constitutive.cu).  scratch: counters at scratch[0..3] (listed,
 // smooth, left edge, right edge), the listed points from scratch + 4, the smooth list from
 // scratch + 4 + n_int, the edge lists from scratch + 4 + 2 n_int.
-// Pass A: zero the counters, screen every point, finish the screened ones, list the others.
+// Pass A: zero the counters, screen every point, finish the screened ones, list the others
+// (write_elastic_ds = false: the DS rows of the screened points are left unwritten).
 int binned_screen(const double *E, const double *c_bar, const double *sin_phi, const double *shear,
                   const double *lame, int n_int, double *S_out, double *DS_out, int8_t *branch_out, int32_t *scratch,
-                  cudaStream_t st);
+                  cudaStream_t st, bool write_elastic_ds = true);
 // Passes B and C: decide the points of n_lists lists (list k: counts[k] entries from
 // lists + k list_stride), finish elastic and apex points, record and list the others by branch,
 // finish those (compensated_ds: the plastic DS in double-float arithmetic).

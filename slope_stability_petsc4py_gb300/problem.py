@@ -229,6 +229,11 @@ class ConstitutiveOperator:
         self._ds_symmetric = False
         self._branch = None  # per-point return branch of the last tangent evaluation (int8, device)
         self._prev_branch = None  # branch codes of the last evaluation that produced them ("previous")
+        # The screened 3D return mappings leave the DS rows of the points that return elastic
+        # unwritten (they equal the elastic matrix, which the tangent's plastic corrections never
+        # read); _owned_local_DS and every path that reads all rows fill them first (_complete_ds).
+        self.lazy_elastic_ds = True
+        self._ds_elastic_pending = False
         self._K_el = None  # elastic tangent CSR values (device), built on first use
         self._blend_base = None  # (r, (1-r) K_el,t + r K_el) for the last regularisation factor
         self._dev = None
@@ -355,13 +360,28 @@ class ConstitutiveOperator:
 
     @property
     def _owned_local_DS(self):
-        return None if self._DS_aos is None else DeviceArray(self._DS_aos)
+        if self._DS_aos is None:
+            return None
+        self._complete_ds()
+        return DeviceArray(self._DS_aos)
 
     @_owned_local_DS.setter
     def _owned_local_DS(self, value):
         self._DS_aos = self._ingest_field(value, self.n_strain * self.n_strain)
         self._ds_symmetric = False  # a caller-provided tangent is not known to be symmetric
         self._branch = None
+        self._ds_elastic_pending = False
+
+    def _complete_ds(self):
+        """Write the DS rows the return mapping left out (lazy_elastic_ds): the rows of the points
+        that returned elastic get the elastic matrix, bit for bit what the return mapping emits."""
+        if not self._ds_elastic_pending or self._DS_aos is None:
+            return
+        pat = self._require_pattern()
+        d = self._dev
+        _lib.call("ssp_fill_elastic_ds", pat.dim, _lib.ptr(self._branch), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]),
+                  int(pat.n_local_int), _lib.ptr(self._DS_aos), _lib.stream_handle())
+        self._ds_elastic_pending = False
 
     def _ingest_field(self, value, rows):
         if value is None:
@@ -381,6 +401,7 @@ class ConstitutiveOperator:
         self._DS_aos = None
         self._ds_symmetric = False
         self._branch = None
+        self._ds_elastic_pending = False
 
     # -------------------------------------------------------------------- hot path
 
@@ -443,6 +464,7 @@ class ConstitutiveOperator:
         args = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
                 _lib.ptr(d["shear"]), _lib.ptr(d["bulk"]), _lib.ptr(d["lame"]), n)
         branch = None
+        pending = False
         mode = self.return_mapping if pat.dim == 3 else ("unsorted" if self.return_mapping == "unsorted" else "binned2d")
         if tangent and mode == "binned2d":  # elastic points finished first, the return mapping on the rest
             branch = t.empty(n, dtype=t.int8, device="cuda")
@@ -459,19 +481,21 @@ class ConstitutiveOperator:
             need = (3 if mode == "binned" else 8) * n + 12
             if self._scratch is None or self._scratch.numel() < need:
                 self._scratch = t.empty(need, dtype=t.int32, device="cuda")
-            mat = (_lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar), _lib.ptr(self._owned_overlap_sin_phi),
-                   _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S), _lib.ptr(DS), _lib.ptr(branch),
-                   _lib.ptr(self._scratch), st)
             # the mixed form: the plastic points' DS in double-float arithmetic (S, branches FP64)
-            sfx = "_mixed" if self.tangent_form == "mixed" else ""
+            options = (_lib.RM_COMPENSATED_DS if self.tangent_form == "mixed" else 0) | \
+                (_lib.RM_PLASTIC_DS_ONLY if self.lazy_elastic_ds else 0)
             if mode == "learned":
                 if self.branch_model is None:
                     raise ValueError("return_mapping='learned' needs a trained branch_model")
-                _lib.call("ssp_constitutive_3d_sds_learned" + sfx, _lib.ptr(self.branch_model.params), *mat)
+                bins, source = _lib.BINS_LEARNED, _lib.ptr(self.branch_model.params)
             elif mode == "previous":
-                _lib.call("ssp_constitutive_3d_sds_proposed" + sfx, _lib.ptr(prev), *mat)
+                bins, source = _lib.BINS_GIVEN, _lib.ptr(prev)
             else:
-                _lib.call("ssp_constitutive_3d_sds_binned" + sfx, *mat)
+                bins, source = _lib.BINS_EXACT, None
+            _lib.call("ssp_constitutive_3d_sds_screened", _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
+                      _lib.ptr(self._owned_overlap_sin_phi), _lib.ptr(d["shear"]), _lib.ptr(d["lame"]), n, _lib.ptr(S),
+                      _lib.ptr(DS), _lib.ptr(branch), _lib.ptr(self._scratch), bins, source, options, st)
+            pending = self.lazy_elastic_ds
         elif tangent:
             branch = t.empty(n, dtype=t.int8, device="cuda")
             _lib.call("ssp_constitutive_sds_branch", pat.dim, _lib.ptr(E), _lib.ptr(self._owned_overlap_c_bar),
@@ -485,6 +509,7 @@ class ConstitutiveOperator:
         self._S_aos = S
         self._DS_aos = DS
         self._branch = branch
+        self._ds_elastic_pending = pending
         if branch is not None:
             self._prev_branch = branch
         self._ds_symmetric = bool(tangent)
@@ -714,6 +739,7 @@ class ConstitutiveOperator:
                 e1.record()
                 ev.append((e0, e1))
         else:
+            self._complete_ds()
             if ev is not None:
                 e0.record()
             self._last_build.clear()
@@ -806,12 +832,16 @@ class ConstitutiveOperator:
             raise ValueError("BDDC subdomain pattern not configured")
         return pattern
 
-    def _bddc_local_DS(self):
+    def _bddc_local_DS(self, complete: bool = True):
         """DS rows of the subdomain's points as an AoS CUDA tensor (n_local, n_strain^2): gathered
-        from the owned (overlap) evaluation, else taken from a global ``DS`` (problem.py:1646-1656)."""
+        from the owned (overlap) evaluation, else taken from a global ``DS`` (problem.py:1646-1656).
+        complete=False: the elastic points' rows may be left as the return mapping left them (the
+        plastic corrections read only the plastic points' rows)."""
         t = _lib.require_cuda()
         pattern = self._bddc_pattern()
         if self._DS_aos is not None:
+            if complete:
+                self._complete_ds()
             if int(pattern.overlap_local_positions.size) != int(pattern.local_int_indices.size):
                 raise RuntimeError("BDDC overlap-local integration-point map is incomplete")
             pos = pattern.device.get("overlap_positions")
@@ -901,10 +931,11 @@ class ConstitutiveOperator:
         from .bddc import bddc_tangent_values_device
 
         pattern = self._bddc_pattern()
-        ds = self._bddc_local_DS()
         d, st = pattern.device, _lib.stream_handle()
         n_el = int(pattern.local_elements.size)
-        if n_el and self._bddc_predictor_ok(pattern):
+        predictor = bool(n_el) and self._bddc_predictor_ok(pattern)
+        ds = self._bddc_local_DS(complete=not predictor)
+        if predictor:
             t = _lib.torch()
             branch = self._branch.index_select(0, d["overlap_positions"])
             if "plastic_list" not in self._bddc:
