@@ -193,49 +193,55 @@ def cpu_model() -> str:
 # ----------------------------------------------------------------------------- the reference on the CPU
 
 
-def oracle_runner(w, owned=None):
+def oracle_runner(w):
     from oracle.newton_step import OracleNewtonStep
 
-    return OracleNewtonStep(w.mesh, w.specs, owned)
+    return OracleNewtonStep(w.mesh, w.specs)
 
 
-def sample_block(mesh, n_points_goal, n_q):
-    """Owned node block [0, n1) of one rank of the reference's contiguous partition whose share of
-    the mesh has about n_points_goal quadrature points (the whole mesh when it is smaller)."""
-    n_int = mesh.n_elem * n_q
-    parts = max(1, int(math.ceil(n_int / n_points_goal)))
-    return (0, int(math.ceil(mesh.n_nodes / parts))), parts
+def cpu_sample(w, n_points_goal, n_q):
+    """A bounded sample of the workload for the CPU: about n_points_goal quadrature points worth of
+    elements (sixteen contiguous runs spread over the element order) as a mesh of its own, and the
+    timed states restricted to its nodes.  The reference does the same work per element on it."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    sub, nodes = synthetic.element_sample(w.mesh, max(1, n_points_goal // n_q))
+    return sub, [U[:, nodes] for U in timed_states(w)]
 
 
-def cpu_reference_figures(w, states, *, steps, warmup, budget_s):
-    """The oracle timed on bounded samples: one rank's block with every host thread, and a smaller
-    block on one thread.  Returns (all-thread runner, result dict)."""
+def cpu_reference_figures(w, *, steps, warmup, budget_s):
+    """The oracle timed on bounded samples of the workload: every host thread on one sample, one
+    thread on a smaller one.  Returns a dict for the line's cpu_baseline."""
     from oracle import oracle_py as o
+    from oracle.newton_step import OracleNewtonStep
     from slope_stability_petsc4py_gb300 import fem
 
     n_q = len(fem.quadrature(w.mesh.dim, w.mesh.elem_type)[1])
-    block, parts = sample_block(w.mesh, SAMPLE_POINTS, n_q)
-    runner = oracle_runner(w, block)
+    sub, states = cpu_sample(w, SAMPLE_POINTS, n_q)
+    runner = OracleNewtonStep(sub, w.specs)
     times = runner.time_steps(states, steps, warmup, LAMBDA, R_REG, budget_s=budget_s)
     t = float(np.median(times))
     threads = o.num_threads()
-    block1, parts1 = sample_block(w.mesh, SAMPLE_POINTS_1T, n_q)
-    one = oracle_runner(w, block1)
+    sub1, states1 = cpu_sample(w, SAMPLE_POINTS_1T, n_q)
+    one = OracleNewtonStep(sub1, w.specs)
     o.set_num_threads(1)
     try:
-        t1 = float(np.median(one.time_steps(states, 2, 1, LAMBDA, R_REG)))
+        t1 = float(np.median(one.time_steps(states1, 2, 1, LAMBDA, R_REG)))
     finally:
         o.set_num_threads(threads)
-    res = {"value": runner.n_int / t, "unit": "quad-pts/s", "cores": threads, "kind": "port",
-           "cpu_model": cpu_model(), "ms_per_step": t * 1e3, "steps": len(times),
-           "sample": f"owned node block {list(block)} of {w.mesh.n_nodes:,} nodes (rank 0 of a {parts}-way "
-                     f"partition: {runner.n_int:,} points of its {runner.p['overlap_elements'].size:,} overlap "
-                     f"elements, {runner.nnz:,} nnz), median of {len(times)} steps after {warmup} warm-up; "
-                     f"the reference's C kernels restated (oracle), OpenMP",
-           "one_thread": {"value": one.n_int / t1, "unit": "quad-pts/s", "cores": 1, "ms_per_step": t1 * 1e3,
-                          "sample": f"owned node block {list(block1)} (rank 0 of {parts1}): {one.n_int:,} points, "
-                                    f"median of 2 steps"}}
-    return runner, res
+    return {"value": runner.n_int / t, "unit": "quad-pts/s", "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(), "ms_per_step": t * 1e3, "steps": len(times),
+            "sample": sample_text(w, sub, runner, len(times), warmup, threads),
+            "one_thread": {"value": one.n_int / t1, "unit": "quad-pts/s", "cores": 1, "ms_per_step": t1 * 1e3,
+                           "sample": f"{sub1.n_elem:,} of the {w.mesh.n_elem:,} elements ({one.n_int:,} points, "
+                                     f"{one.nnz:,} nnz), median of 2 steps after 1 warm-up"}}
+
+
+def sample_text(w, sub, runner, steps, warmup, threads):
+    return (f"{sub.n_elem:,} of the {w.mesh.n_elem:,} elements per step (16 contiguous runs spread over the mesh, "
+            f"as a mesh of their own: {runner.n_int:,} points, {runner.nnz:,} nnz), the same {len(STATE_FACTORS)} "
+            f"states; median of {steps} steps after {warmup} warm-up; the reference's C kernels restated (oracle), "
+            f"OpenMP on {threads} threads; pattern, geometry and elastic values built once outside the steps")
 
 
 # ----------------------------------------------------------------------------- GPU arm helpers
@@ -597,7 +603,16 @@ def measure_e2e(torch, op, states_host, args, form):
 def parity_check(torch, op, runner, U_host, U_dev):
     """Plain and mixed GPU outputs of one state against the oracle's on the same inputs (max-norm
     relative errors; comparisons on the device), the CSR pattern and the element -> CSR map bit for
-    bit.  The oracle builds its own pattern, geometry and elastic values."""
+    bit.  The oracle builds its own pattern, geometry and elastic values.
+
+    Stage by stage as well: the strain against the oracle's strain, and the return mapping against
+    the oracle's return mapping on the GPU's own strain.  And the oracle's own spread: the same
+    restatement compiled without fused multiply-adds, whose outputs move by as much as a change of
+    rounding in the strain moves them (the consistent tangent of a point whose principal strains
+    nearly coincide amplifies last-bit differences of the strain, itself a sum with cancellation)."""
+    from oracle import oracle_py as o
+    from slope_stability_petsc4py_gb300.distributed_tangent import overlap_strain_device
+
     pat = op.owned_tangent_pattern
     t0 = time.perf_counter()
     ref = runner.step(U_host, LAMBDA, R_REG, DAVIS)
@@ -630,13 +645,29 @@ def parity_check(torch, op, runner, U_host, U_dev):
         torch.cuda.synchronize()
         out[form] = {"S": rel(op._S_aos, S_o), "DS": rel(op._owned_local_DS.aos, DS_o), "F_free": rel(F, F_o),
                      "K": rel(K.values, K_o)}
+        if form == "plain":
+            E_g = overlap_strain_device(pat, U_dev)
+            S_gE, DS_gE = runner.constitutive(E_g.cpu().numpy(), LAMBDA, DAVIS)
+            out["stages"] = {"strain": rel(E_g, dev(ref["E"])),
+                             "S_on_gpu_strain": rel(op._S_aos, dev(S_gE)),
+                             "DS_on_gpu_strain": rel(op._owned_local_DS.aos, dev(DS_gE))}
+            del E_g, S_gE, DS_gE
     op.tangent_form = "plain"
-    out["tolerance"] = {"plain": "1e-12 max-norm relative (S, DS, F_free, K)",
+    if runner.dim == 3:
+        nf = runner.step(U_host, LAMBDA, R_REG, DAVIS, library=o.nofma_lib())
+        out["oracle_without_fma"] = {k: rel(dev(nf[k2]), v) for k, k2, v in (
+            ("strain", "E", dev(ref["E"])), ("S", "S", S_o), ("DS", "DS", DS_o), ("K", "K", K_o))}
+        del nf
+    spread = out.get("oracle_without_fma", {}).get("DS", 0.0)
+    out["tolerance"] = {"plain": "1e-12 max-norm relative: strain, S, F_free, K, and DS on the same strain; "
+                                 "DS end to end within max(1e-12, the oracle's own spread without FMA)",
                         "mixed": "1e-6 tangent (K), 1e-11 force (F_free)"}
     out["pass"] = bool(out["indices_bit_exact"] and out["element_map_bit_exact"] and
                        out["constrained_diagonals_bit_exact"] and
-                       all(v <= 1e-12 for v in out["plain"].values()) and out["mixed"]["K"] <= 1e-6 and
-                       out["mixed"]["F_free"] <= 1e-11)
+                       all(out["plain"][k] <= 1e-12 for k in ("S", "F_free", "K")) and
+                       out["plain"]["DS"] <= max(1e-12, spread) and
+                       all(v <= 1e-12 for v in out["stages"].values()) and
+                       out["mixed"]["K"] <= 1e-6 and out["mixed"]["F_free"] <= 1e-11)
     del K_o, F_o, S_o, DS_o
     return out
 
@@ -811,7 +842,7 @@ def run_gpu(args):
         line["parity"] = parity_check(torch, op, runner, states_host[1], states_dev[1])
         del runner
     if rank == 0 and not args.no_cpu_baseline:
-        _runner, line["cpu_baseline"] = cpu_reference_figures(w, states_host, steps=5, warmup=1, budget_s=30.0)
+        line["cpu_baseline"] = cpu_reference_figures(w, steps=5, warmup=1, budget_s=30.0)
     del op, res, states_dev
     torch.cuda.empty_cache()
     if rank == 0 and not args.no_others and args.config == DEFAULT_CONFIG and args.form == "plain":
@@ -828,35 +859,34 @@ def run_gpu(args):
 
 def run_reference(args):
     """The reference arm: the oracle's restatement of the reference's kernels on the host cores,
-    one rank's owned node block per step (all host threads), same workload and states."""
+    every host thread, one bounded sample of the workload per step (same states)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    w = workload(args.config)
     from oracle import oracle_py as o
+    from oracle.newton_step import OracleNewtonStep
     from slope_stability_petsc4py_gb300 import fem
 
-    states = timed_states(w)
+    w = workload(args.config)
     n_q = len(fem.quadrature(w.mesh.dim, w.mesh.elem_type)[1])
-    block, parts = sample_block(w.mesh, SAMPLE_POINTS, n_q)
-    runner = oracle_runner(w, block)
+    sub, states = cpu_sample(w, SAMPLE_POINTS, n_q)
+    runner = OracleNewtonStep(sub, w.specs)
     times = runner.time_steps(states, args.steps, args.warmup, LAMBDA, R_REG)
     t = float(np.median(times))
     value = runner.n_int / t
     n_int = w.mesh.n_elem * n_q
-    nnz_full = int(o.owned_pattern_c(w.mesh.elem, w.mesh.q_mask, (0, w.mesh.n_nodes))["indices"].size) \
-        if parts > 1 else runner.nnz
-    sample = (f"owned node block {list(block)} of {w.mesh.n_nodes:,} nodes per step (rank 0 of a {parts}-way "
-              f"partition: {runner.n_int:,} points of its overlap elements, {runner.nnz:,} nnz), median of "
-              f"{len(times)} steps after {args.warmup} warm-up; the reference's C kernels restated (oracle), "
-              f"OpenMP on {o.num_threads()} threads; pattern, geometry and elastic values built once outside the steps")
+    full = runner if sub is w.mesh else None
+    nnz_full = full.nnz if full is not None else \
+        int(o.owned_pattern_c(w.mesh.elem, w.mesh.q_mask, (0, w.mesh.n_nodes))["indices"].size)
+    threads = o.num_threads()
     line = {"metric": METRIC, "value": value, "unit": "quad-pts/s", "n_gpus": world, "steps": len(times),
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": bench_config(w, n_int, nnz_full),
-            "cpu_baseline": {"value": value, "unit": "quad-pts/s", "cores": o.num_threads(), "kind": "port",
-                             "cpu_model": cpu_model(), "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "quad-pts/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": sample_text(w, sub, runner, len(times), args.warmup, threads)},
             "e2e": {"value": value, "unit": "quad-pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "setup_s": {"pattern": runner.pattern_s, "geometry": runner.geometry_s, "elastic_values": runner.elastic_s}}
     print(json.dumps(line))

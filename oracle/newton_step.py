@@ -67,23 +67,34 @@ class OracleNewtonStep:
         self.elastic_s = time.perf_counter() - t2
         self.n_nodes = mesh.n_nodes
 
-    def _tangent(self, DS):
+    def _tangent(self, DS, library=None):
         o, p, d = self.o, self.p, self.d
         if self.dim == 3:
             return o.tangent_rows_3d(d[0], d[1], d[2], DS, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"],
-                                     p["slot_pos"], self.n_q, self.nnz)
+                                     p["slot_pos"], self.n_q, self.nnz, library=library)
         return o.tangent_scatter(2, d[0], d[1], None, DS, self.w, self.scatter, self.n_q, self.nnz)
 
-    def step(self, U, lam, r, davis="B"):
-        """One Newton iteration at U (dim, n_nodes): dict of S, DS (AoS), F (owned rows) and K."""
+    def constitutive(self, E, lam, davis="B", library=None):
+        """S, DS (AoS) of the reference's return mapping on given strains E (n_int, n_s) at lam."""
+        o, m = self.o, self.mat
+        cb, sp = o.reduction(m["c0"], m["phi"], m["psi"], lam, davis)
+        if self.dim == 3:
+            return o.constitutive_3d(E, cb, sp, m["shear"], m["bulk"], m["lame"], library=library)
+        S4, DS9 = o.constitutive_2d(np.asarray(E).T, cb, sp, m["shear"], m["bulk"], m["lame"])
+        return np.ascontiguousarray(S4.T), np.ascontiguousarray(DS9.T)
+
+    def step(self, U, lam, r, davis="B", library=None):
+        """One Newton iteration at U (dim, n_nodes): dict of E, S, DS (AoS), F (owned rows) and K.
+        library: the C restatement to run the 3D kernels with (default: oracle/_build/liboracle.so;
+        oracle_py.nofma_lib() is the same code without fused multiply-adds)."""
         o, p, d, m = self.o, self.p, self.d, self.mat
         cb, sp = o.reduction(m["c0"], m["phi"], m["psi"], lam, davis)
         u_ov = np.ascontiguousarray(U.reshape(-1, order="F")[p["overlap_global_dofs"]])
         if self.dim == 3:
-            E = o.strain_3d(d[0], d[1], d[2], u_ov, p["overlap_element_dof_lids"], self.n_q)
-            S, DS = o.constitutive_3d(E, cb, sp, m["shear"], m["bulk"], m["lame"])
+            E = o.strain_3d(d[0], d[1], d[2], u_ov, p["overlap_element_dof_lids"], self.n_q, library=library)
+            S, DS = o.constitutive_3d(E, cb, sp, m["shear"], m["bulk"], m["lame"], library=library)
             F = o.force_rows_3d(d[0], d[1], d[2], S, self.w, p["row_slot_ptr"], p["slot_elem"], p["slot_lrow"],
-                                self.n_q)
+                                self.n_q, library=library)
         else:
             E = o.strain_2d(d[0], d[1], u_ov, p["overlap_element_dof_lids"], self.n_q)
             S4, DS9 = o.constitutive_2d(E.T, cb, sp, m["shear"], m["bulk"], m["lame"])
@@ -92,11 +103,11 @@ class OracleNewtonStep:
                                       p["overlap_element_dof_lids"], self.n_q, p["overlap_global_dofs"].size)
             F = f_ov[p["owned_local_overlap_dofs"]]
         F[~self.free] = 0.0
-        K = self._tangent(DS)
+        K = self._tangent(DS, library)
         K[p["constrained_diag_positions"]] = 1.0
         K *= 1.0 - r
         K += r * self.elastic
-        return {"S": S, "DS": DS, "F": F, "K": K}
+        return {"E": E, "S": S, "DS": DS, "F": F, "K": K}
 
     def time_steps(self, states, steps, warmup, lam, r, budget_s=None):
         """Wall-clock seconds of each of `steps` steps cycling through `states` after `warmup`."""

@@ -223,7 +223,7 @@ def strain_3d(dphi1, dphi2, dphi3, u_overlap, dof_lids, n_q, library=None):
     return E
 
 
-def force_rows_3d(dphi1, dphi2, dphi3, S, w, row_slot_ptr, slot_elem, slot_lrow, n_q):
+def force_rows_3d(dphi1, dphi2, dphi3, S, w, row_slot_ptr, slot_elem, slot_lrow, n_q, library=None):
     d1, d2, d3 = (_c(a, np.float64) for a in (dphi1, dphi2, dphi3))
     S = _c(S, np.float64)
     w = _c(w, np.float64)
@@ -231,18 +231,18 @@ def force_rows_3d(dphi1, dphi2, dphi3, S, w, row_slot_ptr, slot_elem, slot_lrow,
     sl = _c(slot_lrow, np.uint8)
     n_rows = rp.size - 1
     F = np.zeros(n_rows)
-    lib().orc_force_rows_3d(_d(d1), _d(d2), _d(d3), _d(S), _d(w), _i(rp), _i(se),
+    (library or lib()).orc_force_rows_3d(_d(d1), _d(d2), _d(d3), _d(S), _d(w), _i(rp), _i(se),
                             sl.ctypes.data_as(_up), n_rows, d1.shape[1], n_q, _d(F))
     return F
 
 
-def tangent_rows_3d(dphi1, dphi2, dphi3, DS, w, row_slot_ptr, slot_elem, slot_lrow, slot_pos, n_q, nnz):
+def tangent_rows_3d(dphi1, dphi2, dphi3, DS, w, row_slot_ptr, slot_elem, slot_lrow, slot_pos, n_q, nnz, library=None):
     d1, d2, d3 = (_c(a, np.float64) for a in (dphi1, dphi2, dphi3))
     DS, w = _c(DS, np.float64), _c(w, np.float64)
     rp, se, sp = _c(row_slot_ptr, np.int32), _c(slot_elem, np.int32), _c(slot_pos, np.int32)
     sl = _c(slot_lrow, np.uint8)
     out = np.zeros(int(nnz))
-    lib().orc_tangent_rows_3d(_d(d1), _d(d2), _d(d3), _d(DS), _d(w), _i(rp), _i(se),
+    (library or lib()).orc_tangent_rows_3d(_d(d1), _d(d2), _d(d3), _d(DS), _d(w), _i(rp), _i(se),
                               sl.ctypes.data_as(_up), _i(sp), rp.size - 1, d1.shape[1], n_q, _d(out))
     return out
 

@@ -423,3 +423,23 @@ def config_workload(name: str):
              for i in range(mats.c0.size)]
     G, V = displacement_basis(mesh, mats, seed=3)
     return SimpleNamespace(name=name, mesh=mesh, mats=mats, specs=specs, G=G, V=V, amp=float(cfg["amplitude"]))
+
+
+def element_sample(mesh: SlopeMesh, n_elem_goal: int, chunks: int = 16) -> tuple[SlopeMesh, np.ndarray]:
+    """A bounded sample of a mesh as a mesh of its own: about n_elem_goal elements taken as `chunks`
+    contiguous runs spread evenly over the element order (so the sample sees every part of the
+    slope, plastic zone included), their nodes renumbered in their original order.  Returns the
+    sample and the original ids of its nodes (to restrict a displacement: U[:, nodes])."""
+    n_el = mesh.n_elem
+    if n_elem_goal >= n_el:
+        return mesh, np.arange(mesh.n_nodes)
+    run = max(1, n_elem_goal // chunks)
+    starts = (np.arange(chunks) * (n_el // chunks)).astype(np.int64)
+    sel = np.unique(np.concatenate([np.arange(s0, min(s0 + run, n_el)) for s0 in starts]))
+    elem = mesh.elem[:, sel]
+    nodes = np.unique(elem)
+    lid = np.full(mesh.n_nodes, -1, dtype=np.int64)
+    lid[nodes] = np.arange(nodes.size)
+    sub = SlopeMesh(mesh.dim, mesh.elem_type, np.ascontiguousarray(mesh.coord[:, nodes]), lid[elem],
+                    np.ascontiguousarray(mesh.q_mask[:, nodes]), np.asarray(mesh.material_id)[sel], dict(mesh.extra))
+    return sub, nodes

@@ -70,6 +70,15 @@ def test_newton_iteration_matches_oracle_at_benchmark_size(name, cuda_device):
           {k: f"{v:.2e}" for k, v in errs.items()})
     assert 0.02 < plastic < 0.5  # the states yield: the return mapping's plastic branches run
     assert all(v <= PLAIN_RTOL for v in errs.values()), errs
+    # stage by stage: the strain against the oracle's, the return mapping on the GPU's own strain
+    from slope_stability_petsc4py_gb300.distributed_tangent import overlap_strain_device
+
+    E_g = overlap_strain_device(pat, U_dev)
+    S_gE, DS_gE = ref_step.constitutive(E_g.cpu().numpy(), LAM)
+    stages = {"strain": _rel(torch, E_g, dev(ref["E"])), "S": _rel(torch, op._S_aos, dev(S_gE)),
+              "DS": _rel(torch, op._owned_local_DS.aos, dev(DS_gE))}
+    print(f"{name}: stage errors", {k: f"{v:.2e}" for k, v in stages.items()})
+    assert all(v <= PLAIN_RTOL for v in stages.values()), stages
     if pat.dim == 3:
         assert pat.affine_p2 is True  # the barycentric P2 strain and force ran
         op.tangent_form = "mixed"

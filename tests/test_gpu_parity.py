@@ -631,7 +631,8 @@ def test_screened_return_mapping_options_and_elastic_fill(oracle):
         assert torch.equal(S2, S0) and torch.equal(DS2, DS0) and torch.equal(b2, b0)
     Sm, DSm, bm = run(_lib.BINS_EXACT, None, _lib.RM_COMPENSATED_DS | _lib.RM_PLASTIC_DS_ONLY)
     assert torch.equal(bm, b0) and torch.equal(Sm, S0)
-    err = ((DSm[~el] - DS0[~el]).abs().max(dim=1).values / DS0[~el].abs().max(dim=1).values).max()
+    pl = (b0 >= 1) & (b0 <= 3)  # smooth face and edges (an apex point's DS is zero)
+    err = ((DSm[pl] - DS0[pl]).abs().max(dim=1).values / DS0[pl].abs().max(dim=1).values).max()
     assert float(err) <= 1e-10  # the compensated plastic DS, as ssp_constitutive_3d_sds_binned_mixed
     with pytest.raises(_lib.SSPError):
         run(7, None, 0)
@@ -651,8 +652,10 @@ def test_operator_lazy_elastic_rows_match_full_rows():
         kt = op._build_owned_tangent_matrix().getValuesCSR()[2].copy()
         kr = op.build_K_regularized(0.25).getValuesCSR()[2].copy()
         outs[lazy] = (np.asarray(op._owned_local_DS), kt, kr)
-    for a, b in zip(outs[False], outs[True]):
-        assert np.array_equal(a, b)
+    assert np.array_equal(outs[False][0], outs[True][0])  # DS bit for bit
+    # the CSR values are sums of FP64 reductions in no fixed order: equal to rounding
+    assert rel_err(outs[True][1], outs[False][1]) <= 1e-14
+    assert rel_err(outs[True][2], outs[False][2]) <= 1e-14
 
 
 def test_device_resident_operator_path():
