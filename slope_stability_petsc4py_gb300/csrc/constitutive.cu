@@ -344,9 +344,87 @@ __device__ __forceinline__ bool edge_ds_compensated(const Principal3 &p, const M
     return true;
 }
 
+// ---- consistent tangent of the plastic branches, FP64, regrouped per point
+//
+// The same regrouping as the double-float form above, in FP64: per point the coefficients A, B, K_k
+// (smooth) or a, kQ, kR (edges) and the vectors K_k P_k, -Dp / den are formed once, and each of the
+// 21 upper entries is a short sum of products (about 300 FP64 operations per smooth point against
+// about 700 for the entry-by-entry form of constitutive_3D_kernel.h:242-262, whose inverse gaps
+// multiply each entry's own combination).  Its terms are larger than the result by about
+// (max|e| / gap)^2, which multiplies the rounding errors: it is used only where every gap is at
+// least kRegroupGap of max|e| (amplification <= 400, errors ~1e-14 of the tangent's scale); other
+// points keep the entry-by-entry form.
+constexpr double kRegroupGap = 0.05;
+
+__device__ __forceinline__ bool smooth_ds_regrouped(const Principal3 &p, const Mat3 &m, const double *P1,
+                                                    const double *P2, const double *P3, double inv1, double inv2,
+                                                    double inv3, double s1, double s2, double s3, const double *Dp,
+                                                    double inv_den, double *DS) {
+    const double e1 = p.e1, e2 = p.e2, e3 = p.e3;
+    if (!(fmin(e1 - e2, e2 - e3) >= kRegroupGap * fmax(fabs(e1), fabs(e3)))) return false;
+    const double a1 = s1 * inv1, a2 = s2 * inv2, a3 = s3 * inv3;
+    const double c1a = 2.0 * e1 - e2 - e3, c1b = e2 - e3;
+    const double c2a = 2.0 * e2 - e1 - e3, c2b = e1 - e3;
+    const double c3a = 2.0 * e3 - e1 - e2, c3b = e1 - e2;
+    const double A = a1 + a2 + a3, B = a1 * (e2 + e3) + a2 * (e1 + e3) + a3 * (e1 + e2);
+    const double G2 = 2.0 * m.shear;
+    const double K1 = G2 - (a1 * c1a + a2 * c2b + a3 * c3b);
+    const double K2 = G2 - (a1 * c1b + a2 * c2a - a3 * c3b);
+    const double K3 = G2 + (a1 * c1b + a2 * c2b - a3 * c3a);
+    double q1[6], q2[6], q3[6], dq[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        q1[i] = K1 * P1[i];
+        q2[i] = K2 * P2[i];
+        q3[i] = K3 * P3[i];
+        dq[i] = -Dp[i] * inv_den;
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+            double v = A * square_jac(p.t, i, j) + q1[i] * P1[j] + q2[i] * P2[j] + q3[i] * P3[j] + dq[i] * Dp[j];
+            if (i == j) v -= half_ident(i) * B;
+            if (j < 3) v += m.lame;
+            store_sym(DS, i, j, v);
+        }
+    }
+    return true;
+}
+
+// Edges: left Q = P12, R = P3, e = e3, em = e1 + e2; right Q = P23, R = P1, e = e1, em = e2 + e3;
+// a the branch's (s_R - s_Q) inv and gap its eigenvalue gap.
+__device__ __forceinline__ bool edge_ds_regrouped(const Principal3 &p, const Mat3 &m, const double *Q, const double *R,
+                                                  double a, double em, double e, double gap, const double *Dp,
+                                                  double inv_den, double *DS) {
+    if (!(gap >= kRegroupGap * fmax(fabs(p.e1), fabs(p.e3)))) return false;
+    const double kQ = a * em + m.shear, kR = a * (em - 2.0 * e) + 2.0 * m.shear, ae = a * e, aem = a * em;
+    double aq[6], kqq[6], krr[6], aeq[6], dq[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        aq[i] = -a * Q[i];
+        kqq[i] = kQ * Q[i];
+        krr[i] = kR * R[i];
+        aeq[i] = ae * Q[i];
+        dq[i] = -Dp[i] * inv_den;
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+            double v = a * square_jac(p.t, i, j) + aq[i] * p.t[j] + p.t[i] * aq[j] + kqq[i] * Q[j] + krr[i] * R[j] +
+                       aeq[i] * R[j] + R[i] * aeq[j] + dq[i] * Dp[j];
+            if (i == j) v -= half_ident(i) * aem;
+            if (j < 3) v += m.lame;
+            store_sym(DS, i, j, v);
+        }
+    }
+    return true;
+}
+
 // Stress and (when DS != null) consistent tangent of the decided branch.  COMP: the plastic
 // branches' DS in double-float arithmetic where the point allows it (S is always FP64 and the
-// same as without COMP).
+// same as without COMP); otherwise the regrouped FP64 form where the gaps allow it.
 template <bool COMP>
 __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, double *S, double *DS) {
     const double sp = m.sin_phi, sin_phi = m.sin_phi, shear = m.shear, lame = m.lame;
@@ -377,6 +455,8 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
             const double inv_den = 1.0 / d.den;
             if constexpr (COMP) {
                 if (smooth_ds_compensated(p, m, P1, P2, P3, inv1, inv2, inv3, s1, s2, s3, Dp, inv_den, DS)) return;
+            } else {
+                if (smooth_ds_regrouped(p, m, P1, P2, P3, inv1, inv2, inv3, s1, s2, s3, Dp, inv_den, DS)) return;
             }
             const double em23 = e2 + e3, em13 = e1 + e3, em12 = e1 + e2;
             const double c1a = 2.0 * e1 - e2 - e3, c1b = e2 - e3;
@@ -420,6 +500,8 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
             const double inv_den = 1.0 / d.den;
             if constexpr (COMP) {
                 if (edge_ds_compensated(p, m, P12, P3, (s3 - s1) * inv3, em12, e3, e2 - e3, Dp, inv_den, DS)) return;
+            } else {
+                if (edge_ds_regrouped(p, m, P12, P3, (s3 - s1) * inv3, em12, e3, e2 - e3, Dp, inv_den, DS)) return;
             }
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
@@ -457,6 +539,8 @@ __device__ void finish3(const Principal3 &p, const Decision3 &d, const Mat3 &m, 
             const double inv_den = 1.0 / d.den;
             if constexpr (COMP) {
                 if (edge_ds_compensated(p, m, P23, P1, (s1 - s3) * inv1, em23, e1, e1 - e2, Dp, inv_den, DS)) return;
+            } else {
+                if (edge_ds_regrouped(p, m, P23, P1, (s1 - s3) * inv1, em23, e1, e1 - e2, Dp, inv_den, DS)) return;
             }
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
