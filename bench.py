@@ -49,6 +49,12 @@ STATE_FACTORS = (0.9, 1.0, 1.1, 1.2)
 SSR_STEPS, SSR_ITERS = 10, 6
 # points per step of the bounded CPU samples (all host threads, and one thread)
 SAMPLE_POINTS, SAMPLE_POINTS_1T = 4_000_000, 250_000
+# DRAM bytes (read + write) per launch of the step kernels, from one ncu capture each (the command in
+# profiles/dram_traffic_3d_p2_large.md), keyed by workload and entry point; reported as roofline.traffic
+# with that source when the bench's dominant kernel is one of them
+NCU_TRAFFIC = {"3d_p2_large": {"ssp_tangent_plastic_correction": (4146e6 + 1475e6,
+                                                                  "ncu capture 2026-12-04, "
+                                                                  "profiles/dram_traffic_3d_p2_large.md")}}
 STEP_TEXT = ("reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + constrained diagonals "
              "+ regularised blend")
 
@@ -805,8 +811,9 @@ def run_gpu(args):
                      "device_pattern_bytes": stats["device_bytes"], "setup_s": res.setup_s},
         "assembled_nnz_per_s": world * nnz / (ms * 1e-3),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "peak_source": hbm_src, "traffic": None,
-                     "traffic_note": "DRAM bytes of the kernels are measured by ncu, outside this run: see profiles/",
+                     "frac": achieved_gbs / hbm_peak, "peak_source": hbm_src,
+                     "traffic": NCU_TRAFFIC.get(args.config, {}).get(dominant, (None, None))[0],
+                     "traffic_source": NCU_TRAFFIC.get(args.config, {}).get(dominant, (None, "not captured"))[1],
                      "ms_per_launch": k_ms, "algorithmic_bytes": alg["bytes"],
                      "units": f"{stats['n_plastic_el']:.0f} plastic elements per launch"
                      if dominant.startswith("ssp_tangent_plastic_correction") else None},
