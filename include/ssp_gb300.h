@@ -205,6 +205,19 @@ int ssp_assemble_force_element_affine_mixed(const float *jinv_hl, const float *g
                                             const double *stress, const int32_t *elem_row, int n_elem, int n_p, int n_q,
                                             int n_rows, double *out_values, void *stream);
 
+/* Straight-sided P1 / P4 tetrahedra in FP64 (no reference counterpart; same results as
+ * ssp_assemble_overlap_strain_3d / ssp_assemble_force_element within rounding): the gradients are
+ * J^{-T} ghat(q), so the kernels read J^{-1} per element (jinv [n_elem][3][3] row-major) and the
+ * reference element's gradient table (ghat [n_q][n_p][3]) instead of per-point gradients.  The
+ * force entry zeroes out_values first; elem_row as in ssp_assemble_force_element.  Tables of more
+ * than 48 KiB of shared memory return SSP_ERR_UNSUPPORTED. */
+int ssp_assemble_overlap_strain_3d_affine(const double *jinv, const double *ghat, const double *u_overlap, int n_u,
+                                          const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                          double *out_values, void *stream);
+int ssp_assemble_force_element_affine(const double *jinv, const double *ghat, const double *stress,
+                                      const double *weight, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                      int n_rows, double *out_values, void *stream);
+
 /* Straight-sided P2 tetrahedra (no reference counterpart; same results as
  * ssp_assemble_overlap_strain_3d / ssp_assemble_force_element within rounding): the strain and
  * the owned force through the barycentric form of the quadratic basis, from J^{-1} per element

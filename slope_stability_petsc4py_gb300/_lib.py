@@ -34,6 +34,8 @@ _SIGS = {
     "ssp_constitutive_2d": [_vp] * 6 + [_c_int, _vp, _vp, _vp],
     "ssp_potential_energy": [_c_int] + [_vp] * 7 + [_c_int] + [_vp] * 5,
     "ssp_assemble_overlap_strain_3d_p2_affine": [_vp] * 3 + [_c_int, _vp, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_overlap_strain_3d_affine": [_vp] * 3 + [_c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp],
+    "ssp_assemble_force_element_affine": [_vp] * 5 + [_c_int] * 4 + [_vp, _vp],
     "ssp_assemble_force_element_p2_affine": [_vp] * 5 + [_c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_overlap_strain_3d_p2_affine_mixed": [_vp] * 3 + [_c_int, _vp, _c_int, _c_int, _c_int, _vp, _vp],
     "ssp_assemble_force_element_p2_affine_mixed": [_vp] * 5 + [_c_int, _c_int, _c_int, _vp, _vp],
@@ -140,6 +142,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
     "ssp_assemble_overlap_strain_3d_affine_mixed": 1, "ssp_assemble_force_element_affine_mixed": 1,
     "ssp_assemble_overlap_strain_3d_p2_affine": 1, "ssp_assemble_force_element_p2_affine": 1,
+    "ssp_assemble_overlap_strain_3d_affine": 1, "ssp_assemble_force_element_affine": 1,
     "ssp_assemble_overlap_strain_3d_p2_affine_mixed": 1, "ssp_assemble_force_element_p2_affine_mixed": 1,
     "ssp_constitutive_2d_sds_binned": 2,
     "ssp_tangent_plastic_correction": 1,

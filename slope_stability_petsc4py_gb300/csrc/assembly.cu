@@ -291,6 +291,148 @@ __global__ void __launch_bounds__(64) strain3_p2_affine_kernel(const double *__r
     }
 }
 
+// ---------------------------------------------------------------------------- affine tetrahedra, FP64
+//
+// Straight-sided tetrahedra (every point of an element has the same Jacobian): dphi_a(q) =
+// J^{-T} ghat_a(q), ghat the reference element's gradient table [n_q][n_p][3], the same for every
+// element.  Instead of the per-point gradients (24 n_p bytes per point: 840 for P4) the kernels
+// read J^{-1} once per element (72 bytes) and the table from shared memory.  Used for P1 and P4
+// (P2 has the barycentric form above).
+
+// Strain: grad u = G J^{-1}, G_ik = sum_{a>=1} (u_a - u_0)_i ghat_a,k(q) (the element's rigid
+// translation removed first, as the mixed form does); E the engineering strains of grad u.
+constexpr int kAffineThreads = 128;
+__global__ void __launch_bounds__(kAffineThreads) strain3_affine_kernel(const double *__restrict__ jinv,
+                                                                        const double *__restrict__ ghat,
+                                                                        const double *__restrict__ u,
+                                                                        const int32_t *__restrict__ dof, long long n_u,
+                                                                        int n_elem, int n_p, int n_q,
+                                                                        double *__restrict__ E) {
+    // shared: the reference table, then the displacements of the elements the block's points
+    // belong to (gathered once per element instead of once per point)
+    extern __shared__ double s_aff[];
+    double *s_ghat = s_aff;                // n_q * n_p * 3
+    double *s_u = s_aff + n_q * n_p * 3;   // (elements of the block) * 3 n_p
+    for (int i = threadIdx.x; i < n_q * n_p * 3; i += blockDim.x) s_ghat[i] = ghat[i];
+    const int nld = 3 * n_p;
+    const long long g0 = (long long)blockIdx.x * blockDim.x;
+    const long long e_first = g0 / n_q;
+    long long e_last = (g0 + blockDim.x - 1) / n_q;
+    if (e_last >= n_elem) e_last = n_elem - 1;
+    const int n_vals = static_cast<int>(e_last - e_first + 1) * nld;
+    bool bad = false;
+    for (int i = threadIdx.x; i < n_vals; i += blockDim.x) {
+        const int32_t lid = dof[e_first * nld + i];
+        if (lid < 0 || lid >= n_u) {
+            bad = true;
+            s_u[i] = 0.0;
+        } else {
+            s_u[i] = u[lid];
+        }
+    }
+    if (bad) flag(SSP_DEV_BAD_INDEX);
+    __syncthreads();
+    const long long g = g0 + threadIdx.x;
+    if (g >= (long long)n_elem * n_q) return;
+    const long long e = g / n_q;
+    const int q = static_cast<int>(g - e * n_q);
+    const double *ue = s_u + (e - e_first) * nld;
+    const double u0x = ue[0], u0y = ue[1], u0z = ue[2];
+    double G[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    const double *gq = s_ghat + q * n_p * 3;
+    for (int a = 1; a < n_p; ++a) {
+        const double du[3] = {ue[3 * a] - u0x, ue[3 * a + 1] - u0y, ue[3 * a + 2] - u0z};
+        const double gh[3] = {gq[3 * a], gq[3 * a + 1], gq[3 * a + 2]};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) G[i][k] = fma(du[i], gh[k], G[i][k]);
+    }
+    double J[3][3];
+    const double *je = jinv + e * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J[k / 3][k % 3] = je[k];
+    // E_11, E_22, E_33: (G J^{-1})_ii; E_12, E_23, E_13: (G J^{-1})_ij + (G J^{-1})_ji
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        s[0] = fma(G[0][k], J[k][0], s[0]);
+        s[1] = fma(G[1][k], J[k][1], s[1]);
+        s[2] = fma(G[2][k], J[k][2], s[2]);
+        s[3] = fma(G[0][k], J[k][1], fma(G[1][k], J[k][0], s[3]));
+        s[4] = fma(G[1][k], J[k][2], fma(G[2][k], J[k][1], s[4]));
+        s[5] = fma(G[0][k], J[k][2], fma(G[2][k], J[k][0], s[5]));
+    }
+    double2 *o = reinterpret_cast<double2 *>(E + 6 * g);
+    o[0] = make_double2(s[0], s[1]);
+    o[1] = make_double2(s[2], s[3]);
+    o[2] = make_double2(s[4], s[5]);
+}
+
+// Force: F_(a,i) = sum_q sum_k T_ik(q) ghat_a,k(q), T(q) = w_q sigma_q J^{-T} (T_ik = w sum_j
+// sigma_ij J^{-1}_kj).  The block forms T of every point of the elements its threads cover in
+// shared memory, once each; one thread per (element, node) then sums its three components over the
+// points and adds them to the owned rows with FP64 reductions.
+__global__ void __launch_bounds__(kAffineThreads) force3_affine_kernel(const double *__restrict__ jinv,
+                                                                       const double *__restrict__ ghat,
+                                                                       const double *__restrict__ w,
+                                                                       const double *__restrict__ S,
+                                                                       const int32_t *__restrict__ elem_row, int n_rows,
+                                                                       int n_elem, int n_p, int n_q,
+                                                                       double *__restrict__ F) {
+    extern __shared__ double s_aff[];
+    double *s_ghat = s_aff;                  // n_q * n_p * 3
+    double *s_T = s_aff + n_q * n_p * 3;     // (elements of the block) * n_q * 9
+    for (int i = threadIdx.x; i < n_q * n_p * 3; i += kAffineThreads) s_ghat[i] = ghat[i];
+    const long long t0 = (long long)blockIdx.x * kAffineThreads;
+    const long long e_first = t0 / n_p;
+    long long e_last = (t0 + kAffineThreads - 1) / n_p;
+    if (e_last >= n_elem) e_last = n_elem - 1;
+    const int n_pts = static_cast<int>(e_last - e_first + 1) * n_q;
+    for (int i = threadIdx.x; i < n_pts; i += kAffineThreads) {
+        const long long g = e_first * n_q + i;
+        const long long e = g / n_q;
+        const double wq = w[g];
+        const double *sg = S + 6 * g;
+        // w sigma, symmetric: sigma_00..22 = s0, s1, s2; sigma_01 = s3, sigma_12 = s4, sigma_02 = s5
+        const double s0 = wq * sg[0], s1 = wq * sg[1], s2 = wq * sg[2], s3 = wq * sg[3], s4 = wq * sg[4],
+                     s5 = wq * sg[5];
+        const double ws[3][3] = {{s0, s3, s5}, {s3, s1, s4}, {s5, s4, s2}};
+        const double *je = jinv + e * 9;
+        double *T = s_T + i * 9;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                T[3 * a + k] = fma(ws[a][0], je[3 * k], fma(ws[a][1], je[3 * k + 1], ws[a][2] * je[3 * k + 2]));
+    }
+    __syncthreads();
+    const long long t = t0 + threadIdx.x;
+    if (t >= (long long)n_elem * n_p) return;
+    const long long e = t / n_p;
+    const int node = static_cast<int>(t - e * n_p);
+    const int32_t *er = elem_row + (e * n_p + node) * 3;
+    const int r0 = er[0], r1 = er[1], r2 = er[2];
+    if (r0 < 0 && r1 < 0 && r2 < 0) return;
+    if (r0 >= n_rows || r1 >= n_rows || r2 >= n_rows) {
+        flag(SSP_DEV_BAD_INDEX);
+        return;
+    }
+    const double *Te = s_T + (e - e_first) * n_q * 9;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int q = 0; q < n_q; ++q) {
+        const double *gh = s_ghat + (q * n_p + node) * 3;
+        const double g0 = gh[0], g1 = gh[1], g2 = gh[2];
+        const double *T = Te + q * 9;
+        a0 = fma(T[0], g0, fma(T[1], g1, fma(T[2], g2, a0)));
+        a1 = fma(T[3], g0, fma(T[4], g1, fma(T[5], g2, a1)));
+        a2 = fma(T[6], g0, fma(T[7], g1, fma(T[8], g2, a2)));
+    }
+    if (r0 >= 0) red_add(F + r0, a0);
+    if (r1 >= 0) red_add(F + r1, a1);
+    if (r2 >= 0) red_add(F + r2, a2);
+}
+
 // One thread per element; elem_row as in force_element_kernel; atomics into F.
 __global__ void __launch_bounds__(64) force3_p2_affine_kernel(const double *__restrict__ jinv,
                                                               const double *__restrict__ bary,
@@ -1181,6 +1323,40 @@ int ssp_assemble_force_element_p2_affine(const double *jinv, const double *bary,
     if (!jinv || !bary || !stress || !weight || !elem_row) return SSP_ERR_INVALID;
     force3_p2_affine_kernel<<<grid_for(n_elem, 64), 64, 0, st>>>(jinv, bary, stress, weight, elem_row, n_rows, n_elem,
                                                                  n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_overlap_strain_3d_affine(const double *jinv, const double *ghat, const double *u_overlap, int n_u,
+                                          const int32_t *elem_dof_lids, int n_int, int n_elem, int n_p, int n_q,
+                                          double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_u < 0) return SSP_ERR_INVALID;
+    if ((long long)n_elem * n_q != n_int) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv || !ghat || !u_overlap || !elem_dof_lids || !out_values) return SSP_ERR_INVALID;
+    // the table plus the displacements of the at most 128 / n_q + 2 elements a block's points cover
+    const size_t smem = sizeof(double) * (3 * (size_t)n_p * n_q + 3 * (size_t)n_p * (kAffineThreads / n_q + 2));
+    if (smem > 48 * 1024) return SSP_ERR_UNSUPPORTED;
+    strain3_affine_kernel<<<grid_for(n_int, kAffineThreads), kAffineThreads, smem, as_stream(stream)>>>(
+        jinv, ghat, u_overlap, elem_dof_lids, n_u, n_elem, n_p, n_q, out_values);
+    return launch_status();
+}
+
+int ssp_assemble_force_element_affine(const double *jinv, const double *ghat, const double *stress,
+                                      const double *weight, const int32_t *elem_row, int n_elem, int n_p, int n_q,
+                                      int n_rows, double *out_values, void *stream) {
+    if (n_elem < 0 || n_p <= 0 || n_q <= 0 || n_rows < 0) return SSP_ERR_INVALID;
+    // a block's threads cover at most 128 / n_p + 2 elements, whose points' T it stages
+    const size_t smem = sizeof(double) * (3 * (size_t)n_p * n_q + 9 * (size_t)(kAffineThreads / n_p + 2) * n_q);
+    if (smem > 48 * 1024) return SSP_ERR_UNSUPPORTED;
+    if (!out_values && n_rows > 0) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (n_rows > 0 && cudaMemsetAsync(out_values, 0, sizeof(double) * n_rows, st) != cudaSuccess) return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv || !ghat || !stress || !weight || !elem_row) return SSP_ERR_INVALID;
+    const long long n = (long long)n_elem * n_p;
+    force3_affine_kernel<<<grid_for(n, kAffineThreads), kAffineThreads, smem, st>>>(jinv, ghat, weight, stress,
+                                                                                    elem_row, n_rows, n_elem, n_p, n_q,
+                                                                                    out_values);
     return launch_status();
 }
 

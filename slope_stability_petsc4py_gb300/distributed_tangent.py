@@ -147,6 +147,9 @@ class OwnedTangentPattern:
     # whether the plain form's regrouped P2 strain and force apply (3D P2, every element affine to
     # rounding); None: not checked
     affine_p2: bool | None = field(default=None, repr=False)
+    # whether the plain form's J^{-1} strain and force apply (3D P1 / P4, every element affine to
+    # rounding); None: not checked
+    affine_fp64: bool | None = field(default=None, repr=False)
 
     # host views of device-resident per-point data (copied on first access)
     def _host(self, key):
@@ -522,6 +525,20 @@ def _p2_affine_inputs(pattern):
     return d if pattern.affine_p2 else None
 
 
+def _affine_fp64_inputs(pattern):
+    """The device arrays with J^{-1} per element and the reference gradient table (FP64) when the
+    pattern is 3D P1 or P4 and every element is affine to rounding (the criterion of
+    _p2_affine_inputs), else None.  Checked once per pattern."""
+    d = pattern.device
+    if pattern.affine_fp64 is None:
+        ok = pattern.dim == 3 and pattern.n_p != 10 and "jinv" in d and _affine_elements(pattern, rtol=1e-12)
+        if ok:
+            table = np.ascontiguousarray(np.transpose(reference_gradients(3, pattern.elem_type), (2, 1, 0)))
+            d["ghat"] = _lib.to_device(table, _lib.torch().float64)  # [n_q][n_p][3]
+        pattern.affine_fp64 = bool(ok)
+    return d if pattern.affine_fp64 else None
+
+
 def _mixed_inputs(pattern):
     """Per-pattern hi + lo pairs of the mixed form's constant inputs, split once and kept with the
     pattern's device arrays: of the gradients and w * gradient, or, when every element is affine,
@@ -574,6 +591,9 @@ def overlap_strain_device(pattern, U, *, mixed: bool = False):
     elif pattern.dim == 3 and _p2_affine_inputs(pattern) is not None:
         _lib.call("ssp_assemble_overlap_strain_3d_p2_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]), _lib.ptr(u_ov),
                   int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_q, _lib.ptr(E), st)
+    elif pattern.dim == 3 and _affine_fp64_inputs(pattern) is not None:
+        _lib.call("ssp_assemble_overlap_strain_3d_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["ghat"]), _lib.ptr(u_ov),
+                  int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p, pattern.n_q, _lib.ptr(E), st)
     elif pattern.dim == 3:
         _lib.call("ssp_assemble_overlap_strain_3d", _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
                   _lib.ptr(u_ov), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n_int, n_el, pattern.n_p, pattern.n_q,
@@ -639,6 +659,11 @@ def owned_force_device(pattern, S_aos, *, mixed: bool = False):
         _lib.call("ssp_assemble_force_element_p2_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]), _lib.ptr(S_aos),
                   _lib.ptr(d["weight"]), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size), pattern.n_q,
                   n_rows, _lib.ptr(F), _lib.stream_handle())
+        return F
+    if pattern.dim == 3 and _affine_fp64_inputs(pattern) is not None:
+        _lib.call("ssp_assemble_force_element_affine", _lib.ptr(d["jinv"]), _lib.ptr(d["ghat"]), _lib.ptr(S_aos),
+                  _lib.ptr(d["weight"]), _lib.ptr(d["elem_row"]), int(pattern.overlap_elements.size), pattern.n_p,
+                  pattern.n_q, n_rows, _lib.ptr(F), _lib.stream_handle())
         return F
     _lib.call("ssp_assemble_force_element", pattern.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
               _lib.ptr(d["dphi3"]) if pattern.dim == 3 else None, _lib.ptr(S_aos), _lib.ptr(d["weight"]),

@@ -555,6 +555,61 @@ def test_p2_affine_strain_and_force_match_gradient_kernels():
         assert err_e <= 1e-13 and err_f <= 1e-13
 
 
+@pytest.mark.parametrize("et,dims", [("P4", (6, 3, 3)), ("P1", (24, 10, 12))])
+def test_affine_fp64_strain_and_force_match_gradient_kernels(oracle, et, dims):
+    """The plain form's J^{-1} strain and force for straight-sided P1 / P4 tetrahedra (reference
+    gradient table in shared memory instead of per-point gradients) against the per-point-gradient
+    kernels and the oracle, on a full and a partial owned node range."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import _lib, synthetic
+    from slope_stability_petsc4py_gb300.distributed_tangent import (
+        _affine_fp64_inputs,
+        _u_overlap_device,
+        overlap_strain_device,
+        owned_force_device,
+        prepare_owned_tangent_pattern,
+    )
+
+    mesh = synthetic.slope_mesh_3d(*dims, elem_type=et, n_layers=4)
+    mats = synthetic.MaterialSet.layered(4, seed=5)
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=0.0, young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.03, seed=6)
+    for rng in ((0, mesh.n_nodes), (mesh.n_nodes // 3, 2 * mesh.n_nodes // 3)):
+        pat = prepare_owned_tangent_pattern(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, rng,
+                                            elem_type=et, include_legacy_scatter=False, keep_slot_metadata=True,
+                                            include_overlap_B=False)
+        d = _affine_fp64_inputs(pat)
+        assert d is not None and pat.affine_fp64
+        E = overlap_strain_device(pat, U)
+        u_ov = _u_overlap_device(pat, U)
+        n_el, n = int(pat.overlap_elements.size), pat.n_local_int
+        E_g = torch.empty_like(E)
+        st = _lib.stream_handle()
+        _lib.call("ssp_assemble_overlap_strain_3d", _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
+                  _lib.ptr(u_ov), int(u_ov.numel()), _lib.ptr(d["dof_lids"]), n, n_el, pat.n_p, pat.n_q,
+                  _lib.ptr(E_g), st)
+        err_e = rel_err(E.cpu().numpy(), E_g.cpu().numpy())
+        S = torch.randn((n, 6), dtype=torch.float64, device="cuda")
+        F = owned_force_device(pat, S)
+        F_g = torch.empty_like(F)
+        _lib.call("ssp_assemble_force_element", 3, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]), _lib.ptr(d["dphi3"]),
+                  _lib.ptr(S), _lib.ptr(d["weight"]), _lib.ptr(d["elem_row"]), n_el, pat.n_p, pat.n_q, int(F.numel()),
+                  _lib.ptr(F_g), st)
+        err_f = rel_err(F.cpu().numpy(), F_g.cpu().numpy())
+        # and the oracle's restatement of the reference's row kernels on the same gradients
+        E_o = oracle.strain_3d(pat.dphi1, pat.dphi2, pat.dphi3, u_ov.cpu().numpy(), pat.overlap_element_dof_lids,
+                               pat.n_q)
+        F_o = oracle.force_rows_3d(pat.dphi1, pat.dphi2, pat.dphi3, S.cpu().numpy(), pat.overlap_assembly_weight,
+                                   pat.row_slot_ptr, pat.slot_elem, pat.slot_lrow, pat.n_q)
+        F_o[~pat.owned_free_mask] = 0.0
+        err_eo, err_fo = rel_err(E.cpu().numpy(), E_o), rel_err(F.cpu().numpy(), F_o)
+        print(f"{et} affine, owned range {rng}: strain {err_e:.2e} / oracle {err_eo:.2e}, "
+              f"force {err_f:.2e} / oracle {err_fo:.2e}")
+        assert max(err_e, err_f) <= 1e-13 and max(err_eo, err_fo) <= PLAIN_RTOL
+
+
 def test_large_mesh_properties():
     """At a benchmark-like size: symmetric == general kernel, K symmetric, linear in DS."""
     import torch
