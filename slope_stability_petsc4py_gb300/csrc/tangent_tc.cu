@@ -16,18 +16,21 @@
 // Accuracy.  A tensor-core MMA rounds its FP32 result once per instruction, so errors grow with
 // the number of MMAs that feed one accumulator.  The points of an element are taken in groups of
 // four (K = 24, three K = 8 steps); each group has its own pair of accumulators (hi*hi: three
-// MMAs, cross terms: six, 2^-11 smaller), and the CUDA cores add every group's two partial sums
-// into compensated (Kahan) FP32 sums in registers (widened exactly to FP64 once per element).  Two accumulator pairs alternate between groups (ping-pong), so the tensor
-// cores multiply group g while the CUDA cores drain group g - 1 and build group g + 1.  The FP64
+// MMAs, cross terms: six, 2^-11 smaller), and every group's two partial sums are added into
+// compensated (Kahan) FP32 sums of the element (widened exactly to FP64 once per element).  The FP64
 // element sums are added to the CSR values with FP64 reductions through the element->CSR map, on
 // both mirror positions of alpha <= beta, so the correction is exactly symmetric.
 //
 // Tile: M = 128 rows (alpha, 105 used), N = 112 columns (beta, 105 used).  One CTA of 512 threads
 // per SM, grid-striding over elements; it owns all 512 tensor-memory columns (two accumulator
-// pairs at columns 0 / 128 and 256 / 384).  One thread issues the MMAs and commits each group to
-// the mbarrier of its buffer.  Warp w drains accumulator lanes 32 (w % 4) .. + 31 (its lane
-// quarter), columns 28 (w / 4) .. + 27.  The element's FP64 sums are staged in shared memory and
-// scattered row by row, so the reductions of a warp fall on neighbouring entries of one CSR row.
+// pairs at columns 0 / 128 and 256 / 384, alternating between groups).  The warps specialise:
+// warps 0-7 build each group's operands into one of two stage buffers and one of their threads
+// issues the group's MMAs; warps 8-15 drain each accumulator pair into the element's compensated
+// sums, which live in shared memory, and scatter the element row by row (so the reductions of a
+// warp fall on neighbouring entries of one CSR row).  The roles hand off through mbarriers (the MMA
+// commit of a pair, and the eight drain warps' release of it) and synchronise inside a role with
+// named barriers, so the builders form group g + 1 while the tensor cores multiply group g and the
+// drain warps read group g - 1 or scatter the previous element.
 //
 // Operand layout in shared memory: K-major, no swizzle, in 8-row x 16-byte core matrices:
 // byte offset(row, kappa) = ((kappa / 4) * (rows / 8) + row / 8) * 128 + (row % 8) * 16 + (kappa % 4) * 4,
@@ -49,11 +52,9 @@ constexpr int kM = 128, kN = 112, kPts = 4, kK = kPts * kNS;  // 24 = three K st
 constexpr int kThreads = 512;
 constexpr int kScatterBatch = 8;                               // map entries a thread loads before its reductions
 constexpr int kTmemCols = 512;                                 // two (hi*hi, cross) accumulator pairs
-constexpr int kColsPerWarp = kN / 4;                           // 28 accumulator columns per drain warp
 constexpr uint32_t kLboA = (kM / 8) * 128, kLboB = (kN / 8) * 128, kSbo = 128;
 constexpr int kABytes = kM * kK * 4, kBBytes = kN * kK * 4;
 static_assert(kABytes % 1024 == 0 && kBBytes % 128 == 0, "operand tiles keep 128-byte alignment");
-static_assert(kColsPerWarp % 4 == 0, "drain loads four columns at a time");
 
 // Instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits 4-5 = 1), A and B TF32
 // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
@@ -74,15 +75,26 @@ struct RawInputs {  // FP64 inputs of the next group, copied ahead by cp.async
     double g[kPts * 3 * kNP];
     double ds[kPts * kNS * kNS], w[kPts * kNS * kNS], sh[kPts * kNS * kNS], la[kPts * kNS * kNS];
 };
+// Warp roles: warps 0-7 build the operands (inputs converted to double-float, H = B^T dD and B
+// split into TF32 pairs, one thread issuing the MMAs); warps 8-15 drain the accumulators into the
+// element's compensated sums and scatter them.  Drain warp w owns tensor-memory lane quarter w % 4
+// (TMEM rows 32 (w % 4) ..+ 31, the row each lane reads) and the column half (w - 8) / 4.
+constexpr int kBuildThreads = 256, kDrainThreads = 256;
+constexpr int kDrainCols = kN / 2;                     // 56 accumulator columns per drain thread
+constexpr int kKeStride = kN + 1;                      // float2 row stride of the element sums (spreads banks)
+constexpr int kBarBuild = 1, kBarDrain = 2;            // named barriers of the two roles
 struct Smem {
     Stage stage[2];
     PointData pts;
     RawInputs raw;
-    double ke[kNLD * kNLD];  // the element's FP64 sums (upper triangle used), staged for a row-wise scatter
-    unsigned long long mbar[2];
+    float2 ke[kNLD * kKeStride];  // the element's compensated FP32 sums (s, c), upper triangle used
+    unsigned long long acc_full[2];   // commit of the MMAs into accumulator pair b (count 1)
+    unsigned long long acc_empty[2];  // the eight drain warps have read pair b (count 8)
     uint32_t tmem_slot;
-    int abort;
-    int nq[2];
+    int abort;   // any role gave up on a wait (the device status has SSP_DEV_TIMEOUT)
+    int babort;  // the builders stop (read only after a builders' barrier)
+    int dabort;  // the drainers stop (read only after a drainers' barrier)
+    int nq;
     int sq[kNQ];
 };
 // Dynamic shared memory requested: more than half of an SM's, so one CTA (which owns all of the
@@ -110,29 +122,6 @@ __device__ __forceinline__ void tmem_ld16f(uint32_t taddr, float *v) {
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
-// The 28 accumulator columns col0 .. col0 + 27 of this thread's lane.
-__device__ __forceinline__ void tmem_ld28(uint32_t taddr0, uint32_t *r) {
-    tmem_ld16(taddr0, r);
-    tmem_ld8(taddr0 + 16, r + 16);
-    tmem_ld4(taddr0 + 24, r + 24);
-}
-
-// Compensated (Kahan) running sums of the groups' partials: sum[j] - comp[j] is the element's
-// value of column j; each group adds its hi*hi and cross partials.
-__device__ __forceinline__ void drain_add(uint32_t taddr_hh, uint32_t taddr_x, float *sum, float *comp) {
-    uint32_t rh[kColsPerWarp], rx[kColsPerWarp];
-    tmem_ld28(taddr_hh, rh);
-    tmem_ld28(taddr_x, rx);
-    tmem_wait_ld();
-#pragma unroll
-    for (int j = 0; j < kColsPerWarp; ++j) {
-        const float x = __fadd_rn(__uint_as_float(rh[j]), __uint_as_float(rx[j]));
-        const float y = __fsub_rn(x, comp[j]);
-        const float t = __fadd_rn(sum[j], y);
-        comp[j] = __fsub_rn(__fsub_rn(t, sum[j]), y);
-        sum[j] = t;
-    }
-}
 
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
@@ -146,19 +135,280 @@ __device__ __forceinline__ double elastic_d3(int i, int j, double G, double lam)
     return 0.0;
 }
 
-// Every thread waits for the commit of group parity b (bounded), then adds that group's two
-// accumulators to its compensated sums.
-__device__ __forceinline__ void drain_group(Smem &S, uint32_t tmem, int b, uint32_t &phase_bits, uint32_t lane_col,
-                                            float *sum, float *comp) {
-    if (!mbar_wait(smem_u32(&S.mbar[b]), (phase_bits >> b) & 1u)) {
-        S.abort = 1;
-        flag(SSP_DEV_TIMEOUT);
+__device__ __forceinline__ void named_bar(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_count(uint32_t addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+__device__ __forceinline__ long long element_at(const int32_t *elist, long long it, int n_elem) {
+    if (!elist) return it;
+    const long long e = elist[it];
+    return (e < 0 || e >= n_elem) ? -1 : e;
+}
+
+// Builders: per group of four plastic points, the inputs (copied one group ahead by cp.async, each
+// thread converting the entries it copied), then H = B^T dD (compensated double-float dot products)
+// and the nonzeros of B, both split into TF32 pairs, into the stage buffer of the group's parity;
+// one thread issues the nine MMAs into the accumulator pair of that parity and commits them to
+// acc_full.  A stage buffer is rewritten only after the MMAs that read it (two groups back) have
+// completed, an accumulator pair only after the drain warps have read it (acc_empty).
+__device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double *__restrict__ d1,
+                                           const double *__restrict__ d2, const double *__restrict__ d3,
+                                           const double *__restrict__ DS, const double *__restrict__ w,
+                                           const int8_t *__restrict__ branch, const double *__restrict__ shear,
+                                           const double *__restrict__ lame, int n_elem, double scale,
+                                           const int32_t *__restrict__ elist, long long n_iter) {
+    const int bt = threadIdx.x, warp = bt >> 5, lane = bt & 31;
+    uint32_t G = 0;  // the CTA's running group count (the drain warps count the same sequence)
+    for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
+        const long long e = element_at(elist, it, n_elem);
+        if (e < 0) {  // uniform
+            if (bt == 0) flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const long long g0 = e * kNQ;
+        if (warp == 0) {
+            const bool pl = lane < kNQ && branch[g0 + lane] != 0;
+            const unsigned mask = __ballot_sync(0xffffffffu, pl);
+            if (pl) S.sq[__popc(mask & ((1u << lane) - 1u))] = lane;
+            if (lane == 0) S.nq = __popc(mask);
+        }
+        named_bar(kBarBuild, kBuildThreads);
+        const int nq = S.nq;
+        if (nq == 0) continue;  // uniform
+        const int groups = (nq + kPts - 1) / kPts;
+        // raw FP64 inputs of group grp: thread t copies gradient values t, t + 256 (< 420) and,
+        // for t < 144, one DS entry with its point's w, shear and lame
+        auto load_group = [&](int grp) {
+            for (int i = bt; i < kPts * 3 * kNP; i += kBuildThreads) {
+                const int gi_pi = i / (3 * kNP), gi_r = (i % (3 * kNP)) / kNP, gi_a = i % kNP;
+                const int k = grp * kPts + gi_pi;
+                if (k < nq) {
+                    const long long src = (g0 + S.sq[k]) * kNP + gi_a;
+                    cp_async8(&S.raw.g[i], (gi_r == 0 ? d1 : (gi_r == 1 ? d2 : d3)) + src);
+                }
+            }
+            if (bt < kPts * kNS * kNS) {
+                const int k = grp * kPts + bt / (kNS * kNS);
+                if (k < nq) {
+                    const long long gq = g0 + S.sq[k];
+                    cp_async8(&S.raw.ds[bt], DS + gq * (kNS * kNS) + bt % (kNS * kNS));
+                    cp_async8(&S.raw.w[bt], w + gq);
+                    cp_async8(&S.raw.sh[bt], shear + gq);
+                    cp_async8(&S.raw.la[bt], lame + gq);
+                }
+            }
+            cp_async_commit();
+        };
+        load_group(0);
+        for (int grp = 0; grp < groups; ++grp, ++G) {
+            const int b = G & 1;
+            cp_async_wait_all();
+            for (int i = bt; i < kPts * 3 * kNP; i += kBuildThreads) {
+                const int gi_pi = i / (3 * kNP), gi_r = (i % (3 * kNP)) / kNP, gi_a = i % kNP;
+                const int k = grp * kPts + gi_pi;
+                S.pts.g[gi_pi][gi_r][gi_a] = k < nq ? df_from_f64(S.raw.g[i]) : df32{0.0f, 0.0f};
+            }
+            if (bt < kPts * kNS * kNS) {
+                const int di_pi = bt / (kNS * kNS), di_kk = bt % (kNS * kNS);
+                const int k = grp * kPts + di_pi;
+                df32 v{0.0f, 0.0f};
+                if (k < nq) {
+                    double d = S.raw.ds[bt];
+                    const double de = elastic_d3(di_kk % kNS, di_kk / kNS, S.raw.sh[bt], S.raw.la[bt]);
+                    if (de != 0.0) d -= de;
+                    v = df_mul(df_from_f64(d), df_from_f64(scale * S.raw.w[bt]));
+                }
+                S.pts.dD[di_pi][di_kk] = v;
+            }
+            if (bt == 0) {  // stage b was last read by the MMAs of group G - 2
+                if (S.abort) {
+                    S.babort = 1;
+                } else if (G >= 2 && !mbar_wait(smem_u32(&S.acc_full[b]), ((G - 2) >> 1) & 1u)) {
+                    S.babort = S.abort = 1;
+                    flag(SSP_DEV_TIMEOUT);
+                }
+            }
+            named_bar(kBarBuild, kBuildThreads);  // inputs converted, stage b free
+            if (S.babort) {
+                cp_async_wait_all();
+                return;
+            }
+            if (grp + 1 < groups) load_group(grp + 1);
+            Stage &st = S.stage[b];
+            unsigned char *a_hi = reinterpret_cast<unsigned char *>(st.a_hi);
+            unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
+            unsigned char *b_hi = reinterpret_cast<unsigned char *>(st.b_hi);
+            unsigned char *b_lo = reinterpret_cast<unsigned char *>(st.b_lo);
+            // H = B^T dD: item (point, alpha, half) forms three strain components of one row,
+            // compensated dot products of three terms on the FP32 pipe; alpha = 3 * node + component
+            for (int i = bt; i < kPts * kNLD * 2; i += kBuildThreads) {
+                const int half = i & 1, rest = i >> 1;
+                const int pi = rest / kNLD, alpha = rest - pi * kNLD;
+                const int a = alpha / 3, c = alpha - 3 * a;
+                const df32 ga = S.pts.g[pi][0][a], gb = S.pts.g[pi][1][a], gc = S.pts.g[pi][2][a];
+                const int k0 = bt_row3(c, 0), k1 = bt_row3(c, 1), k2 = bt_row3(c, 2);
+                const df32 *D = S.pts.dD[pi];
+#pragma unroll
+                for (int mm = 0; mm < 3; ++mm) {
+                    const int m = 3 * half + mm;
+                    const df32 h = df_dot3(ga, D[k0 + kNS * m], gb, D[k1 + kNS * m], gc, D[k2 + kNS * m]);
+                    uint32_t hi, lo;
+                    split_tf32(h, hi, lo);
+                    const int off = kmaj_off<4>(alpha, pi * kNS + m, kM);
+                    *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
+                    *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
+                }
+            }
+            // the nonzeros of Bk: g[pi][r][bn] at beta = 3 bn + cp, kappa = 6 pi + bt_row3(cp, r); the
+            // other entries are zero in every group and were zeroed once
+            for (int i = bt; i < kPts * 3 * kNP * 3; i += kBuildThreads) {
+                const int cp = i % 3, rest = i / 3, bn = rest % kNP, pr = rest / kNP, r = pr % 3, pi = pr / 3;
+                uint32_t hi, lo;
+                split_tf32(S.pts.g[pi][r][bn], hi, lo);
+                const int off = kmaj_off<4>(3 * bn + cp, pi * kNS + bt_row3(cp, r), kN);
+                *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
+                *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
+            }
+            fence_async_smem();  // generic-proxy writes -> visible to the tensor cores
+            named_bar(kBarBuild, kBuildThreads);  // stage b complete
+            if (bt == 0) {
+                bool ok = !S.abort;
+                if (ok && G >= 2 && !mbar_wait(smem_u32(&S.acc_empty[b]), ((G - 2) >> 1) & 1u)) {
+                    ok = false;
+                    S.abort = 1;
+                    flag(SSP_DEV_TIMEOUT);
+                }
+                if (ok) {
+                    fence_after_sync();
+                    const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+                    const uint32_t t_hh = tmem + 256u * b, t_x = t_hh + 128u;
+#pragma unroll
+                    for (int s = 0; s < kK / 8; ++s) {
+                        const uint32_t oa = s * 2 * kLboA, ob = s * 2 * kLboB;
+                        mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc,
+                                 s != 0 ? 1u : 0u);
+                        mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), kIdesc,
+                                 s != 0 ? 1u : 0u);
+                        mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, 1u);
+                    }
+                    mma_commit(smem_u32(&S.acc_full[b]));
+                } else {
+                    S.babort = 1;  // seen by the builders after their next barrier
+                }
+            }
+        }
     }
-    phase_bits ^= 1u << b;
-    fence_after_sync();
-    const uint32_t base = tmem + lane_col + 256u * b;
-    drain_add(base, base + 128u, sum, comp);  // hi * hi, hi * lo + lo * hi
-    fence_before_sync();                      // these reads precede the next MMAs into this pair
+    cp_async_wait_all();
+}
+
+// Drain warps: per group, one lane waits for the commit (acc_full of the group's parity), the warp
+// reads its 32 accumulator rows x 56 columns of both accumulators (hi * hi, cross terms) and adds
+// their sum into the element's compensated sums in shared memory (upper triangle only), then
+// releases the pair (acc_empty).  After an element's last group the 256 drain threads scatter the
+// element's sums to both mirror positions through the element -> CSR map with FP64 reductions.
+__device__ __forceinline__ void drain_role(Smem &S, uint32_t tmem, const int8_t *__restrict__ branch,
+                                           const int32_t *__restrict__ emap, int n_elem, long long nnz,
+                                           double *__restrict__ values, const int32_t *__restrict__ elist,
+                                           long long n_iter) {
+    const int dt = threadIdx.x - kBuildThreads, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lq = warp & 3, chalf = (warp - kBuildThreads / 32) >> 2;
+    const int row = 32 * lq + lane, col0 = kDrainCols * chalf;
+    const uint32_t lane_col = (static_cast<uint32_t>(32 * lq) << 16) + static_cast<uint32_t>(col0);
+    float2 *kr = S.ke + row * kKeStride;  // this lane's row of sums (row < kNLD)
+    uint32_t G = 0;
+    for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
+        const long long e = element_at(elist, it, n_elem);
+        if (e < 0) continue;  // uniform (the builders flag it)
+        const bool pl = lane < kNQ && branch[e * kNQ + lane] != 0;
+        const int nq = __popc(__ballot_sync(0xffffffffu, pl));
+        if (nq == 0) continue;
+        const int groups = (nq + kPts - 1) / kPts;
+        if (row < kNLD) {
+            for (int j = 0; j < kDrainCols; ++j) {
+                const int c = col0 + j;
+                if (c >= row && c < kNLD) kr[c] = make_float2(0.0f, 0.0f);
+            }
+        }
+        bool skipped = false;
+        for (int grp = 0; grp < groups; ++grp, ++G) {
+            const int b = G & 1;
+            int ok = 0;
+            if (lane == 0) {
+                ok = !S.abort;
+                if (ok && !mbar_wait(smem_u32(&S.acc_full[b]), (G >> 1) & 1u)) {
+                    ok = 0;
+                    S.abort = 1;
+                    flag(SSP_DEV_TIMEOUT);
+                }
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (ok) {
+                fence_after_sync();
+                const uint32_t base = tmem + lane_col + 256u * b;
+#pragma unroll
+                for (int part = 0; part < 2; ++part) {  // 28 columns at a time
+                    uint32_t rh[28], rx[28];
+                    const uint32_t t0 = base + 28u * part;
+                    tmem_ld16(t0, rh);
+                    tmem_ld8(t0 + 16u, rh + 16);
+                    tmem_ld4(t0 + 24u, rh + 24);
+                    tmem_ld16(t0 + 128u, rx);
+                    tmem_ld8(t0 + 144u, rx + 16);
+                    tmem_ld4(t0 + 152u, rx + 24);
+                    tmem_wait_ld();
+                    if (row < kNLD) {
+#pragma unroll
+                        for (int j = 0; j < 28; ++j) {
+                            const int c = col0 + 28 * part + j;
+                            if (c >= row && c < kNLD) {
+                                const float x = __fadd_rn(__uint_as_float(rh[j]), __uint_as_float(rx[j]));
+                                const float2 v = kr[c];
+                                const float y = __fsub_rn(x, v.y);
+                                const float t = __fadd_rn(v.x, y);
+                                kr[c] = make_float2(t, __fsub_rn(__fsub_rn(t, v.x), y));
+                            }
+                        }
+                    }
+                }
+                fence_before_sync();  // these reads precede the next MMAs into this pair
+            } else {
+                skipped = true;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&S.acc_empty[b]));
+        }
+        if (skipped && lane == 0) S.dabort = 1;
+        named_bar(kBarDrain, kDrainThreads);  // the element's sums are complete
+        if (S.dabort) return;
+        // every entry, row by row (consecutive threads -> consecutive columns of one CSR row, so the
+        // reductions of a warp share cache lines); the map row (44 KB, not staged) is read
+        // kScatterBatch entries per thread at a time, so a thread's loads are in flight together
+        const int32_t *em = emap + e * kNLD * kNLD;
+        for (int base = dt; base < kNLD * kNLD; base += kDrainThreads * kScatterBatch) {
+            int32_t pp[kScatterBatch];
+#pragma unroll
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kDrainThreads;
+                pp[u] = idx < kNLD * kNLD ? em[idx] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kDrainThreads;
+                if (pp[u] < 0) continue;
+                const int a = idx / kNLD, bcol = idx - a * kNLD;
+                const float2 v = bcol >= a ? S.ke[a * kKeStride + bcol] : S.ke[bcol * kKeStride + a];
+                const double val = df_to_f64({v.x, -v.y});
+                if (pp[u] < nnz) red_add(values + pp[u], val);
+                else flag(SSP_DEV_BAD_INDEX);
+            }
+        }
+        named_bar(kBarDrain, kDrainThreads);  // the sums are read before their owners reset them
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
@@ -169,201 +419,34 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
     const int32_t *__restrict__ elist_count) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem &S = *reinterpret_cast<Smem *>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int lq = warp & 3, cq = warp >> 2;  // drain lane quarter and column quarter
-    const uint32_t lane_col = (static_cast<uint32_t>(32 * lq) << 16) + static_cast<uint32_t>(kColsPerWarp * cq);
-
+    const int tid = threadIdx.x, warp = tid >> 5;
     // zero both stages once: the padding rows (alpha >= 105, beta >= 105) are never written again
     for (int i = tid; i < (int)(sizeof(Stage) * 2 / 4); i += kThreads) reinterpret_cast<uint32_t *>(S.stage)[i] = 0u;
     if (tid == 0) {
-        mbar_init(smem_u32(&S.mbar[0]));
-        mbar_init(smem_u32(&S.mbar[1]));
-        S.abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init(smem_u32(&S.acc_full[0]));
+        mbar_init(smem_u32(&S.acc_full[1]));
+        mbar_init_count(smem_u32(&S.acc_empty[0]), kDrainThreads / 32);
+        mbar_init_count(smem_u32(&S.acc_empty[1]), kDrainThreads / 32);
+        S.abort = S.babort = S.dabort = 0;
+        mbar_init_fence();
     }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_slot)),
-                     "r"(kTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
+    if (warp == 0) tmem_alloc(&S.tmem_slot, kTmemCols);
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = S.tmem_slot;
-    uint32_t phase_bits = 0;
-    int parity = 0;
-
     const long long n_iter = elist ? static_cast<long long>(*elist_count) : static_cast<long long>(n_elem);
-    for (long long it = blockIdx.x; it < n_iter; it += gridDim.x, parity ^= 1) {
-        long long e = it;
-        if (elist) {
-            e = elist[it];
-            if (e < 0 || e >= n_elem) {  // uniform across the CTA
-                if (tid == 0) flag(SSP_DEV_BAD_INDEX);
-                continue;
-            }
-        }
-        const long long g0 = e * kNQ;
-        if (warp == 0) {
-            const bool pl = lane < kNQ && branch[g0 + lane] != 0;
-            const unsigned mask = __ballot_sync(0xffffffffu, pl);
-            if (pl) S.sq[__popc(mask & ((1u << lane) - 1u))] = lane;
-            if (lane == 0) S.nq[parity] = __popc(mask);
-        }
-        __syncthreads();
-        const int nq = S.nq[parity];
-        if (nq == 0) continue;  // uniform across the CTA
-        const int groups = (nq + kPts - 1) / kPts;
-        float sum[kColsPerWarp], comp[kColsPerWarp];
-#pragma unroll
-        for (int j = 0; j < kColsPerWarp; ++j) sum[j] = comp[j] = 0.0f;
-        // the raw FP64 inputs of a group are copied into shared memory one group ahead (cp.async, in
-        // flight while the current group's H is formed and multiplied): thread t < 420 one gradient
-        // value, thread t < 144 one DS entry with its point's w, shear and lame; each thread later
-        // converts only the entries it copied itself
-        // (indices recomputed from tid where used: cheaper than keeping them live across the loop)
-        auto load_group = [&](int grp) {
-            if (tid < kPts * 3 * kNP) {
-                const int gi_pi = tid / (3 * kNP), gi_r = (tid % (3 * kNP)) / kNP, gi_a = tid % kNP;
-                const int k = grp * kPts + gi_pi;
-                if (k < nq) {
-                    const long long src = (g0 + S.sq[k]) * kNP + gi_a;
-                    cp_async8(&S.raw.g[tid], (gi_r == 0 ? d1 : (gi_r == 1 ? d2 : d3)) + src);
-                }
-            }
-            if (tid < kPts * kNS * kNS) {
-                const int k = grp * kPts + tid / (kNS * kNS);
-                if (k < nq) {
-                    const long long gq = g0 + S.sq[k];
-                    cp_async8(&S.raw.ds[tid], DS + gq * (kNS * kNS) + tid % (kNS * kNS));
-                    cp_async8(&S.raw.w[tid], w + gq);
-                    cp_async8(&S.raw.sh[tid], shear + gq);
-                    cp_async8(&S.raw.la[tid], lame + gq);
-                }
-            }
-            cp_async_commit();
-        };
-        load_group(0);
-        for (int grp = 0; grp < groups; ++grp) {
-            const int b = grp & 1;  // stage buffer and accumulator pair; both were released by drain(grp - 2)
-            // inputs of the group's points as hi + lo pairs (absent slots are zero): the gradients,
-            // and w s (DS - D_el) with the FP64 subtraction only where D_el is nonzero
-            cp_async_wait_all();
-            if (tid < kPts * 3 * kNP) {
-                const int gi_pi = tid / (3 * kNP), gi_r = (tid % (3 * kNP)) / kNP, gi_a = tid % kNP;
-                const int k = grp * kPts + gi_pi;
-                S.pts.g[gi_pi][gi_r][gi_a] = k < nq ? df_from_f64(S.raw.g[tid]) : df32{0.0f, 0.0f};
-            }
-            if (tid < kPts * kNS * kNS) {
-                const int di_pi = tid / (kNS * kNS), di_kk = tid % (kNS * kNS);
-                const int k = grp * kPts + di_pi;
-                df32 v{0.0f, 0.0f};
-                if (k < nq) {
-                    double d = S.raw.ds[tid];
-                    const double de = elastic_d3(di_kk % kNS, di_kk / kNS, S.raw.sh[tid], S.raw.la[tid]);
-                    if (de != 0.0) d -= de;
-                    v = df_mul(df_from_f64(d), df_from_f64(scale * S.raw.w[tid]));
-                }
-                S.pts.dD[di_pi][di_kk] = v;
-            }
-            __syncthreads();
-            if (grp + 1 < groups) load_group(grp + 1);
-            Stage &st = S.stage[b];
-            unsigned char *a_hi = reinterpret_cast<unsigned char *>(st.a_hi);
-            unsigned char *a_lo = reinterpret_cast<unsigned char *>(st.a_lo);
-            unsigned char *b_hi = reinterpret_cast<unsigned char *>(st.b_hi);
-            unsigned char *b_lo = reinterpret_cast<unsigned char *>(st.b_lo);
-            if (tid < kPts * kNLD) {
-                // H = B^T dD for one (point, alpha), all six strain components: compensated dot
-                // products of three terms on the FP32 pipe; alpha = 3 * node + component
-                const int pi = tid / kNLD, alpha = tid - pi * kNLD;
-                const int a = alpha / 3, c = alpha - 3 * a;
-                const df32 ga = S.pts.g[pi][0][a], gb = S.pts.g[pi][1][a], gc = S.pts.g[pi][2][a];
-                const int k0 = bt_row3(c, 0), k1 = bt_row3(c, 1), k2 = bt_row3(c, 2);
-                const df32 *D = S.pts.dD[pi];
-#pragma unroll
-                for (int m = 0; m < kNS; ++m) {
-                    const df32 h = df_dot3(ga, D[k0 + kNS * m], gb, D[k1 + kNS * m], gc, D[k2 + kNS * m]);
-                    uint32_t hi, lo;
-                    split_tf32(h, hi, lo);
-                    const int off = kmaj_off<4>(alpha, pi * kNS + m, kM);
-                    *reinterpret_cast<uint32_t *>(a_hi + off) = hi;
-                    *reinterpret_cast<uint32_t *>(a_lo + off) = lo;
-                }
-            } else {
-                // the nonzeros of Bk: g[pi][r][bn] at beta = 3 bn + cp, kappa = 6 pi + bt_row3(cp, r); the
-                // other entries are zero in every group and were zeroed once
-                for (int i = tid - kPts * kNLD; i < kPts * 3 * kNP * 3; i += kThreads - kPts * kNLD) {
-                    const int cp = i % 3, rest = i / 3, bn = rest % kNP, pr = rest / kNP, r = pr % 3, pi = pr / 3;
-                    uint32_t hi, lo;
-                    split_tf32(S.pts.g[pi][r][bn], hi, lo);
-                    const int off = kmaj_off<4>(3 * bn + cp, pi * kNS + bt_row3(cp, r), kN);
-                    *reinterpret_cast<uint32_t *>(b_hi + off) = hi;
-                    *reinterpret_cast<uint32_t *>(b_lo + off) = lo;
-                }
-            }
-            fence_async_smem();  // generic-proxy writes -> visible to the tensor cores
-            __syncthreads();
-            if (S.abort) break;
-            if (tid == 0) {
-                fence_after_sync();
-                const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-                const uint32_t t_hh = tmem + 256u * b, t_x = t_hh + 128u;
-#pragma unroll
-                for (int s = 0; s < kK / 8; ++s) {
-                    const uint32_t oa = s * 2 * kLboA, ob = s * 2 * kLboB;
-                    mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, s != 0 ? 1u : 0u);
-                    mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), kIdesc, s != 0 ? 1u : 0u);
-                    mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, 1u);
-                }
-                mma_commit(smem_u32(&S.mbar[b]));
-            }
-            if (grp >= 1) drain_group(S, tmem, b ^ 1, phase_bits, lane_col, sum, comp);
-        }
-        if (S.abort) break;
-        drain_group(S, tmem, (groups - 1) & 1, phase_bits, lane_col, sum, comp);
-        __syncthreads();  // also orders this element's shared-memory reads before the next element's writes
-        if (S.abort) break;
-        // stage the upper triangle, then scatter every entry row by row (consecutive threads ->
-        // consecutive columns of one CSR row, so the reductions of a warp share cache lines)
-        const int row = 32 * lq + lane;
-        if (row < kNLD) {
-#pragma unroll
-            for (int j = 0; j < kColsPerWarp; ++j) {
-                const int beta = kColsPerWarp * cq + j;
-                if (beta >= row && beta < kNLD) S.ke[row * kNLD + beta] = df_to_f64({sum[j], -comp[j]});
-            }
-        }
-        __syncthreads();
-        // the element's map row (44 KB, not staged) is read kScatterBatch entries per thread at a
-        // time, so a thread's loads are in flight together before its reductions
-        const int32_t *em = emap + (long long)e * kNLD * kNLD;
-        for (int base = tid; base < kNLD * kNLD; base += kThreads * kScatterBatch) {
-            int32_t p[kScatterBatch];
-#pragma unroll
-            for (int u = 0; u < kScatterBatch; ++u) {
-                const int idx = base + u * kThreads;
-                p[u] = idx < kNLD * kNLD ? em[idx] : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < kScatterBatch; ++u) {
-                const int idx = base + u * kThreads;
-                if (p[u] < 0) continue;
-                const int a = idx / kNLD, bcol = idx - a * kNLD;
-                const double val = bcol >= a ? S.ke[idx] : S.ke[bcol * kNLD + a];
-                if (p[u] < nnz) red_add(values + p[u], val);
-                else flag(SSP_DEV_BAD_INDEX);
-            }
-        }
-    }
-    // all tensor-core work of this CTA has been waited for (or abandoned after a timeout)
+    if (tid < kBuildThreads)
+        build_role(S, tmem, d1, d2, d3, DS, w, branch, shear, lame, n_elem, scale, elist, n_iter);
+    else
+        drain_role(S, tmem, branch, emap, n_elem, nnz, values, elist, n_iter);
+    // every MMA has been drained (or abandoned after a timeout)
     fence_before_sync();
     __syncthreads();
     if (warp == 0) {
         fence_after_sync();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        tmem_dealloc(tmem, kTmemCols);
     }
 }
 
