@@ -396,17 +396,28 @@ def time_steps(torch, step, warmup, steps):
     return e0.elapsed_time(e1) / steps
 
 
-def train_branch_model(torch, op, w, *, max_per_state=500_000):
+def train_branch_model(torch, op, w, *, total=5_000_000, max_per_state=500_000):
     """Train the branch-proposal network on the exact return mapping's (features, branch) pairs of a
-    strength-reduction sequence: the last Newton iterate of each of its ten lambda steps (plastic
-    fraction about 2 % to 35 %), at most max_per_state screen-listed points per state.  The timed
-    states are not among them."""
+    strength-reduction sequence: every Newton iterate of its ten lambda steps (plastic fraction about
+    2 % to 40 %), at most max_per_state screen-listed points of each, then a seeded uniform sample of
+    `total` of them.  The timed states are not among them."""
     from slope_stability_petsc4py_gb300 import learned
 
     t0 = time.perf_counter()
-    states = [(lam, torch.as_tensor(U, device="cuda")) for k, it, lam, U in ssr_states(w) if it == SSR_ITERS - 1]
-    X, y = learned.collect_training_data(op, states, max_per_state=max_per_state)
-    del states
+    Xs, ys = [], []
+    for k, it, lam, U in ssr_states(w):
+        X, y = learned.collect_training_data(op, [(lam, torch.as_tensor(U, device="cuda"))],
+                                             max_per_state=max_per_state, seed=7 * k + it)
+        Xs.append(X)
+        ys.append(y)
+    X, y = torch.cat(Xs), torch.cat(ys)
+    del Xs, ys
+    collected = int(X.shape[0])
+    if collected > total:
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(11)
+        pick = torch.randperm(collected, device="cuda", generator=gen)[:total]
+        X, y = X.index_select(0, pick).contiguous(), y.index_select(0, pick).contiguous()
     model = learned.BranchProposal(seed=0)
     epochs = 4
     hist = model.train(X, y, epochs=epochs, batch=16384, lr=3e-3)
@@ -414,11 +425,12 @@ def train_branch_model(torch, op, w, *, max_per_state=500_000):
     op.branch_model = model
     counts = torch.bincount(y.long(), minlength=5).cpu().numpy()
     op.reduction(LAMBDA)
-    return {"training_samples": int(X.shape[0]), "samples": "points the elastic screen lists",
+    return {"training_samples": int(X.shape[0]), "collected": collected, "samples": "points the elastic screen lists",
             "label_counts": {b: int(c) for b, c in zip(learned.BRANCHES, counts)}, "epochs": epochs, "batch": 16384,
             "final_loss": hist[-1][0], "final_train_accuracy": hist[-1][1], "training_s": time.perf_counter() - t0,
-            "training_states": f"the last iterate of each of the {SSR_STEPS} lambda steps of the strength-reduction "
-                               f"sequence (lambda 1.0..1.45), at most {max_per_state:,} listed points each"}
+            "training_states": f"every Newton iterate ({SSR_STEPS} lambda steps x {SSR_ITERS}) of the strength-reduction "
+                               f"sequence (lambda 1.0..1.45), at most {max_per_state:,} listed points each, then "
+                               f"{total:,} drawn uniformly"}
 
 
 def compare_forms(torch, lib, op, w, states_dev, args, ms_plain):

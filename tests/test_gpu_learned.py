@@ -142,3 +142,49 @@ def test_training_learns_the_branches_and_gains(cuda_device):
     print(f"distinct branches per warp over the listed points: screen order {mix_natural:.3f}, "
           f"learned bins {mix_learned:.3f}")
     assert mix_learned < mix_natural
+
+
+def test_binning_sources_gain_time_over_the_unsorted_return_mapping(cuda_device):
+    """Time of the return mapping on the 100,800-element benchmark slope (1.1 M points) with each
+    binning source -- none (unsorted, one divergent pass), the exact screen-decide binning, the
+    previous iteration's branches, the trained network's proposal -- with identical results.  Each
+    binned form must beat the unsorted pass by at least 5 %."""
+    import torch
+
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, learned, synthetic
+
+    w = synthetic.config_workload("3d_p2_homo")
+    mesh = w.mesh
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, w.specs,
+                                        elem_type=mesh.elem_type)
+    op.host_outputs = False
+    train = [(float(lam), torch.as_tensor(w.G + (f * w.amp) * w.V, device="cuda"))
+             for lam, f in zip(np.linspace(1.0, 1.3, 6), np.linspace(0.5, 1.6, 6))]
+    X, y = learned.collect_training_data(op, train)
+    model = learned.BranchProposal(seed=0)
+    model.train(X, y, epochs=4, batch=8192, lr=3e-3)
+    op.branch_model = model
+    U = torch.as_tensor(w.G + (1.05 * w.amp) * w.V, device="cuda")  # a state outside the training set
+    op.reduction(1.1)
+    times, outs = {}, {}
+    for mode in ("unsorted", "binned", "previous", "learned"):
+        op.return_mapping = mode
+        op.constitutive_problem_stress_tangent(U)  # warm-up (and the previous codes for "previous")
+        ts = []
+        for _ in range(7):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            op.constitutive_problem_stress_tangent(U)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        times[mode] = float(np.median(ts))
+        outs[mode] = (op._S_aos.clone(), op._owned_local_DS.aos.clone(), op._branch.clone())
+    print("return mapping, ms:", {k: round(v, 3) for k, v in times.items()},
+          "plastic fraction", round(float((outs["binned"][2] != 0).float().mean()), 4))
+    for mode in ("binned", "previous", "learned"):
+        assert torch.equal(outs[mode][2], outs["unsorted"][2])
+        assert rel_err(outs[mode][0].cpu().numpy(), outs["unsorted"][0].cpu().numpy()) <= 1e-14
+        assert rel_err(outs[mode][1].cpu().numpy(), outs["unsorted"][1].cpu().numpy()) <= PLAIN_RTOL
+        assert times[mode] < 0.95 * times["unsorted"], (mode, times)
