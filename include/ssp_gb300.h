@@ -298,6 +298,26 @@ int ssp_tangent_plastic_correction(int dim, const double *dphi1, const double *d
 int ssp_plastic_elements(const int8_t *branch, int n_elem, int n_q, int32_t *list_out, int32_t *count_out,
                          void *stream);
 
+/* No reference counterpart.  The plastic elements (elements with a point whose branch is not 0)
+ * split by their number of plastic points: fewer than min_points into list_few, at least
+ * min_points into list_many (each n_elem long; the counts are zeroed first). */
+int ssp_plastic_elements_split(const int8_t *branch, int n_elem, int n_q, int min_points, int32_t *list_few,
+                               int32_t *count_few, int32_t *list_many, int32_t *count_many, void *stream);
+
+/* No reference counterpart; the same result as ssp_tangent_plastic_correction (3D P2) to rounding.
+ * The plastic correction of straight-sided P2 tetrahedra in moment form: with the gradients linear
+ * in the barycentric coordinates, an element's correction is assembled from the ten moments
+ * sum_q lambda_qm lambda_qn w_q s (DS_q - D_el,q) of its plastic points (jinv [n_elem][3][3], row k
+ * the gradient of barycentric coordinate k+1; bary [n_q][4] the points' barycentric coordinates),
+ * about 8,200 + 231 n_pl FP64 operations per element instead of about 1,935 per plastic point.
+ * Visits the elements of elem_list[0 .. *elem_count) (e.g. list_many of ssp_plastic_elements_split);
+ * n_q <= 11. */
+int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *bary, const double *ds,
+                                              const double *weight, const int8_t *branch, const double *shear,
+                                              const double *lame, const int32_t *scatter_map, int n_elem, int n_q,
+                                              long long nnz_out, double scale, double *out_values,
+                                              const int32_t *elem_list, const int32_t *elem_count, void *stream);
+
 /* Mixed-precision form of ssp_tangent_plastic_correction.  H = B^T (w * scale * (DS - D_el)) is
  * formed in FP64 and split into hi + lo parts.  P1/P2 elements: the products B^T H are taken and
  * accumulated in FP32 on the CUDA cores.  P4 elements (3D, 35 nodes, 24 points): the element's

@@ -1079,6 +1079,238 @@ __global__ void fill_elastic_ds_kernel(const int8_t *__restrict__ branch, const 
     DS[t] = elastic_d<DIM>(kk % NS, kk / NS, shear[g], lame[g]);
 }
 
+// ---------------------------------------------------------------------------- P2 correction, moment form
+//
+// The plastic correction K_e = sum_q B_q^T dD_q B_q of a straight-sided P2 tetrahedron, regrouped.
+// Every shape-function gradient is linear in the barycentric coordinates, grad phi_a(q) =
+// sum_m lambda_qm c_am grad lambda_k(a,m): vertex i has c = 4 delta_im - 1 and k = i; the edge node
+// (i, j) has c = 4 with k = j for m = i and k = i for m = j.  Hence
+//   K_e[(a,c),(b,d)] = sum_{m,n} c_am c_bn R_mn[(k(a,m), c), (k(b,n), d)],
+//   R_mn = beta^T M_mn beta,   M_mn = sum_q lambda_qm lambda_qn dD_q   (ten pairs m <= n),
+// where beta_(k,c) is the strain of grad lambda_k (x) e_c (three nonzeros).  FP64 work per element:
+// 21 n_pl (dD) + 210 n_pl (moments) + 2,160 (beta^T M) + 2,340 (R) + 3,660 (K) instead of about
+// 1,935 per plastic point for the point-by-point contraction: fewer from six plastic points up, and
+// half for a fully plastic 11-point element.  Elements with fewer plastic points keep the
+// point-by-point kernel (the element lists are split by ssp_plastic_elements_split).  The result is
+// the reference's contraction (assemble_tangent_values_3d.c:135-214) regrouped: equal to rounding.
+constexpr int kMomWarps = 4, kMaxQ = 11;
+
+struct MomentWarp {
+    double dD[kMaxQ][21];   // w s (DS - D_el) of the plastic points, packed upper triangle
+    double lam[kMaxQ][4];   // their barycentric coordinates
+    double M[10][21];       // moments, pair p = (m <= n), packed upper triangle
+    double v[4][3];         // grad lambda_0..3
+    union {
+        double T[10][12][6];  // (beta_(k,c)^T M_p)[t]
+        double ke[30][31];    // the element's correction, padded rows
+    } u;
+    double R[10][78];       // R_p, packed upper triangle of 12 x 12
+};
+
+// packed upper-triangle index of (i, j), i <= j, in an n x n symmetric matrix (row-major upper)
+__device__ __forceinline__ int sym_index(int i, int j, int n) {
+    if (i > j) {
+        const int t = i;
+        i = j;
+        j = t;
+    }
+    return i * n - (i * (i - 1)) / 2 + (j - i);
+}
+// pair index of (m, n), m, n in 0..3
+__device__ __forceinline__ int pair_index(int m, int n) { return sym_index(m, n, 4); }
+
+// the (strain row, gradient component) pairs of beta_(k,c)'s three nonzeros (B^T's row of component c)
+__device__ __forceinline__ void beta_rows(int c, int *srow, int *gcomp) {
+    if (c == 0) { srow[0] = 0; gcomp[0] = 0; srow[1] = 3; gcomp[1] = 1; srow[2] = 5; gcomp[2] = 2; }
+    else if (c == 1) { srow[0] = 3; gcomp[0] = 0; srow[1] = 1; gcomp[1] = 1; srow[2] = 4; gcomp[2] = 2; }
+    else { srow[0] = 5; gcomp[0] = 0; srow[1] = 4; gcomp[1] = 1; srow[2] = 2; gcomp[2] = 2; }
+}
+
+// term t (0..3) of node a's gradient: (m, coefficient, k); vertices have four terms, edge nodes
+// two (coefficient 0 for t >= 2)
+__device__ __forceinline__ void node_term(int a, int t, int &m, double &coef, int &k) {
+    if (a < 4) {
+        m = t;
+        coef = t == a ? 3.0 : -1.0;
+        k = a;
+        return;
+    }
+    // edges 01, 12, 02, 13, 23, 03
+    const int i = (a == 5 || a == 7) ? 1 : (a == 8 ? 2 : 0);
+    const int j = a == 4 ? 1 : (a == 5 || a == 6) ? 2 : 3;
+    m = t == 0 ? i : j;
+    k = t == 0 ? j : i;
+    coef = t < 2 ? 4.0 : 0.0;
+}
+
+__global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
+    const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
+    const double *__restrict__ w, const int8_t *__restrict__ branch, const double *__restrict__ shear,
+    const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
+    double scale, double *__restrict__ values, const int32_t *__restrict__ elist, const int32_t *__restrict__ elist_count) {
+    extern __shared__ __align__(16) unsigned char mom_raw[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    MomentWarp &W = reinterpret_cast<MomentWarp *>(mom_raw)[wid];
+    const long long n_iter = *elist_count;
+    for (long long it = (long long)blockIdx.x * kMomWarps + wid; it < n_iter; it += (long long)gridDim.x * kMomWarps) {
+        const int32_t e32 = elist[it];
+        if (e32 < 0 || e32 >= n_elem) {  // warp-uniform
+            if (lane == 0) flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const long long e = e32, g0 = e * n_q;
+        const bool pl = lane < n_q && branch[g0 + lane] != 0;
+        const unsigned qmask = __ballot_sync(0xffffffffu, pl);
+        const int nq = __popc(qmask);
+        __syncwarp();  // the previous element of this warp is done with its shared slice
+        // inputs: dD of the plastic points, their barycentric coordinates, grad lambda
+        for (int i = lane; i < nq * 21; i += 32) {
+            const int kk = i / 21, ee = i - 21 * kk;
+            int q = -1;  // the kk-th plastic point
+            unsigned m = qmask;
+            for (int t = 0; t <= kk; ++t) {
+                q = __ffs(m) - 1;
+                m &= m - 1u;
+            }
+            const long long g = g0 + q;
+            int r = 0, c = ee;  // packed upper (r <= c) of 6 x 6
+            while (c >= 6 - r) {
+                c -= 6 - r;
+                ++r;
+            }
+            c += r;
+            const double v = scale * (DS[g * 36 + r + 6 * c] - elastic_d<3>(r, c, shear[g], lame[g]));
+            W.dD[kk][ee] = w[g] * v;
+        }
+        for (int i = lane; i < nq * 4; i += 32) {
+            const int kk = i >> 2;
+            int q = -1;
+            unsigned m = qmask;
+            for (int t = 0; t <= kk; ++t) {
+                q = __ffs(m) - 1;
+                m &= m - 1u;
+            }
+            W.lam[kk][i & 3] = bary[q * 4 + (i & 3)];
+        }
+        if (lane < 9) W.v[1 + lane / 3][lane % 3] = jinv[e * 9 + lane];
+        __syncwarp();
+        if (lane < 3) W.v[0][lane] = -(W.v[1][lane] + W.v[2][lane] + W.v[3][lane]);
+        // moments M_p = sum_q lambda_qm lambda_qn dD_q
+        for (int i = lane; i < 210; i += 32) {
+            const int pp = i / 21, ee = i - 21 * pp;
+            int m = 0, n = pp;  // pair p = (m <= n) packed
+            while (n >= 4 - m) {
+                n -= 4 - m;
+                ++m;
+            }
+            n += m;
+            double acc = 0.0;
+            for (int kk = 0; kk < nq; ++kk) acc = fma(W.lam[kk][m] * W.lam[kk][n], W.dD[kk][ee], acc);
+            W.M[pp][ee] = acc;
+        }
+        __syncwarp();
+        // T_p[(k,c)][t] = sum over beta_(k,c)'s nonzeros of grad lambda_k[comp] M_p[s][t]
+        for (int i = lane; i < 720; i += 32) {
+            const int pp = i / 72, rr = i - 72 * pp, kc = rr / 6, t = rr - 6 * kc, k = kc / 3, c = kc - 3 * k;
+            int sr[3], gc[3];
+            beta_rows(c, sr, gc);
+            double acc = 0.0;
+#pragma unroll
+            for (int z = 0; z < 3; ++z) acc = fma(W.v[k][gc[z]], W.M[pp][sym_index(sr[z], t, 6)], acc);
+            W.u.T[pp][kc][t] = acc;
+        }
+        __syncwarp();
+        // R_p[(k,c),(l,d)] = sum over beta_(l,d)'s nonzeros of T_p[(k,c)][s] grad lambda_l[comp]
+        for (int i = lane; i < 780; i += 32) {
+            const int pp = i / 78, ee = i - 78 * pp;
+            int kc = 0, ld = ee;
+            while (ld >= 12 - kc) {
+                ld -= 12 - kc;
+                ++kc;
+            }
+            ld += kc;
+            const int l = ld / 3, d = ld - 3 * l;
+            int sr[3], gc[3];
+            beta_rows(d, sr, gc);
+            double acc = 0.0;
+#pragma unroll
+            for (int z = 0; z < 3; ++z) acc = fma(W.u.T[pp][kc][sr[z]], W.v[l][gc[z]], acc);
+            W.R[pp][ee] = acc;
+        }
+        __syncwarp();  // T is dead: its storage becomes the element matrix
+        // K[(a,c),(b,d)], alpha = 3 a + c <= beta = 3 b + d, both mirror positions
+        for (int i = lane; i < 465; i += 32) {
+            int al = 0, be = i;
+            while (be >= 30 - al) {
+                be -= 30 - al;
+                ++al;
+            }
+            be += al;
+            const int a = al / 3, c = al - 3 * a, b = be / 3, d = be - 3 * b;
+            const int na = a < 4 ? 4 : 2, nb = b < 4 ? 4 : 2;
+            double acc = 0.0;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                if (x >= na) break;
+                int mx, kx;
+                double cx;
+                node_term(a, x, mx, cx, kx);
+                double inner = 0.0;
+#pragma unroll
+                for (int y = 0; y < 4; ++y) {
+                    if (y >= nb) break;
+                    int my, ky;
+                    double cy;
+                    node_term(b, y, my, cy, ky);
+                    inner = fma(cy, W.R[pair_index(mx, my)][sym_index(3 * kx + c, 3 * ky + d, 12)], inner);
+                }
+                acc = fma(cx, inner, acc);
+            }
+            W.u.ke[al][be] = acc;
+            W.u.ke[be][al] = acc;
+        }
+        __syncwarp();
+        // scatter through the element -> CSR map (both mirror positions were written)
+        const int32_t *em = emap + e * 900;
+        for (int i = lane; i < 900; i += 32) {
+            const int32_t pos = em[i];
+            if (pos < 0) continue;
+            if (pos >= nnz) {
+                flag(SSP_DEV_BAD_INDEX);
+                continue;
+            }
+            red_add(values + pos, W.u.ke[i / 30][i % 30]);
+        }
+    }
+}
+
+// Plastic elements split by their number of plastic points: fewer than min_points to list_few,
+// at least min_points to list_many (warp-aggregated appends).
+__global__ void plastic_elements_split_kernel(const int8_t *__restrict__ branch, int n_elem, int n_q, int min_points,
+                                              int32_t *__restrict__ list_few, int32_t *__restrict__ count_few,
+                                              int32_t *__restrict__ list_many, int32_t *__restrict__ count_many) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    int np = 0;
+    if (e < n_elem) {
+        const int8_t *b = branch + (long long)e * n_q;
+        for (int q = 0; q < n_q; ++q) np += b[q] != 0;
+    }
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int which = 0; which < 2; ++which) {
+        const bool want = which == 0 ? (np > 0 && np < min_points) : np >= min_points;
+        int32_t *list = which == 0 ? list_few : list_many;
+        int32_t *count = which == 0 ? count_few : count_many;
+        const unsigned mask = __ballot_sync(0xffffffffu, want);
+        if (mask == 0u) continue;
+        const int leader = __ffs(mask) - 1;
+        int base = 0;
+        if ((int)lane == leader) base = atomicAdd(count, __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (want) list[base + __popc(mask & ((1u << lane) - 1u))] = e;
+    }
+}
+
 // ---------------------------------------------------------------------------- epilogue
 
 __global__ void set_positions_kernel(double *__restrict__ values, const int32_t *__restrict__ pos, int n, long long nnz,
@@ -1443,6 +1675,49 @@ int ssp_plastic_elements(const int8_t *branch, int n_elem, int n_q, int32_t *lis
     if (n_elem == 0) return SSP_OK;
     if (!branch || !list_out) return SSP_ERR_INVALID;
     plastic_elements_kernel<<<grid_for(n_elem, 256), 256, 0, st>>>(branch, n_elem, n_q, list_out, count_out);
+    return launch_status();
+}
+
+int ssp_plastic_elements_split(const int8_t *branch, int n_elem, int n_q, int min_points, int32_t *list_few,
+                               int32_t *count_few, int32_t *list_many, int32_t *count_many, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || min_points < 1) return SSP_ERR_INVALID;
+    if (!count_few || !count_many) return SSP_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(count_few, 0, sizeof(int32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(count_many, 0, sizeof(int32_t), st) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    if (n_elem == 0) return SSP_OK;
+    if (!branch || !list_few || !list_many) return SSP_ERR_INVALID;
+    plastic_elements_split_kernel<<<grid_for(n_elem, 256), 256, 0, st>>>(branch, n_elem, n_q, min_points, list_few,
+                                                                         count_few, list_many, count_many);
+    return launch_status();
+}
+
+int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *bary, const double *ds,
+                                              const double *weight, const int8_t *branch, const double *shear,
+                                              const double *lame, const int32_t *scatter_map, int n_elem, int n_q,
+                                              long long nnz_out, double scale, double *out_values,
+                                              const int32_t *elem_list, const int32_t *elem_count, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || n_q > kMaxQ || nnz_out < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
+        (nnz_out > 0 && !out_values))
+        return SSP_ERR_INVALID;
+    const size_t smem = sizeof(MomentWarp) * kMomWarps;
+    if (cudaFuncSetAttribute(correction_p2_moment_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    int dev = 0, sms = 148, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, correction_p2_moment_kernel, 32 * kMomWarps, smem);
+    if (per_sm < 1) per_sm = 1;
+    long long grid = (long long)sms * per_sm;
+    const long long need = (n_elem + kMomWarps - 1) / kMomWarps;
+    if (grid > need) grid = need;
+    correction_p2_moment_kernel<<<static_cast<unsigned>(grid), 32 * kMomWarps, smem, as_stream(stream)>>>(
+        jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale, out_values, elem_list,
+        elem_count);
     return launch_status();
 }
 

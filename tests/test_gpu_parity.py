@@ -610,6 +610,44 @@ def test_affine_fp64_strain_and_force_match_gradient_kernels(oracle, et, dims):
         assert max(err_e, err_f) <= 1e-13 and max(err_eo, err_fo) <= PLAIN_RTOL
 
 
+def test_p2_moment_correction_matches_point_by_point(oracle):
+    """The plain tangent of straight-sided P2 elements with the plastic correction in moment form
+    (every plastic element, and the default split at six plastic points) against the
+    point-by-point correction and against the oracle's rows tangent, on a strongly yielding slope."""
+    from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
+
+    mats = synthetic.MaterialSet.layered(4, seed=2)
+    mesh = synthetic.slope_mesh_3d(12, 5, 6, elem_type="P2", n_layers=4)
+    specs = [dict(c0=float(mats.c0[i]), phi=float(mats.phi[i]), psi=0.0, young=float(mats.young[i]),
+                  poisson=float(mats.poisson[i]), gamma_sat=20.0, gamma_unsat=20.0) for i in range(mats.c0.size)]
+    op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.08, seed=9)
+    op.reduction(1.3)
+    out = {}
+    for mp in (0, 1, 6):
+        op.moment_min_points = mp
+        op.constitutive_problem_stress_tangent(U)
+        kt = op._build_owned_tangent_matrix().getValuesCSR()[2].copy()
+        kr = op.build_K_regularized(0.2).getValuesCSR()[2].copy()
+        out[mp] = (kt, kr)
+    pat = op.owned_tangent_pattern
+    assert pat.affine_p2
+    per_elem = (np.asarray(op._branch.cpu()).reshape(-1, pat.n_q) != 0).sum(axis=1)
+    assert (per_elem >= 6).sum() > 50 and ((per_elem > 0) & (per_elem < 6)).sum() > 0
+    for mp in (1, 6):
+        assert rel_err(out[mp][0], out[0][0]) <= 1e-13
+        assert rel_err(out[mp][1], out[0][1]) <= 1e-13
+    DS = np.ascontiguousarray(np.asarray(op._owned_local_DS).T)
+    K_o = oracle.tangent_scatter(3, pat.dphi1, pat.dphi2, pat.dphi3, DS, pat.overlap_assembly_weight,
+                                 _p2_scatter_map(pat), pat.n_q, pat.nnz)
+    K_o[pat.constrained_diag_positions] = 1.0
+    assert rel_err(out[1][0], K_o) <= PLAIN_RTOL
+
+
+def _p2_scatter_map(pat):
+    return pat.device["scatter_map"].cpu().numpy()
+
+
 def test_large_mesh_properties():
     """At a benchmark-like size: symmetric == general kernel, K symmetric, linear in DS."""
     import torch
