@@ -327,9 +327,14 @@ def kernel_profile(torch, lib, op, states_dev):
 
 
 def workload_plastic(op):
+    """Plastic points and elements of the current state; with the moment form of the P2 correction,
+    also the elements (and their plastic points) at or above its plastic-point split."""
     n_q = op.owned_tangent_pattern.n_q
     plastic = op._branch.view(-1, n_q) != 0
-    return {"n_plastic": int(plastic.sum().item()), "n_plastic_el": int(plastic.any(dim=1).sum().item())}
+    per_el = plastic.sum(dim=1)
+    many = per_el >= max(int(getattr(op, "moment_min_points", 0) or 0), 1)
+    return {"n_plastic": int(plastic.sum().item()), "n_plastic_el": int(plastic.any(dim=1).sum().item()),
+            "n_many_el": int(many.sum().item()), "n_plastic_many": int(per_el[many].sum().item())}
 
 
 def workload_stats(op, plastic):
@@ -339,6 +344,8 @@ def workload_stats(op, plastic):
             "n_u": int(pat.overlap_global_dofs.size),
             "n_plastic": float(np.mean([p["n_plastic"] for p in plastic])),
             "n_plastic_el": float(np.mean([p["n_plastic_el"] for p in plastic])),
+            "n_many_el": float(np.mean([p["n_many_el"] for p in plastic])),
+            "n_plastic_many": float(np.mean([p["n_plastic_many"] for p in plastic])),
             "device_bytes": sum(v.numel() * v.element_size() for v in pat.device.values())}
 
 
@@ -370,12 +377,22 @@ def algorithmic(name, st):
         return {"bytes": n * per_pt + 8 * st["n_rows"], "flops": n * 2 * ns * nld, "fp64": fp64}
     per_el = 288 * n_q + 24 * n_p * n_q + 8 * n_q + 4 * nld * nld + 8 * st["nnz"] / max(n_el, 1)
     fl_el = 2 * n_q * nld * (18 + 9 * n_p)
+    if name == "ssp_tangent_plastic_correction_p2_moments":
+        # elements at or above the split: 7,530 FP64 operations per element + 261 per plastic point
+        # (DS - D_el, weighted coordinate products, moments, beta^T M, R, the R sums, K), FMA-equivalent
+        units = st["n_many_el"]
+        return {"bytes": units * per_el, "flops": units * fl_el,
+                "fp64": 2.0 * (7530 * units + 261 * st["n_plastic_many"]),
+                "units": f"{units:.0f} plastic elements at or above the moment-form split per launch"}
     if name.startswith("ssp_tangent_plastic_correction"):
-        units = st["n_plastic_el"]
-        fp64 = st["n_plastic"] * 2.0 * nld * ns * dim  # H = B^T (w dD): FP64 in both forms
+        units, n_pl = st["n_plastic_el"], st["n_plastic"]
+        if st.get("moments") and not name.endswith("_mixed"):  # the elements below the split
+            units, n_pl = units - st["n_many_el"], n_pl - st["n_plastic_many"]
+        fp64 = n_pl * 2.0 * nld * ns * dim  # H = B^T (w dD): FP64 in both forms
         if not name.endswith("_mixed"):
-            fp64 += st["n_plastic"] * 2.0 * nld * (nld + 1) // 2 * dim  # the B^T H products, upper half
-        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": fp64}
+            fp64 += n_pl * 2.0 * nld * (nld + 1) // 2 * dim  # the B^T H products, upper half
+        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": fp64,
+                "units": f"{units:.0f} plastic elements per launch"}
     if name in ("ssp_tangent_element", "ssp_assemble_tangent_values_3d_rows", "ssp_assemble_tangent_values_3d_p2"):
         return {"bytes": n_el * per_el, "flops": n_el * fl_el, "fp64": n_el * fl_el}
     if name == "ssp_blend_values":
@@ -796,6 +813,7 @@ def run_gpu(args):
 
     kernels, plastic = kernel_profile(torch, _lib, op, states_dev)
     stats = workload_stats(op, plastic)
+    stats["moments"] = "ssp_tangent_plastic_correction_p2_moments" in kernels
     hbm_peak, hbm_src = peaks()
     fp64_tf = fp64_peak(torch)
     dominant = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
@@ -827,8 +845,7 @@ def run_gpu(args):
                      "traffic": NCU_TRAFFIC.get(args.config, {}).get(dominant, (None, None))[0],
                      "traffic_source": NCU_TRAFFIC.get(args.config, {}).get(dominant, (None, "not captured"))[1],
                      "ms_per_launch": k_ms, "algorithmic_bytes": alg["bytes"],
-                     "units": f"{stats['n_plastic_el']:.0f} plastic elements per launch"
-                     if dominant.startswith("ssp_tangent_plastic_correction") else None},
+                     "units": alg.get("units")},
         "roofline_fp64": {"bound": "fp64", "kernel": dominant, "achieved": alg["fp64"] / (k_ms * 1e-3) / 1e12,
                           "peak": fp64_tf, "unit": "TFLOP/s", "frac": alg["fp64"] / (k_ms * 1e-3) / 1e12 / fp64_tf,
                           "peak_source": "measured live (bench-only FP64 FMA probe)",

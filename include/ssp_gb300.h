@@ -309,7 +309,8 @@ int ssp_plastic_elements_split(const int8_t *branch, int n_elem, int n_q, int mi
  * in the barycentric coordinates, an element's correction is assembled from the ten moments
  * sum_q lambda_qm lambda_qn w_q s (DS_q - D_el,q) of its plastic points (jinv [n_elem][3][3], row k
  * the gradient of barycentric coordinate k+1; bary [n_q][4] the points' barycentric coordinates),
- * about 8,200 + 231 n_pl FP64 operations per element instead of about 1,935 per plastic point.
+ * about 7,500 + 261 n_pl FP64 operations per element instead of about 1,935 per plastic point
+ * (fewer from five plastic points up).
  * Visits the elements of elem_list[0 .. *elem_count) (e.g. list_many of ssp_plastic_elements_split);
  * n_q <= 11. */
 int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *bary, const double *ds,

@@ -1082,32 +1082,52 @@ __global__ void fill_elastic_ds_kernel(const int8_t *__restrict__ branch, const 
 // ---------------------------------------------------------------------------- P2 correction, moment form
 //
 // The plastic correction K_e = sum_q B_q^T dD_q B_q of a straight-sided P2 tetrahedron, regrouped.
-// Every shape-function gradient is linear in the barycentric coordinates, grad phi_a(q) =
-// sum_m lambda_qm c_am grad lambda_k(a,m): vertex i has c = 4 delta_im - 1 and k = i; the edge node
-// (i, j) has c = 4 with k = j for m = i and k = i for m = j.  Hence
-//   K_e[(a,c),(b,d)] = sum_{m,n} c_am c_bn R_mn[(k(a,m), c), (k(b,n), d)],
-//   R_mn = beta^T M_mn beta,   M_mn = sum_q lambda_qm lambda_qn dD_q   (ten pairs m <= n),
-// where beta_(k,c) is the strain of grad lambda_k (x) e_c (three nonzeros).  FP64 work per element:
-// 21 n_pl (dD) + 210 n_pl (moments) + 2,160 (beta^T M) + 2,340 (R) + 3,660 (K) instead of about
-// 1,935 per plastic point for the point-by-point contraction: fewer from six plastic points up, and
-// half for a fully plastic 11-point element.  Elements with fewer plastic points keep the
-// point-by-point kernel (the element lists are split by ssp_plastic_elements_split).  The result is
-// the reference's contraction (assemble_tangent_values_3d.c:135-214) regrouped: equal to rounding.
+// Every shape-function gradient is linear in the barycentric coordinates.  With the constant
+// lambda_4 = 1 as a fifth coordinate, every node's gradient has exactly two terms
+// c lambda_m grad lambda_k:
+//   vertex i:     (4 lambda_i - 1) grad lambda_i = 4 lambda_i grad lambda_i - lambda_4 grad lambda_i,
+//   edge (i, j):  4 lambda_i grad lambda_j + 4 lambda_j grad lambda_i.
+// Hence, with the moments M_mn = sum_q w_q s lambda_qm lambda_qn dD_q (m, n in 0..4) and
+// beta_(k,c) the strain of grad lambda_k (x) e_c (three nonzeros),
+//   K_e[(a,c),(b,d)] = sum_{x,y = 1,2} c_ax c_by R_(m_ax m_by)[(k_ax, c), (k_by, d)],   R_mn = beta^T M_mn beta,
+// four terms per entry for every node pair, so the lanes of a warp do equal work.  Only the ten
+// pairs m <= n < 4 are formed from the points; since the coordinates sum to one,
+// R_m4 = sum_n R_mn and R_44 = sum_m R_m4.  FP64 operations per element: 21 n_pl (DS - D_el),
+// 30 n_pl (weighted coordinate products), 210 n_pl (moments), 2,160 (beta^T M), 2,340 (R),
+// 1,170 (the sums), 1,860 (K): about 7,500 + 260 n_pl against about 1,935 n_pl point by point,
+// fewer from five plastic points up.  Elements with fewer plastic points keep the point-by-point
+// kernel (the element lists are split by ssp_plastic_elements_split).  The result is the
+// reference's contraction (assemble_tangent_values_3d.c:135-214) regrouped: equal to rounding.
 constexpr int kMomWarps = 4, kMaxQ = 11;
+constexpr int kMomEntries = 465;  // alpha <= beta of the 30 x 30 element matrix
 
 struct MomentWarp {
-    double dD[kMaxQ][21];   // w s (DS - D_el) of the plastic points, packed upper triangle
-    double lam[kMaxQ][4];   // their barycentric coordinates
-    double M[10][21];       // moments, pair p = (m <= n), packed upper triangle
-    double v[4][3];         // grad lambda_0..3
     union {
-        double T[10][12][6];  // (beta_(k,c)^T M_p)[t]
-        double ke[30][31];    // the element's correction, padded rows
-    } u;
-    double R[10][78];       // R_p, packed upper triangle of 12 x 12
+        struct {
+            double M[10][21];  // moments of the pairs m <= n < 4, packed upper triangle of 6 x 6
+            double v[4][3];    // grad lambda_0..3
+            union {
+                struct {
+                    double dD[kMaxQ][21];  // DS - D_el of the plastic points, packed upper triangle
+                    double ll[kMaxQ][10];  // w s lambda_m lambda_n of the plastic points, pair order
+                } in;
+                double T[10][12][6];  // (beta_(k,c)^T M_p)[t]
+            } t;
+        } a;
+        double ke[30][31];  // the element's correction, padded rows
+    } x;
+    double R[15][78];  // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
+    int8_t qidx[16];   // the plastic points of the element, in order
 };
 
-// packed upper-triangle index of (i, j), i <= j, in an n x n symmetric matrix (row-major upper)
+struct MomentTables {
+    unsigned long long k_terms[kMomEntries];  // four (R offset | coefficient code << 11) fields of 16 bits
+    uint16_t k_pos[kMomEntries];              // alpha << 5 | beta
+    uint16_t r_pos[78];                       // (k,c) << 8 | (l,d), packed upper triangle of 12 x 12
+    uint8_t s_pos[21];                        // r << 4 | c, packed upper triangle of 6 x 6
+};
+
+// packed upper-triangle index of (i, j) in an n x n symmetric matrix (row-major upper)
 __device__ __forceinline__ int sym_index(int i, int j, int n) {
     if (i > j) {
         const int t = i;
@@ -1116,8 +1136,15 @@ __device__ __forceinline__ int sym_index(int i, int j, int n) {
     }
     return i * n - (i * (i - 1)) / 2 + (j - i);
 }
-// pair index of (m, n), m, n in 0..3
-__device__ __forceinline__ int pair_index(int m, int n) { return sym_index(m, n, 4); }
+// (i, j), i <= j, of the packed upper-triangle index p of an n x n matrix
+__device__ __forceinline__ void sym_pair(int p, int n, int &i, int &j) {
+    i = 0;
+    while (p >= n - i) {
+        p -= n - i;
+        ++i;
+    }
+    j = i + p;
+}
 
 // the (strain row, gradient component) pairs of beta_(k,c)'s three nonzeros (B^T's row of component c)
 __device__ __forceinline__ void beta_rows(int c, int *srow, int *gcomp) {
@@ -1126,22 +1153,56 @@ __device__ __forceinline__ void beta_rows(int c, int *srow, int *gcomp) {
     else { srow[0] = 5; gcomp[0] = 0; srow[1] = 4; gcomp[1] = 1; srow[2] = 2; gcomp[2] = 2; }
 }
 
-// term t (0..3) of node a's gradient: (m, coefficient, k); vertices have four terms, edge nodes
-// two (coefficient 0 for t >= 2)
-__device__ __forceinline__ void node_term(int a, int t, int &m, double &coef, int &k) {
+// term t (0, 1) of node a's gradient: coordinate m (0..4), coefficient 4 or -1, gradient k (0..3).
+// Nodes 4..9 are the mid-edge nodes of edges 01, 12, 02, 13, 23, 03.
+__device__ __forceinline__ void node_term(int a, int t, int &m, int &coef, int &k) {
     if (a < 4) {
-        m = t;
-        coef = t == a ? 3.0 : -1.0;
+        m = t == 0 ? a : 4;
+        coef = t == 0 ? 4 : -1;
         k = a;
         return;
     }
-    // edges 01, 12, 02, 13, 23, 03
     const int i = (a == 5 || a == 7) ? 1 : (a == 8 ? 2 : 0);
     const int j = a == 4 ? 1 : (a == 5 || a == 6) ? 2 : 3;
     m = t == 0 ? i : j;
     k = t == 0 ? j : i;
-    coef = t < 2 ? 4.0 : 0.0;
+    coef = 4;
 }
+
+__device__ void build_moment_tables(MomentTables &tb) {
+    for (int i = threadIdx.x; i < kMomEntries; i += blockDim.x) {
+        int al, be;
+        sym_pair(i, 30, al, be);
+        const int a = al / 3, c = al - 3 * a, b = be / 3, d = be - 3 * b;
+        unsigned long long packed = 0;
+        for (int x = 0; x < 2; ++x)
+            for (int y = 0; y < 2; ++y) {
+                int mx, cx, kx, my, cy, ky;
+                node_term(a, x, mx, cx, kx);
+                node_term(b, y, my, cy, ky);
+                const int cc = cx * cy;  // 16, -4 or 1
+                const unsigned code = cc == 16 ? 0u : (cc == -4 ? 1u : 2u);
+                const unsigned off = static_cast<unsigned>(sym_index(mx, my, 5) * 78 + sym_index(3 * kx + c, 3 * ky + d, 12));
+                packed |= static_cast<unsigned long long>(off | (code << 11)) << (16 * (2 * x + y));
+            }
+        tb.k_terms[i] = packed;
+        tb.k_pos[i] = static_cast<uint16_t>(al << 5 | be);
+    }
+    for (int i = threadIdx.x; i < 78; i += blockDim.x) {
+        int kc, ld;
+        sym_pair(i, 12, kc, ld);
+        tb.r_pos[i] = static_cast<uint16_t>(kc << 8 | ld);
+    }
+    for (int i = threadIdx.x; i < 21; i += blockDim.x) {
+        int r, c;
+        sym_pair(i, 6, r, c);
+        tb.s_pos[i] = static_cast<uint8_t>(r << 4 | c);
+    }
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+__device__ __forceinline__ double moment_coef(unsigned code) { return code == 0u ? 16.0 : (code == 1u ? -4.0 : 1.0); }
 
 __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
     const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
@@ -1149,137 +1210,189 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
     const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
     double scale, double *__restrict__ values, const int32_t *__restrict__ elist, const int32_t *__restrict__ elist_count) {
     extern __shared__ __align__(16) unsigned char mom_raw[];
+    MomentTables &tb = *reinterpret_cast<MomentTables *>(mom_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    MomentWarp &W = reinterpret_cast<MomentWarp *>(mom_raw)[wid];
+    MomentWarp &W = reinterpret_cast<MomentWarp *>(mom_raw + sizeof(MomentTables))[wid];
+    build_moment_tables(tb);
+    __syncthreads();
     const long long n_iter = *elist_count;
-    for (long long it = (long long)blockIdx.x * kMomWarps + wid; it < n_iter; it += (long long)gridDim.x * kMomWarps) {
+    const long long stride = (long long)gridDim.x * kMomWarps;
+    constexpr int kInRounds = (kMaxQ * 21 + 31) / 32;  // DS entries a lane loads per element
+    constexpr int kMapBatch = 8;                        // map entries a lane loads at a time
+    for (long long it = (long long)blockIdx.x * kMomWarps + wid; it < n_iter; it += stride) {
         const int32_t e32 = elist[it];
         if (e32 < 0 || e32 >= n_elem) {  // warp-uniform
             if (lane == 0) flag(SSP_DEV_BAD_INDEX);
             continue;
         }
         const long long e = e32, g0 = e * n_q;
+        if (it + stride < n_iter) {  // the next element's DS rows and map row towards L2
+            const int32_t en = elist[it + stride];
+            if (en >= 0 && en < n_elem) {
+                const char *ds_next = reinterpret_cast<const char *>(DS + (long long)en * n_q * 36);
+                const char *em_next = reinterpret_cast<const char *>(emap + (long long)en * 900);
+                if (lane * 128 < n_q * 288) prefetch_l2(ds_next + lane * 128);
+                if (lane * 128 < 3600) prefetch_l2(em_next + lane * 128);
+            }
+        }
         const bool pl = lane < n_q && branch[g0 + lane] != 0;
         const unsigned qmask = __ballot_sync(0xffffffffu, pl);
         const int nq = __popc(qmask);
         __syncwarp();  // the previous element of this warp is done with its shared slice
-        // inputs: dD of the plastic points, their barycentric coordinates, grad lambda
-        for (int i = lane; i < nq * 21; i += 32) {
-            const int kk = i / 21, ee = i - 21 * kk;
-            int q = -1;  // the kk-th plastic point
-            unsigned m = qmask;
-            for (int t = 0; t <= kk; ++t) {
-                q = __ffs(m) - 1;
-                m &= m - 1u;
-            }
-            const long long g = g0 + q;
-            int r = 0, c = ee;  // packed upper (r <= c) of 6 x 6
-            while (c >= 6 - r) {
-                c -= 6 - r;
-                ++r;
-            }
-            c += r;
-            const double v = scale * (DS[g * 36 + r + 6 * c] - elastic_d<3>(r, c, shear[g], lame[g]));
-            W.dD[kk][ee] = w[g] * v;
-        }
-        for (int i = lane; i < nq * 4; i += 32) {
-            const int kk = i >> 2;
-            int q = -1;
-            unsigned m = qmask;
-            for (int t = 0; t <= kk; ++t) {
-                q = __ffs(m) - 1;
-                m &= m - 1u;
-            }
-            W.lam[kk][i & 3] = bary[q * 4 + (i & 3)];
-        }
-        if (lane < 9) W.v[1 + lane / 3][lane % 3] = jinv[e * 9 + lane];
+        if (pl) W.qidx[__popc(qmask & ((1u << lane) - 1u))] = static_cast<int8_t>(lane);
+        if (lane < 9) W.x.a.v[1 + lane / 3][lane % 3] = jinv[e * 9 + lane];
         __syncwarp();
-        if (lane < 3) W.v[0][lane] = -(W.v[1][lane] + W.v[2][lane] + W.v[3][lane]);
-        // moments M_p = sum_q lambda_qm lambda_qn dD_q
-        for (int i = lane; i < 210; i += 32) {
-            const int pp = i / 21, ee = i - 21 * pp;
-            int m = 0, n = pp;  // pair p = (m <= n) packed
-            while (n >= 4 - m) {
-                n -= 4 - m;
-                ++m;
+        if (lane < 3) W.x.a.v[0][lane] = -(W.x.a.v[1][lane] + W.x.a.v[2][lane] + W.x.a.v[3][lane]);
+        // inputs: DS - D_el of the plastic points (every load of a lane issued before its first use)
+        // and their weighted coordinate products
+        {
+            const int n_in = nq * 21;
+            double dsv[kInRounds], gv[kInRounds], lv[kInRounds];
+#pragma unroll
+            for (int u = 0; u < kInRounds; ++u) {
+                const int i = lane + 32 * u;
+                if (i < n_in) {
+                    const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
+                    const long long g = g0 + W.qidx[kk];
+                    dsv[u] = DS[g * 36 + (rc >> 4) + 6 * (rc & 15)];
+                    gv[u] = shear[g];
+                    lv[u] = lame[g];
+                }
             }
-            n += m;
-            double acc = 0.0;
-            for (int kk = 0; kk < nq; ++kk) acc = fma(W.lam[kk][m] * W.lam[kk][n], W.dD[kk][ee], acc);
-            W.M[pp][ee] = acc;
+#pragma unroll
+            for (int u = 0; u < kInRounds; ++u) {
+                const int i = lane + 32 * u;
+                if (i < n_in) {
+                    const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
+                    W.x.a.t.in.dD[kk][ee] = dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]);
+                }
+            }
+        }
+        for (int i = lane; i < nq * 10; i += 32) {
+            const int kk = i / 10, pp = i - 10 * kk, q = W.qidx[kk];
+            int m, n;
+            sym_pair(pp, 4, m, n);
+            W.x.a.t.in.ll[kk][pp] = (scale * w[g0 + q]) * (bary[q * 4 + m] * bary[q * 4 + n]);
+        }
+        __syncwarp();
+        // moments M_p = sum_q (w s lambda_qm lambda_qn) dD_q, two entries per lane at a time
+        for (int i0 = lane; i0 < 210; i0 += 64) {
+            const int i1 = i0 + 32 < 210 ? i0 + 32 : i0;
+            const int p0 = i0 / 21, e0 = i0 - 21 * p0, p1 = i1 / 21, e1 = i1 - 21 * p1;
+            double a0 = 0.0, a1 = 0.0;
+            for (int kk = 0; kk < nq; ++kk) {
+                a0 = fma(W.x.a.t.in.ll[kk][p0], W.x.a.t.in.dD[kk][e0], a0);
+                a1 = fma(W.x.a.t.in.ll[kk][p1], W.x.a.t.in.dD[kk][e1], a1);
+            }
+            W.x.a.M[p0][e0] = a0;
+            W.x.a.M[p1][e1] = a1;
         }
         __syncwarp();
         // T_p[(k,c)][t] = sum over beta_(k,c)'s nonzeros of grad lambda_k[comp] M_p[s][t]
-        for (int i = lane; i < 720; i += 32) {
-            const int pp = i / 72, rr = i - 72 * pp, kc = rr / 6, t = rr - 6 * kc, k = kc / 3, c = kc - 3 * k;
-            int sr[3], gc[3];
-            beta_rows(c, sr, gc);
-            double acc = 0.0;
+        for (int i0 = lane; i0 < 720; i0 += 64) {
+            double acc[2];
+            int idx[2];
 #pragma unroll
-            for (int z = 0; z < 3; ++z) acc = fma(W.v[k][gc[z]], W.M[pp][sym_index(sr[z], t, 6)], acc);
-            W.u.T[pp][kc][t] = acc;
+            for (int h = 0; h < 2; ++h) {
+                const int i = i0 + 32 * h < 720 ? i0 + 32 * h : i0;
+                const int pp = i / 72, rr = i - 72 * pp, kc = rr / 6, t = rr - 6 * kc, k = kc / 3, c = kc - 3 * k;
+                int sr[3], gc[3];
+                beta_rows(c, sr, gc);
+                double a = 0.0;
+#pragma unroll
+                for (int z = 0; z < 3; ++z) a = fma(W.x.a.v[k][gc[z]], W.x.a.M[pp][sym_index(sr[z], t, 6)], a);
+                acc[h] = a;
+                idx[h] = i;
+            }
+            (&W.x.a.t.T[0][0][0])[idx[0]] = acc[0];
+            (&W.x.a.t.T[0][0][0])[idx[1]] = acc[1];
         }
         __syncwarp();
         // R_p[(k,c),(l,d)] = sum over beta_(l,d)'s nonzeros of T_p[(k,c)][s] grad lambda_l[comp]
-        for (int i = lane; i < 780; i += 32) {
-            const int pp = i / 78, ee = i - 78 * pp;
-            int kc = 0, ld = ee;
-            while (ld >= 12 - kc) {
-                ld -= 12 - kc;
-                ++kc;
-            }
-            ld += kc;
-            const int l = ld / 3, d = ld - 3 * l;
-            int sr[3], gc[3];
-            beta_rows(d, sr, gc);
-            double acc = 0.0;
+        for (int i0 = lane; i0 < 780; i0 += 64) {
+            double acc[2];
+            int dst[2];
 #pragma unroll
-            for (int z = 0; z < 3; ++z) acc = fma(W.u.T[pp][kc][sr[z]], W.v[l][gc[z]], acc);
-            W.R[pp][ee] = acc;
+            for (int h = 0; h < 2; ++h) {
+                const int i = i0 + 32 * h < 780 ? i0 + 32 * h : i0;
+                const int pp = i / 78, ee = i - 78 * pp;
+                const int kc = tb.r_pos[ee] >> 8, ld = tb.r_pos[ee] & 0xff, l = ld / 3, d = ld - 3 * l;
+                int m, n;
+                sym_pair(pp, 4, m, n);
+                int sr[3], gc[3];
+                beta_rows(d, sr, gc);
+                double a = 0.0;
+#pragma unroll
+                for (int z = 0; z < 3; ++z) a = fma(W.x.a.t.T[pp][kc][sr[z]], W.x.a.v[l][gc[z]], a);
+                acc[h] = a;
+                dst[h] = sym_index(m, n, 5) * 78 + ee;
+            }
+            (&W.R[0][0])[dst[0]] = acc[0];
+            (&W.R[0][0])[dst[1]] = acc[1];
         }
-        __syncwarp();  // T is dead: its storage becomes the element matrix
-        // K[(a,c),(b,d)], alpha = 3 a + c <= beta = 3 b + d, both mirror positions
-        for (int i = lane; i < 465; i += 32) {
-            int al = 0, be = i;
-            while (be >= 30 - al) {
-                be -= 30 - al;
-                ++al;
-            }
-            be += al;
-            const int a = al / 3, c = al - 3 * a, b = be / 3, d = be - 3 * b;
-            const int na = a < 4 ? 4 : 2, nb = b < 4 ? 4 : 2;
-            double acc = 0.0;
+        __syncwarp();
+        // R_m4 = sum_n R_mn, then R_44 = sum_m R_m4
+        for (int i = lane; i < 4 * 78; i += 32) {
+            const int m = i / 78, ee = i - 78 * m;
+            W.R[sym_index(m, 4, 5)][ee] = (W.R[sym_index(m, 0, 5)][ee] + W.R[sym_index(m, 1, 5)][ee]) +
+                                         (W.R[sym_index(m, 2, 5)][ee] + W.R[sym_index(m, 3, 5)][ee]);
+        }
+        __syncwarp();
+        for (int ee = lane; ee < 78; ee += 32)
+            W.R[14][ee] = (W.R[4][ee] + W.R[8][ee]) + (W.R[11][ee] + W.R[13][ee]);
+        // the first batch of the element -> CSR map, in flight during K
+        const int32_t *em = emap + e * 900;
+        int32_t pos[kMapBatch];
 #pragma unroll
-            for (int x = 0; x < 4; ++x) {
-                if (x >= na) break;
-                int mx, kx;
-                double cx;
-                node_term(a, x, mx, cx, kx);
-                double inner = 0.0;
+        for (int u = 0; u < kMapBatch; ++u) {
+            const int i = lane + 32 * u;
+            pos[u] = i < 900 ? em[i] : -1;
+        }
+        __syncwarp();  // M, T and grad lambda are dead: their storage becomes the element matrix
+        const double *Rf = &W.R[0][0];
+        for (int i0 = lane; i0 < kMomEntries; i0 += 96) {
+            double acc[3];
+            int at[3];
 #pragma unroll
-                for (int y = 0; y < 4; ++y) {
-                    if (y >= nb) break;
-                    int my, ky;
-                    double cy;
-                    node_term(b, y, my, cy, ky);
-                    inner = fma(cy, W.R[pair_index(mx, my)][sym_index(3 * kx + c, 3 * ky + d, 12)], inner);
+            for (int h = 0; h < 3; ++h) {
+                const int i = i0 + 32 * h < kMomEntries ? i0 + 32 * h : i0;
+                const unsigned long long tm = tb.k_terms[i];
+                double a = 0.0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const unsigned f = static_cast<unsigned>(tm >> (16 * t)) & 0xffffu;
+                    a = fma(moment_coef(f >> 11), Rf[f & 0x7ffu], a);
                 }
-                acc = fma(cx, inner, acc);
+                acc[h] = a;
+                at[h] = tb.k_pos[i];
             }
-            W.u.ke[al][be] = acc;
-            W.u.ke[be][al] = acc;
+#pragma unroll
+            for (int h = 0; h < 3; ++h) {
+                const int al = at[h] >> 5, be = at[h] & 31;
+                W.x.ke[al][be] = acc[h];
+                W.x.ke[be][al] = acc[h];
+            }
         }
         __syncwarp();
         // scatter through the element -> CSR map (both mirror positions were written)
-        const int32_t *em = emap + e * 900;
-        for (int i = lane; i < 900; i += 32) {
-            const int32_t pos = em[i];
-            if (pos < 0) continue;
-            if (pos >= nnz) {
-                flag(SSP_DEV_BAD_INDEX);
-                continue;
+        for (int base = 0; base < 900; base += 32 * kMapBatch) {
+            if (base > 0) {
+#pragma unroll
+                for (int u = 0; u < kMapBatch; ++u) {
+                    const int i = base + lane + 32 * u;
+                    pos[u] = i < 900 ? em[i] : -1;
+                }
             }
-            red_add(values + pos, W.u.ke[i / 30][i % 30]);
+#pragma unroll
+            for (int u = 0; u < kMapBatch; ++u) {
+                const int i = base + lane + 32 * u;
+                if (pos[u] < 0) continue;
+                if (pos[u] >= nnz) {
+                    flag(SSP_DEV_BAD_INDEX);
+                    continue;
+                }
+                red_add(values + pos[u], W.x.ke[i / 30][i % 30]);
+            }
         }
     }
 }
@@ -1703,7 +1816,7 @@ int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *
     if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    const size_t smem = sizeof(MomentWarp) * kMomWarps;
+    const size_t smem = sizeof(MomentTables) + sizeof(MomentWarp) * kMomWarps;
     if (cudaFuncSetAttribute(correction_p2_moment_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
         return SSP_ERR_CUDA;

@@ -50,6 +50,7 @@ using namespace tc;
 constexpr int kNP = 35, kNQ = 24, kNLD = 105, kNS = 6;
 constexpr int kM = 128, kN = 112, kPts = 4, kK = kPts * kNS;  // 24 = three K steps of 8
 constexpr int kThreads = 512;
+constexpr int kScatterBatch = 8;                               // map entries a thread loads before its reductions
 constexpr int kTmemCols = 512;                                 // two (hi*hi, cross) accumulator pairs
 constexpr uint32_t kLboA = (kM / 8) * 128, kLboB = (kN / 8) * 128, kSbo = 128;
 constexpr int kABytes = kM * kK * 4, kBBytes = kN * kK * 4;
@@ -384,38 +385,24 @@ __device__ __forceinline__ void drain_role(Smem &S, uint32_t tmem, const int8_t 
         if (skipped && lane == 0) S.dabort = 1;
         named_bar(kBarDrain, kDrainThreads);  // the element's sums are complete
         if (S.dabort) return;
-        // the sums widened to FP64 in place (a float2 and a double take the same 8 bytes), once per
-        // upper entry, each by its owner
-        if (row < kNLD) {
-            double *kd = reinterpret_cast<double *>(kr);
-            for (int j = 0; j < kDrainCols; ++j) {
-                const int c = col0 + j;
-                if (c >= row && c < kNLD) {
-                    const float2 v = kr[c];
-                    kd[c] = df_to_f64({v.x, -v.y});
-                }
-            }
-        }
-        named_bar(kBarDrain, kDrainThreads);
-        // every entry, row by row: each drain warp takes whole rows, its lanes consecutive columns of
-        // one CSR row (so the reductions of a warp share cache lines and the map row is read
-        // coalesced); the lower triangle reads the mirrored upper entry
-        const double *ked = reinterpret_cast<const double *>(S.ke);
-        const int dw = warp - kBuildThreads / 32;
+        // every entry, row by row (consecutive threads -> consecutive columns of one CSR row, so the
+        // reductions of a warp share cache lines); the map row (44 KB, not staged) is read
+        // kScatterBatch entries per thread at a time, so a thread's loads are in flight together
         const int32_t *em = emap + e * kNLD * kNLD;
-        for (int a = dw; a < kNLD; a += kDrainThreads / 32) {
-            const int32_t *emr = em + a * kNLD;
-            int32_t pp[4];
+        for (int base = dt; base < kNLD * kNLD; base += kDrainThreads * kScatterBatch) {
+            int32_t pp[kScatterBatch];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int bcol = lane + 32 * u;
-                pp[u] = bcol < kNLD ? emr[bcol] : -1;
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kDrainThreads;
+                pp[u] = idx < kNLD * kNLD ? em[idx] : -1;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int bcol = lane + 32 * u;
+            for (int u = 0; u < kScatterBatch; ++u) {
+                const int idx = base + u * kDrainThreads;
                 if (pp[u] < 0) continue;
-                const double val = bcol >= a ? ked[a * kKeStride + bcol] : ked[bcol * kKeStride + a];
+                const int a = idx / kNLD, bcol = idx - a * kNLD;
+                const float2 v = bcol >= a ? S.ke[a * kKeStride + bcol] : S.ke[bcol * kKeStride + a];
+                const double val = df_to_f64({v.x, -v.y});
                 if (pp[u] < nnz) red_add(values + pp[u], val);
                 else flag(SSP_DEV_BAD_INDEX);
             }

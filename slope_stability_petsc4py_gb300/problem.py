@@ -264,8 +264,8 @@ class ConstitutiveOperator:
         self._energy_scratch = None  # block partials + total of potential_energy
         # plain form on straight-sided P2 tetrahedra: elements with at least this many plastic points
         # get their correction in moment form (ssp_tangent_plastic_correction_p2_moments, fewer FP64
-        # operations from six points up), the others point by point; 0 disables it
-        self.moment_min_points = 6
+        # operations from five points up), the others point by point; 0 disables it
+        self.moment_min_points = 5
         # "plain": FP64 throughout (the drop-in, parity 1e-12 with the reference);
         # "mixed": the plastic-point tangent products in FP32 (CUDA cores for P1/P2, tensor cores
         # for P4) with H = w D B formed in compensated double-float arithmetic, and the 3D strain and

@@ -612,7 +612,7 @@ def test_affine_fp64_strain_and_force_match_gradient_kernels(oracle, et, dims):
 
 def test_p2_moment_correction_matches_point_by_point(oracle):
     """The plain tangent of straight-sided P2 elements with the plastic correction in moment form
-    (every plastic element, and the default split at six plastic points) against the
+    (every plastic element, and the default split by plastic-point count) against the
     point-by-point correction and against the oracle's rows tangent, on a strongly yielding slope."""
     from slope_stability_petsc4py_gb300 import ConstitutiveOperator, synthetic
 
@@ -623,8 +623,10 @@ def test_p2_moment_correction_matches_point_by_point(oracle):
     op = ConstitutiveOperator.from_mesh(mesh.coord, mesh.elem, mesh.q_mask, mesh.material_id, specs, elem_type="P2")
     U = synthetic.displacement_field(mesh, mats, amplitude=0.08, seed=9)
     op.reduction(1.3)
+    split = op.moment_min_points
+    assert split > 1
     out = {}
-    for mp in (0, 1, 6):
+    for mp in (0, 1, split):
         op.moment_min_points = mp
         op.constitutive_problem_stress_tangent(U)
         kt = op._build_owned_tangent_matrix().getValuesCSR()[2].copy()
@@ -633,8 +635,8 @@ def test_p2_moment_correction_matches_point_by_point(oracle):
     pat = op.owned_tangent_pattern
     assert pat.affine_p2
     per_elem = (np.asarray(op._branch.cpu()).reshape(-1, pat.n_q) != 0).sum(axis=1)
-    assert (per_elem >= 6).sum() > 50 and ((per_elem > 0) & (per_elem < 6)).sum() > 0
-    for mp in (1, 6):
+    assert (per_elem >= split).sum() > 50 and ((per_elem > 0) & (per_elem < split)).sum() > 0
+    for mp in (1, split):
         assert rel_err(out[mp][0], out[0][0]) <= 1e-13
         assert rel_err(out[mp][1], out[0][1]) <= 1e-13
     DS = np.ascontiguousarray(np.asarray(op._owned_local_DS).T)
