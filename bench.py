@@ -332,7 +332,8 @@ def workload_plastic(op):
     n_q = op.owned_tangent_pattern.n_q
     plastic = op._branch.view(-1, n_q) != 0
     per_el = plastic.sum(dim=1)
-    many = per_el >= max(int(getattr(op, "moment_min_points", 0) or 0), 1)
+    split = op.moment_min_points_mixed if op.tangent_form == "mixed" else op.moment_min_points
+    many = per_el >= max(int(split or 0), 1)
     return {"n_plastic": int(plastic.sum().item()), "n_plastic_el": int(plastic.any(dim=1).sum().item()),
             "n_many_el": int(many.sum().item()), "n_plastic_many": int(per_el[many].sum().item())}
 
@@ -369,7 +370,7 @@ def algorithmic(name, st):
         return {"bytes": per * n, "flops": 0, "fp64": 0}
     if name.startswith("ssp_assemble_overlap_strain"):
         per_pt = 24 * n_p + 48 if dim == 3 else 16 * n_p + 24
-        fp64 = 0 if "mixed" in name else (n_el * 2 * (204 + 24 * n_q) if "p2_affine" in name else n * 2 * 9 * n_p)
+        fp64 = 0 if "mixed" in name else (n_el * 2 * (222 + 18 * n_q) if "p2_affine" in name else n * 2 * 9 * n_p)
         return {"bytes": n * per_pt + n_el * nld * 12, "flops": n * 2 * ns * dim * n_p, "fp64": fp64}
     if name.startswith("ssp_assemble_force"):
         per_pt = 48 + 24 * n_p if dim == 3 else 32 + 16 * n_p
@@ -377,6 +378,11 @@ def algorithmic(name, st):
         return {"bytes": n * per_pt + 8 * st["n_rows"], "flops": n * 2 * ns * nld, "fp64": fp64}
     per_el = 288 * n_q + 24 * n_p * n_q + 8 * n_q + 4 * nld * nld + 8 * st["nnz"] / max(n_el, 1)
     fl_el = 2 * n_q * nld * (18 + 9 * n_p)
+    if name == "ssp_tangent_plastic_correction_p2_moments_mixed":
+        # FP64 only for DS - D_el (12 nonzero D_el entries) and w s per plastic point; the rest FP32
+        units = st["n_many_el"]
+        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": 2.0 * 13 * st["n_plastic_many"],
+                "units": f"{units:.0f} plastic elements in moment form per launch"}
     if name == "ssp_tangent_plastic_correction_p2_moments":
         # elements at or above the split: 7,530 FP64 operations per element + 261 per plastic point
         # (DS - D_el, weighted coordinate products, moments, beta^T M, R, the R sums, K), FMA-equivalent
@@ -386,7 +392,7 @@ def algorithmic(name, st):
                 "units": f"{units:.0f} plastic elements at or above the moment-form split per launch"}
     if name.startswith("ssp_tangent_plastic_correction"):
         units, n_pl = st["n_plastic_el"], st["n_plastic"]
-        if st.get("moments") and not name.endswith("_mixed"):  # the elements below the split
+        if st.get("moments"):  # the elements below the split
             units, n_pl = units - st["n_many_el"], n_pl - st["n_plastic_many"]
         fp64 = n_pl * 2.0 * nld * ns * dim  # H = B^T (w dD): FP64 in both forms
         if not name.endswith("_mixed"):
@@ -813,7 +819,7 @@ def run_gpu(args):
 
     kernels, plastic = kernel_profile(torch, _lib, op, states_dev)
     stats = workload_stats(op, plastic)
-    stats["moments"] = "ssp_tangent_plastic_correction_p2_moments" in kernels
+    stats["moments"] = any(k.startswith("ssp_tangent_plastic_correction_p2_moments") for k in kernels)
     hbm_peak, hbm_src = peaks()
     fp64_tf = fp64_peak(torch)
     dominant = max(kernels, key=lambda k: kernels[k]["ms_per_step"])

@@ -319,6 +319,17 @@ int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *
                                               long long nnz_out, double scale, double *out_values,
                                               const int32_t *elem_list, const int32_t *elem_count, void *stream);
 
+/* Mixed-precision form of ssp_tangent_plastic_correction_p2_moments: DS - D_el and w * scale are
+ * formed in FP64 and rounded to FP32 by bit operations; the moments, beta^T M beta and the element
+ * matrix in FP32 (about 2e-7 of the correction's scale); the element sums widened exactly and added
+ * to the FP64 CSR values with FP64 reductions.  Cheaper than ssp_tangent_plastic_correction_mixed
+ * from one plastic point up. */
+int ssp_tangent_plastic_correction_p2_moments_mixed(const double *jinv, const double *bary, const double *ds,
+                                                    const double *weight, const int8_t *branch, const double *shear,
+                                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_q,
+                                                    long long nnz_out, double scale, double *out_values,
+                                                    const int32_t *elem_list, const int32_t *elem_count, void *stream);
+
 /* Mixed-precision form of ssp_tangent_plastic_correction.  H = B^T (w * scale * (DS - D_el)) is
  * formed in FP64 and split into hi + lo parts.  P1/P2 elements: the products B^T H are taken and
  * accumulated in FP32 on the CUDA cores.  P4 elements (3D, 35 nodes, 24 points): the element's

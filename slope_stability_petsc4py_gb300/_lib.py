@@ -56,6 +56,8 @@ _SIGS = {
     "ssp_plastic_elements": [_vp, _c_int, _c_int, _vp, _vp, _vp],
     "ssp_plastic_elements_split": [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     "ssp_tangent_plastic_correction_p2_moments": [_vp] * 8 + [_c_int, _c_int, _c_ll, _c_dbl, _vp, _vp, _vp, _vp],
+    "ssp_tangent_plastic_correction_p2_moments_mixed": [_vp] * 8 + [_c_int, _c_int, _c_ll, _c_dbl, _vp, _vp, _vp,
+                                                                    _vp],
     "ssp_tangent_plastic_correction_mixed": [_c_int] + [_vp] * 8 + [_vp, _c_int, _c_int, _c_int, _c_ll, _c_dbl, _vp,
                                              _vp, _vp, _vp],
     "ssp_elastic_tangent_blocks": [_c_int, _vp, _vp, _c_int, _vp, _vp],
@@ -148,7 +150,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_overlap_strain_3d_p2_affine_mixed": 1, "ssp_assemble_force_element_p2_affine_mixed": 1,
     "ssp_constitutive_2d_sds_binned": 2,
     "ssp_tangent_plastic_correction": 1, "ssp_plastic_elements_split": 1,
-    "ssp_tangent_plastic_correction_p2_moments": 1,
+    "ssp_tangent_plastic_correction_p2_moments": 1, "ssp_tangent_plastic_correction_p2_moments_mixed": 1,
     "ssp_constitutive_3d_sds_binned": 3, "ssp_constitutive_3d_sds_binned_noalloc": 3,
     "ssp_constitutive_3d_sds_binned_mixed": 3, "ssp_constitutive_3d_sds_learned_mixed": 4,
     "ssp_tangent_plastic_correction_mixed": 1, "ssp_branch_features": 1, "ssp_mlp_predict": 1,

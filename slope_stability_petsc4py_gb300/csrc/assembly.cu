@@ -279,11 +279,16 @@ __global__ void __launch_bounds__(64) strain3_p2_affine_kernel(const double *__r
         S[m][4] = G[1][2] + G[2][1];
         S[m][5] = G[0][2] + G[2][0];
     }
+    // the coordinates sum to one: E(q) = S_0 + sum_{m>=1} lambda_qm (S_m - S_0), 18 FMA per point
+#pragma unroll
+    for (int m = 1; m < 4; ++m)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) S[m][c] -= S[0][c];
     for (int q = 0; q < n_q; ++q) {
-        const double l0 = bary[4 * q], l1 = bary[4 * q + 1], l2 = bary[4 * q + 2], l3 = bary[4 * q + 3];
+        const double l1 = bary[4 * q + 1], l2 = bary[4 * q + 2], l3 = bary[4 * q + 3];
         double v[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v[c] = l0 * S[0][c] + l1 * S[1][c] + l2 * S[2][c] + l3 * S[3][c];
+        for (int c = 0; c < 6; ++c) v[c] = fma(l3, S[3][c], fma(l2, S[2][c], fma(l1, S[1][c], S[0][c])));
         double2 *o = reinterpret_cast<double2 *>(E + 6 * (e * n_q + q));
         o[0] = make_double2(v[0], v[1]);
         o[1] = make_double2(v[2], v[3]);
@@ -1098,25 +1103,27 @@ __global__ void fill_elastic_ds_kernel(const int8_t *__restrict__ branch, const 
 // fewer from five plastic points up.  Elements with fewer plastic points keep the point-by-point
 // kernel (the element lists are split by ssp_plastic_elements_split).  The result is the
 // reference's contraction (assemble_tangent_values_3d.c:135-214) regrouped: equal to rounding.
-constexpr int kMomWarps = 4, kMaxQ = 11;
+constexpr int kMaxQ = 11;
+template <bool MIXED> constexpr int kMomWarps = MIXED ? 8 : 4;  // warps per CTA (one element per warp)
 constexpr int kMomEntries = 465;  // alpha <= beta of the 30 x 30 element matrix
 
+template <typename Real>
 struct MomentWarp {
     union {
         struct {
-            double M[10][21];  // moments of the pairs m <= n < 4, packed upper triangle of 6 x 6
-            double v[4][3];    // grad lambda_0..3
+            Real M[10][21];  // moments of the pairs m <= n < 4, packed upper triangle of 6 x 6
+            Real v[4][3];      // grad lambda_0..3
             union {
                 struct {
-                    double dD[kMaxQ][21];  // DS - D_el of the plastic points, packed upper triangle
-                    double ll[kMaxQ][10];  // w s lambda_m lambda_n of the plastic points, pair order
+                    Real dD[kMaxQ][21];    // DS - D_el of the plastic points, packed upper triangle
+                    Real ll[kMaxQ][10];    // w s lambda_m lambda_n of the plastic points, pair order
                 } in;
-                double T[10][12][6];  // (beta_(k,c)^T M_p)[t]
+                Real T[10][12][6];    // (beta_(k,c)^T M_p)[t]
             } t;
         } a;
-        double ke[30][31];  // the element's correction, padded rows
+        Real ke[30][31];    // the element's correction, padded rows
     } x;
-    double R[15][78];  // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
+    Real R[15][78];    // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
     int8_t qidx[16];   // the plastic points of the element, in order
 };
 
@@ -1202,24 +1209,47 @@ __device__ void build_moment_tables(MomentTables &tb) {
 
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-__device__ __forceinline__ double moment_coef(unsigned code) { return code == 0u ? 16.0 : (code == 1u ? -4.0 : 1.0); }
+template <typename Real>
+__device__ __forceinline__ Real moment_coef(unsigned code) {
+    return code == 0u ? Real(16) : (code == 1u ? Real(-4) : Real(1));
+}
+__device__ __forceinline__ double mom_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float mom_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// an FP64 input in the working precision: itself, or rounded to a float by bit operations
+template <typename Real>
+__device__ __forceinline__ Real mom_in(double x) {
+    if constexpr (sizeof(Real) == sizeof(double)) {
+        return x;
+    } else {
+        const df32 d = df_from_f64(x);
+        return __fadd_rn(d.hi, d.lo);
+    }
+}
+template <typename Real>
+__device__ __forceinline__ double mom_out(Real x) {
+    if constexpr (sizeof(Real) == sizeof(double)) return x;
+    else return f32_widen(x);
+}
 
-__global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
+template <bool MIXED>
+__global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correction_p2_moment_kernel(
     const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
     const double *__restrict__ w, const int8_t *__restrict__ branch, const double *__restrict__ shear,
     const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
     double scale, double *__restrict__ values, const int32_t *__restrict__ elist, const int32_t *__restrict__ elist_count) {
+    using Real = typename std::conditional<MIXED, float, double>::type;
+    constexpr int kWarps = kMomWarps<MIXED>;
     extern __shared__ __align__(16) unsigned char mom_raw[];
     MomentTables &tb = *reinterpret_cast<MomentTables *>(mom_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    MomentWarp &W = reinterpret_cast<MomentWarp *>(mom_raw + sizeof(MomentTables))[wid];
+    MomentWarp<Real> &W = reinterpret_cast<MomentWarp<Real> *>(mom_raw + sizeof(MomentTables))[wid];
     build_moment_tables(tb);
     __syncthreads();
     const long long n_iter = *elist_count;
-    const long long stride = (long long)gridDim.x * kMomWarps;
-    constexpr int kInRounds = (kMaxQ * 21 + 31) / 32;  // DS entries a lane loads per element
+    const long long stride = (long long)gridDim.x * kWarps;
+    constexpr int kInBatch = MIXED ? 4 : (kMaxQ * 21 + 31) / 32;  // DS entries a lane loads at a time
     constexpr int kMapBatch = 8;                        // map entries a lane loads at a time
-    for (long long it = (long long)blockIdx.x * kMomWarps + wid; it < n_iter; it += stride) {
+    for (long long it = (long long)blockIdx.x * kWarps + wid; it < n_iter; it += stride) {
         const int32_t e32 = elist[it];
         if (e32 < 0 || e32 >= n_elem) {  // warp-uniform
             if (lane == 0) flag(SSP_DEV_BAD_INDEX);
@@ -1240,17 +1270,17 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
         const int nq = __popc(qmask);
         __syncwarp();  // the previous element of this warp is done with its shared slice
         if (pl) W.qidx[__popc(qmask & ((1u << lane) - 1u))] = static_cast<int8_t>(lane);
-        if (lane < 9) W.x.a.v[1 + lane / 3][lane % 3] = jinv[e * 9 + lane];
+        if (lane < 9) W.x.a.v[1 + lane / 3][lane % 3] = mom_in<Real>(jinv[e * 9 + lane]);
         __syncwarp();
         if (lane < 3) W.x.a.v[0][lane] = -(W.x.a.v[1][lane] + W.x.a.v[2][lane] + W.x.a.v[3][lane]);
         // inputs: DS - D_el of the plastic points (every load of a lane issued before its first use)
         // and their weighted coordinate products
-        {
-            const int n_in = nq * 21;
-            double dsv[kInRounds], gv[kInRounds], lv[kInRounds];
+        const int n_in = nq * 21;
+        for (int base = 0; base < n_in; base += 32 * kInBatch) {
+            double dsv[kInBatch], gv[kInBatch], lv[kInBatch];
 #pragma unroll
-            for (int u = 0; u < kInRounds; ++u) {
-                const int i = lane + 32 * u;
+            for (int u = 0; u < kInBatch; ++u) {
+                const int i = base + lane + 32 * u;
                 if (i < n_in) {
                     const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
                     const long long g = g0 + W.qidx[kk];
@@ -1260,11 +1290,11 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kInRounds; ++u) {
-                const int i = lane + 32 * u;
+            for (int u = 0; u < kInBatch; ++u) {
+                const int i = base + lane + 32 * u;
                 if (i < n_in) {
                     const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
-                    W.x.a.t.in.dD[kk][ee] = dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]);
+                    W.x.a.t.in.dD[kk][ee] = mom_in<Real>(dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]));
                 }
             }
         }
@@ -1272,17 +1302,17 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
             const int kk = i / 10, pp = i - 10 * kk, q = W.qidx[kk];
             int m, n;
             sym_pair(pp, 4, m, n);
-            W.x.a.t.in.ll[kk][pp] = (scale * w[g0 + q]) * (bary[q * 4 + m] * bary[q * 4 + n]);
+            W.x.a.t.in.ll[kk][pp] = mom_in<Real>(scale * w[g0 + q]) * (mom_in<Real>(bary[q * 4 + m]) * mom_in<Real>(bary[q * 4 + n]));
         }
         __syncwarp();
         // moments M_p = sum_q (w s lambda_qm lambda_qn) dD_q, two entries per lane at a time
         for (int i0 = lane; i0 < 210; i0 += 64) {
             const int i1 = i0 + 32 < 210 ? i0 + 32 : i0;
             const int p0 = i0 / 21, e0 = i0 - 21 * p0, p1 = i1 / 21, e1 = i1 - 21 * p1;
-            double a0 = 0.0, a1 = 0.0;
+            Real a0 = 0, a1 = 0;
             for (int kk = 0; kk < nq; ++kk) {
-                a0 = fma(W.x.a.t.in.ll[kk][p0], W.x.a.t.in.dD[kk][e0], a0);
-                a1 = fma(W.x.a.t.in.ll[kk][p1], W.x.a.t.in.dD[kk][e1], a1);
+                a0 = mom_fma(W.x.a.t.in.ll[kk][p0], W.x.a.t.in.dD[kk][e0], a0);
+                a1 = mom_fma(W.x.a.t.in.ll[kk][p1], W.x.a.t.in.dD[kk][e1], a1);
             }
             W.x.a.M[p0][e0] = a0;
             W.x.a.M[p1][e1] = a1;
@@ -1290,7 +1320,7 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
         __syncwarp();
         // T_p[(k,c)][t] = sum over beta_(k,c)'s nonzeros of grad lambda_k[comp] M_p[s][t]
         for (int i0 = lane; i0 < 720; i0 += 64) {
-            double acc[2];
+            Real acc[2];
             int idx[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -1298,9 +1328,9 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
                 const int pp = i / 72, rr = i - 72 * pp, kc = rr / 6, t = rr - 6 * kc, k = kc / 3, c = kc - 3 * k;
                 int sr[3], gc[3];
                 beta_rows(c, sr, gc);
-                double a = 0.0;
+                Real a = 0;
 #pragma unroll
-                for (int z = 0; z < 3; ++z) a = fma(W.x.a.v[k][gc[z]], W.x.a.M[pp][sym_index(sr[z], t, 6)], a);
+                for (int z = 0; z < 3; ++z) a = mom_fma(W.x.a.v[k][gc[z]], W.x.a.M[pp][sym_index(sr[z], t, 6)], a);
                 acc[h] = a;
                 idx[h] = i;
             }
@@ -1310,7 +1340,7 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
         __syncwarp();
         // R_p[(k,c),(l,d)] = sum over beta_(l,d)'s nonzeros of T_p[(k,c)][s] grad lambda_l[comp]
         for (int i0 = lane; i0 < 780; i0 += 64) {
-            double acc[2];
+            Real acc[2];
             int dst[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -1321,9 +1351,9 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
                 sym_pair(pp, 4, m, n);
                 int sr[3], gc[3];
                 beta_rows(d, sr, gc);
-                double a = 0.0;
+                Real a = 0;
 #pragma unroll
-                for (int z = 0; z < 3; ++z) a = fma(W.x.a.t.T[pp][kc][sr[z]], W.x.a.v[l][gc[z]], a);
+                for (int z = 0; z < 3; ++z) a = mom_fma(W.x.a.t.T[pp][kc][sr[z]], W.x.a.v[l][gc[z]], a);
                 acc[h] = a;
                 dst[h] = sym_index(m, n, 5) * 78 + ee;
             }
@@ -1349,19 +1379,19 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
             pos[u] = i < 900 ? em[i] : -1;
         }
         __syncwarp();  // M, T and grad lambda are dead: their storage becomes the element matrix
-        const double *Rf = &W.R[0][0];
+        const Real *Rf = &W.R[0][0];
         for (int i0 = lane; i0 < kMomEntries; i0 += 96) {
-            double acc[3];
+            Real acc[3];
             int at[3];
 #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int i = i0 + 32 * h < kMomEntries ? i0 + 32 * h : i0;
                 const unsigned long long tm = tb.k_terms[i];
-                double a = 0.0;
+                Real a = 0;
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const unsigned f = static_cast<unsigned>(tm >> (16 * t)) & 0xffffu;
-                    a = fma(moment_coef(f >> 11), Rf[f & 0x7ffu], a);
+                    a = mom_fma(moment_coef<Real>(f >> 11), Rf[f & 0x7ffu], a);
                 }
                 acc[h] = a;
                 at[h] = tb.k_pos[i];
@@ -1391,7 +1421,7 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
                     flag(SSP_DEV_BAD_INDEX);
                     continue;
                 }
-                red_add(values + pos[u], W.x.ke[i / 30][i % 30]);
+                red_add(values + pos[u], mom_out<Real>(W.x.ke[i / 30][i % 30]));
             }
         }
     }
@@ -1564,6 +1594,32 @@ int dispatch_element(int dim, int n_p, int n_q, const ElemArgs &a, cudaStream_t 
     if (dim == 2 && n_p == 3 && n_q == 1) return launch_element<2, 3, 1, 32, SYM, CORR>(a, st);
     if (dim == 2 && n_p == 15 && n_q == 12) return launch_element_warp<2, 15, 12, SYM, CORR>(a, st);
     return SSP_ERR_UNSUPPORTED;
+}
+
+// persistent grid: as many CTAs as fit on the device, one element per warp at a time
+template <bool MIXED>
+int launch_p2_moments(const double *jinv, const double *bary, const double *ds, const double *weight,
+                      const int8_t *branch, const double *shear, const double *lame, const int32_t *scatter_map,
+                      int n_elem, int n_q, long long nnz_out, double scale, double *out_values,
+                      const int32_t *elem_list, const int32_t *elem_count, cudaStream_t st) {
+    using Real = typename std::conditional<MIXED, float, double>::type;
+    constexpr int kWarps = kMomWarps<MIXED>;
+    const size_t smem = sizeof(MomentTables) + sizeof(MomentWarp<Real>) * kWarps;
+    if (cudaFuncSetAttribute(correction_p2_moment_kernel<MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+        return SSP_ERR_CUDA;
+    int dev = 0, sms = 148, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, correction_p2_moment_kernel<MIXED>, 32 * kWarps, smem);
+    if (per_sm < 1) per_sm = 1;
+    long long grid = (long long)sms * per_sm;
+    const long long need = (n_elem + kWarps - 1) / kWarps;
+    if (grid > need) grid = need;
+    correction_p2_moment_kernel<MIXED><<<static_cast<unsigned>(grid), 32 * kWarps, smem, st>>>(
+        jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale, out_values, elem_list,
+        elem_count);
+    return launch_status();
 }
 
 }  // namespace
@@ -1816,22 +1872,22 @@ int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *
     if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    const size_t smem = sizeof(MomentTables) + sizeof(MomentWarp) * kMomWarps;
-    if (cudaFuncSetAttribute(correction_p2_moment_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem)) != cudaSuccess)
-        return SSP_ERR_CUDA;
-    int dev = 0, sms = 148, per_sm = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, correction_p2_moment_kernel, 32 * kMomWarps, smem);
-    if (per_sm < 1) per_sm = 1;
-    long long grid = (long long)sms * per_sm;
-    const long long need = (n_elem + kMomWarps - 1) / kMomWarps;
-    if (grid > need) grid = need;
-    correction_p2_moment_kernel<<<static_cast<unsigned>(grid), 32 * kMomWarps, smem, as_stream(stream)>>>(
-        jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale, out_values, elem_list,
-        elem_count);
-    return launch_status();
+    return launch_p2_moments<false>(jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out,
+                                    scale, out_values, elem_list, elem_count, as_stream(stream));
+}
+
+int ssp_tangent_plastic_correction_p2_moments_mixed(const double *jinv, const double *bary, const double *ds,
+                                                    const double *weight, const int8_t *branch, const double *shear,
+                                                    const double *lame, const int32_t *scatter_map, int n_elem, int n_q,
+                                                    long long nnz_out, double scale, double *out_values,
+                                                    const int32_t *elem_list, const int32_t *elem_count, void *stream) {
+    if (n_elem < 0 || n_q <= 0 || n_q > kMaxQ || nnz_out < 0) return SSP_ERR_INVALID;
+    if (n_elem == 0) return SSP_OK;
+    if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
+        (nnz_out > 0 && !out_values))
+        return SSP_ERR_INVALID;
+    return launch_p2_moments<true>(jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out,
+                                   scale, out_values, elem_list, elem_count, as_stream(stream));
 }
 
 int ssp_fill_elastic_ds(int dim, const int8_t *branch, const double *shear, const double *lame, int n_int,

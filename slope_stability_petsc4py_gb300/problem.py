@@ -264,8 +264,11 @@ class ConstitutiveOperator:
         self._energy_scratch = None  # block partials + total of potential_energy
         # plain form on straight-sided P2 tetrahedra: elements with at least this many plastic points
         # get their correction in moment form (ssp_tangent_plastic_correction_p2_moments, fewer FP64
-        # operations from five points up), the others point by point; 0 disables it
+        # operations from five points up), the others point by point; 0 disables it.  The mixed form's
+        # moment kernel (FP32 after the FP64 DS - D_el) costs less than its point-by-point kernel from
+        # one plastic point up: every plastic element by default.
         self.moment_min_points = 5
+        self.moment_min_points_mixed = 1
         # "plain": FP64 throughout (the drop-in, parity 1e-12 with the reference);
         # "mixed": the plastic-point tangent products in FP32 (CUDA cores for P1/P2, tensor cores
         # for P4) with H = w D B formed in compensated double-float arithmetic, and the 3D strain and
@@ -732,29 +735,33 @@ class ConstitutiveOperator:
             # the correction visits the plastic elements only (an even share per warp)
             _lib.call("ssp_plastic_elements", _lib.ptr(self._branch), n_el, pat.n_q, _lib.ptr(elist), _lib.ptr(ecount),
                       st)
-            moments = (entry == "ssp_tangent_plastic_correction" and self.moment_min_points and pat.dim == 3 and
-                       pat.n_p == 10 and _p2_affine_inputs(pat) is not None)
-            if moments:  # elements with many plastic points in moment form, the others point by point
+            mixed_entry = entry == "ssp_tangent_plastic_correction_mixed"
+            split = int(self.moment_min_points_mixed if mixed_entry else self.moment_min_points)
+            moments = split > 0 and pat.dim == 3 and pat.n_p == 10 and _p2_affine_inputs(pat) is not None
+            clist, ccount = elist, ecount
+            if moments and split <= 1:  # every plastic element in moment form
+                many, n_many, clist = elist, ecount, None
+            elif moments:  # elements with many plastic points in moment form, the others point by point
                 if "split_lists" not in dv:
                     t = _lib.torch()
                     dv["split_lists"] = tuple(t.empty(max(n, 1), dtype=t.int32, device="cuda")
                                               for n in (n_el, 1, n_el, 1))
                 few, n_few, many, n_many = dv["split_lists"]
-                _lib.call("ssp_plastic_elements_split", _lib.ptr(self._branch), n_el, pat.n_q,
-                          int(self.moment_min_points), _lib.ptr(few), _lib.ptr(n_few), _lib.ptr(many),
-                          _lib.ptr(n_many), st)
+                _lib.call("ssp_plastic_elements_split", _lib.ptr(self._branch), n_el, pat.n_q, split, _lib.ptr(few),
+                          _lib.ptr(n_few), _lib.ptr(many), _lib.ptr(n_many), st)
                 clist, ccount = few, n_few
-            else:
-                clist, ccount = elist, ecount
-            _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
-                      _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
-                      _lib.ptr(self._branch), _lib.ptr(dv["shear"]), _lib.ptr(dv["lame"]), _lib.ptr(d["scatter_map"]),
-                      n_el, pat.n_p, pat.n_q, pat.nnz, scale, _lib.ptr(values), _lib.ptr(clist), _lib.ptr(ccount), st)
+            if clist is not None:
+                _lib.call(entry, pat.dim, _lib.ptr(d["dphi1"]), _lib.ptr(d["dphi2"]),
+                          _lib.ptr(d["dphi3"]) if pat.dim == 3 else None, _lib.ptr(self._DS_aos),
+                          _lib.ptr(d["weight"]), _lib.ptr(self._branch), _lib.ptr(dv["shear"]), _lib.ptr(dv["lame"]),
+                          _lib.ptr(d["scatter_map"]), n_el, pat.n_p, pat.n_q, pat.nnz, scale, _lib.ptr(values),
+                          _lib.ptr(clist), _lib.ptr(ccount), st)
             if moments:
-                _lib.call("ssp_tangent_plastic_correction_p2_moments", _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]),
-                          _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]), _lib.ptr(self._branch), _lib.ptr(dv["shear"]),
-                          _lib.ptr(dv["lame"]), _lib.ptr(d["scatter_map"]), n_el, pat.n_q, pat.nnz, scale,
-                          _lib.ptr(values), _lib.ptr(many), _lib.ptr(n_many), st)
+                _lib.call("ssp_tangent_plastic_correction_p2_moments" + ("_mixed" if mixed_entry else ""),
+                          _lib.ptr(d["jinv"]), _lib.ptr(d["bary"]), _lib.ptr(self._DS_aos), _lib.ptr(d["weight"]),
+                          _lib.ptr(self._branch), _lib.ptr(dv["shear"]), _lib.ptr(dv["lame"]),
+                          _lib.ptr(d["scatter_map"]), n_el, pat.n_q, pat.nnz, scale, _lib.ptr(values), _lib.ptr(many),
+                          _lib.ptr(n_many), st)
             self._build_no += 1
             self._last_build[kind] = {"kind": kind, "key": key, "values": values, "list": cur,
                                       "prev": last["list"] if same else None, "no": self._build_no,

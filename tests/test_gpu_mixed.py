@@ -57,6 +57,35 @@ def test_mixed_tangent_error_bound(cuda_device, elem_type, dims, amp):
         assert fro <= MIXED_RTOL
 
 
+def test_mixed_p2_moment_correction(cuda_device):
+    """Straight-sided P2, mixed form: the correction of every plastic element in moment form (FP32
+    after the FP64 DS - D_el) against the mixed point-by-point kernel and against the FP64 form, on
+    a strongly yielding slope; the split by plastic-point count gives the same tangent."""
+    from slope_stability_petsc4py_gb300 import synthetic
+
+    mesh, mats, op = _operator(12, 5, 6)
+    U = synthetic.displacement_field(mesh, mats, amplitude=0.08, seed=9)
+    op.reduction(1.3)
+    assert op.moment_min_points_mixed == 1
+    op.tangent_form = "plain"
+    op.constitutive_problem_stress_tangent(U)
+    per_elem = (np.asarray(op._branch.cpu()).reshape(-1, op.owned_tangent_pattern.n_q) != 0).sum(axis=1)
+    assert (per_elem > 0).sum() > 100 and (per_elem == 1).sum() > 0
+    kp = op.build_K_regularized(0.2).getValuesCSR()[2].copy()
+    assert op.owned_tangent_pattern.affine_p2  # decided at the first tangent build
+    op.tangent_form = "mixed"
+    out = {}
+    for mm in (1, 0, 4):  # every plastic element, none (point by point), split at four points
+        op.moment_min_points_mixed = mm
+        op.constitutive_problem_stress_tangent(U)
+        out[mm] = op.build_K_regularized(0.2).getValuesCSR()[2].copy()
+    op.moment_min_points_mixed = 1
+    e_mom, e_pt, e_split = rel_err(out[1], kp), rel_err(out[0], kp), rel_err(out[4], kp)
+    print(f"P2 mixed tangent error: moment form {e_mom:.3e}, point by point {e_pt:.3e}, split {e_split:.3e}")
+    assert 0.0 < e_mom <= MIXED_RTOL and e_pt <= MIXED_RTOL and e_split <= MIXED_RTOL
+    assert rel_err(out[1], out[0]) <= MIXED_RTOL
+
+
 @pytest.mark.parametrize("elem_type,dims", [("P2", (8, 4, 4)), ("P4", (4, 2, 2))])
 def test_mixed_form_newton_iterations_unchanged(cuda_device, elem_type, dims):
     from slope_stability_petsc4py_gb300.newton_check import newton_compare, newton_iterations
