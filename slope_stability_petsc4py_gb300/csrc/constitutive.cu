@@ -48,17 +48,18 @@ __device__ __forceinline__ void principal3(const double *E, Principal3 &p) {
     const double I2 = t[0] * t[1] + t[0] * t[2] + t[1] * t[2] - t[3] * t[3] - t[4] * t[4] - t[5] * t[5];
     const double I3 = t[0] * t[1] * t[2] - t[2] * t[3] * t[3] - t[1] * t[5] * t[5] - t[0] * t[4] * t[4] +
                       2.0 * t[3] * t[4] * t[5];
-    double Q = (I1 * I1 - 3.0 * I2) / 9.0;
+    // divisions by constants as products with the rounded reciprocals (an ulp from the quotients)
+    double Q = (I1 * I1 - 3.0 * I2) * (1.0 / 9.0);
     if (Q < 0.0) Q = 0.0;
-    const double R = (-2.0 * I1 * I1 * I1 + 9.0 * I1 * I2 - 27.0 * I3) / 54.0;
+    const double R = (-2.0 * I1 * I1 * I1 + 9.0 * I1 * I2 - 27.0 * I3) * (1.0 / 54.0);
     const double rq = sqrt(Q);
     double theta = 0.0;
     if (!(Q < 1e-30)) {
         double c = R / (rq * Q);
         c = fmin(1.0, fmax(-1.0, c));
-        theta = acos(c) / 3.0;
+        theta = acos(c) * (1.0 / 3.0);
     }
-    const double third = I1 / 3.0;
+    const double third = I1 * (1.0 / 3.0);
     p.I1 = I1;
     // cos(theta -+ 2 pi/3) = -cos(theta)/2 +- (sqrt(3)/2) sin(theta): one sincos instead of three cos
     double st, ct;
@@ -138,20 +139,21 @@ __device__ __forceinline__ Decision3 decide3(const Principal3 &p, const Mat3 &m)
     const double sp = m.sin_phi;
     const double f_tr = trial_yield(p, m);
     if (f_tr <= 0.0) return {kElastic, 0.0, 1.0};
-    const double g_sl = (p.e1 - p.e2) / (1.0 + sp);
-    const double g_sr = (p.e2 - p.e3) / (1.0 - sp);
+    // the reference's bounds g = x / d (d = 1 +- sin phi, 3 -+ sin phi, all positive) compared as
+    // lam d against x, and g_sl against g_sr cross-multiplied: no division for the tests
+    const double a_sl = p.e1 - p.e2, d_sl = 1.0 + sp;  // g_sl = a_sl / d_sl
+    const double a_sr = p.e2 - p.e3, d_sr = 1.0 - sp;  // g_sr = a_sr / d_sr
     double lam, den;
     smooth_lam(p, m, f_tr, lam, den);
-    if (lam <= g_sl && lam <= g_sr) return {kSmooth, lam, den};
-    if (g_sl < g_sr) {
+    if (lam * d_sl <= a_sl && lam * d_sr <= a_sr) return {kSmooth, lam, den};
+    const double l_sl = a_sl * d_sr, l_sr = a_sr * d_sl;  // g_sl < g_sr <=> l_sl < l_sr
+    if (l_sl < l_sr) {
         left_lam(p, m, lam, den);
-        const double g_la = (p.e1 + p.e2 - 2.0 * p.e3) / (3.0 - sp);
-        if (lam >= g_sl && lam <= g_la) return {kLeft, lam, den};
+        if (lam * d_sl >= a_sl && lam * (3.0 - sp) <= p.e1 + p.e2 - 2.0 * p.e3) return {kLeft, lam, den};
     }
-    if (g_sl > g_sr) {
+    if (l_sl > l_sr) {
         right_lam(p, m, lam, den);
-        const double g_ra = (2.0 * p.e1 - p.e2 - p.e3) / (3.0 + sp);
-        if (lam >= g_sr && lam <= g_ra) return {kRight, lam, den};
+        if (lam * d_sr >= a_sr && lam * (3.0 + sp) <= 2.0 * p.e1 - p.e2 - p.e3) return {kRight, lam, den};
     }
     return {kApex, 0.0, 1.0};
 }
