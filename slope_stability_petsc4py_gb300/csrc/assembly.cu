@@ -15,8 +15,6 @@
 // Layout (all FP64 unless stated): points are element-major (g = e*n_q + q); dphi arrays are
 // [n_int][n_p]; strains/stresses/tangents are per-point AoS ([n_int][6], [n_int][36]), which is
 // the reference's C layout and makes each element's data one contiguous block.
-#include <type_traits>
-
 #include "ssp_internal.cuh"
 
 namespace ssp {
@@ -1104,26 +1102,25 @@ __global__ void fill_elastic_ds_kernel(const int8_t *__restrict__ branch, const 
 // kernel (the element lists are split by ssp_plastic_elements_split).  The result is the
 // reference's contraction (assemble_tangent_values_3d.c:135-214) regrouped: equal to rounding.
 constexpr int kMaxQ = 11;
-template <bool MIXED> constexpr int kMomWarps = MIXED ? 8 : 4;  // warps per CTA (one element per warp)
+constexpr int kMomWarps = 4;  // warps per CTA (one element per warp)
 constexpr int kMomEntries = 465;  // alpha <= beta of the 30 x 30 element matrix
 
-template <typename Real>
 struct MomentWarp {
     union {
         struct {
-            Real M[10][21];  // moments of the pairs m <= n < 4, packed upper triangle of 6 x 6
-            Real v[4][3];      // grad lambda_0..3
+            double M[10][21];  // moments of the pairs m <= n < 4, packed upper triangle of 6 x 6
+            double v[4][3];    // grad lambda_0..3
             union {
                 struct {
-                    Real dD[kMaxQ][21];    // DS - D_el of the plastic points, packed upper triangle
-                    Real ll[kMaxQ][10];    // w s lambda_m lambda_n of the plastic points, pair order
+                    double dD[kMaxQ][21];  // DS - D_el of the plastic points, packed upper triangle
+                    double ll[kMaxQ][10];  // w s lambda_m lambda_n of the plastic points, pair order
                 } in;
-                Real T[10][12][6];    // (beta_(k,c)^T M_p)[t]
+                double T[10][12][6];  // (beta_(k,c)^T M_p)[t]
             } t;
         } a;
-        Real ke[30][31];    // the element's correction, padded rows
+        double ke[30][31];  // the element's correction, padded rows
     } x;
-    Real R[15][78];    // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
+    double R[15][78];  // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
     int8_t qidx[16];   // the plastic points of the element, in order
 };
 
@@ -1209,45 +1206,23 @@ __device__ void build_moment_tables(MomentTables &tb) {
 
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-template <typename Real>
-__device__ __forceinline__ Real moment_coef(unsigned code) {
-    return code == 0u ? Real(16) : (code == 1u ? Real(-4) : Real(1));
-}
-__device__ __forceinline__ double mom_fma(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float mom_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-// an FP64 input in the working precision: itself, or rounded to a float by bit operations
-template <typename Real>
-__device__ __forceinline__ Real mom_in(double x) {
-    if constexpr (sizeof(Real) == sizeof(double)) {
-        return x;
-    } else {
-        const df32 d = df_from_f64(x);
-        return __fadd_rn(d.hi, d.lo);
-    }
-}
-template <typename Real>
-__device__ __forceinline__ double mom_out(Real x) {
-    if constexpr (sizeof(Real) == sizeof(double)) return x;
-    else return f32_widen(x);
-}
+__device__ __forceinline__ double moment_coef(unsigned code) { return code == 0u ? 16.0 : (code == 1u ? -4.0 : 1.0); }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correction_p2_moment_kernel(
+__global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
     const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
     const double *__restrict__ w, const int8_t *__restrict__ branch, const double *__restrict__ shear,
     const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
     double scale, double *__restrict__ values, const int32_t *__restrict__ elist, const int32_t *__restrict__ elist_count) {
-    using Real = typename std::conditional<MIXED, float, double>::type;
-    constexpr int kWarps = kMomWarps<MIXED>;
+    constexpr int kWarps = kMomWarps;
     extern __shared__ __align__(16) unsigned char mom_raw[];
     MomentTables &tb = *reinterpret_cast<MomentTables *>(mom_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    MomentWarp<Real> &W = reinterpret_cast<MomentWarp<Real> *>(mom_raw + sizeof(MomentTables))[wid];
+    MomentWarp &W = reinterpret_cast<MomentWarp *>(mom_raw + sizeof(MomentTables))[wid];
     build_moment_tables(tb);
     __syncthreads();
     const long long n_iter = *elist_count;
     const long long stride = (long long)gridDim.x * kWarps;
-    constexpr int kInBatch = MIXED ? 4 : (kMaxQ * 21 + 31) / 32;  // DS entries a lane loads at a time
+    constexpr int kInBatch = (kMaxQ * 21 + 31) / 32;  // DS entries a lane loads at a time
     constexpr int kMapBatch = 8;                        // map entries a lane loads at a time
     for (long long it = (long long)blockIdx.x * kWarps + wid; it < n_iter; it += stride) {
         const int32_t e32 = elist[it];
@@ -1270,7 +1245,7 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
         const int nq = __popc(qmask);
         __syncwarp();  // the previous element of this warp is done with its shared slice
         if (pl) W.qidx[__popc(qmask & ((1u << lane) - 1u))] = static_cast<int8_t>(lane);
-        if (lane < 9) W.x.a.v[1 + lane / 3][lane % 3] = mom_in<Real>(jinv[e * 9 + lane]);
+        if (lane < 9) W.x.a.v[1 + lane / 3][lane % 3] = jinv[e * 9 + lane];
         __syncwarp();
         if (lane < 3) W.x.a.v[0][lane] = -(W.x.a.v[1][lane] + W.x.a.v[2][lane] + W.x.a.v[3][lane]);
         // inputs: DS - D_el of the plastic points (every load of a lane issued before its first use)
@@ -1294,7 +1269,7 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
                 const int i = base + lane + 32 * u;
                 if (i < n_in) {
                     const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
-                    W.x.a.t.in.dD[kk][ee] = mom_in<Real>(dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]));
+                    W.x.a.t.in.dD[kk][ee] = dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]);
                 }
             }
         }
@@ -1302,17 +1277,17 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
             const int kk = i / 10, pp = i - 10 * kk, q = W.qidx[kk];
             int m, n;
             sym_pair(pp, 4, m, n);
-            W.x.a.t.in.ll[kk][pp] = mom_in<Real>(scale * w[g0 + q]) * (mom_in<Real>(bary[q * 4 + m]) * mom_in<Real>(bary[q * 4 + n]));
+            W.x.a.t.in.ll[kk][pp] = (scale * w[g0 + q]) * (bary[q * 4 + m] * bary[q * 4 + n]);
         }
         __syncwarp();
         // moments M_p = sum_q (w s lambda_qm lambda_qn) dD_q, two entries per lane at a time
         for (int i0 = lane; i0 < 210; i0 += 64) {
             const int i1 = i0 + 32 < 210 ? i0 + 32 : i0;
             const int p0 = i0 / 21, e0 = i0 - 21 * p0, p1 = i1 / 21, e1 = i1 - 21 * p1;
-            Real a0 = 0, a1 = 0;
+            double a0 = 0.0, a1 = 0.0;
             for (int kk = 0; kk < nq; ++kk) {
-                a0 = mom_fma(W.x.a.t.in.ll[kk][p0], W.x.a.t.in.dD[kk][e0], a0);
-                a1 = mom_fma(W.x.a.t.in.ll[kk][p1], W.x.a.t.in.dD[kk][e1], a1);
+                a0 = fma(W.x.a.t.in.ll[kk][p0], W.x.a.t.in.dD[kk][e0], a0);
+                a1 = fma(W.x.a.t.in.ll[kk][p1], W.x.a.t.in.dD[kk][e1], a1);
             }
             W.x.a.M[p0][e0] = a0;
             W.x.a.M[p1][e1] = a1;
@@ -1320,7 +1295,7 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
         __syncwarp();
         // T_p[(k,c)][t] = sum over beta_(k,c)'s nonzeros of grad lambda_k[comp] M_p[s][t]
         for (int i0 = lane; i0 < 720; i0 += 64) {
-            Real acc[2];
+            double acc[2];
             int idx[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -1328,9 +1303,9 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
                 const int pp = i / 72, rr = i - 72 * pp, kc = rr / 6, t = rr - 6 * kc, k = kc / 3, c = kc - 3 * k;
                 int sr[3], gc[3];
                 beta_rows(c, sr, gc);
-                Real a = 0;
+                double a = 0.0;
 #pragma unroll
-                for (int z = 0; z < 3; ++z) a = mom_fma(W.x.a.v[k][gc[z]], W.x.a.M[pp][sym_index(sr[z], t, 6)], a);
+                for (int z = 0; z < 3; ++z) a = fma(W.x.a.v[k][gc[z]], W.x.a.M[pp][sym_index(sr[z], t, 6)], a);
                 acc[h] = a;
                 idx[h] = i;
             }
@@ -1340,7 +1315,7 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
         __syncwarp();
         // R_p[(k,c),(l,d)] = sum over beta_(l,d)'s nonzeros of T_p[(k,c)][s] grad lambda_l[comp]
         for (int i0 = lane; i0 < 780; i0 += 64) {
-            Real acc[2];
+            double acc[2];
             int dst[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -1351,9 +1326,9 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
                 sym_pair(pp, 4, m, n);
                 int sr[3], gc[3];
                 beta_rows(d, sr, gc);
-                Real a = 0;
+                double a = 0.0;
 #pragma unroll
-                for (int z = 0; z < 3; ++z) a = mom_fma(W.x.a.t.T[pp][kc][sr[z]], W.x.a.v[l][gc[z]], a);
+                for (int z = 0; z < 3; ++z) a = fma(W.x.a.t.T[pp][kc][sr[z]], W.x.a.v[l][gc[z]], a);
                 acc[h] = a;
                 dst[h] = sym_index(m, n, 5) * 78 + ee;
             }
@@ -1379,19 +1354,19 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
             pos[u] = i < 900 ? em[i] : -1;
         }
         __syncwarp();  // M, T and grad lambda are dead: their storage becomes the element matrix
-        const Real *Rf = &W.R[0][0];
+        const double *Rf = &W.R[0][0];
         for (int i0 = lane; i0 < kMomEntries; i0 += 96) {
-            Real acc[3];
+            double acc[3];
             int at[3];
 #pragma unroll
             for (int h = 0; h < 3; ++h) {
                 const int i = i0 + 32 * h < kMomEntries ? i0 + 32 * h : i0;
                 const unsigned long long tm = tb.k_terms[i];
-                Real a = 0;
+                double a = 0.0;
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const unsigned f = static_cast<unsigned>(tm >> (16 * t)) & 0xffffu;
-                    a = mom_fma(moment_coef<Real>(f >> 11), Rf[f & 0x7ffu], a);
+                    a = fma(moment_coef(f >> 11), Rf[f & 0x7ffu], a);
                 }
                 acc[h] = a;
                 at[h] = tb.k_pos[i];
@@ -1421,7 +1396,295 @@ __global__ void __launch_bounds__(32 * kMomWarps<MIXED>, MIXED ? 3 : 1) correcti
                     flag(SSP_DEV_BAD_INDEX);
                     continue;
                 }
-                red_add(values + pos[u], mom_out<Real>(W.x.ke[i / 30][i % 30]));
+                red_add(values + pos[u], W.x.ke[i / 30][i % 30]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- P2 correction, moment form, FP32
+//
+// The mixed form of the kernel above: DS - D_el and w s in FP64, rounded to FP32; the moments,
+// beta^T M beta, the lambda_4 sums and the element matrix in FP32; the element's 900 sums widened
+// exactly and reduced into the FP64 CSR values.  With the FP32 pipe far faster than the FP64 one,
+// the layout is chosen for few instructions rather than few operations: full 6 x 6 moments and full
+// 12 x 12 R blocks (shared-memory addresses are a lane base plus constants), beta^T M beta formed
+// in registers by one lane per (pair, component), the K entries grouped by node-pair type so each
+// group's four coefficients are constants, the element matrix unpadded.
+constexpr int kF32Warps = 8;
+constexpr int kF32KEntries = 512;        // vertex-vertex 78 -> 96, vertex-edge 216 -> 224, edge-edge 171 -> 192
+constexpr int kF32VertexVertexIters = 3, kF32VertexEdgeIters = 7;
+
+struct MomentF32Tables {
+    unsigned long long k_terms[kF32KEntries];  // four R offsets (12 bits in 16-bit fields), term order (x, y)
+    uint16_t k_pos[kF32KEntries];             // alpha << 5 | beta; 0xFFFF pads a type group
+    float lam[kMaxQ][4];                      // the points' barycentric coordinates, rounded to FP32
+    uint8_t s_pos[21];                        // r << 4 | c of the packed upper triangle of 6 x 6
+    uint8_t pair_mn[10];                      // m << 4 | n of the pairs m <= n < 4
+};
+
+struct MomentF32Warp {
+    union {
+        struct {
+            float dD[kMaxQ][21];  // DS - D_el of the plastic points, packed upper triangle
+            float ws[12];         // w s of the plastic points
+            float ll[kMaxQ][10];  // w s lambda_m lambda_n, pair order
+            float M[10][36];      // moments, full 6 x 6
+        } a;
+        float ke[900];  // the element's correction, 30 x 30 row-major
+    } x;
+    float v[4][3];      // grad lambda_0..3
+    float R[15][144];   // R over the pairs m <= n of five coordinates, full 12 x 12
+    int8_t qidx[16];
+};
+
+// FP64 -> FP32 rounded to nearest even by integer operations (values below the FP32 normal range
+// flush to a signed zero; overflow gives +-inf, nan stays nan).
+__device__ __forceinline__ float f64_to_f32_bits(double x) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned sign = static_cast<unsigned>(u >> 32) & 0x80000000u;
+    const int e = static_cast<int>((u >> 52) & 0x7FFull);
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x400000u : 0u));
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sign);
+    if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);
+    unsigned f = (static_cast<unsigned>(ef) << 23) | static_cast<unsigned>(m >> 29);
+    const unsigned r = static_cast<unsigned>(m & 0x1FFFFFFFull);
+    f += (r > 0x10000000u || (r == 0x10000000u && (f & 1u))) ? 1u : 0u;  // a carry into the exponent rounds up
+    return __uint_as_float(sign | f);
+}
+
+__device__ void build_moment_f32_tables(MomentF32Tables &tb, const double *bary, int n_q) {
+    for (int i = threadIdx.x; i < kF32KEntries; i += blockDim.x) {
+        int al = -1, be = -1;
+        if (i < 32 * kF32VertexVertexIters) {
+            if (i < 78) sym_pair(i, 12, al, be);
+        } else if (i < 32 * (kF32VertexVertexIters + kF32VertexEdgeIters)) {
+            const int j = i - 32 * kF32VertexVertexIters;
+            if (j < 216) {
+                al = j / 18;
+                be = 12 + j % 18;
+            }
+        } else {
+            const int j = i - 32 * (kF32VertexVertexIters + kF32VertexEdgeIters);
+            if (j < 171) {
+                sym_pair(j, 18, al, be);
+                al += 12;
+                be += 12;
+            }
+        }
+        unsigned long long packed = 0;
+        if (al >= 0) {
+            const int a = al / 3, c = al - 3 * a, b = be / 3, d = be - 3 * b;
+            for (int x = 0; x < 2; ++x)
+                for (int y = 0; y < 2; ++y) {
+                    int mx, cx, kx, my, cy, ky;
+                    node_term(a, x, mx, cx, kx);
+                    node_term(b, y, my, cy, ky);
+                    const unsigned off = static_cast<unsigned>(sym_index(mx, my, 5) * 144 + (3 * kx + c) * 12 + 3 * ky + d);
+                    packed |= static_cast<unsigned long long>(off) << (16 * (2 * x + y));
+                }
+        }
+        tb.k_terms[i] = packed;
+        tb.k_pos[i] = al >= 0 ? static_cast<uint16_t>(al << 5 | be) : static_cast<uint16_t>(0xFFFFu);
+    }
+    for (int i = threadIdx.x; i < n_q * 4; i += blockDim.x) tb.lam[i >> 2][i & 3] = f64_to_f32_bits(bary[i]);
+    for (int i = threadIdx.x; i < 21; i += blockDim.x) {
+        int r, c;
+        sym_pair(i, 6, r, c);
+        tb.s_pos[i] = static_cast<uint8_t>(r << 4 | c);
+    }
+    for (int i = threadIdx.x; i < 10; i += blockDim.x) {
+        int m, n;
+        sym_pair(i, 4, m, n);
+        tb.pair_mn[i] = static_cast<uint8_t>(m << 4 | n);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kF32Warps, 2) correction_p2_moment_f32_kernel(
+    const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
+    const double *__restrict__ w, const int8_t *__restrict__ branch, const double *__restrict__ shear,
+    const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
+    double scale, double *__restrict__ values, const int32_t *__restrict__ elist, const int32_t *__restrict__ elist_count) {
+    extern __shared__ __align__(16) unsigned char mom_raw[];
+    MomentF32Tables &tb = *reinterpret_cast<MomentF32Tables *>(mom_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    MomentF32Warp &W = reinterpret_cast<MomentF32Warp *>(mom_raw + sizeof(MomentF32Tables))[wid];
+    build_moment_f32_tables(tb, bary, n_q);
+    __syncthreads();
+    const long long n_iter = *elist_count;
+    const long long stride = (long long)gridDim.x * kF32Warps;
+    constexpr int kInBatch = 4;   // DS entries a lane loads at a time
+    constexpr int kMapBatch = 8;  // map entries a lane loads at a time
+    for (long long it = (long long)blockIdx.x * kF32Warps + wid; it < n_iter; it += stride) {
+        const int32_t e32 = elist[it];
+        if (e32 < 0 || e32 >= n_elem) {  // warp-uniform
+            if (lane == 0) flag(SSP_DEV_BAD_INDEX);
+            continue;
+        }
+        const long long e = e32, g0 = e * n_q;
+        if (it + stride < n_iter) {  // the next element's DS rows and map row towards L2
+            const int32_t en = elist[it + stride];
+            if (en >= 0 && en < n_elem) {
+                const char *ds_next = reinterpret_cast<const char *>(DS + (long long)en * n_q * 36);
+                const char *em_next = reinterpret_cast<const char *>(emap + (long long)en * 900);
+                if (lane * 128 < n_q * 288) prefetch_l2(ds_next + lane * 128);
+                if (lane * 128 < 3600) prefetch_l2(em_next + lane * 128);
+            }
+        }
+        const bool pl = lane < n_q && branch[g0 + lane] != 0;
+        const unsigned qmask = __ballot_sync(0xffffffffu, pl);
+        const int nq = __popc(qmask);
+        __syncwarp();  // the previous element of this warp is done with its shared slice
+        if (pl) {
+            const int kk = __popc(qmask & ((1u << lane) - 1u));
+            W.qidx[kk] = static_cast<int8_t>(lane);
+            W.x.a.ws[kk] = f64_to_f32_bits(scale * w[g0 + lane]);
+        }
+        if (lane < 9) W.v[1 + lane / 3][lane % 3] = f64_to_f32_bits(jinv[e * 9 + lane]);
+        __syncwarp();
+        if (lane < 3) W.v[0][lane] = -(W.v[1][lane] + W.v[2][lane] + W.v[3][lane]);
+        // DS - D_el in FP64, rounded to FP32 (every load of a batch issued before its first use)
+        const int n_in = nq * 21;
+        for (int base = 0; base < n_in; base += 32 * kInBatch) {
+            double dsv[kInBatch], gv[kInBatch], lv[kInBatch];
+#pragma unroll
+            for (int u = 0; u < kInBatch; ++u) {
+                const int i = base + lane + 32 * u;
+                if (i < n_in) {
+                    const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
+                    const long long g = g0 + W.qidx[kk];
+                    dsv[u] = DS[g * 36 + (rc >> 4) + 6 * (rc & 15)];
+                    gv[u] = shear[g];
+                    lv[u] = lame[g];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kInBatch; ++u) {
+                const int i = base + lane + 32 * u;
+                if (i < n_in) {
+                    const int kk = i / 21, ee = i - 21 * kk, rc = tb.s_pos[ee];
+                    W.x.a.dD[kk][ee] = f64_to_f32_bits(dsv[u] - elastic_d<3>(rc >> 4, rc & 15, gv[u], lv[u]));
+                }
+            }
+        }
+        for (int i = lane; i < nq * 10; i += 32) {
+            const int kk = i / 10, pp = i - 10 * kk, q = W.qidx[kk], mn = tb.pair_mn[pp];
+            W.x.a.ll[kk][pp] = W.x.a.ws[kk] * (tb.lam[q][mn >> 4] * tb.lam[q][mn & 15]);
+        }
+        __syncwarp();
+        // moments, both mirror positions of the full 6 x 6
+        for (int i0 = lane; i0 < 210; i0 += 64) {
+            const int i1 = i0 + 32 < 210 ? i0 + 32 : i0;
+            const int p0 = i0 / 21, e0 = i0 - 21 * p0, p1 = i1 / 21, e1 = i1 - 21 * p1;
+            float a0 = 0.0f, a1 = 0.0f;
+            for (int kk = 0; kk < nq; ++kk) {
+                a0 = __fmaf_rn(W.x.a.ll[kk][p0], W.x.a.dD[kk][e0], a0);
+                a1 = __fmaf_rn(W.x.a.ll[kk][p1], W.x.a.dD[kk][e1], a1);
+            }
+            const int rc0 = tb.s_pos[e0], rc1 = tb.s_pos[e1];
+            W.x.a.M[p0][(rc0 >> 4) * 6 + (rc0 & 15)] = a0;
+            W.x.a.M[p0][(rc0 & 15) * 6 + (rc0 >> 4)] = a0;
+            W.x.a.M[p1][(rc1 >> 4) * 6 + (rc1 & 15)] = a1;
+            W.x.a.M[p1][(rc1 & 15) * 6 + (rc1 >> 4)] = a1;
+        }
+        __syncwarp();
+        // R_p = beta^T M_p beta: lane (p, c) forms T[k][t] = sum_z grad lambda_k[z] M_p[s_z(c)][t] and
+        // the rows (k, c) of R_p, R[(k,c),(l,d)] = sum_z T[k][s_z(d)] grad lambda_l[z]
+        if (lane < 30) {
+            const int p = lane / 3, c = lane - 3 * p, mn = tb.pair_mn[p];
+            float vk[4][3];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int z = 0; z < 3; ++z) vk[k][z] = W.v[k][z];
+            int sr[3], gc[3];
+            beta_rows(c, sr, gc);  // gc = (0, 1, 2) for every c
+            const float *m0 = &W.x.a.M[p][sr[0] * 6], *m1 = &W.x.a.M[p][sr[1] * 6], *m2 = &W.x.a.M[p][sr[2] * 6];
+            float T[4][6];
+#pragma unroll
+            for (int t = 0; t < 6; ++t) {
+                const float x0 = m0[t], x1 = m1[t], x2 = m2[t];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) T[k][t] = __fmaf_rn(vk[k][2], x2, __fmaf_rn(vk[k][1], x1, vk[k][0] * x0));
+            }
+            float *Rp = &W.R[sym_index(mn >> 4, mn & 15, 5)][c * 12];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                int sd[3], gd[3];
+                beta_rows(d, sd, gd);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                    for (int l = 0; l < 4; ++l)
+                        Rp[k * 36 + 3 * l + d] =
+                            __fmaf_rn(T[k][sd[2]], vk[l][2], __fmaf_rn(T[k][sd[1]], vk[l][1], T[k][sd[0]] * vk[l][0]));
+            }
+        }
+        __syncwarp();
+        // R_m4 = sum_n R_mn, R_44 = sum_m R_m4 (pair indices over five coordinates)
+        for (int ee = lane; ee < 144; ee += 32) {
+            const float r00 = W.R[0][ee], r01 = W.R[1][ee], r02 = W.R[2][ee], r03 = W.R[3][ee];
+            const float r11 = W.R[5][ee], r12 = W.R[6][ee], r13 = W.R[7][ee];
+            const float r22 = W.R[9][ee], r23 = W.R[10][ee], r33 = W.R[12][ee];
+            const float s0 = (r00 + r01) + (r02 + r03), s1 = (r01 + r11) + (r12 + r13);
+            const float s2 = (r02 + r12) + (r22 + r23), s3 = (r03 + r13) + (r23 + r33);
+            W.R[4][ee] = s0;
+            W.R[8][ee] = s1;
+            W.R[11][ee] = s2;
+            W.R[13][ee] = s3;
+            W.R[14][ee] = (s0 + s1) + (s2 + s3);
+        }
+        // the first batch of the element -> CSR map, in flight during K
+        const int32_t *em = emap + e * 900;
+        int32_t pos[kMapBatch];
+#pragma unroll
+        for (int u = 0; u < kMapBatch; ++u) {
+            const int i = lane + 32 * u;
+            pos[u] = i < 900 ? em[i] : -1;
+        }
+        __syncwarp();  // the moments and inputs are dead: their storage becomes the element matrix
+        const float *Rf = &W.R[0][0];
+#pragma unroll 1
+        for (int k0 = 0; k0 < kF32KEntries / 32; ++k0) {
+            const int i = 32 * k0 + lane;
+            const unsigned long long tm = tb.k_terms[i];
+            const float r0 = Rf[tm & 0xFFFu], r1 = Rf[(tm >> 16) & 0xFFFu], r2 = Rf[(tm >> 32) & 0xFFFu],
+                        r3 = Rf[(tm >> 48) & 0xFFFu];
+            float kv;
+            if (k0 < kF32VertexVertexIters)  // (4, -1) x (4, -1)
+                kv = __fmaf_rn(16.0f, r0, __fmaf_rn(-4.0f, r1 + r2, r3));
+            else if (k0 < kF32VertexVertexIters + kF32VertexEdgeIters)  // (4, -1) x (4, 4)
+                kv = __fmaf_rn(16.0f, r0 + r1, -4.0f * (r2 + r3));
+            else  // (4, 4) x (4, 4)
+                kv = 16.0f * ((r0 + r1) + (r2 + r3));
+            const unsigned pk = tb.k_pos[i];
+            if (pk != 0xFFFFu) {
+                const int al = pk >> 5, be = pk & 31;
+                W.x.ke[al * 30 + be] = kv;
+                W.x.ke[be * 30 + al] = kv;
+            }
+        }
+        __syncwarp();
+        // scatter through the element -> CSR map (both mirror positions were written)
+        for (int base = 0; base < 900; base += 32 * kMapBatch) {
+            if (base > 0) {
+#pragma unroll
+                for (int u = 0; u < kMapBatch; ++u) {
+                    const int i = base + lane + 32 * u;
+                    pos[u] = i < 900 ? em[i] : -1;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kMapBatch; ++u) {
+                const int i = base + lane + 32 * u;
+                if (pos[u] < 0) continue;
+                if (pos[u] >= nnz) {
+                    flag(SSP_DEV_BAD_INDEX);
+                    continue;
+                }
+                red_add(values + pos[u], f32_widen(W.x.ke[i]));
             }
         }
     }
@@ -1597,28 +1860,24 @@ int dispatch_element(int dim, int n_p, int n_q, const ElemArgs &a, cudaStream_t 
 }
 
 // persistent grid: as many CTAs as fit on the device, one element per warp at a time
-template <bool MIXED>
-int launch_p2_moments(const double *jinv, const double *bary, const double *ds, const double *weight,
-                      const int8_t *branch, const double *shear, const double *lame, const int32_t *scatter_map,
-                      int n_elem, int n_q, long long nnz_out, double scale, double *out_values,
-                      const int32_t *elem_list, const int32_t *elem_count, cudaStream_t st) {
-    using Real = typename std::conditional<MIXED, float, double>::type;
-    constexpr int kWarps = kMomWarps<MIXED>;
-    const size_t smem = sizeof(MomentTables) + sizeof(MomentWarp<Real>) * kWarps;
-    if (cudaFuncSetAttribute(correction_p2_moment_kernel<MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem)) != cudaSuccess)
+template <typename Kernel>
+int launch_p2_moments(Kernel kernel, int warps, size_t smem, const double *jinv, const double *bary, const double *ds,
+                      const double *weight, const int8_t *branch, const double *shear, const double *lame,
+                      const int32_t *scatter_map, int n_elem, int n_q, long long nnz_out, double scale,
+                      double *out_values, const int32_t *elem_list, const int32_t *elem_count, cudaStream_t st) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
         return SSP_ERR_CUDA;
     int dev = 0, sms = 148, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, correction_p2_moment_kernel<MIXED>, 32 * kWarps, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * warps, smem);
     if (per_sm < 1) per_sm = 1;
     long long grid = (long long)sms * per_sm;
-    const long long need = (n_elem + kWarps - 1) / kWarps;
+    const long long need = (n_elem + warps - 1) / warps;
     if (grid > need) grid = need;
-    correction_p2_moment_kernel<MIXED><<<static_cast<unsigned>(grid), 32 * kWarps, smem, st>>>(
-        jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale, out_values, elem_list,
-        elem_count);
+    kernel<<<static_cast<unsigned>(grid), 32 * warps, smem, st>>>(jinv, bary, ds, weight, branch, shear, lame,
+                                                                 scatter_map, n_elem, n_q, nnz_out, scale, out_values,
+                                                                 elem_list, elem_count);
     return launch_status();
 }
 
@@ -1872,8 +2131,9 @@ int ssp_tangent_plastic_correction_p2_moments(const double *jinv, const double *
     if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    return launch_p2_moments<false>(jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out,
-                                    scale, out_values, elem_list, elem_count, as_stream(stream));
+    return launch_p2_moments(correction_p2_moment_kernel, kMomWarps, sizeof(MomentTables) + sizeof(MomentWarp) * kMomWarps,
+                             jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale,
+                             out_values, elem_list, elem_count, as_stream(stream));
 }
 
 int ssp_tangent_plastic_correction_p2_moments_mixed(const double *jinv, const double *bary, const double *ds,
@@ -1886,8 +2146,10 @@ int ssp_tangent_plastic_correction_p2_moments_mixed(const double *jinv, const do
     if (!jinv || !bary || !ds || !weight || !branch || !shear || !lame || !scatter_map || !elem_list || !elem_count ||
         (nnz_out > 0 && !out_values))
         return SSP_ERR_INVALID;
-    return launch_p2_moments<true>(jinv, bary, ds, weight, branch, shear, lame, scatter_map, n_elem, n_q, nnz_out,
-                                   scale, out_values, elem_list, elem_count, as_stream(stream));
+    return launch_p2_moments(correction_p2_moment_f32_kernel, kF32Warps,
+                             sizeof(MomentF32Tables) + sizeof(MomentF32Warp) * kF32Warps, jinv, bary, ds, weight,
+                             branch, shear, lame, scatter_map, n_elem, n_q, nnz_out, scale, out_values, elem_list,
+                             elem_count, as_stream(stream));
 }
 
 int ssp_fill_elastic_ds(int dim, const int8_t *branch, const double *shear, const double *lame, int n_int,
