@@ -379,9 +379,9 @@ def algorithmic(name, st):
     per_el = 288 * n_q + 24 * n_p * n_q + 8 * n_q + 4 * nld * nld + 8 * st["nnz"] / max(n_el, 1)
     fl_el = 2 * n_q * nld * (18 + 9 * n_p)
     if name == "ssp_tangent_plastic_correction_p2_moments_mixed":
-        # FP64 only for DS - D_el (12 nonzero D_el entries) and w s per plastic point; the rest FP32
+        # FP64 only for DS - D_el (21 entries) and w s per plastic point; the rest FP32
         units = st["n_many_el"]
-        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": 2.0 * 13 * st["n_plastic_many"],
+        return {"bytes": units * per_el, "flops": units * fl_el, "fp64": 2.0 * 22 * st["n_plastic_many"],
                 "units": f"{units:.0f} plastic elements in moment form per launch"}
     if name == "ssp_tangent_plastic_correction_p2_moments":
         # elements at or above the split: 7,530 FP64 operations per element + 261 per plastic point

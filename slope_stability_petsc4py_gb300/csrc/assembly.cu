@@ -1407,16 +1407,17 @@ __global__ void __launch_bounds__(32 * kMomWarps) correction_p2_moment_kernel(
 // The mixed form of the kernel above: DS - D_el and w s in FP64, rounded to FP32; the moments,
 // beta^T M beta, the lambda_4 sums and the element matrix in FP32; the element's 900 sums widened
 // exactly and reduced into the FP64 CSR values.  With the FP32 pipe far faster than the FP64 one,
-// the layout is chosen for few instructions rather than few operations: full 6 x 6 moments and full
-// 12 x 12 R blocks (shared-memory addresses are a lane base plus constants), beta^T M beta formed
-// in registers by one lane per (pair, component), the K entries grouped by node-pair type so each
-// group's four coefficients are constants, the element matrix unpadded.
+// the layout is chosen for few instructions rather than few operations: full 6 x 6 moments (their
+// shared-memory addresses a lane base plus constants), beta^T M beta formed in registers by one
+// lane per (pair, component) and stored by rows of the packed 12 x 12 upper triangle, the K entries
+// grouped by node-pair type so each group's four coefficients are constants, the element matrix
+// unpadded.  8.4 KB of shared memory per warp: three 8-warp CTAs per SM.
 constexpr int kF32Warps = 8;
 constexpr int kF32KEntries = 512;        // vertex-vertex 78 -> 96, vertex-edge 216 -> 224, edge-edge 171 -> 192
 constexpr int kF32VertexVertexIters = 3, kF32VertexEdgeIters = 7;
 
 struct MomentF32Tables {
-    unsigned long long k_terms[kF32KEntries];  // four R offsets (12 bits in 16-bit fields), term order (x, y)
+    unsigned long long k_terms[kF32KEntries];  // four packed R offsets (16-bit fields), term order (x, y)
     uint16_t k_pos[kF32KEntries];             // alpha << 5 | beta; 0xFFFF pads a type group
     float lam[kMaxQ][4];                      // the points' barycentric coordinates, rounded to FP32
     uint8_t s_pos[21];                        // r << 4 | c of the packed upper triangle of 6 x 6
@@ -1434,7 +1435,7 @@ struct MomentF32Warp {
         float ke[900];  // the element's correction, 30 x 30 row-major
     } x;
     float v[4][3];      // grad lambda_0..3
-    float R[15][144];   // R over the pairs m <= n of five coordinates, full 12 x 12
+    float R[15][78];    // R over the pairs m <= n of five coordinates, packed upper triangle of 12 x 12
     int8_t qidx[16];
 };
 
@@ -1482,7 +1483,7 @@ __device__ void build_moment_f32_tables(MomentF32Tables &tb, const double *bary,
                     int mx, cx, kx, my, cy, ky;
                     node_term(a, x, mx, cx, kx);
                     node_term(b, y, my, cy, ky);
-                    const unsigned off = static_cast<unsigned>(sym_index(mx, my, 5) * 144 + (3 * kx + c) * 12 + 3 * ky + d);
+                    const unsigned off = static_cast<unsigned>(sym_index(mx, my, 5) * 78 + sym_index(3 * kx + c, 3 * ky + d, 12));
                     packed |= static_cast<unsigned long long>(off) << (16 * (2 * x + y));
                 }
         }
@@ -1502,7 +1503,7 @@ __device__ void build_moment_f32_tables(MomentF32Tables &tb, const double *bary,
     }
 }
 
-__global__ void __launch_bounds__(32 * kF32Warps, 2) correction_p2_moment_f32_kernel(
+__global__ void __launch_bounds__(32 * kF32Warps, 3) correction_p2_moment_f32_kernel(
     const double *__restrict__ jinv, const double *__restrict__ bary, const double *__restrict__ DS,
     const double *__restrict__ w, const int8_t *__restrict__ branch, const double *__restrict__ shear,
     const double *__restrict__ lame, const int32_t *__restrict__ emap, int n_elem, int n_q, long long nnz,
@@ -1609,22 +1610,28 @@ __global__ void __launch_bounds__(32 * kF32Warps, 2) correction_p2_moment_f32_ke
 #pragma unroll
                 for (int k = 0; k < 4; ++k) T[k][t] = __fmaf_rn(vk[k][2], x2, __fmaf_rn(vk[k][1], x1, vk[k][0] * x0));
             }
-            float *Rp = &W.R[sym_index(mn >> 4, mn & 15, 5)][c * 12];
+            // row i = 3k + c of the packed upper triangle starts at i * 12 - i (i - 1) / 2 - i; the
+            // entries j = 3l + d >= i are stored (l > k always, l == k when d >= c)
+            float *Rp = &W.R[sym_index(mn >> 4, mn & 15, 5)][0];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                int sd[3], gd[3];
-                beta_rows(d, sd, gd);
+            for (int k = 0; k < 4; ++k) {
+                const int i = 3 * k + c;
+                float *row = Rp + (i * 11 - (i * (i - 1)) / 2);
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
+                for (int l = k; l < 4; ++l)
 #pragma unroll
-                    for (int l = 0; l < 4; ++l)
-                        Rp[k * 36 + 3 * l + d] =
-                            __fmaf_rn(T[k][sd[2]], vk[l][2], __fmaf_rn(T[k][sd[1]], vk[l][1], T[k][sd[0]] * vk[l][0]));
+                    for (int d = 0; d < 3; ++d) {
+                        int sd[3], gd[3];
+                        beta_rows(d, sd, gd);
+                        if (l > k || d >= c)
+                            row[3 * l + d] = __fmaf_rn(T[k][sd[2]], vk[l][2],
+                                                       __fmaf_rn(T[k][sd[1]], vk[l][1], T[k][sd[0]] * vk[l][0]));
+                    }
             }
         }
         __syncwarp();
         // R_m4 = sum_n R_mn, R_44 = sum_m R_m4 (pair indices over five coordinates)
-        for (int ee = lane; ee < 144; ee += 32) {
+        for (int ee = lane; ee < 78; ee += 32) {
             const float r00 = W.R[0][ee], r01 = W.R[1][ee], r02 = W.R[2][ee], r03 = W.R[3][ee];
             const float r11 = W.R[5][ee], r12 = W.R[6][ee], r13 = W.R[7][ee];
             const float r22 = W.R[9][ee], r23 = W.R[10][ee], r33 = W.R[12][ee];
@@ -1781,12 +1788,13 @@ __global__ void mark_rows_kernel(const int32_t *__restrict__ elem_row, int n_ele
     }
 }
 
-// The marked CSR rows of src stored to dst (device-mapped host memory), a warp per row: each store
-// instruction writes 256 contiguous bytes of one row over the host link; unmarked rows cost one
-// byte read.
+// The marked CSR rows of src stored to dst (device-mapped host memory), a warp per row.  With both
+// arrays 16-byte aligned (vec) the row's body goes as 16-byte stores, 512 contiguous bytes per warp
+// instruction over the host link, an odd first or last value as one 8-byte store; unmarked rows
+// cost one byte read.
 __global__ void copy_rows_out_kernel(const double *__restrict__ src, const int32_t *__restrict__ indptr,
                                      const uint8_t *__restrict__ mark, int n_rows, long long nnz,
-                                     double *__restrict__ dst) {
+                                     double *__restrict__ dst, int vec) {
     const int lane = threadIdx.x & 31;
     const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < n_rows; row += warps) {
@@ -1796,7 +1804,20 @@ __global__ void copy_rows_out_kernel(const double *__restrict__ src, const int32
             if (lane == 0) flag(SSP_DEV_BAD_INDEX);
             continue;
         }
-        for (long long k = b + lane; k < e; k += 32) dst[k] = src[k];
+        if (!vec) {
+            for (long long k = b + lane; k < e; k += 32) dst[k] = src[k];
+            continue;
+        }
+        const long long b2 = (b + 1) & ~1ll, e2 = e & ~1ll;  // [b2, e2): whole 16-byte pairs
+        if (b2 >= e2) {  // fewer than two values past an odd start
+            for (long long k = b + lane; k < e; k += 32) dst[k] = src[k];
+            continue;
+        }
+        if (lane == 0 && b < b2) dst[b] = src[b];
+        if (lane == 1 && e2 < e) dst[e2] = src[e2];
+        const double2 *s2 = reinterpret_cast<const double2 *>(src + b2);
+        double2 *d2 = reinterpret_cast<double2 *>(dst + b2);
+        for (long long k = lane; k < (e2 - b2) / 2; k += 32) d2[k] = s2[k];
     }
 }
 
@@ -2257,8 +2278,9 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 ? 1 : 0;
     copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
-                                                                                       nnz, dst);
+                                                                                       nnz, dst, vec);
     return launch_status();
 }
 
@@ -2270,8 +2292,9 @@ int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 ? 1 : 0;
     copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
-                                                                                       nnz, dst);
+                                                                                       nnz, dst, vec);
     return launch_status();
 }
 

@@ -156,4 +156,23 @@ def test_copy_out_into_pinned_memory(cuda_device):
     rows = mark.cpu().numpy().astype(bool).repeat(per)
     expect = np.where(rows, src.cpu().numpy(), 0.0)
     assert np.array_equal(host.numpy(), expect)
+    # ragged rows (0 to 9 values, odd and even starts and ends: scalar heads / tails around the
+    # 16-byte body), to the host and device to device
+    lengths = np.random.default_rng(3).integers(0, 10, size=997)
+    rp = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int32)
+    nnz = int(rp[-1])
+    src = torch.randn(nnz, dtype=torch.float64, device="cuda")
+    mark = torch.as_tensor(np.random.default_rng(4).random(lengths.size) < 0.5, device="cuda").to(torch.uint8)
+    indptr = torch.as_tensor(rp, device="cuda")
+    sel = np.repeat(mark.cpu().numpy().astype(bool), lengths)
+    host = torch.zeros(nnz, dtype=torch.float64, pin_memory=True)
+    _lib.call("ssp_copy_rows_out", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), lengths.size, nnz,
+              host.data_ptr(), _lib.stream_handle())
+    dev = torch.zeros(nnz, dtype=torch.float64, device="cuda")
+    _lib.call("ssp_copy_rows_device", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), lengths.size, nnz,
+              _lib.ptr(dev), _lib.stream_handle())
+    torch.cuda.synchronize()
+    expect = np.where(sel, src.cpu().numpy(), 0.0)
+    assert np.array_equal(host.numpy(), expect)
+    assert np.array_equal(dev.cpu().numpy(), expect)
     _lib.raise_on_device_status()
