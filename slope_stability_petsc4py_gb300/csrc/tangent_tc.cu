@@ -15,22 +15,23 @@
 //
 // Accuracy.  A tensor-core MMA rounds its FP32 result once per instruction, so errors grow with
 // the number of MMAs that feed one accumulator.  The points of an element are taken in groups of
-// four (K = 24, three K = 8 steps); each group has its own pair of accumulators (hi*hi: three
-// MMAs, cross terms: six, 2^-11 smaller), and every group's two partial sums are added into
-// compensated (Kahan) FP32 sums of the element (widened exactly to FP64 once per element).  The FP64
+// four (K = 24, three K = 8 steps), and two consecutive groups of an element (a batch) share a pair
+// of accumulators (hi*hi: up to six MMAs, cross terms: up to twelve, 2^-11 smaller); every batch's
+// two partial sums are added into compensated (Kahan) FP32 sums of the element (widened exactly
+// to FP64 once per element).  The FP64
 // element sums are added to the CSR values with FP64 reductions through the element->CSR map, on
 // both mirror positions of alpha <= beta, so the correction is exactly symmetric.
 //
 // Tile: M = 128 rows (alpha, 105 used), N = 112 columns (beta, 105 used).  One CTA of 512 threads
 // per SM, grid-striding over elements; it owns all 512 tensor-memory columns (two accumulator
-// pairs at columns 0 / 128 and 256 / 384, alternating between groups).  The warps specialise:
+// pairs at columns 0 / 128 and 256 / 384, alternating between batches).  The warps specialise:
 // warps 0-7 build each group's operands into one of two stage buffers and one of their threads
 // issues the group's MMAs; warps 8-15 drain each accumulator pair into the element's compensated
-// sums, which live in shared memory, and scatter the element row by row (so the reductions of a
-// warp fall on neighbouring entries of one CSR row).  The roles hand off through mbarriers (the MMA
-// commit of a pair, and the eight drain warps' release of it) and synchronise inside a role with
-// named barriers, so the builders form group g + 1 while the tensor cores multiply group g and the
-// drain warps read group g - 1 or scatter the previous element.
+// sums, which live in shared memory, and scatter the finished element.  The roles hand off through
+// mbarriers (the MMA commit of a stage buffer, the MMA commit of a batch into a pair, and the
+// eight drain warps' release of the pair) and synchronise inside a role with named barriers, so
+// the builders form group g + 1 while the tensor cores multiply group g and the drain warps read
+// the previous batch or scatter the previous element.
 //
 // Operand layout in shared memory: K-major, no swizzle, in 8-row x 16-byte core matrices:
 // byte offset(row, kappa) = ((kappa / 4) * (rows / 8) + row / 8) * 128 + (row % 8) * 16 + (kappa % 4) * 4,
@@ -88,8 +89,9 @@ struct Smem {
     PointData pts;
     RawInputs raw;
     float2 ke[kNLD * kKeStride];  // the element's compensated FP32 sums (s, c), upper triangle used
-    unsigned long long acc_full[2];   // commit of the MMAs into accumulator pair b (count 1)
-    unsigned long long acc_empty[2];  // the eight drain warps have read pair b (count 8)
+    unsigned long long stage_free[2];  // commit of the MMAs that read stage buffer b (count 1)
+    unsigned long long acc_full[2];    // commit of a batch's MMAs into accumulator pair b (count 1)
+    unsigned long long acc_empty[2];   // the eight drain warps have read pair b (count 8)
     uint32_t tmem_slot;
     int abort;   // any role gave up on a wait (the device status has SSP_DEV_TIMEOUT)
     int babort;  // the builders stop (read only after a builders' barrier)
@@ -153,9 +155,10 @@ __device__ __forceinline__ long long element_at(const int32_t *elist, long long 
 // Builders: per group of four plastic points, the inputs (copied one group ahead by cp.async, each
 // thread converting the entries it copied), then H = B^T dD (compensated double-float dot products)
 // and the nonzeros of B, both split into TF32 pairs, into the stage buffer of the group's parity;
-// one thread issues the nine MMAs into the accumulator pair of that parity and commits them to
-// acc_full.  A stage buffer is rewritten only after the MMAs that read it (two groups back) have
-// completed, an accumulator pair only after the drain warps have read it (acc_empty).
+// one thread issues the nine MMAs into the accumulator pair of the batch's parity and commits them
+// to stage_free (and, after a batch's last group, to acc_full).  A stage buffer is rewritten only
+// after the MMAs that read it (two groups back) have completed, an accumulator pair only after the
+// drain warps have read it (acc_empty, two batches back).
 __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double *__restrict__ d1,
                                            const double *__restrict__ d2, const double *__restrict__ d3,
                                            const double *__restrict__ DS, const double *__restrict__ w,
@@ -163,7 +166,8 @@ __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double 
                                            const double *__restrict__ lame, int n_elem, double scale,
                                            const int32_t *__restrict__ elist, long long n_iter) {
     const int bt = threadIdx.x, warp = bt >> 5, lane = bt & 31;
-    uint32_t G = 0;  // the CTA's running group count (the drain warps count the same sequence)
+    uint32_t G = 0;   // the CTA's running group count (stage buffer G & 1)
+    uint32_t Bn = 0;  // the CTA's running batch count (accumulator pair Bn & 1; the drain warps count the same)
     for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
         const long long e = element_at(elist, it, n_elem);
         if (e < 0) {  // uniform
@@ -206,7 +210,9 @@ __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double 
         };
         load_group(0);
         for (int grp = 0; grp < groups; ++grp, ++G) {
-            const int b = G & 1;
+            const int b = G & 1, pb = Bn & 1;
+            // a batch is two consecutive groups of the element (the last one alone when their number is odd)
+            const bool first = (grp & 1) == 0, last = (grp & 1) == 1 || grp + 1 == groups;
             cp_async_wait_all();
             for (int i = bt; i < kPts * 3 * kNP; i += kBuildThreads) {
                 const int gi_pi = i / (3 * kNP), gi_r = (i % (3 * kNP)) / kNP, gi_a = i % kNP;
@@ -228,7 +234,7 @@ __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double 
             if (bt == 0) {  // stage b was last read by the MMAs of group G - 2
                 if (S.abort) {
                     S.babort = 1;
-                } else if (G >= 2 && !mbar_wait(smem_u32(&S.acc_full[b]), ((G - 2) >> 1) & 1u)) {
+                } else if (G >= 2 && !mbar_wait(smem_u32(&S.stage_free[b]), ((G - 2) >> 1) & 1u)) {
                     S.babort = S.abort = 1;
                     flag(SSP_DEV_TIMEOUT);
                 }
@@ -278,7 +284,7 @@ __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double 
             named_bar(kBarBuild, kBuildThreads);  // stage b complete
             if (bt == 0) {
                 bool ok = !S.abort;
-                if (ok && G >= 2 && !mbar_wait(smem_u32(&S.acc_empty[b]), ((G - 2) >> 1) & 1u)) {
+                if (ok && first && Bn >= 2 && !mbar_wait(smem_u32(&S.acc_empty[pb]), ((Bn - 2) >> 1) & 1u)) {
                     ok = false;
                     S.abort = 1;
                     flag(SSP_DEV_TIMEOUT);
@@ -286,27 +292,28 @@ __device__ __forceinline__ void build_role(Smem &S, uint32_t tmem, const double 
                 if (ok) {
                     fence_after_sync();
                     const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-                    const uint32_t t_hh = tmem + 256u * b, t_x = t_hh + 128u;
+                    const uint32_t t_hh = tmem + 256u * pb, t_x = t_hh + 128u;
 #pragma unroll
                     for (int s = 0; s < kK / 8; ++s) {
                         const uint32_t oa = s * 2 * kLboA, ob = s * 2 * kLboB;
-                        mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc,
-                                 s != 0 ? 1u : 0u);
-                        mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), kIdesc,
-                                 s != 0 ? 1u : 0u);
+                        const uint32_t acc = (s != 0 || !first) ? 1u : 0u;  // a batch's first MMAs overwrite
+                        mma_tf32(t_hh, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, acc);
+                        mma_tf32(t_x, smem_desc(ah + oa, kLboA, kSbo), smem_desc(bl + ob, kLboB, kSbo), kIdesc, acc);
                         mma_tf32(t_x, smem_desc(al + oa, kLboA, kSbo), smem_desc(bh + ob, kLboB, kSbo), kIdesc, 1u);
                     }
-                    mma_commit(smem_u32(&S.acc_full[b]));
+                    mma_commit(smem_u32(&S.stage_free[b]));
+                    if (last) mma_commit(smem_u32(&S.acc_full[pb]));
                 } else {
                     S.babort = 1;  // seen by the builders after their next barrier
                 }
             }
+            if (last) ++Bn;
         }
     }
     cp_async_wait_all();
 }
 
-// Drain warps: per group, one lane waits for the commit (acc_full of the group's parity), the warp
+// Drain warps: per batch, one lane waits for the commit (acc_full of the batch's parity), the warp
 // reads its 32 accumulator rows x 56 columns of both accumulators (hi * hi, cross terms) and adds
 // their sum into the element's compensated sums in shared memory (upper triangle only), then
 // releases the pair (acc_empty).  After an element's last group the 256 drain threads scatter the
@@ -320,7 +327,7 @@ __device__ __forceinline__ void drain_role(Smem &S, uint32_t tmem, const int8_t 
     const int row = 32 * lq + lane, col0 = kDrainCols * chalf;
     const uint32_t lane_col = (static_cast<uint32_t>(32 * lq) << 16) + static_cast<uint32_t>(col0);
     float2 *kr = S.ke + row * kKeStride;  // this lane's row of sums (row < kNLD)
-    uint32_t G = 0;
+    uint32_t Bn = 0;  // running batch count, as the builders count it
     for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
         const long long e = element_at(elist, it, n_elem);
         if (e < 0) continue;  // uniform (the builders flag it)
@@ -335,12 +342,13 @@ __device__ __forceinline__ void drain_role(Smem &S, uint32_t tmem, const int8_t 
             }
         }
         bool skipped = false;
-        for (int grp = 0; grp < groups; ++grp, ++G) {
-            const int b = G & 1;
+        const int batches = (groups + 1) / 2;
+        for (int bi = 0; bi < batches; ++bi, ++Bn) {
+            const int b = Bn & 1;
             int ok = 0;
             if (lane == 0) {
                 ok = !S.abort;
-                if (ok && !mbar_wait(smem_u32(&S.acc_full[b]), (G >> 1) & 1u)) {
+                if (ok && !mbar_wait(smem_u32(&S.acc_full[b]), (Bn >> 1) & 1u)) {
                     ok = 0;
                     S.abort = 1;
                     flag(SSP_DEV_TIMEOUT);
@@ -423,6 +431,8 @@ __global__ void __launch_bounds__(kThreads, 1) correction_tc_p4_kernel(
     // zero both stages once: the padding rows (alpha >= 105, beta >= 105) are never written again
     for (int i = tid; i < (int)(sizeof(Stage) * 2 / 4); i += kThreads) reinterpret_cast<uint32_t *>(S.stage)[i] = 0u;
     if (tid == 0) {
+        mbar_init(smem_u32(&S.stage_free[0]));
+        mbar_init(smem_u32(&S.stage_free[1]));
         mbar_init(smem_u32(&S.acc_full[0]));
         mbar_init(smem_u32(&S.acc_full[1]));
         mbar_init_count(smem_u32(&S.acc_empty[0]), kDrainThreads / 32);
