@@ -602,43 +602,42 @@ __device__ __forceinline__ double elastic_d(int i, int j, double G, double lam) 
 // full tangent with the FP64 work of the plastic points only: for an elastic point DS_q equals
 // D_el,q exactly, so its term vanishes.
 template <int DIM, int NP, int NQ, int THREADS, bool SYM, bool CORR>
-__global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
+__global__ void __launch_bounds__(THREADS, SYM ? 2 : 1) tangent_element_kernel(ElemArgs A) {
     constexpr int NS = DIM == 3 ? 6 : 3;
     constexpr int NLD = DIM * NP;
     constexpr int NENT = SYM ? NLD * (NLD + 1) / 2 : NLD * NLD;
     constexpr int PER = (NENT + THREADS - 1) / THREADS;
+    static_assert(NLD < 256, "entry codes hold alpha and beta in 8 bits each");
     __shared__ double sg[NQ][DIM][NP];
     __shared__ double sD[NQ][NS * NS];
     __shared__ double sH[NLD * NS];
+    // SYM: entry id -> alpha | beta << 8 of the row-major upper triangle, 0xFFFF past the last entry
+    // (in shared memory rather than registers, so two CTAs fit an SM); the full matrix decodes
+    // id = alpha NLD + beta directly
+    __shared__ uint16_t scode[SYM ? PER * THREADS : 1];
     __shared__ int sq[NQ];
     __shared__ int snq;
 
     const int tid = threadIdx.x;
-    // per-thread entry descriptors: alpha | beta << 8 (alpha, beta < 256), or -1
-    int code[PER];
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        const int id = tid + i * THREADS;
-        int c = -1;
-        if (id < NENT) {
-            int a, b;
-            if (SYM) {
-                // row-major upper triangle: row a holds NLD - a entries
-                int rem = id;
-                a = 0;
+    if (SYM) {
+        for (int id = tid; id < PER * THREADS; id += THREADS) {
+            uint16_t c = 0xFFFFu;
+            if (id < NENT) {
+                int rem = id, a = 0;  // row a holds NLD - a entries
                 while (rem >= NLD - a) {
                     rem -= NLD - a;
                     ++a;
                 }
-                b = a + rem;
-            } else {
-                a = id / NLD;
-                b = id % NLD;
+                c = static_cast<uint16_t>(a | ((a + rem) << 8));
             }
-            c = a | (b << 8);
+            scode[id] = c;
         }
-        code[i] = c;
     }
+    auto entry_code = [&](int i) -> int {
+        const int id = tid + i * THREADS;
+        if (SYM) return scode[id];
+        return id < NENT ? ((id / NLD) | ((id % NLD) << 8)) : 0xFFFF;
+    };
 
     const long long n_iter = element_iterations(A);
     for (long long it = blockIdx.x; it < n_iter; it += gridDim.x) {
@@ -689,8 +688,8 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < PER; ++i) {
-                const int c = code[i];
-                if (c >= 0) {
+                const int c = entry_code(i);
+                if (c != 0xFFFF) {
                     const int alpha = c & 0xff, beta = c >> 8;
                     const int b = beta / DIM, cp = beta % DIM;
                     double v = acc[i];
@@ -708,8 +707,8 @@ __global__ void __launch_bounds__(THREADS) tangent_element_kernel(ElemArgs A) {
         const int32_t *em = A.emap + (long long)e * NLD * NLD;
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
-            const int c = code[i];
-            if (c < 0) continue;
+            const int c = entry_code(i);
+            if (c == 0xFFFF) continue;
             const int alpha = c & 0xff, beta = c >> 8;
             const int32_t p = em[alpha * NLD + beta];
             if (p >= 0) {
