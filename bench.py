@@ -52,9 +52,12 @@ SAMPLE_POINTS, SAMPLE_POINTS_1T = 4_000_000, 250_000
 # DRAM bytes (read + write) per launch of the step kernels, from one ncu capture each (the command in
 # profiles/dram_traffic_3d_p2_large.md), keyed by workload and entry point; reported as roofline.traffic
 # with that source when the bench's dominant kernel is one of them
-NCU_TRAFFIC = {"3d_p2_large": {"ssp_tangent_plastic_correction": (4146e6 + 1475e6,
-                                                                  "ncu capture 2026-12-04, "
-                                                                  "profiles/dram_traffic_3d_p2_large.md")}}
+NCU_TRAFFIC = {"3d_p2_large": {
+    "ssp_tangent_plastic_correction_p2_moments": (2994.5e6 + 1058.4e6,
+                                                  "ncu capture 2026-12-04, profiles/dram_traffic_3d_p2_large.md"),
+    "ssp_tangent_plastic_correction_p2_moments_mixed": (4694.0e6 + 1440.7e6,
+                                                        "ncu capture 2026-12-04, profiles/dram_traffic_3d_p2_large.md"),
+}}
 STEP_TEXT = ("reduction + strain + return mapping (S, DS) + owned force + tangent CSR values + constrained diagonals "
              "+ regularised blend")
 
