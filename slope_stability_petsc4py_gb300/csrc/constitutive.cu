@@ -34,6 +34,33 @@ struct Principal3 {
     double I1, e1, e2, e3;
 };
 
+// sin and cos of a Lode angle theta in [0, pi/3] from their Taylor series, Horner in theta^2: the
+// first omitted terms, theta^19 / 19! and theta^20 / 20!, are below 2e-17 there, and without a
+// branch every lane of a warp runs the same instructions (a general sincos reduces its argument by
+// quadrants, and pi/4 < pi/3).  Within one ulp of the correctly rounded values on [0, pi/3].
+__device__ __forceinline__ void sincos_lode(double theta, double &s, double &c) {
+    const double z = theta * theta;
+    double ps = 1.0 / 355687428096000.0;  // 1/17!
+    ps = fma(ps, z, -1.0 / 1307674368000.0);
+    ps = fma(ps, z, 1.0 / 6227020800.0);
+    ps = fma(ps, z, -1.0 / 39916800.0);
+    ps = fma(ps, z, 1.0 / 362880.0);
+    ps = fma(ps, z, -1.0 / 5040.0);
+    ps = fma(ps, z, 1.0 / 120.0);
+    ps = fma(ps, z, -1.0 / 6.0);
+    s = fma(theta * z, ps, theta);
+    double pc = -1.0 / 6402373705728000.0;  // -1/18!
+    pc = fma(pc, z, 1.0 / 20922789888000.0);
+    pc = fma(pc, z, -1.0 / 87178291200.0);
+    pc = fma(pc, z, 1.0 / 479001600.0);
+    pc = fma(pc, z, -1.0 / 3628800.0);
+    pc = fma(pc, z, 1.0 / 40320.0);
+    pc = fma(pc, z, -1.0 / 720.0);
+    pc = fma(pc, z, 1.0 / 24.0);
+    pc = fma(pc, z, -0.5);
+    c = fma(z, pc, 1.0);
+}
+
 __device__ __forceinline__ void principal3(const double *E, Principal3 &p) {
 #pragma unroll
     for (int i = 0; i < 6; ++i) p.t[i] = half_ident(i) * E[i];
@@ -61,9 +88,10 @@ __device__ __forceinline__ void principal3(const double *E, Principal3 &p) {
     }
     const double third = I1 * (1.0 / 3.0);
     p.I1 = I1;
-    // cos(theta -+ 2 pi/3) = -cos(theta)/2 +- (sqrt(3)/2) sin(theta): one sincos instead of three cos
+    // cos(theta -+ 2 pi/3) = -cos(theta)/2 +- (sqrt(3)/2) sin(theta): one sine and cosine instead of
+    // three cosines
     double st, ct;
-    sincos(theta, &st, &ct);
+    sincos_lode(theta, st, ct);
     const double r3 = 1.7320508075688772 * st;
     p.e1 = rq * (ct + r3) + third;
     p.e2 = rq * (ct - r3) + third;
