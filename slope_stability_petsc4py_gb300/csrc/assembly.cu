@@ -2283,8 +2283,9 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
     return launch_status();
 }
 
-int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
-                         double *dst, void *stream) {
+namespace {
+int copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                     double *dst, int blocks_per_sm, void *stream) {
     if (n_rows < 0 || nnz < 0) return SSP_ERR_INVALID;
     if (n_rows == 0 || nnz == 0) return SSP_OK;
     if (!src || !indptr || !row_mark || !dst) return SSP_ERR_INVALID;
@@ -2292,9 +2293,23 @@ int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 ? 1 : 0;
-    copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
-                                                                                       nnz, dst, vec);
+    copy_rows_out_kernel<<<static_cast<unsigned>(sms * blocks_per_sm), 256, 0, as_stream(stream)>>>(
+        src, indptr, row_mark, n_rows, nnz, dst, vec);
     return launch_status();
+}
+}  // namespace
+
+int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
+                         double *dst, void *stream) {
+    return copy_rows_device(src, indptr, row_mark, n_rows, nnz, dst, 8, stream);
+}
+
+// Two 256-thread blocks per SM: on a second stream beside FP64-bound kernels the copy takes a small
+// share of each SM's threads and registers and leaves the rest to them (a grid that fills every SM
+// would run before them instead of beside them).
+int ssp_copy_rows_device_beside(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
+                                long long nnz, double *dst, void *stream) {
+    return copy_rows_device(src, indptr, row_mark, n_rows, nnz, dst, 2, stream);
 }
 
 int ssp_copy_device(const double *src, long long n, double *dst, void *stream) {

@@ -629,7 +629,7 @@ class ConstitutiveOperator:
         else:
             dst.copy_(src)
 
-    def _restore_start(self, values, start, kind, key):
+    def _restore_start(self, values, start, kind, key, staged=False):
         """values := start.  When values holds start plus the corrections of the last build of this
         kind with the same start (key), only the rows of that build's plastic elements differ from
         start, and only those rows are copied (row marks through the element -> row map, then a row
@@ -649,8 +649,12 @@ class ConstitutiveOperator:
         elist, ecount = dv["plastic_lists"][kind][last["list"]]
         _lib.call("ssp_mark_element_rows", _lib.ptr(d["elem_row"]), n_el, pat.dim * pat.n_p, _lib.ptr(elist),
                   _lib.ptr(ecount), n_rows, _lib.ptr(mark), st)
-        _lib.call("ssp_copy_rows_device", _lib.ptr(start), _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows,
-                  int(values.numel()), _lib.ptr(values), st)
+        # staged beside the strain and return mapping: with many points per CSR entry (P2) those run
+        # long enough to hide a slower copy on a small share of the SMs; with few (P4) the copy takes
+        # the whole device ahead of them
+        beside = staged and pat.n_local_int >= 0.01 * pat.nnz
+        _lib.call("ssp_copy_rows_device_beside" if beside else "ssp_copy_rows_device", _lib.ptr(start),
+                  _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows, int(values.numel()), _lib.ptr(values), st)
 
     def _stage_values(self, r):
         """Issue the copy of the regularised tangent's starting values into its values array on the
@@ -672,7 +676,7 @@ class ConstitutiveOperator:
         main, side = t.cuda.current_stream(), self._aux_stream()
         side.wait_stream(main)
         with t.cuda.stream(side):
-            self._restore_start(values, start, "regularized", ("regularized", float(r)))
+            self._restore_start(values, start, "regularized", ("regularized", float(r)), staged=True)
         values.record_stream(side)
         start.record_stream(side)
         done = t.cuda.Event()
