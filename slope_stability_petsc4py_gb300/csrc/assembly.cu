@@ -2278,7 +2278,9 @@ int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *r
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 ? 1 : 0;
-    copy_rows_out_kernel<<<static_cast<unsigned>(sms * 8), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
+    // two 256-thread blocks per SM keep the host link busy and leave most of each SM to the kernels
+    // that run beside the copy (the internal force of the same Newton iteration)
+    copy_rows_out_kernel<<<static_cast<unsigned>(sms * 2), 256, 0, as_stream(stream)>>>(src, indptr, row_mark, n_rows,
                                                                                        nnz, dst, vec);
     return launch_status();
 }

@@ -651,8 +651,11 @@ class ConstitutiveOperator:
                   _lib.ptr(ecount), n_rows, _lib.ptr(mark), st)
         # staged beside the strain and return mapping: with many points per CSR entry (P2) those run
         # long enough to hide a slower copy on a small share of the SMs; with few (P4) the copy takes
-        # the whole device ahead of them
-        beside = staged and pat.n_local_int >= 0.01 * pat.nnz
+        # the whole device ahead of them.  The single-pass (unsorted) and learned return mappings run
+        # kernels that need a whole SM (their registers, or the network's tensor memory) and would
+        # wait for the copy instead: there too it takes the whole device
+        beside = (staged and self.return_mapping in ("binned", "previous") and
+                  pat.n_local_int >= 0.01 * pat.nnz)
         _lib.call("ssp_copy_rows_device_beside" if beside else "ssp_copy_rows_device", _lib.ptr(start),
                   _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows, int(values.numel()), _lib.ptr(values), st)
 
