@@ -15,6 +15,8 @@
 // Layout (all FP64 unless stated): points are element-major (g = e*n_q + q); dphi arrays are
 // [n_int][n_p]; strains/stresses/tangents are per-point AoS ([n_int][6], [n_int][36]), which is
 // the reference's C layout and makes each element's data one contiguous block.
+#include <type_traits>
+
 #include "ssp_internal.cuh"
 
 namespace ssp {
