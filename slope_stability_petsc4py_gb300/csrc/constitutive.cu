@@ -795,7 +795,9 @@ __global__ void __launch_bounds__(128) mc3d_bin_kernel(const double *__restrict_
     if (listed) scratch[4 + slot] = p;
 }
 
-__global__ void __launch_bounds__(128) mc3d_decide_kernel(const double *__restrict__ E,
+// five CTAs per SM (at most 102 registers; 96 used without spills): the pass is FP64-bound with long
+// dependent chains per point, and more resident warps hide more of their latency
+__global__ void __launch_bounds__(128, 5) mc3d_decide_kernel(const double *__restrict__ E,
                                                           const double *__restrict__ c_bar,
                                                           const double *__restrict__ sin_phi,
                                                           const double *__restrict__ shear,
