@@ -396,11 +396,11 @@ int ssp_copy_device(const double *src, long long n, double *dst, void *stream);
 int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
                          double *dst, void *stream);
 
-/* No reference counterpart.  ssp_copy_rows_device with a grid of two 256-thread blocks per SM, for a
- * copy issued on a second stream beside long FP64-bound kernels: it runs beside them rather than
- * ahead of them, at a lower rate of its own. */
-int ssp_copy_rows_device_beside(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
-                                long long nnz, double *dst, void *stream);
+/* No reference counterpart.  ssp_copy_rows_device with a grid of blocks_per_sm (1..8) 256-thread
+ * blocks per SM (ssp_copy_rows_device: 8), for a copy issued on a second stream beside long kernels:
+ * with a small share it runs beside them rather than ahead of them, at a lower rate of its own. */
+int ssp_copy_rows_device_share(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
+                               long long nnz, double *dst, int blocks_per_sm, void *stream);
 
 /* dst_host[0..n) = src[0..n) written by the SMs into pinned, device-mapped host memory
  * (ssp_host_writable(dst_host) must hold, else SSP_ERR_INVALID); asynchronous on the stream.

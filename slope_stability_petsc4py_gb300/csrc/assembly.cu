@@ -2308,12 +2308,13 @@ int ssp_copy_rows_device(const double *src, const int32_t *indptr, const uint8_t
     return copy_rows_device(src, indptr, row_mark, n_rows, nnz, dst, 8, stream);
 }
 
-// Two 256-thread blocks per SM: on a second stream beside FP64-bound kernels the copy takes a small
-// share of each SM's threads and registers and leaves the rest to them (a grid that fills every SM
-// would run before them instead of beside them).
-int ssp_copy_rows_device_beside(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
-                                long long nnz, double *dst, void *stream) {
-    return copy_rows_device(src, indptr, row_mark, n_rows, nnz, dst, 2, stream);
+// A grid of blocks_per_sm 256-thread blocks per SM (1..8): on a second stream beside long kernels a
+// small share of each SM's threads and registers leaves the rest to them (a grid that fills every
+// SM would run before them instead of beside them).
+int ssp_copy_rows_device_share(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
+                               long long nnz, double *dst, int blocks_per_sm, void *stream) {
+    if (blocks_per_sm < 1 || blocks_per_sm > 8) return SSP_ERR_INVALID;
+    return copy_rows_device(src, indptr, row_mark, n_rows, nnz, dst, blocks_per_sm, stream);
 }
 
 int ssp_copy_device(const double *src, long long n, double *dst, void *stream) {

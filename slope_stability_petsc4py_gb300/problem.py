@@ -279,6 +279,8 @@ class ConstitutiveOperator:
         # time as the tangent; measured 2-5 % slower than one stream on the GB300 (the two compete
         # for the SMs), so off by default
         self.concurrent_force = False
+        # blocks per SM of the staged row restore (1..8); None: chosen from the points per CSR entry
+        self.restore_share = None
         self._force_stream = None
         self._owned_overlap_c_bar = None
         self._owned_overlap_sin_phi = None
@@ -650,14 +652,16 @@ class ConstitutiveOperator:
         _lib.call("ssp_mark_element_rows", _lib.ptr(d["elem_row"]), n_el, pat.dim * pat.n_p, _lib.ptr(elist),
                   _lib.ptr(ecount), n_rows, _lib.ptr(mark), st)
         # staged beside the strain and return mapping: with many points per CSR entry (P2) those run
-        # long enough to hide a slower copy on a small share of the SMs; with few (P4) the copy takes
-        # the whole device ahead of them.  The single-pass (unsorted) and learned return mappings run
-        # kernels that need a whole SM (their registers, or the network's tensor memory) and would
-        # wait for the copy instead: there too it takes the whole device
-        beside = (staged and self.return_mapping in ("binned", "previous") and
-                  pat.n_local_int >= 0.01 * pat.nnz)
-        _lib.call("ssp_copy_rows_device_beside" if beside else "ssp_copy_rows_device", _lib.ptr(start),
-                  _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows, int(values.numel()), _lib.ptr(values), st)
+        # long enough to hide a slower copy on a small share of the SMs (two blocks per SM); with few
+        # (P4) they are short, and shares of 4 to 8 blocks per SM measured the same, so the copy
+        # keeps the whole device.  The single-pass (unsorted) and learned return mappings run kernels
+        # that need a whole SM (their registers, or the network's tensor memory) and would wait for
+        # the copy instead: there too it takes the whole device
+        share = 8
+        if staged and self.return_mapping in ("binned", "previous"):
+            share = self.restore_share or (2 if pat.n_local_int >= 0.01 * pat.nnz else 8)
+        _lib.call("ssp_copy_rows_device_share", _lib.ptr(start), _lib.ptr(d["indptr"]), _lib.ptr(mark), n_rows,
+                  int(values.numel()), _lib.ptr(values), int(share), st)
 
     def _stage_values(self, r):
         """Issue the copy of the regularised tangent's starting values into its values array on the
