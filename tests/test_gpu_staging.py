@@ -171,8 +171,15 @@ def test_copy_out_into_pinned_memory(cuda_device):
     dev = torch.zeros(nnz, dtype=torch.float64, device="cuda")
     _lib.call("ssp_copy_rows_device", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), lengths.size, nnz,
               _lib.ptr(dev), _lib.stream_handle())
+    dev2 = torch.zeros(nnz, dtype=torch.float64, device="cuda")  # the small grid of a staged restore
+    _lib.call("ssp_copy_rows_device_share", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), lengths.size, nnz,
+              _lib.ptr(dev2), 2, _lib.stream_handle())
     torch.cuda.synchronize()
     expect = np.where(sel, src.cpu().numpy(), 0.0)
     assert np.array_equal(host.numpy(), expect)
     assert np.array_equal(dev.cpu().numpy(), expect)
+    assert np.array_equal(dev2.cpu().numpy(), expect)
+    with pytest.raises(_lib.SSPError):  # 1..8 blocks per SM
+        _lib.call("ssp_copy_rows_device_share", _lib.ptr(src), _lib.ptr(indptr), _lib.ptr(mark), lengths.size,
+                  nnz, _lib.ptr(dev2), 9, _lib.stream_handle())
     _lib.raise_on_device_status()
