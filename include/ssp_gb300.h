@@ -419,6 +419,11 @@ int ssp_mark_element_rows(const int32_t *elem_row, int n_elem, int n_ld, const i
 int ssp_copy_rows_out(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows, long long nnz,
                       double *dst_host, void *stream);
 
+/* No reference counterpart.  ssp_copy_rows_out with a grid of blocks_per_sm (1..8) 256-thread blocks
+ * per SM (ssp_copy_rows_out: 4, which leaves half of each SM's threads to the kernels beside it). */
+int ssp_copy_rows_out_share(const double *src, const int32_t *indptr, const uint8_t *row_mark, int n_rows,
+                            long long nnz, double *dst_host, int blocks_per_sm, void *stream);
+
 /* Reads the device status word (SSP_DEV_* bits); clear != 0 resets it.  Synchronous. */
 int ssp_device_status(int *status_out, int clear);
 

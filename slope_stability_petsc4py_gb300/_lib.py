@@ -46,6 +46,7 @@ _SIGS = {
     "ssp_copy_rows_device_share": [_vp, _vp, _vp, _c_int, _c_ll, _vp, _c_int, _vp],
     "ssp_mark_element_rows": [_vp, _c_int, _c_int, _vp, _vp, _c_int, _vp, _vp],
     "ssp_copy_rows_out": [_vp, _vp, _vp, _c_int, _c_ll, _vp, _vp],
+    "ssp_copy_rows_out_share": [_vp, _vp, _vp, _c_int, _c_ll, _vp, _c_int, _vp],
     "ssp_tc_tf32_probe": [_vp, _vp, _c_int, _c_int, _vp, _vp],
     "ssp_tc_wait_probe": [_c_ll, _vp, _vp],
     "ssp_constitutive_sds_branch": [_c_int] + [_vp] * 5 + [_c_int, _vp, _vp, _vp, _vp],
@@ -143,7 +144,7 @@ _KERNELS_PER_CALL = {
     "ssp_assemble_tangent_values_3d_rows": 1, "ssp_assemble_tangent_values_3d_p2": 1, "ssp_tangent_element": 1,
     "ssp_gather": 1, "ssp_tc_tf32_probe": 1, "ssp_tc_wait_probe": 1, "ssp_constitutive_sds_branch": 1,
     "ssp_copy_out": 1, "ssp_copy_device": 1, "ssp_copy_rows_device": 1, "ssp_copy_rows_device_share": 1, "ssp_host_writable": 0, "ssp_plastic_elements": 1, "ssp_mark_element_rows": 1,
-    "ssp_copy_rows_out": 1,
+    "ssp_copy_rows_out": 1, "ssp_copy_rows_out_share": 1,
     "ssp_assemble_overlap_strain_3d_mixed": 1, "ssp_assemble_force_element_mixed": 1, "ssp_split_f64": 1,
     "ssp_assemble_overlap_strain_3d_affine_mixed": 1, "ssp_assemble_force_element_affine_mixed": 1,
     "ssp_assemble_overlap_strain_3d_p2_affine": 1, "ssp_assemble_force_element_p2_affine": 1,

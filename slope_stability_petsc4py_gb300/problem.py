@@ -79,6 +79,9 @@ class OwnedCSRMatrix:
         self._indptr_dev = t.as_tensor(self.indptr, device=values.device)  # for the row-wise refresh
         # which build the host mirror holds: (start key, build number) or None (unknown)
         self.mirror = None
+        # blocks per SM of the row-wise host refresh (1..8): a part of each SM runs it beside the
+        # internal force of the same iteration instead of ahead of it
+        self.copy_share = 4
         self.handle = OwnedCSRMatrix._next_handle
         OwnedCSRMatrix._next_handle += 1
 
@@ -92,9 +95,9 @@ class OwnedCSRMatrix:
         self._copy_stream.wait_stream(cur)
         with t.cuda.stream(self._copy_stream):
             if rows is not None:
-                _lib.call("ssp_copy_rows_out", _lib.ptr(self.values), _lib.ptr(self._indptr_dev), _lib.ptr(rows),
-                          int(self.shape[0]), int(self.values.numel()), self._host.data_ptr(),
-                          self._copy_stream.cuda_stream)
+                _lib.call("ssp_copy_rows_out_share", _lib.ptr(self.values), _lib.ptr(self._indptr_dev),
+                          _lib.ptr(rows), int(self.shape[0]), int(self.values.numel()), self._host.data_ptr(),
+                          int(self.copy_share), self._copy_stream.cuda_stream)
             else:
                 self._host.copy_(self.values, non_blocking=True)
             self._copied = t.cuda.Event()
