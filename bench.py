@@ -13,7 +13,11 @@ set moves from step to step.
 * ``parity``: the GPU outputs (plain and mixed forms) of one state against the oracle -- the CPU
   restatement of the reference's kernels -- on the whole workload, pattern included.
 * ``cpu_baseline`` / ``--impl reference``: the oracle's restatement of the reference's kernels on
-  the host cores, on a bounded sample of the workload (the owned node block of one rank).
+  the host cores, on a bounded sample of the workload (contiguous runs of elements spread over the
+  mesh, built as a mesh of their own), the same states.
+* ``roofline`` / ``roofline_fp64``: the dominant kernel's algorithmic bytes over its CUDA-event
+  time against the measured HBM bandwidth, and its FP64 operations against the live FP64 probe;
+  ``kernel_rooflines`` the same for every step kernel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3d_p2_large] [--impl reference]
 """
