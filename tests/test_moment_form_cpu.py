@@ -11,7 +11,9 @@ terms c lambda_m grad lambda_k, so
 
 This restates that construction in numpy (node order, term table and strain layout as the kernels
 use them) and checks it against the direct contraction with the reference element's own P2
-gradients (`fem.reference_gradients`, the reference's basis.py tables) mapped by J^-T.
+gradients (`fem.reference_gradients`, the reference's basis.py tables) mapped by J^-T; models the
+mixed form's FP32 regrouping against the same contraction; and checks the Taylor polynomials the
+return mapping uses for the sine and cosine of the Lode angle.
 """
 
 from __future__ import annotations
@@ -113,3 +115,66 @@ def test_two_term_gradients_match_the_reference_table():
     for a in range(10):
         g = sum(c * lam5[:, m][:, None] * dlam[k][None, :] for m, c, k in node_terms(a))
         assert np.allclose(g, ghat[:, a, :].T, rtol=0, atol=1e-14)
+
+
+def test_moment_form_in_fp32_stays_within_the_mixed_tolerance():
+    """The mixed form's kernel runs the regrouping in FP32 after FP64 DS - D_el: modelled here by
+    rounding the inputs to float32 and carrying out every stage in float32, the element
+    correction stays within a few 1e-7 of its own scale (the mixed form's bound on the tangent,
+    which also holds the elastic part, is 1e-6)."""
+    from slope_stability_petsc4py_gb300 import fem
+
+    rng = np.random.default_rng(5)
+    ghat = fem.reference_gradients(3, "P2")
+    xi, _ = fem.quadrature(3, "P2")
+    lam_all = np.column_stack([1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]])
+    worst = 0.0
+    for trial in range(4):
+        J = np.eye(3) + 0.4 * rng.standard_normal((3, 3))
+        jinv = np.linalg.inv(J)
+        A = rng.standard_normal((11, 6, 6))
+        dD = -(A @ A.transpose(0, 2, 1)) * 1e7
+        K_direct = sum(b_matrix(ghat[:, :, q].T @ jinv).T @ dD[q] @ b_matrix(ghat[:, :, q].T @ jinv)
+                       for q in range(11))
+        f32 = np.float32
+        v = np.vstack([-jinv.sum(axis=0), jinv]).astype(f32)
+        lam5 = np.hstack([lam_all, np.ones((11, 1))]).astype(f32)
+        bt = beta(v.astype(np.float64)).astype(f32)
+        R = {}
+        for m in range(4):
+            for n in range(m, 4):
+                M = np.einsum("q,qij->ij", (lam5[:, m] * lam5[:, n]).astype(f32), dD.astype(f32)).astype(f32)
+                R[(m, n)] = (bt @ M @ bt.T).astype(f32)
+        for m in range(4):
+            R[(m, 4)] = sum(R[(min(m, n), max(m, n))] for n in range(4)).astype(f32)
+        R[(4, 4)] = sum(R[(m, 4)] for m in range(4)).astype(f32)
+        K = np.zeros((30, 30), f32)
+        for a in range(10):
+            for b in range(10):
+                for ma, ca, ka in node_terms(a):
+                    for mb, cb, kb in node_terms(b):
+                        blk = R[(min(ma, mb), max(ma, mb))]
+                        K[3 * a:3 * a + 3, 3 * b:3 * b + 3] += f32(ca * cb) * blk[3 * ka:3 * ka + 3, 3 * kb:3 * kb + 3]
+        worst = max(worst, np.abs(K.astype(np.float64) - K_direct).max() / np.abs(K_direct).max())
+    assert 1e-9 < worst < 1e-6, worst
+
+
+def test_lode_angle_sine_and_cosine_polynomials():
+    """The Taylor polynomials the return mapping evaluates for sin and cos of the Lode angle
+    (`sincos_lode`, csrc/constitutive.cu: through theta^17 and theta^18, Horner in theta^2) agree
+    with the library functions to within one ulp on [0, pi/3]."""
+    from math import factorial
+
+    theta = np.linspace(0.0, np.pi / 3.0, 400_001)
+    z = theta * theta
+    ps = np.zeros_like(z)
+    for k in range(8, 0, -1):  # 1/17! .. -1/3!
+        ps = ps * z + (-1.0) ** k / factorial(2 * k + 1)
+    s = theta * z * ps + theta
+    pc = np.zeros_like(z)
+    for k in range(9, 0, -1):  # -1/18! .. -1/2!
+        pc = pc * z + (-1.0) ** k / factorial(2 * k)
+    c = z * pc + 1.0
+    ulp_s = np.abs(s - np.sin(theta))[1:] / np.spacing(np.sin(theta[1:]))
+    ulp_c = np.abs(c - np.cos(theta)) / np.spacing(np.cos(theta))
+    assert ulp_s.max() <= 1.0 and ulp_c.max() <= 1.0
