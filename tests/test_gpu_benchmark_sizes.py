@@ -18,7 +18,7 @@ import pytest
 from conftest import PLAIN_RTOL
 
 LAM, R = 1.1, 0.1
-# mixed form: tangent error bound of the benchmark spec's target, force (residual) in double-float
+# mixed form: its 1e-6 bound on the tangent error; the force (residual) is formed in double-float
 MIXED_K_RTOL, MIXED_F_RTOL = 1.0e-6, 1.0e-11
 
 
