@@ -1,7 +1,7 @@
 """The reference's Newton iteration on the host cores, through the oracle.
 
-TEST INFRASTRUCTURE ONLY: the checker of the benchmark's and the tests' GPU runs, and the CPU
-baseline of the benchmark.  The product package never imports it.
+TEST INFRASTRUCTURE ONLY: the oracle the benchmark and the tests compare the GPU runs with, and
+the CPU baseline of the benchmark.  The product package never imports it.
 
 One step is what the reference's ``ConstitutiveOperator.build_F_K_regularized_all_free`` does per
 Newton iteration on its owned rows (src/slope_stability/constitutive/problem.py:2114-2146):

@@ -2,7 +2,7 @@
  * oracle.c -- CPU restatement of the reference's Newton hot-path arithmetic.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product package links or calls
- * this file.  It is used by the tests (as the checker for the CUDA kernels),
+ * this file.  It is used by the tests (the oracle for the CUDA kernels),
  * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.
  *
  * Every function restates one reference routine (paths relative to the

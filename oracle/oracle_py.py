@@ -1,7 +1,7 @@
 """Python side of the oracle: ctypes access to the C restatement plus NumPy restatements.
 
 TEST INFRASTRUCTURE ONLY.  The product package never imports this module; it is the
-checker used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+oracle used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py``.
 
 Restated reference routines (paths relative to the reference project root):
@@ -625,7 +625,7 @@ def owned_pattern(elem, q_mask, owned_node_range):
 
 
 # --------------------------------------------------------------------------- learned branch proposal
-# (no reference counterpart: the checker of the product's MLP kernels, in float64)
+# (no reference counterpart: the oracle for the product's MLP kernels, in float64)
 
 MLP_SHAPES = (("W1", (32, 6)), ("b1", (32,)), ("W2", (32, 32)), ("b2", (32,)), ("W3", (5, 32)), ("b3", (5,)))
 

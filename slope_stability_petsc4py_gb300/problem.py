@@ -828,7 +828,7 @@ class ConstitutiveOperator:
     def _changed_rows(self, info, mat):
         """Row marks of the CSR rows that can differ between the host mirror and the device values:
         when the mirror holds the previous build of the same kind and start (the same r), only the
-        rows of that build's and this build's plastic elements (every other entry equals the start
+        rows of that build's and the current build's plastic elements (every other entry equals the start
         values in both).  None: refresh everything."""
         if not self.incremental_host_copy or info["prev"] is None or mat.mirror != (info["key"], info["prev_no"]):
             return None

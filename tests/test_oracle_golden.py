@@ -1,4 +1,4 @@
-"""Pin the oracle (the CPU restatement used as the checker) against the reference's outputs.
+"""Pin the oracle (the CPU restatement the CUDA kernels are compared with) against the reference's outputs.
 
 The fixtures were produced by ``tests/golden/make_golden.py`` from the reference itself: its
 compiled C kernels and its NumPy/Python paths.  These tests run on the CPU.
