@@ -60,3 +60,25 @@ def test_reference_arm_other_ranks_print_nothing(oracle_built):
     out = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip() == ""
+
+
+def test_correction_accounting_splits_the_plastic_elements():
+    """bench.algorithmic charges the FP64 moment kernel with the elements at or above the split and
+    the point-by-point kernel with the others: units add up to the plastic elements, FP64 work to
+    7,530 per element + 261 per plastic point on one side and 1,935 per plastic point on the other."""
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    st = {"n": 22_360_800, "n_el": 2_032_800, "n_p": 10, "n_q": 11, "dim": 3, "ns": 6, "nnz": 690_405_587,
+          "n_rows": 8_000_000, "n_plastic": 2_600_000.0, "n_plastic_el": 300_000.0,
+          "n_many_el": 240_000.0, "n_plastic_many": 2_300_000.0, "moments": True}
+    mom = bench.algorithmic("ssp_tangent_plastic_correction_p2_moments", st)
+    pt = bench.algorithmic("ssp_tangent_plastic_correction", st)
+    per_el = mom["bytes"] / st["n_many_el"]
+    assert abs(pt["bytes"] - per_el * (st["n_plastic_el"] - st["n_many_el"])) < 1e-3 * pt["bytes"]
+    assert mom["fp64"] == 2.0 * (7530 * 240_000 + 261 * 2_300_000)
+    assert pt["fp64"] == 2.0 * 1935 * (2_600_000 - 2_300_000)
+    mixed = bench.algorithmic("ssp_tangent_plastic_correction_p2_moments_mixed", st)
+    assert mixed["fp64"] == 2.0 * 22 * 2_300_000
+    without = bench.algorithmic("ssp_tangent_plastic_correction", dict(st, moments=False))
+    assert without["fp64"] == 2.0 * 1935 * 2_600_000
